@@ -1,0 +1,188 @@
+/*
+ * qt_rgf.h -- C-ABI of the GB300 (sm_103a) batched recursive Green's function
+ * library (libqtgpu.so).  Plain pointers and sizes only.
+ *
+ * Storage: every n x n block is complex128 COLUMN-MAJOR with interleaved
+ * (re, im) doubles -- the memory image of Fortran complex(8) arrays, so a
+ * Fortran caller passes its arrays unchanged through iso_c_binding.
+ * Points are ordered energy-major, k-minor: p = ie*nk + ik, the loop order of
+ * negf_solve (src/negf_mod.f90:115-116).
+ *
+ * Pointers are HOST pointers unless QT_FLAG_DEVICE_POINTERS is set, in which
+ * case every array argument must be device memory of the context's GPU.
+ */
+#ifndef QT_RGF_H
+#define QT_RGF_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  QT_OK = 0,
+  QT_ERR_ARG = 1,         /* invalid argument (sizes, null pointers)             */
+  QT_ERR_CUDA = 2,        /* CUDA runtime error; see qt_last_error()             */
+  QT_ERR_NOMEM = 3,       /* device allocation failed                           */
+  QT_ERR_UNSUPPORTED = 4, /* configuration not supported (e.g. nm > 128 mixed)   */
+  QT_ERR_POINTS = 5       /* finished, but at least one point has status != 0   */
+} qt_status;
+
+/* per-point status bits (qt_outputs.status) */
+#define QT_PT_OK 0
+#define QT_PT_SINGULAR 1              /* zero/non-finite pivot in a block inverse */
+#define QT_PT_SANCHO_NOT_CONVERGED 2  /* decimation hit max_iter above tol        */
+#define QT_PT_NONFINITE 4             /* NaN/Inf in an output block               */
+
+typedef enum {
+  QT_PREC_FP64 = 0,  /* complex128 on the FP64 pipes (plain path)                 */
+  QT_PREC_MIXED = 1  /* Ozaki-split bf16 tensor-core GEMMs (tcgen05, FP32 TMEM
+                        accumulation, exact leading digit levels), FP32 block LU +
+                        one residual refinement; Sancho at FP64-grade digits     */
+} qt_precision;
+
+#define QT_FLAG_DEVICE_POINTERS 1u /* all arrays are device pointers            */
+#define QT_FLAG_CAROLI 2u          /* also compute Caroli T(E) (qt_outputs.T)    */
+#define QT_FLAG_SYNC 4u            /* synchronise the stream before returning   */
+
+/* Reference-quirk switches (default 0 = the behaviour that produced the
+ * reference's test_cnt/ outputs).                                            */
+#define QT_QUIRK_CPU_FERMI 1u    /* contact Fermi/temperature pairing and tr
+                                    sign of rgf_variableblock_forward
+                                    (src/rgf_mod.f90:100,182,196-202,258)    */
+#define QT_QUIRK_GLP_ZERO 2u     /* G^> recursion seeded with Glp == 0 as in
+                                    src/cuda_rgf_mod.f90:78,351-372          */
+#define QT_QUIRK_BACK_H1I_NEXT 4u /* backward step couples l,l+1 through
+                                    H1i(l+1) instead of the reference's H1i(l)
+                                    (identical for slab-independent coupling) */
+
+typedef struct qt_ctx qt_ctx;
+
+/* Replaces cuda_rgf_init(nm) / cuda_rgf_finish() (src/cuda_rgf_mod.f90:32-51):
+ * the context owns a CUDA stream and grow-only device scratch; contexts are
+ * independent (no module-level state, unlike src/cuda_rgf_mod.f90:24-28).  */
+qt_status qt_ctx_create(qt_ctx** ctx, int device);
+qt_status qt_ctx_destroy(qt_ctx* ctx);
+qt_status qt_ctx_sync(qt_ctx* ctx);
+/* Bound (bytes) on the per-wave device scratch; default 48 GiB.            */
+qt_status qt_ctx_set_scratch_limit(qt_ctx* ctx, int64_t bytes);
+/* Message of the last error on this thread ("" if none).                   */
+const char* qt_last_error(void);
+/* Library version string.                                                   */
+const char* qt_version(void);
+
+/* Block-tridiagonal device of nx slabs of constant block size nm at nk
+ * transverse k-points (cuda_rgf_constblocksize's Hii(nx), H1i(nx+1), Sii(nx),
+ * src/cuda_rgf_mod.f90:55; built per k by devH_build_fromWannierFile,
+ * src/deviceHam_mod.f90:269-287).
+ *   Hii block (k, l) at Hii + 2*(k*hii_kstride + l*hii_lstride) doubles
+ *   H1i block (k, l) at H1i + 2*(k*h1i_kstride + l*h1i_lstride), l = 0..nx,
+ *       H1i[l] = H_{l,l-1}; H1i[0] couples the left lead, H1i[nx] the right
+ *   Sii: NULL => identity (the only case any reference driver uses)
+ * A stride of 0 means "identical for all k" / "identical for all slabs".   */
+typedef struct {
+  int nm, nx, nk;
+  const double* Hii;
+  int64_t hii_kstride, hii_lstride;
+  const double* H1i;
+  int64_t h1i_kstride, h1i_lstride;
+  const double* Sii;
+  int64_t sii_kstride, sii_lstride;
+} qt_device;
+
+/* Contacts and Sancho-Rubio settings.  Reference values: eta_lead = 1e-5
+ * (src/cuda_rgf_mod.f90:671), eta_interior = 0 (:68), sancho_max_iter = 50
+ * (:670), sancho_tol = 1e-100 (:661), mu/temp from negf_solve (:82-85).      */
+typedef struct {
+  double mul, mur;       /* chemical potentials (eV)          */
+  double templ, tempr;   /* temperatures (K)                  */
+  double eta_lead;       /* Sancho Im(z)                      */
+  double eta_interior;   /* Im(z) of interior slabs           */
+  double sancho_tol;     /* exit when sum_ij |H_01(i,j)| < tol */
+  int sancho_max_iter;
+  unsigned quirks;       /* QT_QUIRK_* bits                   */
+} qt_contacts;
+
+/* Outputs, per point p (any pointer may be NULL = not wanted).
+ *   tr, tre   [npts]  terminal-current spectra of cuda_rgf_constblocksize
+ *                     (src/cuda_rgf_mod.f90:271-277, 403-407)
+ *   T         [npts]  Caroli transmission (needs QT_FLAG_CAROLI)
+ *   diag_gr/gl/gg [npts][nx*nm] complex128 diagonals of G^R, G^<, G^>
+ *                     (the per-orbital data behind ldos/ndos/pdos,
+ *                     src/negf_mod.f90:141-149)
+ *   G_r, G_lesser, G_greater [npts][nx][nm*nm] full diagonal blocks
+ *                     (cuda_rgf_constblocksize's G_r, G_lesser, G_greater)
+ *   status    [npts]  QT_PT_* bits
+ *   sancho_iters [npts][2] iterations of the left/right decimation          */
+typedef struct {
+  double* tr;
+  double* tre;
+  double* T;
+  double* diag_gr;
+  double* diag_gl;
+  double* diag_gg;
+  double* G_r;
+  double* G_lesser;
+  double* G_greater;
+  int* status;
+  int* sancho_iters;
+} qt_outputs;
+
+/* Batched ballistic/phonon RGF over nE energies x nk k-points: the whole
+ * ``do ie / do ik / call cuda_rgf_constblocksize`` loop of negf_solve
+ * (src/negf_mod.f90:115-127) in one call.
+ *   E [nE] energies (eV)
+ *   sigma_r_ph, sigma_lesser_ph: NULL (=> 0, the negf_solve case) or
+ *       [npts][nx][nm*nm] complex128 scattering self-energies
+ *       (cuda_rgf_constblocksize's sigma_r_ph / sigma_lesser_ph)         */
+qt_status qt_rgf_solve(qt_ctx* ctx, const qt_device* dev, const double* E, int nE,
+                       const qt_contacts* contacts, const double* sigma_r_ph,
+                       const double* sigma_lesser_ph, qt_precision prec, unsigned flags,
+                       qt_outputs* out);
+
+/* Single-point drop-in with the argument list of cuda_rgf_constblocksize
+ * (src/cuda_rgf_mod.f90:53-59): contiguous (nm, nm, nx) arrays for Hii, Sii,
+ * sigma_lesser_ph, sigma_r_ph, G_r, G_lesser, G_greater, Jdens and
+ * (nm, nm, nx+1) for H1i; mu/T scalars (the reference broadcasts them into
+ * constant nm x nm matrices, src/negf_mod.f90:78-85).  Host pointers; Sii,
+ * the sigmas and Jdens may be NULL.  Runs in FP64.                         */
+qt_status qt_rgf_constblocksize(qt_ctx* ctx, int nm, int nx, double En, double mul, double mur,
+                                double templ, double tempr, const double* Hii, const double* H1i,
+                                const double* Sii, const double* sigma_lesser_ph,
+                                const double* sigma_r_ph, double* G_r, double* G_lesser,
+                                double* G_greater, double* Jdens, double* tr, double* tre);
+
+/* Batched Sancho-Rubio decimation, ``sancho(nm, E, S00, H00, H10, G00, GBB)``
+ * (src/rgf_mod.f90:482; GPU variant src/cuda_rgf_mod.f90:657-765) for npts
+ * independent leads.  H00/H10/S00 block b at ptr + 2*b*stride doubles (stride
+ * 0 = shared); S00 NULL => identity.  G00/GBB [npts][nm*nm]; iters [npts].   */
+qt_status qt_sancho_batch(qt_ctx* ctx, int nm, int npts, const double* E, const double* H00,
+                          int64_t h00_stride, const double* H10, int64_t h10_stride,
+                          const double* S00, int64_t s00_stride, double eta, double tol,
+                          int max_iter, qt_precision prec, unsigned flags, double* G00,
+                          double* GBB, int* iters, int* status);
+
+/* Batched block product C_b = alpha op(A_b) op(B_b) + beta D_b (the
+ * reference's MUL_C / zgemm, src/matrix_c.f90:615-660), square n x n blocks,
+ * op 'N' / 'C' / 'T'.  Strides in complex elements (0 = shared block).  D may
+ * be NULL.  prec selects the FP64 pipes or the tensor-core split product
+ * with `slices` 8-bit digits per operand (ignored for FP64; 0 = default 4). */
+qt_status qt_zgemm_batch(qt_ctx* ctx, int n, int batch, char opA, const double* A,
+                         int64_t a_stride, char opB, const double* B, int64_t b_stride,
+                         const double* alpha, const double* beta, const double* D,
+                         int64_t d_stride, double* C, int64_t c_stride, qt_precision prec,
+                         int slices, unsigned flags);
+
+/* Batched block inverse (the reference's ``invert``, src/linalg.f90:42-62,
+ * src/cuda_rgf_mod.f90:624-654).  X may equal A.  status [batch] gets
+ * QT_PT_SINGULAR bits.  MIXED: FP32 elimination + one refinement step.   */
+qt_status qt_zinv_batch(qt_ctx* ctx, int n, int batch, const double* A, int64_t a_stride,
+                        double* X, int64_t x_stride, qt_precision prec, unsigned flags,
+                        int* status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QT_RGF_H */

@@ -1,0 +1,91 @@
+"""ctypes binding of libqtgpu.so (include/qt_rgf.h).
+
+The library is built in-tree by ``quantum_transport_gb300.build``.  There is
+no CPU fallback: if the shared library is missing or cannot be loaded, every
+entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libqtgpu.so")
+
+QT_OK, QT_ERR_ARG, QT_ERR_CUDA, QT_ERR_NOMEM, QT_ERR_UNSUPPORTED, QT_ERR_POINTS = range(6)
+QT_PREC_FP64, QT_PREC_MIXED = 0, 1
+QT_FLAG_DEVICE_POINTERS, QT_FLAG_CAROLI, QT_FLAG_SYNC = 1, 2, 4
+QT_QUIRK_CPU_FERMI, QT_QUIRK_GLP_ZERO, QT_QUIRK_BACK_H1I_NEXT = 1, 2, 4
+QT_PT_SINGULAR, QT_PT_SANCHO_NOT_CONVERGED, QT_PT_NONFINITE = 1, 2, 4
+
+# every symbol include/qt_rgf.h declares
+EXPORTS = [
+    "qt_ctx_create", "qt_ctx_destroy", "qt_ctx_sync", "qt_ctx_set_scratch_limit",
+    "qt_last_error", "qt_version", "qt_rgf_solve", "qt_rgf_constblocksize",
+    "qt_sancho_batch", "qt_zgemm_batch", "qt_zinv_batch",
+]
+
+
+class QtDevice(C.Structure):
+    _fields_ = [("nm", C.c_int), ("nx", C.c_int), ("nk", C.c_int),
+                ("Hii", C.c_void_p), ("hii_kstride", C.c_int64), ("hii_lstride", C.c_int64),
+                ("H1i", C.c_void_p), ("h1i_kstride", C.c_int64), ("h1i_lstride", C.c_int64),
+                ("Sii", C.c_void_p), ("sii_kstride", C.c_int64), ("sii_lstride", C.c_int64)]
+
+
+class QtContacts(C.Structure):
+    _fields_ = [("mul", C.c_double), ("mur", C.c_double), ("templ", C.c_double),
+                ("tempr", C.c_double), ("eta_lead", C.c_double), ("eta_interior", C.c_double),
+                ("sancho_tol", C.c_double), ("sancho_max_iter", C.c_int), ("quirks", C.c_uint)]
+
+
+class QtOutputs(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("tr", "tre", "T", "diag_gr", "diag_gl", "diag_gg",
+                                          "G_r", "G_lesser", "G_greater", "status",
+                                          "sancho_iters")]
+
+
+class QtError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"qt status {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load libqtgpu.so (raises if absent: the CUDA path has no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise QtError(-1, f"{path} not built; run quantum_transport_gb300.build.build()")
+    lib = C.CDLL(path)
+    vp, i64, dbl, ci = C.c_void_p, C.c_int64, C.c_double, C.c_int
+    lib.qt_ctx_create.argtypes = [C.POINTER(vp), ci]
+    lib.qt_ctx_destroy.argtypes = [vp]
+    lib.qt_ctx_sync.argtypes = [vp]
+    lib.qt_ctx_set_scratch_limit.argtypes = [vp, i64]
+    lib.qt_last_error.restype = C.c_char_p
+    lib.qt_version.restype = C.c_char_p
+    lib.qt_rgf_solve.argtypes = [vp, C.POINTER(QtDevice), vp, ci, C.POINTER(QtContacts), vp, vp,
+                                 ci, C.c_uint, C.POINTER(QtOutputs)]
+    lib.qt_rgf_constblocksize.argtypes = [vp, ci, ci, dbl, dbl, dbl, dbl, dbl] + [vp] * 9 + [vp, vp]
+    lib.qt_sancho_batch.argtypes = [vp, ci, ci, vp, vp, i64, vp, i64, vp, i64, dbl, dbl, ci, ci,
+                                    C.c_uint, vp, vp, vp, vp]
+    lib.qt_zgemm_batch.argtypes = [vp, ci, ci, C.c_char, vp, i64, C.c_char, vp, i64, vp, vp, vp,
+                                   i64, vp, i64, ci, ci, C.c_uint]
+    lib.qt_zinv_batch.argtypes = [vp, ci, ci, vp, i64, vp, i64, ci, C.c_uint, vp]
+    for name in EXPORTS:
+        f = getattr(lib, name)
+        if name not in ("qt_last_error", "qt_version"):
+            f.restype = C.c_int
+    _lib = lib
+    return lib
+
+
+def check(code, allow_points=False):
+    if code == QT_OK or (allow_points and code == QT_ERR_POINTS):
+        return code
+    raise QtError(code, load().qt_last_error().decode())

@@ -1,0 +1,369 @@
+// O(n^2) per-block helpers of the RGF sweep: the zaxpy/zscal/zcopy chains,
+// the contact broadening -(Sigma - Sigma^+) f (src/cuda_rgf_mod.f90:113,242,
+// 254-264, 387-396), the Sancho error measure (src/cuda_rgf_mod.f90:721-726)
+// and the diagonal traces behind tr/tre (src/cuda_rgf_mod.f90:271-277,
+// 403-407) and the per-cell LDOS/n/p spectra (src/output_mod.f90:37-59).
+//
+// Every helper is templated on the block storage: double2 (complex128,
+// arithmetic on the FP64 pipes) or float2 (complex64, FP32 arithmetic -- the
+// split-precision sweep, where GB300's slow FP64 pipes must stay idle).
+// Reductions (traces, sums) always accumulate in double.
+#include "qt_common.cuh"
+#include "qt_kernels.h"
+
+namespace qt {
+
+namespace {
+
+constexpr int NT = 256;
+
+template <typename TC> struct CT;
+template <> struct CT<double2> {
+  using R = double;
+};
+template <> struct CT<float2> {
+  using R = float;
+};
+
+template <typename TC> __device__ __forceinline__ TC mk(double a, double b);
+template <> __device__ __forceinline__ double2 mk<double2>(double a, double b) {
+  return make_double2(a, b);
+}
+template <> __device__ __forceinline__ float2 mk<float2>(double a, double b) {
+  return make_float2((float)a, (float)b);
+}
+template <typename TC> __device__ __forceinline__ TC tadd(TC a, TC b) {
+  TC r; r.x = a.x + b.x; r.y = a.y + b.y; return r;
+}
+template <typename TC> __device__ __forceinline__ TC tsub(TC a, TC b) {
+  TC r; r.x = a.x - b.x; r.y = a.y - b.y; return r;
+}
+template <typename TC, typename R> __device__ __forceinline__ TC tmul(R ar, R ai, TC b) {
+  TC r; r.x = ar * b.x - ai * b.y; r.y = ar * b.y + ai * b.x; return r;
+}
+template <typename TC> __device__ __forceinline__ TC tconj(TC a) { a.y = -a.y; return a; }
+
+inline unsigned grid_for(long long batch) {
+  return (unsigned)(batch < 65535LL * 8 ? batch : 65535LL * 8);
+}
+
+template <typename TC>
+__global__ void zaxpby_kernel(int n, long long batch, BatchRef X, double ar, double ai, BatchRef W,
+                              double br, double bi, BatchRef Z, BatchRef Y,
+                              const unsigned char* active) {
+  using R = typename CT<TC>::R;
+  for (long long b = blockIdx.x; b < batch; b += gridDim.x) {
+    if (active && !active[b]) continue;
+    const TC* x = X.p ? batch_ptr<const TC>(X, b) : nullptr;
+    const TC* w = W.p ? batch_ptr<const TC>(W, b) : nullptr;
+    TC* y = batch_ptr<TC>(Y, b);
+    TC z = mk<TC>(0.0, 0.0);
+    if (Z.p) {
+      const double2 zz = *batch_ptr<const double2>(Z, b);  // shifts are always complex128
+      z = mk<TC>(zz.x, zz.y);
+    }
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      const int i = e % n, j = e / n;
+      TC v = mk<TC>(0.0, 0.0);
+      if (x) v = tmul<TC, R>((R)ar, (R)ai, x[i + (long long)j * X.ld]);
+      if (w) v = tadd(v, tmul<TC, R>((R)br, (R)bi, w[i + (long long)j * W.ld]));
+      if (i == j) v = tadd(v, z);
+      y[i + (long long)j * Y.ld] = v;
+    }
+  }
+}
+
+template <typename TC>
+__global__ void zantiherm_kernel(int n, long long batch, BatchRef X, double cr, double ci,
+                                 BatchRef W, BatchRef Y) {
+  using R = typename CT<TC>::R;
+  for (long long b = blockIdx.x; b < batch; b += gridDim.x) {
+    const TC* x = batch_ptr<const TC>(X, b);
+    const TC* w = W.p ? batch_ptr<const TC>(W, b) : nullptr;
+    TC* y = batch_ptr<TC>(Y, b);
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      const int i = e % n, j = e / n;
+      const TC d = tsub(x[i + (long long)j * X.ld], tconj(x[j + (long long)i * X.ld]));
+      TC v = tmul<TC, R>((R)cr, (R)ci, d);
+      if (w) v = tadd(v, w[i + (long long)j * W.ld]);
+      y[i + (long long)j * Y.ld] = v;
+    }
+  }
+}
+
+template <typename TC>
+__global__ void zdagger_kernel(int n, long long batch, BatchRef X, BatchRef Y) {
+  for (long long b = blockIdx.x; b < batch; b += gridDim.x) {
+    const TC* x = batch_ptr<const TC>(X, b);
+    TC* y = batch_ptr<TC>(Y, b);
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      const int i = e % n, j = e / n;
+      y[i + (long long)j * Y.ld] = tconj(x[j + (long long)i * X.ld]);
+    }
+  }
+}
+
+__device__ double block_sum(double v) {
+  __shared__ double red[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  }
+  __syncthreads();
+  return v;  // valid in thread 0
+}
+
+template <typename TC>
+__global__ void zabssum_kernel(int n, long long batch, BatchRef X, double* out,
+                               const unsigned char* active) {
+  for (long long b = blockIdx.x; b < batch; b += gridDim.x) {
+    if (active && !active[b]) continue;
+    const TC* x = batch_ptr<const TC>(X, b);
+    double s = 0.0;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      const TC v = x[e % n + (long long)(e / n) * X.ld];
+      s += sqrt((double)v.x * v.x + (double)v.y * v.y);
+    }
+    s = block_sum(s);
+    if (threadIdx.x == 0) out[b] = s;
+  }
+}
+
+// out_b = sign * Re( f Tr[K Y1] - (f-1) Tr[K Y2] ),  K = -(X - X^+), f = fermi[b]
+// (src/cuda_rgf_mod.f90:256-277 with Y1 = G^>, Y2 = G^<)
+template <typename TC>
+__global__ void ztrace_current_kernel(int n, long long batch, BatchRef X, BatchRef Y1,
+                                      BatchRef Y2, double sign, const double* fermi, double* out) {
+  for (long long b = blockIdx.x; b < batch; b += gridDim.x) {
+    const TC* x = batch_ptr<const TC>(X, b);
+    const TC* y1 = batch_ptr<const TC>(Y1, b);
+    const TC* y2 = batch_ptr<const TC>(Y2, b);
+    const double f = fermi[b];
+    double s = 0.0;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      const int i = e % n, j = e / n;
+      const TC xa = x[j + (long long)i * X.ld], xb = x[i + (long long)j * X.ld];
+      const double kx = (double)xa.x - xb.x, ky = -(double)xa.y - xb.y;  // conj(X(j,i)) - X(i,j)
+      const TC u = y1[j + (long long)i * Y1.ld], v = y2[j + (long long)i * Y2.ld];
+      const double t1 = kx * u.x - ky * u.y, t2 = kx * v.x - ky * v.y;
+      s += f * t1 - (f - 1.0) * t2;
+    }
+    s = block_sum(s);
+    if (threadIdx.x == 0) out[b] = sign * s;
+  }
+}
+
+template <typename TC>
+__global__ void ztrace_prod_kernel(int n, long long batch, BatchRef X, BatchRef Y, double scale,
+                                   double* out) {
+  for (long long b = blockIdx.x; b < batch; b += gridDim.x) {
+    const TC* x = batch_ptr<const TC>(X, b);
+    const TC* y = batch_ptr<const TC>(Y, b);
+    double s = 0.0;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      const int i = e % n, j = e / n;
+      const TC u = x[i + (long long)j * X.ld], v = y[j + (long long)i * Y.ld];
+      s += (double)u.x * v.x - (double)u.y * v.y;
+    }
+    s = block_sum(s);
+    if (threadIdx.x == 0) out[b] = scale * s;
+  }
+}
+
+template <typename TC>
+__global__ void zdiag_kernel(int n, long long batch, BatchRef X, double* out, long long ostride,
+                             long long ooff) {
+  const long long total = batch * n;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long b = t / n;
+    const int i = (int)(t % n);
+    const TC v = batch_ptr<const TC>(X, b)[i + (long long)i * X.ld];
+    reinterpret_cast<double2*>(out)[b * ostride + ooff + i] = make_double2(v.x, v.y);
+  }
+}
+
+// diag of G^> = G^< + (G - G^+): Y(i,i) + 2i Im X(i,i)
+template <typename TC>
+__global__ void zdiag_greater_kernel(int n, long long batch, BatchRef X, BatchRef Y, double* out,
+                                     long long ostride, long long ooff) {
+  const long long total = batch * n;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long b = t / n;
+    const int i = (int)(t % n);
+    const TC g = batch_ptr<const TC>(X, b)[i + (long long)i * X.ld];
+    const TC l = batch_ptr<const TC>(Y, b)[i + (long long)i * Y.ld];
+    reinterpret_cast<double2*>(out)[b * ostride + ooff + i] =
+        make_double2(l.x, (double)l.y + 2.0 * (double)g.y);
+  }
+}
+
+template <typename TC>
+__global__ void zscale_add_kernel(int n, long long batch, BatchRef X, const double* f, BatchRef W,
+                                  BatchRef Y) {
+  using R = typename CT<TC>::R;
+  for (long long b = blockIdx.x; b < batch; b += gridDim.x) {
+    const TC* x = batch_ptr<const TC>(X, b);
+    const TC* w = W.p ? batch_ptr<const TC>(W, b) : nullptr;
+    TC* y = batch_ptr<TC>(Y, b);
+    const R fb = (R)f[b];
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      const int i = e % n, j = e / n;
+      const TC xv = x[i + (long long)j * X.ld];
+      TC v;
+      v.x = fb * xv.x;
+      v.y = fb * xv.y;
+      if (w) v = tadd(v, w[i + (long long)j * W.ld]);
+      y[i + (long long)j * Y.ld] = v;
+    }
+  }
+}
+
+template <typename TS, typename TD>
+__global__ void zconvert_kernel(int n, long long batch, BatchRef X, BatchRef Y) {
+  for (long long b = blockIdx.x; b < batch; b += gridDim.x) {
+    const TS* x = batch_ptr<const TS>(X, b);
+    TD* y = batch_ptr<TD>(Y, b);
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      const int i = e % n, j = e / n;
+      const TS v = x[i + (long long)j * X.ld];
+      y[i + (long long)j * Y.ld] = mk<TD>((double)v.x, (double)v.y);
+    }
+  }
+}
+
+template <typename TC>
+__global__ void zcheck_finite_kernel(int n, long long batch, BatchRef X, int* status) {
+  for (long long b = blockIdx.x; b < batch; b += gridDim.x) {
+    const TC* x = batch_ptr<const TC>(X, b);
+    int bad = 0;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      const TC v = x[e % n + (long long)(e / n) * X.ld];
+      if (!isfinite((double)v.x) || !isfinite((double)v.y)) bad = 1;
+    }
+    bad = __syncthreads_or(bad);
+    if (bad && threadIdx.x == 0) atomicOr(&status[b], PT_NONFINITE);
+  }
+}
+
+inline unsigned gdiag(long long total) {
+  const long long g = (total + NT - 1) / NT;
+  return (unsigned)(g < 65535LL * 16 ? (g < 1 ? 1 : g) : 65535LL * 16);
+}
+
+}  // namespace
+
+template <typename TC>
+cudaError_t zaxpby(int n, long long batch, BatchRef X, double ar, double ai, BatchRef W, double br,
+                   double bi, BatchRef Z, BatchRef Y, const unsigned char* active, cudaStream_t s) {
+  if (batch <= 0) return cudaSuccess;
+  zaxpby_kernel<TC><<<grid_for(batch), NT, 0, s>>>(n, batch, X, ar, ai, W, br, bi, Z, Y, active);
+  return cudaGetLastError();
+}
+template <typename TC>
+cudaError_t zantiherm(int n, long long batch, BatchRef X, double cr, double ci, BatchRef W,
+                      BatchRef Y, cudaStream_t s) {
+  if (batch <= 0) return cudaSuccess;
+  zantiherm_kernel<TC><<<grid_for(batch), NT, 0, s>>>(n, batch, X, cr, ci, W, Y);
+  return cudaGetLastError();
+}
+template <typename TC>
+cudaError_t zdagger(int n, long long batch, BatchRef X, BatchRef Y, cudaStream_t s) {
+  if (batch <= 0) return cudaSuccess;
+  zdagger_kernel<TC><<<grid_for(batch), NT, 0, s>>>(n, batch, X, Y);
+  return cudaGetLastError();
+}
+template <typename TC>
+cudaError_t zabssum(int n, long long batch, BatchRef X, double* out, const unsigned char* active,
+                    cudaStream_t s) {
+  if (batch <= 0) return cudaSuccess;
+  zabssum_kernel<TC><<<grid_for(batch), NT, 0, s>>>(n, batch, X, out, active);
+  return cudaGetLastError();
+}
+template <typename TC>
+cudaError_t ztrace_current(int n, long long batch, BatchRef X, BatchRef Y1, BatchRef Y2,
+                           double sign, const double* fermi, double* out, cudaStream_t s) {
+  if (batch <= 0) return cudaSuccess;
+  ztrace_current_kernel<TC><<<grid_for(batch), NT, 0, s>>>(n, batch, X, Y1, Y2, sign, fermi, out);
+  return cudaGetLastError();
+}
+template <typename TC>
+cudaError_t ztrace_prod(int n, long long batch, BatchRef X, BatchRef Y, double scale, double* out,
+                        cudaStream_t s) {
+  if (batch <= 0) return cudaSuccess;
+  ztrace_prod_kernel<TC><<<grid_for(batch), NT, 0, s>>>(n, batch, X, Y, scale, out);
+  return cudaGetLastError();
+}
+template <typename TC>
+cudaError_t zscale_add(int n, long long batch, BatchRef X, const double* f, BatchRef W, BatchRef Y,
+                       cudaStream_t s) {
+  if (batch <= 0) return cudaSuccess;
+  zscale_add_kernel<TC><<<grid_for(batch), NT, 0, s>>>(n, batch, X, f, W, Y);
+  return cudaGetLastError();
+}
+template <typename TC>
+cudaError_t zdiag(int n, long long batch, BatchRef X, double* out, long long ostride,
+                  long long ooff, cudaStream_t s) {
+  if (batch <= 0) return cudaSuccess;
+  zdiag_kernel<TC><<<gdiag(batch * n), NT, 0, s>>>(n, batch, X, out, ostride, ooff);
+  return cudaGetLastError();
+}
+template <typename TC>
+cudaError_t zdiag_greater(int n, long long batch, BatchRef X, BatchRef Y, double* out,
+                          long long ostride, long long ooff, cudaStream_t s) {
+  if (batch <= 0) return cudaSuccess;
+  zdiag_greater_kernel<TC><<<gdiag(batch * n), NT, 0, s>>>(n, batch, X, Y, out, ostride, ooff);
+  return cudaGetLastError();
+}
+template <typename TC>
+cudaError_t zcopy(int n, long long batch, BatchRef X, BatchRef Y, cudaStream_t s) {
+  if (batch <= 0) return cudaSuccess;
+  zconvert_kernel<TC, TC><<<grid_for(batch), NT, 0, s>>>(n, batch, X, Y);
+  return cudaGetLastError();
+}
+template <typename TS, typename TD>
+cudaError_t zconvert(int n, long long batch, BatchRef X, BatchRef Y, cudaStream_t s) {
+  if (batch <= 0) return cudaSuccess;
+  zconvert_kernel<TS, TD><<<grid_for(batch), NT, 0, s>>>(n, batch, X, Y);
+  return cudaGetLastError();
+}
+template <typename TC>
+cudaError_t zcheck_finite(int n, long long batch, BatchRef X, int* status, cudaStream_t s) {
+  if (batch <= 0) return cudaSuccess;
+  zcheck_finite_kernel<TC><<<grid_for(batch), NT, 0, s>>>(n, batch, X, status);
+  return cudaGetLastError();
+}
+
+#define QT_INST(TC)                                                                               \
+  template cudaError_t zaxpby<TC>(int, long long, BatchRef, double, double, BatchRef, double,     \
+                                  double, BatchRef, BatchRef, const unsigned char*, cudaStream_t); \
+  template cudaError_t zantiherm<TC>(int, long long, BatchRef, double, double, BatchRef,          \
+                                     BatchRef, cudaStream_t);                                     \
+  template cudaError_t zdagger<TC>(int, long long, BatchRef, BatchRef, cudaStream_t);             \
+  template cudaError_t zabssum<TC>(int, long long, BatchRef, double*, const unsigned char*,       \
+                                   cudaStream_t);                                                 \
+  template cudaError_t ztrace_current<TC>(int, long long, BatchRef, BatchRef, BatchRef, double,   \
+                                          const double*, double*, cudaStream_t);                  \
+  template cudaError_t ztrace_prod<TC>(int, long long, BatchRef, BatchRef, double, double*,       \
+                                       cudaStream_t);                                             \
+  template cudaError_t zscale_add<TC>(int, long long, BatchRef, const double*, BatchRef,          \
+                                      BatchRef, cudaStream_t);                                    \
+  template cudaError_t zdiag<TC>(int, long long, BatchRef, double*, long long, long long,         \
+                                 cudaStream_t);                                                   \
+  template cudaError_t zdiag_greater<TC>(int, long long, BatchRef, BatchRef, double*, long long,  \
+                                         long long, cudaStream_t);                                \
+  template cudaError_t zcopy<TC>(int, long long, BatchRef, BatchRef, cudaStream_t);               \
+  template cudaError_t zcheck_finite<TC>(int, long long, BatchRef, int*, cudaStream_t);
+QT_INST(double2)
+QT_INST(float2)
+template cudaError_t zconvert<double2, float2>(int, long long, BatchRef, BatchRef, cudaStream_t);
+template cudaError_t zconvert<float2, double2>(int, long long, BatchRef, BatchRef, cudaStream_t);
+
+}  // namespace qt

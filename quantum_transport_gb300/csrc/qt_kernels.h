@@ -1,0 +1,91 @@
+// Internal launch interfaces of the batched kernels (not part of the C-ABI).
+#pragma once
+#include "qt_common.cuh"
+
+namespace qt {
+
+enum { OP_N = 0, OP_C = 1, OP_T = 2 };
+
+// C_b = alpha * op(A_b) op(B_b) + beta * D_b + z_b * I   (m x n result, inner k)
+struct GemmArgs {
+  int m, n, k;
+  BatchRef A, B, C, D, Z;  // D.p / Z.p may be null; Z entries are single complex
+  int opA, opB;
+  double alpha_re, alpha_im, beta_re, beta_im;
+  long long batch;
+  const unsigned char* active;  // optional per-batch mask: skip entry when 0
+};
+
+cudaError_t zgemm_f64(const GemmArgs& a, cudaStream_t s);
+
+// Split-precision (Ozaki-style bf16 digits) tensor-core GEMM; same contract.
+//   slices: digits per operand row/column (8 bits each)
+//   levels: highest digit-product level kept (level = i + j)
+cudaError_t zgemm_oz(const GemmArgs& a, int slices, int levels, cudaStream_t s);
+// complex64 in/out variant (3 or 4 digits): the split-precision RGF sweep
+cudaError_t zgemm_oz_c64(const GemmArgs& a, int slices, cudaStream_t s);
+// number of bounded waits that timed out in the tensor-core kernel since the last call
+int oz_timeouts_and_reset();
+
+// X_b = inv(A_b), Gauss-Jordan with partial pivoting; status_b |= PT_SINGULAR
+// on a zero or non-finite pivot.  X may alias A.
+struct InvArgs {
+  int n;
+  BatchRef A, X;
+  long long batch;
+  int* status;                  // per batch (may be null)
+  const unsigned char* active;  // optional mask
+};
+cudaError_t zinv_f64(const InvArgs& a, cudaStream_t s);
+// FP32 elimination in shared memory (n <= 128); TC = storage of A and X
+template <typename TC>
+cudaError_t zinv_f32(const InvArgs& a, cudaStream_t s);
+
+// ---- elementwise helpers, TC = double2 (complex128) or float2 (complex64);
+// n x n column-major blocks; diagonal shifts Z are always complex128 scalars.
+// Y_b = alpha*X_b + beta*W_b + z_b*I   (X or W may be null -> 0)
+template <typename TC>
+cudaError_t zaxpby(int n, long long batch, BatchRef X, double alpha_re, double alpha_im,
+                   BatchRef W, double beta_re, double beta_im, BatchRef Z, BatchRef Y,
+                   const unsigned char* active, cudaStream_t s);
+// Y_b = c * (X_b - X_b^+) + W_b  (W may be null)
+template <typename TC>
+cudaError_t zantiherm(int n, long long batch, BatchRef X, double c_re, double c_im, BatchRef W,
+                      BatchRef Y, cudaStream_t s);
+// Y_b = X_b^+
+template <typename TC>
+cudaError_t zdagger(int n, long long batch, BatchRef X, BatchRef Y, cudaStream_t s);
+// out_b = sum_ij |X_b(i,j)|  (the reference's Sancho error measure)
+template <typename TC>
+cudaError_t zabssum(int n, long long batch, BatchRef X, double* out, const unsigned char* active,
+                    cudaStream_t s);
+// out_b = sign * Re(f Tr[K Y1] - (f-1) Tr[K Y2]), K = -(X - X^+), f = fermi[b]
+template <typename TC>
+cudaError_t ztrace_current(int n, long long batch, BatchRef X, BatchRef Y1, BatchRef Y2,
+                           double sign, const double* fermi, double* out, cudaStream_t s);
+// out_b = scale * Re Tr[X_b Y_b]
+template <typename TC>
+cudaError_t ztrace_prod(int n, long long batch, BatchRef X, BatchRef Y, double scale, double* out,
+                        cudaStream_t s);
+// Y_b = f[b] * X_b + W_b   (W may be null)
+template <typename TC>
+cudaError_t zscale_add(int n, long long batch, BatchRef X, const double* f, BatchRef W, BatchRef Y,
+                       cudaStream_t s);
+// out[b*ostride + ooff + i] = X_b(i,i)   (complex128 output)
+template <typename TC>
+cudaError_t zdiag(int n, long long batch, BatchRef X, double* out, long long ostride,
+                  long long ooff, cudaStream_t s);
+// out[b*ostride + ooff + i] = Y_b(i,i) + X_b(i,i) - conj(X_b(i,i))   (diag of G^< + G - G^+)
+template <typename TC>
+cudaError_t zdiag_greater(int n, long long batch, BatchRef X, BatchRef Y, double* out,
+                          long long ostride, long long ooff, cudaStream_t s);
+template <typename TC>
+cudaError_t zcopy(int n, long long batch, BatchRef X, BatchRef Y, cudaStream_t s);
+// storage conversion complex128 <-> complex64
+template <typename TS, typename TD>
+cudaError_t zconvert(int n, long long batch, BatchRef X, BatchRef Y, cudaStream_t s);
+// status_b |= PT_NONFINITE if any element of X_b is not finite
+template <typename TC>
+cudaError_t zcheck_finite(int n, long long batch, BatchRef X, int* status, cudaStream_t s);
+
+}  // namespace qt

@@ -1,0 +1,1019 @@
+// Host orchestration of the batched RGF sweep and the C-ABI (include/qt_rgf.h).
+//
+// The reference solves one (E, k) point per call of cuda_rgf_constblocksize
+// (src/cuda_rgf_mod.f90:53-413), crossing the host<->device boundary around
+// every cuBLAS/cuSOLVER call.  Here a WAVE of P points (P a multiple of nk,
+// so point index modulo nk is the k index) advances through the sweep
+// together: every block operation is one batched launch over the wave, all
+// state stays in HBM, and only final reductions leave the device.
+//
+// Per wave:
+//   1. Sancho-Rubio decimation of both leads, batched, with a per-point
+//      convergence mask (src/cuda_rgf_mod.f90:657-765).
+//   2. left contact   (src/cuda_rgf_mod.f90:90-134)
+//   3. forward sweep  g_l, g^<_l (src/cuda_rgf_mod.f90:140-188)
+//   4. right contact  G_NN, G^<_NN, tr (src/cuda_rgf_mod.f90:192-277)
+//   5. backward sweep G_l, G^<_l (src/cuda_rgf_mod.f90:283-381), with the
+//      minimal 8-product form (see DESIGN notes in the backward loop)
+//   6. left-contact current tre (src/cuda_rgf_mod.f90:387-407)
+//   7. optional Caroli T(E) from the left-connected chain G_{N1}.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/qt_rgf.h"
+#include "qt_common.cuh"
+#include "qt_kernels.h"
+
+using qt::BatchRef;
+using qt::cd;
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+extern "C" void qt_set_last_error(const char* msg, const char* file, int line) {
+  char buf[512];
+  snprintf(buf, sizeof(buf), "%s (%s:%d)", msg, file, line);
+  g_last_error = buf;
+}
+
+extern "C" const char* qt_last_error(void) { return g_last_error.c_str(); }
+extern "C" const char* qt_version(void) { return "qtgpu 0.1 sm_103a"; }
+
+#define QT_FAIL(code, msg)                             \
+  do {                                                 \
+    qt_set_last_error((msg), __FILE__, __LINE__);      \
+    return (code);                                     \
+  } while (0)
+
+#define QT_TRY(expr)                                   \
+  do {                                                 \
+    qt_status _s = (expr);                             \
+    if (_s != QT_OK) return _s;                        \
+  } while (0)
+
+struct qt_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int64_t scratch_limit = 48LL << 30;
+  void* arena = nullptr;
+  size_t arena_bytes = 0;
+  void* io = nullptr;  // staging for host-pointer calls
+  size_t io_bytes = 0;
+  void* conv = nullptr;  // complex64 copies of H / sigma for the split-precision sweep
+  size_t conv_bytes = 0;
+};
+
+namespace {
+
+constexpr double BOLTZ = 8.61734e-05;  // eV/K, src/cuda_rgf_mod.f90:22
+
+qt_status ensure(void*& p, size_t& have, size_t need) {
+  if (need <= have) return QT_OK;
+  if (p) cudaFree(p);
+  p = nullptr;
+  have = 0;
+  cudaError_t e = cudaMalloc(&p, need);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    QT_FAIL(QT_ERR_NOMEM, "device allocation failed");
+  }
+  have = need;
+  return QT_OK;
+}
+
+struct Arena {
+  char* base;
+  size_t cap, off = 0;
+  template <typename T>
+  T* take(size_t count) {
+    size_t bytes = (count * sizeof(T) + 255) & ~size_t(255);
+    if (off + bytes > cap) return nullptr;
+    T* r = reinterpret_cast<T*>(base + off);
+    off += bytes;
+    return r;
+  }
+};
+
+inline BatchRef ref(const void* p, long long stride, int ld, int mod = 0, const int* idx = nullptr) {
+  BatchRef r;
+  r.p = const_cast<void*>(p);
+  r.stride = stride;
+  r.mod = mod;
+  r.ld = ld;
+  r.idx = idx;
+  return r;
+}
+inline BatchRef nullref() { return ref(nullptr, 0, 1); }
+
+__global__ void make_z_kernel(const double* E, long long p0, long long P, int nk, double eta,
+                              cd* z) {
+  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < P;
+       b += (long long)gridDim.x * blockDim.x) {
+    z[b] = cd{E[(p0 + b) / nk], eta};
+  }
+}
+
+// fermi factors per point: f = 1/(1+exp((E-mu)/(k T)))  (src/cuda_rgf_mod.f90:859-863)
+__global__ void make_fermi_kernel(const double* E, long long p0, long long P, int nk, double mu,
+                                  double temp, double* f) {
+  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < P;
+       b += (long long)gridDim.x * blockDim.x) {
+    f[b] = 1.0 / (1.0 + exp((E[(p0 + b) / nk] - mu) / (BOLTZ * temp)));
+  }
+}
+
+__global__ void sancho_update_kernel(long long P, const double* err, double tol, int it,
+                                     unsigned char* active, int* iters, int* n_active) {
+  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < P;
+       b += (long long)gridDim.x * blockDim.x) {
+    if (!active[b]) continue;
+    iters[b] = it;
+    if (fabs(err[b]) < tol) active[b] = 0;
+    else atomicAdd(n_active, 1);
+  }
+}
+
+__global__ void flag_unconverged_kernel(long long P, const unsigned char* active, int* status) {
+  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < P;
+       b += (long long)gridDim.x * blockDim.x)
+    if (active[b]) status[b] |= qt::PT_SANCHO_NOT_CONVERGED;
+}
+
+inline unsigned g1d(long long n) {
+  long long g = (n + 255) / 256;
+  if (g < 1) g = 1;
+  if (g > 65535LL * 8) g = 65535LL * 8;
+  return (unsigned)g;
+}
+
+__global__ void flat_d2f_kernel(const double2* x, float2* y, long long count) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < count;
+       t += (long long)gridDim.x * blockDim.x)
+    y[t] = make_float2((float)x[t].x, (float)x[t].y);
+}
+
+// ----------------------------------------------------------------- ops
+// Block operations on storage TC.  Plain path: TC = double2 on the FP64
+// pipes.  Split path: TC = double2 with FP64-grade digits (Sancho and the
+// contact self-energies) or TC = float2 with `slices` digits (the sweep);
+// inverses are FP32 eliminations followed by `refine` residual steps
+// X <- X + X (I - A X) computed with the tensor-core product.
+template <typename TC>
+struct Ops {
+  cudaStream_t s;
+  int n;
+  qt_precision prec;
+  int slices = 4;
+  int refine = 1;
+  const cd* one = nullptr;  // device scalar (1, 0)
+  TC* rt1 = nullptr;        // P * n*n refinement scratch
+  TC* rt2 = nullptr;
+  long long P = 0;
+
+  qt_status gemm(BatchRef A, int opA, BatchRef B, int opB, BatchRef C, long long batch,
+                 cd alpha = {1, 0}, BatchRef D = nullref(), cd beta = {0, 0},
+                 BatchRef Z = nullref(), const unsigned char* active = nullptr) {
+    qt::GemmArgs g;
+    g.m = g.n = g.k = n;
+    g.A = A; g.B = B; g.C = C; g.D = D; g.Z = Z;
+    g.opA = opA; g.opB = opB;
+    g.alpha_re = alpha.x; g.alpha_im = alpha.y; g.beta_re = beta.x; g.beta_im = beta.y;
+    g.batch = batch;
+    g.active = active;
+    cudaError_t e;
+    if constexpr (sizeof(TC) == 16) {
+      e = prec == QT_PREC_FP64 ? qt::zgemm_f64(g, s) : qt::zgemm_oz(g, slices, slices - 1, s);
+    } else {
+      e = qt::zgemm_oz_c64(g, slices, s);
+    }
+    if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+    return QT_OK;
+  }
+  // X = inv(A); A is preserved (X must differ from A in the split path)
+  qt_status inv(BatchRef A, BatchRef X, long long batch, int* status,
+                const unsigned char* active = nullptr) {
+    qt::InvArgs a;
+    a.n = n; a.A = A; a.X = X; a.batch = batch; a.status = status; a.active = active;
+    cudaError_t e;
+    if (prec == QT_PREC_FP64) {
+      if constexpr (sizeof(TC) == 16) e = qt::zinv_f64(a, s);
+      else e = cudaErrorInvalidValue;
+      if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+      return QT_OK;
+    }
+    if (X.p == A.p) QT_FAIL(QT_ERR_ARG, "split-precision inverse needs X != A");
+    e = qt::zinv_f32<TC>(a, s);
+    if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+    if (refine > 0 && (batch > P || !rt1 || !rt2)) QT_FAIL(QT_ERR_ARG, "refinement scratch too small");
+    const BatchRef R = ref(rt1, (long long)n * n, n), T = ref(rt2, (long long)n * n, n);
+    for (int it = 0; it < refine; ++it) {
+      QT_TRY(gemm(A, qt::OP_N, X, qt::OP_N, R, batch, cd{-1, 0}, nullref(), cd{0, 0},
+                  ref(one, 0, 1), active));  // R = I - A X
+      QT_TRY(gemm(X, qt::OP_N, R, qt::OP_N, T, batch, cd{1, 0}, X, cd{1, 0}, nullref(), active));
+      qt::zcopy<TC>(n, batch, T, X, s);
+    }
+    return QT_OK;
+  }
+};
+
+// ----------------------------------------------------------- the solve
+struct Problem {
+  int nm, nx, nk;
+  long long npts;
+  const cd* Hii; long long hk, hl;   // complex128 blocks (device)
+  const cd* H1i; long long h1k, h1l;
+  const float2* Hii32;               // complex64 copies (split path)
+  const float2* H1i32;
+  const cd* sigr;                    // per point [npts][nx][nm2] or null
+  const cd* sigl;
+  const float2* sigr32;
+  const float2* sigl32;
+  const double* E;
+  qt_contacts c;
+  qt_precision prec;
+  unsigned flags;
+  int sweep_slices, lead_slices;
+  // device outputs (may be null)
+  double *tr, *tre, *T, *dgr, *dgl, *dgg;
+  cd *Gr, *Gl, *Gg;
+  int *status, *iters;
+};
+
+size_t wave_bytes(const Problem& pb, long long P) {
+  const size_t nm2 = (size_t)pb.nm * pb.nm;
+  const size_t tc = pb.prec == QT_PREC_FP64 ? 16 : 8;
+  const size_t sweep = (2 * (size_t)pb.nx + 14 + 2) * tc;  // g_l, g^<_l, temporaries, refinement
+  const size_t lead = (7 + 2 + 6) * 16;                     // Sancho state + refinement + contact
+  return (sweep + lead) * nm2 * P + (size_t)P * 512 + (512 << 10);
+}
+
+// Batched Sancho-Rubio on the wave (complex128 state).  H00 per point, H_10 the
+// decimation's coupling argument (dag_in: it is H10in^+, the left lead,
+// src/cuda_rgf_mod.f90:101).  G00 = (zS - H_SS)^-1, GBB = (zS - H_BB)^-1.
+qt_status sancho_wave(const Ops<double2>& op0, Arena& ar, long long P, BatchRef H00,
+                      BatchRef H10in, bool dag_in, const cd* zlead, double tol, int max_iter,
+                      BatchRef G00, BatchRef GBB, int* status, int* iters_out, int iters_stride) {
+  Ops<double2> op = op0;
+  const int n = op.n;
+  const long long nm2 = (long long)n * n;
+  cudaStream_t s = op.s;
+  const size_t mark = ar.off;  // the Sancho state is released on return
+  cd* buf = ar.take<cd>((size_t)7 * P * nm2);
+  double* err = ar.take<double>(P);
+  unsigned char* active = ar.take<unsigned char>(P);
+  int* iters = ar.take<int>(P);
+  int* nact = ar.take<int>(1);
+  if (op.prec != QT_PREC_FP64) {
+    op.rt1 = reinterpret_cast<double2*>(ar.take<cd>((size_t)P * nm2));
+    op.rt2 = reinterpret_cast<double2*>(ar.take<cd>((size_t)P * nm2));
+    op.P = P;
+    if (!op.rt1 || !op.rt2) QT_FAIL(QT_ERR_NOMEM, "wave arena exhausted (sancho refinement)");
+  }
+  if (!buf || !err || !active || !iters || !nact) QT_FAIL(QT_ERR_NOMEM, "wave arena exhausted (sancho)");
+  BatchRef HBB = ref(buf + 0 * P * nm2, nm2, n), HSS = ref(buf + 1 * P * nm2, nm2, n);
+  BatchRef H10 = ref(buf + 2 * P * nm2, nm2, n), H01 = ref(buf + 3 * P * nm2, nm2, n);
+  BatchRef A = ref(buf + 4 * P * nm2, nm2, n), B = ref(buf + 5 * P * nm2, nm2, n);
+  BatchRef C = ref(buf + 6 * P * nm2, nm2, n);
+  const BatchRef Zl = ref(zlead, 1, 1);
+  qt::zcopy<double2>(n, P, H00, HBB, s);
+  qt::zcopy<double2>(n, P, H00, HSS, s);
+  if (dag_in) {
+    qt::zdagger<double2>(n, P, H10in, H10, s);
+    qt::zcopy<double2>(n, P, H10in, H01, s);
+  } else {
+    qt::zcopy<double2>(n, P, H10in, H10, s);
+    qt::zdagger<double2>(n, P, H10in, H01, s);
+  }
+  cudaMemsetAsync(active, 1, P, s);
+  cudaMemsetAsync(iters, 0, P * sizeof(int), s);
+  const cd one{1, 0};
+  for (int it = 1; it <= max_iter; ++it) {
+    // A = (z S - H_BB)^-1           (src/cuda_rgf_mod.f90:687-696)
+    qt::zaxpby<double2>(n, P, HBB, -1, 0, nullref(), 0, 0, Zl, C, active, s);
+    QT_TRY(op.inv(C, A, P, status, active));
+    // B = A H_10 ; H_SS += H_01 B ; H_BB += H_01 B      (:698-702)
+    QT_TRY(op.gemm(A, qt::OP_N, H10, qt::OP_N, B, P, one, nullref(), {0, 0}, nullref(), active));
+    QT_TRY(op.gemm(H01, qt::OP_N, B, qt::OP_N, C, P, one, nullref(), {0, 0}, nullref(), active));
+    qt::zaxpby<double2>(n, P, HSS, 1, 0, C, 1, 0, nullref(), HSS, active, s);
+    qt::zaxpby<double2>(n, P, HBB, 1, 0, C, 1, 0, nullref(), HBB, active, s);
+    // C = H_10 B ; B = A H_01 ; A = H_10 B ; H_10 = C ; H_BB += A    (:704-711)
+    QT_TRY(op.gemm(H10, qt::OP_N, B, qt::OP_N, C, P, one, nullref(), {0, 0}, nullref(), active));
+    QT_TRY(op.gemm(A, qt::OP_N, H01, qt::OP_N, B, P, one, nullref(), {0, 0}, nullref(), active));
+    QT_TRY(op.gemm(H10, qt::OP_N, B, qt::OP_N, A, P, one, nullref(), {0, 0}, nullref(), active));
+    std::swap(H10, C);
+    qt::zaxpby<double2>(n, P, HBB, 1, 0, A, 1, 0, nullref(), HBB, active, s);
+    // H_01 = H_01 B ; error = sum |H_01|            (:712-726)
+    QT_TRY(op.gemm(H01, qt::OP_N, B, qt::OP_N, C, P, one, nullref(), {0, 0}, nullref(), active));
+    std::swap(H01, C);
+    qt::zabssum<double2>(n, P, H01, err, active, s);
+    cudaMemsetAsync(nact, 0, sizeof(int), s);
+    sancho_update_kernel<<<g1d(P), 256, 0, s>>>(P, err, tol, it, active, iters, nact);
+    if ((it % 4) == 0 || it == max_iter) {
+      int h = 0;
+      cudaMemcpyAsync(&h, nact, sizeof(int), cudaMemcpyDeviceToHost, s);
+      cudaError_t e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+      if (h == 0) break;
+    }
+  }
+  flag_unconverged_kernel<<<g1d(P), 256, 0, s>>>(P, active, status);
+  // G00 = (z S - H_SS)^-1 ; GBB = (z S - H_BB)^-1    (:740-761)
+  qt::zaxpby<double2>(n, P, HSS, -1, 0, nullref(), 0, 0, Zl, C, nullptr, s);
+  QT_TRY(op.inv(C, G00, P, status));
+  if (GBB.p) {
+    qt::zaxpby<double2>(n, P, HBB, -1, 0, nullref(), 0, 0, Zl, C, nullptr, s);
+    QT_TRY(op.inv(C, GBB, P, status));
+  }
+  if (iters_out)
+    cudaMemcpy2DAsync(iters_out, iters_stride * sizeof(int), iters, sizeof(int), sizeof(int), P,
+                      cudaMemcpyDeviceToDevice, s);
+  ar.off = mark;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+  return QT_OK;
+}
+
+template <typename TC>
+void zconvert_or_copy(int n, long long P, BatchRef X, BatchRef Y, cudaStream_t s) {
+  if constexpr (sizeof(TC) == 16) qt::zcopy<double2>(n, P, X, Y, s);
+  else qt::zconvert<double2, float2>(n, P, X, Y, s);
+}
+template <typename TC>
+void to_c128(int n, long long P, BatchRef X, BatchRef Y, cudaStream_t s) {
+  if constexpr (sizeof(TC) == 16) qt::zcopy<double2>(n, P, X, Y, s);
+  else qt::zconvert<float2, double2>(n, P, X, Y, s);
+}
+
+template <typename TC>
+qt_status solve_wave(qt_ctx* ctx, const Problem& pb, long long p0, long long P, Arena& ar) {
+  const int n = pb.nm, nx = pb.nx, nk = pb.nk;
+  const long long nm2 = (long long)n * n;
+  cudaStream_t s = ctx->stream;
+  const unsigned q = pb.c.quirks;
+  const bool split = pb.prec != QT_PREC_FP64;
+
+  cd* zint = ar.take<cd>(P);
+  cd* zlead = ar.take<cd>(P);
+  double* fl = ar.take<double>(P);
+  double* fr = ar.take<double>(P);
+  double* fe = ar.take<double>(P);
+  cd* one = ar.take<cd>(1);
+  int* status = ar.take<int>(P);
+  TC* gl_all = ar.take<TC>((size_t)nx * P * nm2);   // g_l   [l][b]
+  TC* gln_all = ar.take<TC>((size_t)nx * P * nm2);  // g^<_l [l][b]
+  TC* tmp = ar.take<TC>((size_t)14 * P * nm2);
+  TC* rt1 = ar.take<TC>((size_t)P * nm2);
+  TC* rt2 = ar.take<TC>((size_t)P * nm2);
+  cd* cbuf = ar.take<cd>((size_t)6 * P * nm2);      // complex128 contact scratch
+  if (!zint || !zlead || !fl || !fr || !fe || !one || !status || !gl_all || !gln_all || !tmp ||
+      !rt1 || !rt2 || !cbuf)
+    QT_FAIL(QT_ERR_NOMEM, "wave arena exhausted");
+  // sweep operations on TC, contact operations on complex128
+  Ops<TC> op{s, n, pb.prec};
+  op.slices = pb.sweep_slices;
+  op.refine = split ? 1 : 0;
+  op.one = one; op.rt1 = rt1; op.rt2 = rt2; op.P = P;
+  Ops<double2> cop{s, n, pb.prec};
+  cop.slices = pb.lead_slices;
+  cop.refine = split ? 2 : 0;
+  cop.one = one;
+
+  const cd h1{1.0, 0.0};
+  cudaMemcpyAsync(one, &h1, sizeof(cd), cudaMemcpyHostToDevice, s);
+  cudaMemsetAsync(status, 0, P * sizeof(int), s);
+  make_z_kernel<<<g1d(P), 256, 0, s>>>(pb.E, p0, P, nk, pb.c.eta_interior, zint);
+  make_z_kernel<<<g1d(P), 256, 0, s>>>(pb.E, p0, P, nk, pb.c.eta_lead, zlead);
+  // Contact Fermi pairings: GPU routine src/cuda_rgf_mod.f90:113 (mul,TEMPl), :242 (mur,TEMPl),
+  // :388 (mul,TEMPr); CPU routine src/rgf_mod.f90:100 (mur,TEMPr), :182 (mul,TEMPl), :258 (mur,TEMPr).
+  const bool cpu = (q & QT_QUIRK_CPU_FERMI) != 0;
+  make_fermi_kernel<<<g1d(P), 256, 0, s>>>(pb.E, p0, P, nk, cpu ? pb.c.mur : pb.c.mul,
+                                           cpu ? pb.c.tempr : pb.c.templ, fl);
+  make_fermi_kernel<<<g1d(P), 256, 0, s>>>(pb.E, p0, P, nk, cpu ? pb.c.mul : pb.c.mur, pb.c.templ,
+                                           fr);
+  make_fermi_kernel<<<g1d(P), 256, 0, s>>>(pb.E, p0, P, nk, cpu ? pb.c.mur : pb.c.mul, pb.c.tempr,
+                                           fe);
+  const double tr_sign = cpu ? 1.0 : -1.0;
+
+  const bool c64 = sizeof(TC) == 8;
+  auto T = [&](int i) { return ref(tmp + (size_t)i * P * nm2, nm2, n); };
+  auto C8 = [&](int i) { return ref(cbuf + (size_t)i * P * nm2, nm2, n); };
+  auto GL = [&](int l) { return ref(gl_all + (size_t)l * P * nm2, nm2, n); };
+  auto GLN = [&](int l) { return ref(gln_all + (size_t)l * P * nm2, nm2, n); };
+  // Hamiltonian blocks in complex128 (contacts) and in the sweep's storage
+  auto HII8 = [&](int l) { return ref(pb.Hii + l * pb.hl, pb.hk, n, pb.hk ? nk : 0); };
+  auto H1I8 = [&](int l) { return ref(pb.H1i + l * pb.h1l, pb.h1k, n, pb.h1k ? nk : 0); };
+  auto HII = [&](int l) {
+    return c64 ? ref(pb.Hii32 + l * pb.hl, pb.hk, n, pb.hk ? nk : 0) : HII8(l);
+  };
+  auto H1I = [&](int l) {
+    return c64 ? ref(pb.H1i32 + l * pb.h1l, pb.h1k, n, pb.h1k ? nk : 0) : H1I8(l);
+  };
+  auto SIGR8 = [&](int l) {
+    return pb.sigr ? ref(pb.sigr + (p0 * nx + l) * nm2, nx * nm2, n) : nullref();
+  };
+  auto SIGR = [&](int l) {
+    if (!pb.sigr) return nullref();
+    return c64 ? ref(pb.sigr32 + (p0 * nx + l) * nm2, nx * nm2, n) : SIGR8(l);
+  };
+  auto SIGL = [&](int l) {
+    if (!pb.sigl) return nullref();
+    return c64 ? ref(pb.sigl32 + (p0 * nx + l) * nm2, nx * nm2, n)
+               : ref(pb.sigl + (p0 * nx + l) * nm2, nx * nm2, n);
+  };
+  auto OUTB = [&](cd* base, int l) { return ref(base + (p0 * nx + l) * nm2, nx * nm2, n); };
+  const BatchRef Zi = ref(zint, 1, 1);
+  const cd one_c{1, 0}, mone{-1, 0};
+  const BatchRef SigL = T(13), Pch = T(12);
+  const bool caroli = (pb.flags & QT_FLAG_CAROLI) && pb.T;
+
+  // ---------------- left contact (src/cuda_rgf_mod.f90:90-134)
+  // lead decimation and Sigma_L = H10 G00 H10^+ at FP64 grade, then stored as TC
+  qt::zaxpby<double2>(n, P, HII8(0), 1, 0, SIGR8(0), 1, 0, nullref(), C8(0), nullptr, s);
+  QT_TRY(sancho_wave(cop, ar, P, C8(0), H1I8(0), true, zlead, pb.c.sancho_tol,
+                     pb.c.sancho_max_iter, C8(1), nullref(), status,
+                     pb.iters ? pb.iters + p0 * 2 : nullptr, 2));
+  QT_TRY(cop.gemm(H1I8(0), qt::OP_N, C8(1), qt::OP_N, C8(2), P));
+  QT_TRY(cop.gemm(C8(2), qt::OP_N, H1I8(0), qt::OP_C, C8(3), P));
+  zconvert_or_copy<TC>(n, P, C8(3), SigL, s);
+  // H00 = Hii(1) + sigma_r_ph(1) S ;  g_1 = (z S - H00 - Sigma_L)^-1
+  BatchRef H00 = T(0);
+  qt::zaxpby<TC>(n, P, HII(0), 1, 0, SIGR(0), 1, 0, nullref(), H00, nullptr, s);
+  qt::zaxpby<TC>(n, P, H00, -1, 0, SigL, -1, 0, Zi, T(3), nullptr, s);
+  QT_TRY(op.inv(T(3), GL(0), P, status));
+  // Sigma^< = -(Sigma_L - Sigma_L^+) f_L + sigma_lesser_ph S ;  g^<_1 = g Sigma^< g^+
+  qt::zantiherm<TC>(n, P, SigL, -1, 0, nullref(), T(4), s);
+  qt::zscale_add<TC>(n, P, T(4), fl, SIGL(0), T(4), s);
+  QT_TRY(op.gemm(GL(0), qt::OP_N, T(4), qt::OP_N, T(5), P));
+  QT_TRY(op.gemm(T(5), qt::OP_N, GL(0), qt::OP_C, GLN(0), P));
+  if (caroli) qt::zcopy<TC>(n, P, GL(0), Pch, s);  // P_0 = g_0
+
+  // ---------------- forward sweep (src/cuda_rgf_mod.f90:140-188)
+  for (int l = 1; l <= nx - 2; ++l) {
+    const BatchRef H10 = H1I(l);
+    // A = z S - (Hii + sigma_r_ph) - H10 g_{l-1} H10^+   (sigma_r_ph without *S, :142)
+    QT_TRY(op.gemm(H10, qt::OP_N, GL(l - 1), qt::OP_N, T(0), P));
+    if (pb.sigr) {
+      qt::zaxpby<TC>(n, P, HII(l), 1, 0, SIGR(l), 1, 0, nullref(), T(2), nullptr, s);
+      QT_TRY(op.gemm(T(0), qt::OP_N, H10, qt::OP_C, T(1), P, mone, T(2), mone, Zi));
+    } else {
+      QT_TRY(op.gemm(T(0), qt::OP_N, H10, qt::OP_C, T(1), P, mone, HII(l), mone, Zi));
+    }
+    QT_TRY(op.inv(T(1), GL(l), P, status));
+    // g^<_l = g (H10 g^<_{l-1} H10^+ + sigma_lesser_ph S) g^+
+    QT_TRY(op.gemm(H10, qt::OP_N, GLN(l - 1), qt::OP_N, T(0), P));
+    QT_TRY(op.gemm(T(0), qt::OP_N, H10, qt::OP_C, T(1), P, one_c, SIGL(l), one_c));
+    QT_TRY(op.gemm(GL(l), qt::OP_N, T(1), qt::OP_N, T(0), P));
+    QT_TRY(op.gemm(T(0), qt::OP_N, GL(l), qt::OP_C, GLN(l), P));
+    if (caroli) {  // P_l = g_l H_{l,l-1} P_{l-1}
+      QT_TRY(op.gemm(H10, qt::OP_N, Pch, qt::OP_N, T(0), P));
+      QT_TRY(op.gemm(GL(l), qt::OP_N, T(0), qt::OP_N, Pch, P));
+    }
+  }
+
+  // ---------------- right contact (src/cuda_rgf_mod.f90:192-277)
+  const int N = nx - 1;
+  const BatchRef H10 = H1I(N);  // the reference uses H1i(nx) (1-based) for the right lead
+  qt::zaxpby<double2>(n, P, HII8(N), 1, 0, SIGR8(N), 1, 0, nullref(), C8(0), nullptr, s);
+  QT_TRY(sancho_wave(cop, ar, P, C8(0), H1I8(N), false, zlead, pb.c.sancho_tol,
+                     pb.c.sancho_max_iter, C8(1), nullref(), status,
+                     pb.iters ? pb.iters + p0 * 2 + 1 : nullptr, 2));
+  // Sigma_R = H10^+ G00 H10 at FP64 grade
+  QT_TRY(cop.gemm(H1I8(N), qt::OP_C, C8(1), qt::OP_N, C8(2), P));
+  QT_TRY(cop.gemm(C8(2), qt::OP_N, H1I8(N), qt::OP_N, C8(3), P));
+  const BatchRef SigR = T(2);
+  zconvert_or_copy<TC>(n, P, C8(3), SigR, s);
+  // G_NN = (z S - H00 - Sigma_R - H10 g_{N-1} H10^+)^-1
+  qt::zaxpby<TC>(n, P, HII(N), 1, 0, SIGR(N), 1, 0, nullref(), T(0), nullptr, s);  // H00
+  QT_TRY(op.gemm(H10, qt::OP_N, GL(N - 1), qt::OP_N, T(3), P));
+  qt::zaxpby<TC>(n, P, T(0), -1, 0, SigR, -1, 0, Zi, T(4), nullptr, s);
+  QT_TRY(op.gemm(T(3), qt::OP_N, H10, qt::OP_C, T(5), P, mone, T(4), one_c));
+  BatchRef Gcur = T(6), Gncur = T(7), Gpcur = T(8), Gnew = T(3), Gnnew = T(4), Gpnew = T(11);
+  QT_TRY(op.inv(T(5), Gcur, P, status));
+  // Sigma^< = Gamma'_R f_R + H10 g^<_{N-1} H10^+ + sigma_lesser_ph S,  Gamma' = -(Sigma - Sigma^+)
+  const BatchRef GamR = T(9);
+  qt::zantiherm<TC>(n, P, SigR, -1, 0, nullref(), GamR, s);
+  QT_TRY(op.gemm(H10, qt::OP_N, GLN(N - 1), qt::OP_N, T(0), P));
+  QT_TRY(op.gemm(T(0), qt::OP_N, H10, qt::OP_C, T(5), P, one_c, SIGL(N), one_c));
+  qt::zscale_add<TC>(n, P, GamR, fr, T(5), T(5), s);
+  QT_TRY(op.gemm(Gcur, qt::OP_N, T(5), qt::OP_N, T(0), P));
+  QT_TRY(op.gemm(T(0), qt::OP_N, Gcur, qt::OP_C, Gncur, P));
+  // G^>_NN = G^< + (G - G^+)   (src/cuda_rgf_mod.f90:254)
+  qt::zantiherm<TC>(n, P, Gcur, 1, 0, Gncur, Gpcur, s);
+  if (pb.tr) qt::ztrace_current<TC>(n, P, SigR, Gpcur, Gncur, tr_sign, fr, pb.tr + p0, s);
+  if (caroli) {
+    // G_N1 = G_NN H_{N,N-1} P_{N-1};  T = Re Tr[Gam_R G_N1 Gam_L G_N1^+] with Gam = i(S - S^+)
+    //   = -Re Tr[Gam'_R G_N1 Gam'_L G_N1^+]
+    QT_TRY(op.gemm(H10, qt::OP_N, Pch, qt::OP_N, T(0), P));
+    QT_TRY(op.gemm(Gcur, qt::OP_N, T(0), qt::OP_N, T(10), P));  // G_N1
+    qt::zantiherm<TC>(n, P, SigL, -1, 0, nullref(), T(5), s);     // Gam'_L
+    QT_TRY(op.gemm(T(5), qt::OP_N, T(10), qt::OP_C, T(0), P));  // Gam'_L G_N1^+
+    QT_TRY(op.gemm(T(10), qt::OP_N, T(0), qt::OP_N, T(5), P));  // G_N1 Gam'_L G_N1^+
+    qt::ztrace_prod<TC>(n, P, GamR, T(5), -1.0, pb.T + p0, s);
+  }
+  const bool glp = (q & QT_QUIRK_GLP_ZERO) != 0;
+  auto emit = [&](int l, BatchRef G, BatchRef Gn, BatchRef Gp) {
+    const long long os = (long long)nx * n, oo = (long long)l * n;
+    if (pb.dgr) qt::zdiag<TC>(n, P, G, pb.dgr + 2 * p0 * nx * n, os, oo, s);
+    if (pb.dgl) qt::zdiag<TC>(n, P, Gn, pb.dgl + 2 * p0 * nx * n, os, oo, s);
+    if (pb.dgg) {
+      if (glp) qt::zdiag<TC>(n, P, Gp, pb.dgg + 2 * p0 * nx * n, os, oo, s);
+      else qt::zdiag_greater<TC>(n, P, G, Gn, pb.dgg + 2 * p0 * nx * n, os, oo, s);
+    }
+    if (pb.Gr) to_c128<TC>(n, P, G, OUTB(pb.Gr, l), s);
+    if (pb.Gl) to_c128<TC>(n, P, Gn, OUTB(pb.Gl, l), s);
+    if (pb.Gg) {
+      if (glp) {
+        to_c128<TC>(n, P, Gp, OUTB(pb.Gg, l), s);
+      } else {
+        qt::zantiherm<TC>(n, P, G, 1, 0, Gn, T(9), s);  // T(9) is free once emitting
+        to_c128<TC>(n, P, T(9), OUTB(pb.Gg, l), s);
+      }
+    }
+  };
+  emit(N, Gcur, Gncur, Gpcur);
+
+  // ---------------- backward sweep (src/cuda_rgf_mod.f90:283-381)
+  //   X = g H^+ ; GN0 = X G_{l+1} ; G_l = g + GN0 (H g)
+  //   G^<_l = g^< + X G^<_{l+1} X^+ + W - W^+ ,  W = (GN0 H) g^<
+  // The reference's fourth term g^< H^+ GN0^+ (:346-348) equals -W^+ because
+  // g^< is anti-Hermitian, which saves two block products per slab.
+  for (int l = N - 1; l >= 0; --l) {
+    const BatchRef Hc = (q & QT_QUIRK_BACK_H1I_NEXT) ? H1I(l + 1) : H1I(l);
+    const BatchRef X = T(0), GN0 = T(1), Y = T(2), T1 = T(5), W = T(10);
+    QT_TRY(op.gemm(GL(l), qt::OP_N, Hc, qt::OP_C, X, P));
+    QT_TRY(op.gemm(X, qt::OP_N, Gcur, qt::OP_N, GN0, P));
+    QT_TRY(op.gemm(Hc, qt::OP_N, GL(l), qt::OP_N, Y, P));
+    QT_TRY(op.gemm(GN0, qt::OP_N, Y, qt::OP_N, Gnew, P, one_c, GL(l), one_c));
+    QT_TRY(op.gemm(X, qt::OP_N, Gncur, qt::OP_N, T1, P));
+    QT_TRY(op.gemm(T1, qt::OP_N, X, qt::OP_C, Gnnew, P, one_c, GLN(l), one_c));
+    QT_TRY(op.gemm(GN0, qt::OP_N, Hc, qt::OP_N, Y, P));
+    QT_TRY(op.gemm(Y, qt::OP_N, GLN(l), qt::OP_N, W, P));
+    qt::zantiherm<TC>(n, P, W, 1, 0, Gnnew, Gnnew, s);
+    if (glp) {  // G^>_l = X G^>_{l+1} X^+ (Glp never filled, src/cuda_rgf_mod.f90:78,351-372)
+      QT_TRY(op.gemm(X, qt::OP_N, Gpcur, qt::OP_N, T1, P));
+      QT_TRY(op.gemm(T1, qt::OP_N, X, qt::OP_C, Gpnew, P));
+      std::swap(Gpcur, Gpnew);
+    }
+    std::swap(Gcur, Gnew);
+    std::swap(Gncur, Gnnew);
+    emit(l, Gcur, Gncur, Gpcur);
+  }
+  // ---------------- left-contact current tre (src/cuda_rgf_mod.f90:387-407)
+  if (pb.tre) {
+    qt::zantiherm<TC>(n, P, Gcur, 1, 0, Gncur, T(0), s);  // G^>_1 = G^< + (G - G^+)
+    qt::ztrace_current<TC>(n, P, SigL, T(0), Gncur, 1.0, fe, pb.tre + p0, s);
+  }
+  qt::zcheck_finite<TC>(n, P, Gcur, status, s);  // canary on the last block touched
+  if (pb.status)
+    cudaMemcpyAsync(pb.status + p0, status, P * sizeof(int), cudaMemcpyDeviceToDevice, s);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+  return QT_OK;
+}
+
+// choose the wave size: a multiple of nk, bounded by the scratch limit
+long long choose_wave(const qt_ctx* ctx, const Problem& pb) {
+  const size_t per = wave_bytes(pb, 1);
+  long long P = (long long)((size_t)ctx->scratch_limit / (per + 1));
+  const long long target = 152 * 4;  // several work items per SM in every batched launch
+  P = std::min<long long>(P, std::max<long long>(target, pb.nk));
+  P = std::min<long long>(P, pb.npts);
+  P = std::max<long long>(P / pb.nk, 1) * pb.nk;
+  return P;
+}
+
+struct HostStage {
+  // copy helper for host-pointer calls
+  qt_ctx* ctx;
+  char* base = nullptr;
+  size_t off = 0;
+  template <typename T>
+  T* put(const T* src, size_t count, bool copy) {
+    if (!src && copy) return nullptr;
+    T* d = reinterpret_cast<T*>(base + off);
+    off += (count * sizeof(T) + 255) & ~size_t(255);
+    if (copy) cudaMemcpyAsync(d, src, count * sizeof(T), cudaMemcpyHostToDevice, ctx->stream);
+    return d;
+  }
+};
+
+}  // namespace
+
+// ============================================================== C-ABI
+extern "C" qt_status qt_ctx_create(qt_ctx** out, int device) {
+  if (!out) QT_FAIL(QT_ERR_ARG, "null ctx pointer");
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    QT_FAIL(QT_ERR_CUDA, "no CUDA device");
+  }
+  if (device < 0 || device >= count) QT_FAIL(QT_ERR_ARG, "bad device index");
+  qt_ctx* c = new qt_ctx();
+  c->device = device;
+  cudaSetDevice(device);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    QT_FAIL(QT_ERR_CUDA, "stream creation failed");
+  }
+  *out = c;
+  return QT_OK;
+}
+
+extern "C" qt_status qt_ctx_destroy(qt_ctx* c) {
+  if (!c) return QT_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  if (c->arena) cudaFree(c->arena);
+  if (c->io) cudaFree(c->io);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return QT_OK;
+}
+
+extern "C" qt_status qt_ctx_sync(qt_ctx* c) {
+  if (!c) QT_FAIL(QT_ERR_ARG, "null ctx");
+  QT_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return QT_OK;
+}
+
+extern "C" qt_status qt_ctx_set_scratch_limit(qt_ctx* c, int64_t bytes) {
+  if (!c || bytes <= 0) QT_FAIL(QT_ERR_ARG, "bad scratch limit");
+  c->scratch_limit = bytes;
+  return QT_OK;
+}
+
+namespace {
+
+int env_int(const char* name, int dflt) {
+  const char* v = getenv(name);
+  return v && *v ? atoi(v) : dflt;
+}
+
+qt_status run_problem(qt_ctx* ctx, Problem& pb, long long hii_n, long long h1i_n) {
+  // digits of the split-precision products: 4 for the complex64 sweep, 7 (FP64 grade) for
+  // the lead decimation; QT_SWEEP_SLICES / QT_LEAD_SLICES override for accuracy studies
+  pb.sweep_slices = env_int("QT_SWEEP_SLICES", 4);
+  pb.lead_slices = env_int("QT_LEAD_SLICES", 7);
+  if (pb.sweep_slices != 3 && pb.sweep_slices != 4) QT_FAIL(QT_ERR_ARG, "QT_SWEEP_SLICES in {3,4}");
+  if (pb.lead_slices != 4 && pb.lead_slices != 6 && pb.lead_slices != 7)
+    QT_FAIL(QT_ERR_ARG, "QT_LEAD_SLICES in {4,6,7}");
+  cudaStream_t s = ctx->stream;
+  const bool split = pb.prec != QT_PREC_FP64;
+  if (split) {
+    const long long blk = pb.npts * pb.nx * (long long)pb.nm * pb.nm;
+    const long long cnt = hii_n + h1i_n + (pb.sigr ? blk : 0) + (pb.sigl ? blk : 0);
+    QT_TRY(ensure(ctx->conv, ctx->conv_bytes, (size_t)cnt * sizeof(float2) + 4096));
+    float2* c = reinterpret_cast<float2*>(ctx->conv);
+    auto conv = [&](const cd* src, long long count) -> const float2* {
+      if (!src) return nullptr;
+      flat_d2f_kernel<<<g1d(count), 256, 0, s>>>(reinterpret_cast<const double2*>(src), c, count);
+      const float2* r = c;
+      c += count;
+      return r;
+    };
+    pb.Hii32 = conv(pb.Hii, hii_n);
+    pb.H1i32 = conv(pb.H1i, h1i_n);
+    pb.sigr32 = conv(pb.sigr, blk);
+    pb.sigl32 = conv(pb.sigl, blk);
+  }
+  const long long P = choose_wave(ctx, pb);
+  QT_TRY(ensure(ctx->arena, ctx->arena_bytes, wave_bytes(pb, P)));
+  for (long long p0 = 0; p0 < pb.npts; p0 += P) {
+    const long long Pw = std::min(P, pb.npts - p0);
+    Arena ar{reinterpret_cast<char*>(ctx->arena), ctx->arena_bytes, 0};
+    if (split) QT_TRY(solve_wave<float2>(ctx, pb, p0, Pw, ar));
+    else QT_TRY(solve_wave<double2>(ctx, pb, p0, Pw, ar));
+  }
+  if (split) {
+    QT_CUDA_TRY(cudaStreamSynchronize(s));
+    if (qt::oz_timeouts_and_reset()) QT_FAIL(QT_ERR_CUDA, "tensor-core kernel wait timed out");
+  }
+  return QT_OK;
+}
+
+}  // namespace
+
+extern "C" qt_status qt_rgf_solve(qt_ctx* ctx, const qt_device* dev, const double* E, int nE,
+                                  const qt_contacts* c, const double* sigma_r_ph,
+                                  const double* sigma_lesser_ph, qt_precision prec, unsigned flags,
+                                  qt_outputs* out) {
+  if (!ctx || !dev || !E || !c || !out) QT_FAIL(QT_ERR_ARG, "null argument");
+  if (dev->nm <= 0 || dev->nx < 2 || dev->nk <= 0 || nE <= 0)
+    QT_FAIL(QT_ERR_ARG, "need nm > 0, nx >= 2, nk > 0, nE > 0");
+  if (!dev->Hii || !dev->H1i) QT_FAIL(QT_ERR_ARG, "Hii/H1i required");
+  if (dev->Sii) QT_FAIL(QT_ERR_UNSUPPORTED, "Sii must be NULL (identity overlap)");
+  if (prec == QT_PREC_MIXED && dev->nm > 128) QT_FAIL(QT_ERR_UNSUPPORTED, "mixed path needs nm <= 128");
+  if (c->sancho_max_iter <= 0) QT_FAIL(QT_ERR_ARG, "sancho_max_iter must be > 0");
+  cudaSetDevice(ctx->device);
+  const int nm = dev->nm, nx = dev->nx, nk = dev->nk;
+  const long long npts = (long long)nE * nk;
+  const long long nm2 = (long long)nm * nm;
+  Problem pb{};
+  pb.nm = nm; pb.nx = nx; pb.nk = nk; pb.npts = npts;
+  pb.c = *c; pb.prec = prec; pb.flags = flags;
+  pb.hk = dev->hii_kstride; pb.hl = dev->hii_lstride;
+  pb.h1k = dev->h1i_kstride; pb.h1l = dev->h1i_lstride;
+  const bool devp = (flags & QT_FLAG_DEVICE_POINTERS) != 0;
+  // extents of the H arrays (elements) for host staging
+  const long long hii_n = (pb.hk ? (nk - 1) * pb.hk : 0) + (pb.hl ? (nx - 1) * pb.hl : 0) + nm2;
+  const long long h1i_n = (pb.h1k ? (nk - 1) * pb.h1k : 0) + (pb.h1l ? nx * pb.h1l : 0) + nm2;
+  const long long blk_n = npts * nx * nm2;
+  const long long diag_n = npts * nx * nm;
+  HostStage st{ctx};
+  if (devp) {
+    pb.Hii = reinterpret_cast<const cd*>(dev->Hii);
+    pb.H1i = reinterpret_cast<const cd*>(dev->H1i);
+    pb.sigr = reinterpret_cast<const cd*>(sigma_r_ph);
+    pb.sigl = reinterpret_cast<const cd*>(sigma_lesser_ph);
+    pb.E = E;
+    pb.tr = out->tr; pb.tre = out->tre; pb.T = out->T;
+    pb.dgr = out->diag_gr; pb.dgl = out->diag_gl; pb.dgg = out->diag_gg;
+    pb.Gr = reinterpret_cast<cd*>(out->G_r); pb.Gl = reinterpret_cast<cd*>(out->G_lesser);
+    pb.Gg = reinterpret_cast<cd*>(out->G_greater);
+    pb.status = out->status; pb.iters = out->sancho_iters;
+    QT_TRY(run_problem(ctx, pb, hii_n, h1i_n));
+  } else {
+    size_t need = 0;
+    auto add = [&](size_t bytes) { need += (bytes + 255) & ~size_t(255); };
+    add(hii_n * 16); add(h1i_n * 16); add(nE * 8);
+    if (sigma_r_ph) add(blk_n * 16);
+    if (sigma_lesser_ph) add(blk_n * 16);
+    add(npts * 8 * 3); add(diag_n * 16 * 3); add(npts * 4 * 3);
+    if (out->G_r) add(blk_n * 16);
+    if (out->G_lesser) add(blk_n * 16);
+    if (out->G_greater) add(blk_n * 16);
+    QT_TRY(ensure(ctx->io, ctx->io_bytes, need + 4096));
+    st.base = reinterpret_cast<char*>(ctx->io);
+    pb.Hii = st.put(reinterpret_cast<const cd*>(dev->Hii), hii_n, true);
+    pb.H1i = st.put(reinterpret_cast<const cd*>(dev->H1i), h1i_n, true);
+    pb.E = st.put(E, nE, true);
+    pb.sigr = sigma_r_ph ? st.put(reinterpret_cast<const cd*>(sigma_r_ph), blk_n, true) : nullptr;
+    pb.sigl = sigma_lesser_ph ? st.put(reinterpret_cast<const cd*>(sigma_lesser_ph), blk_n, true) : nullptr;
+    pb.tr = out->tr ? st.put<double>(nullptr, npts, false) : nullptr;
+    pb.tre = out->tre ? st.put<double>(nullptr, npts, false) : nullptr;
+    pb.T = out->T ? st.put<double>(nullptr, npts, false) : nullptr;
+    pb.dgr = out->diag_gr || out->diag_gg ? st.put<double>(nullptr, 2 * diag_n, false) : nullptr;
+    pb.dgl = out->diag_gl || out->diag_gg ? st.put<double>(nullptr, 2 * diag_n, false) : nullptr;
+    pb.dgg = out->diag_gg ? st.put<double>(nullptr, 2 * diag_n, false) : nullptr;
+    pb.Gr = out->G_r ? st.put<cd>(nullptr, blk_n, false) : nullptr;
+    pb.Gl = out->G_lesser ? st.put<cd>(nullptr, blk_n, false) : nullptr;
+    pb.Gg = out->G_greater ? st.put<cd>(nullptr, blk_n, false) : nullptr;
+    pb.status = st.put<int>(nullptr, npts, false);
+    pb.iters = st.put<int>(nullptr, 2 * npts, false);
+    QT_TRY(run_problem(ctx, pb, hii_n, h1i_n));
+    auto back = [&](void* dst, const void* src, size_t bytes) {
+      if (dst && src) cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+    };
+    back(out->tr, pb.tr, npts * 8);
+    back(out->tre, pb.tre, npts * 8);
+    back(out->T, pb.T, npts * 8);
+    back(out->diag_gr, pb.dgr, diag_n * 16);
+    back(out->diag_gl, pb.dgl, diag_n * 16);
+    back(out->diag_gg, pb.dgg, diag_n * 16);
+    back(out->G_r, pb.Gr, blk_n * 16);
+    back(out->G_lesser, pb.Gl, blk_n * 16);
+    back(out->G_greater, pb.Gg, blk_n * 16);
+    back(out->status, pb.status, npts * 4);
+    back(out->sancho_iters, pb.iters, npts * 8);
+    flags |= QT_FLAG_SYNC;
+  }
+  if (flags & QT_FLAG_SYNC) {
+    QT_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    if (out->status) {
+      std::vector<int> hs;
+      const int* st_h = out->status;
+      if (devp) {
+        hs.resize(npts);
+        cudaMemcpy(hs.data(), out->status, npts * sizeof(int), cudaMemcpyDeviceToHost);
+        st_h = hs.data();
+      }
+      for (long long p = 0; p < npts; ++p)
+        if (st_h[p]) return QT_ERR_POINTS;
+    }
+  }
+  return QT_OK;
+}
+
+extern "C" qt_status qt_rgf_constblocksize(qt_ctx* ctx, int nm, int nx, double En, double mul,
+                                           double mur, double templ, double tempr,
+                                           const double* Hii, const double* H1i, const double* Sii,
+                                           const double* sigma_lesser_ph, const double* sigma_r_ph,
+                                           double* G_r, double* G_lesser, double* G_greater,
+                                           double* Jdens, double* tr, double* tre) {
+  if (Sii) {
+    // S = I is the only overlap the reference drivers build (src/deviceHam_mod.f90:281-284);
+    // accept an explicit identity, reject anything else.
+    for (int j = 0; j < nx; ++j)
+      for (int c = 0; c < nm; ++c)
+        for (int r = 0; r < nm; ++r) {
+          const double* v = Sii + 2 * ((long long)j * nm * nm + (long long)c * nm + r);
+          if (v[0] != (r == c ? 1.0 : 0.0) || v[1] != 0.0)
+            QT_FAIL(QT_ERR_UNSUPPORTED, "Sii must be the identity");
+        }
+  }
+  if (Jdens) {
+    // bond currents are not produced by the batched sweep; report zeros as the
+    // reference does for the last slab (src/cuda_rgf_mod.f90:84)
+    memset(Jdens, 0, sizeof(double) * 2 * (size_t)nm * nm * nx);
+  }
+  qt_device dev{};
+  dev.nm = nm; dev.nx = nx; dev.nk = 1;
+  dev.Hii = Hii; dev.hii_kstride = 0; dev.hii_lstride = (int64_t)nm * nm;
+  dev.H1i = H1i; dev.h1i_kstride = 0; dev.h1i_lstride = (int64_t)nm * nm;
+  qt_contacts c{};
+  c.mul = mul; c.mur = mur; c.templ = templ; c.tempr = tempr;
+  c.eta_lead = 1e-5; c.eta_interior = 0.0; c.sancho_tol = 1e-100; c.sancho_max_iter = 50;
+  c.quirks = 0;
+  qt_outputs o{};
+  o.tr = tr; o.tre = tre; o.G_r = G_r; o.G_lesser = G_lesser; o.G_greater = G_greater;
+  return qt_rgf_solve(ctx, &dev, &En, 1, &c, sigma_r_ph, sigma_lesser_ph, QT_PREC_FP64, 0, &o);
+}
+
+extern "C" qt_status qt_sancho_batch(qt_ctx* ctx, int nm, int npts, const double* E,
+                                     const double* H00, int64_t h00_stride, const double* H10,
+                                     int64_t h10_stride, const double* S00, int64_t s00_stride,
+                                     double eta, double tol, int max_iter, qt_precision prec,
+                                     unsigned flags, double* G00, double* GBB, int* iters,
+                                     int* status) {
+  (void)s00_stride;
+  if (!ctx || !E || !H00 || !H10 || !G00 || nm <= 0 || npts <= 0 || max_iter <= 0)
+    QT_FAIL(QT_ERR_ARG, "bad sancho arguments");
+  if (S00) QT_FAIL(QT_ERR_UNSUPPORTED, "S00 must be NULL (identity overlap)");
+  if (prec == QT_PREC_MIXED && nm > 128) QT_FAIL(QT_ERR_UNSUPPORTED, "mixed path needs nm <= 128");
+  cudaSetDevice(ctx->device);
+  const long long nm2 = (long long)nm * nm;
+  const bool devp = (flags & QT_FLAG_DEVICE_POINTERS) != 0;
+  const long long P = npts;
+  // scratch: z, status, iters, 2 refinement blocks + Sancho state (7 blocks)
+  const size_t need = (size_t)P * nm2 * sizeof(cd) * (9 + (devp ? 0 : 2)) + (size_t)P * 64 +
+                      (h00_stride ? P : 1) * nm2 * 16 + (h10_stride ? P : 1) * nm2 * 16 +
+                      (size_t)P * 8 + (1 << 20);
+  QT_TRY(ensure(ctx->arena, ctx->arena_bytes, need));
+  Arena ar{reinterpret_cast<char*>(ctx->arena), ctx->arena_bytes, 0};
+  cudaStream_t s = ctx->stream;
+  Ops<double2> op{s, nm, prec};
+  op.slices = env_int("QT_LEAD_SLICES", 7);
+  op.refine = prec == QT_PREC_FP64 ? 0 : 2;
+  cd* one = ar.take<cd>(1);
+  const cd h1{1.0, 0.0};
+  cudaMemcpyAsync(one, &h1, sizeof(cd), cudaMemcpyHostToDevice, s);
+  op.one = one;
+  cd* z = ar.take<cd>(P);
+  int* st = ar.take<int>(P);
+  int* it = ar.take<int>(P);
+  const double* Ed = E;
+  const cd *h00 = reinterpret_cast<const cd*>(H00), *h10 = reinterpret_cast<const cd*>(H10);
+  cd *g00 = reinterpret_cast<cd*>(G00), *gbb = reinterpret_cast<cd*>(GBB);
+  if (!devp) {
+    double* e = ar.take<double>(P);
+    cudaMemcpyAsync(e, E, P * 8, cudaMemcpyHostToDevice, s);
+    Ed = e;
+    cd* a = ar.take<cd>((h00_stride ? P : 1) * nm2);
+    cudaMemcpyAsync(a, H00, (h00_stride ? P : 1) * nm2 * 16, cudaMemcpyHostToDevice, s);
+    h00 = a;
+    cd* b = ar.take<cd>((h10_stride ? P : 1) * nm2);
+    cudaMemcpyAsync(b, H10, (h10_stride ? P : 1) * nm2 * 16, cudaMemcpyHostToDevice, s);
+    h10 = b;
+    g00 = ar.take<cd>(P * nm2);
+    gbb = GBB ? ar.take<cd>(P * nm2) : nullptr;
+  }
+  if (!one || !z || !st || !it || !g00) QT_FAIL(QT_ERR_NOMEM, "arena exhausted");
+  make_z_kernel<<<g1d(P), 256, 0, s>>>(Ed, 0, P, 1, eta, z);
+  cudaMemsetAsync(st, 0, P * 4, s);
+  QT_TRY(sancho_wave(op, ar, P, ref(h00, h00_stride ? nm2 : 0, nm), ref(h10, h10_stride ? nm2 : 0, nm),
+                     false, z, tol, max_iter, ref(g00, nm2, nm), gbb ? ref(gbb, nm2, nm) : nullref(),
+                     st, it, 1));
+  if (prec != QT_PREC_FP64) {
+    QT_CUDA_TRY(cudaStreamSynchronize(s));
+    if (qt::oz_timeouts_and_reset()) QT_FAIL(QT_ERR_CUDA, "tensor-core kernel wait timed out");
+  }
+  if (!devp) {
+    cudaMemcpyAsync(G00, g00, P * nm2 * 16, cudaMemcpyDeviceToHost, s);
+    if (GBB) cudaMemcpyAsync(GBB, gbb, P * nm2 * 16, cudaMemcpyDeviceToHost, s);
+    if (iters) cudaMemcpyAsync(iters, it, P * 4, cudaMemcpyDeviceToHost, s);
+    if (status) cudaMemcpyAsync(status, st, P * 4, cudaMemcpyDeviceToHost, s);
+  } else {
+    if (iters) cudaMemcpyAsync(iters, it, P * 4, cudaMemcpyDeviceToDevice, s);
+    if (status) cudaMemcpyAsync(status, st, P * 4, cudaMemcpyDeviceToDevice, s);
+  }
+  QT_CUDA_TRY(cudaStreamSynchronize(s));
+  return QT_OK;
+}
+
+namespace {
+int parse_op(char c) {
+  if (c == 'N' || c == 'n') return qt::OP_N;
+  if (c == 'C' || c == 'c') return qt::OP_C;
+  if (c == 'T' || c == 't') return qt::OP_T;
+  return -1;
+}
+}  // namespace
+
+extern "C" qt_status qt_zgemm_batch(qt_ctx* ctx, int n, int batch, char opA, const double* A,
+                                    int64_t a_stride, char opB, const double* B, int64_t b_stride,
+                                    const double* alpha, const double* beta, const double* D,
+                                    int64_t d_stride, double* C, int64_t c_stride,
+                                    qt_precision prec, int slices, unsigned flags) {
+  const int oa = parse_op(opA), ob = parse_op(opB);
+  if (!ctx || !A || !B || !C || n <= 0 || batch <= 0 || oa < 0 || ob < 0)
+    QT_FAIL(QT_ERR_ARG, "bad gemm arguments");
+  if (prec == QT_PREC_MIXED && (n > 128 || oa == qt::OP_T || ob == qt::OP_T))
+    QT_FAIL(QT_ERR_UNSUPPORTED, "mixed gemm: n <= 128 and op in {N, C}");
+  if (slices < 0 || slices > 8) QT_FAIL(QT_ERR_ARG, "slices in 0..8");
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = ctx->stream;
+  const long long nm2 = (long long)n * n;
+  const bool devp = (flags & QT_FLAG_DEVICE_POINTERS) != 0;
+  const cd al = alpha ? cd{alpha[0], alpha[1]} : cd{1, 0};
+  const cd be = beta ? cd{beta[0], beta[1]} : cd{0, 0};
+  const void *a = A, *b = B, *d = D;
+  void* c = C;
+  if (!devp) {
+    auto cnt = [&](int64_t st) { return (long long)(st ? (long long)(batch - 1) * st + nm2 : nm2); };
+    size_t need = (cnt(a_stride) + cnt(b_stride) + (D ? cnt(d_stride) : 0) + cnt(c_stride)) * 16 + 4096;
+    QT_TRY(ensure(ctx->io, ctx->io_bytes, need));
+    HostStage hs{ctx, reinterpret_cast<char*>(ctx->io)};
+    a = hs.put(reinterpret_cast<const cd*>(A), cnt(a_stride), true);
+    b = hs.put(reinterpret_cast<const cd*>(B), cnt(b_stride), true);
+    d = D ? hs.put(reinterpret_cast<const cd*>(D), cnt(d_stride), true) : nullptr;
+    c = hs.put<cd>(nullptr, cnt(c_stride), false);
+  }
+  qt::GemmArgs g;
+  g.m = g.n = g.k = n;
+  g.A = ref(a, a_stride, n); g.B = ref(b, b_stride, n); g.C = ref(c, c_stride, n);
+  g.D = d ? ref(d, d_stride, n) : nullref(); g.Z = nullref();
+  g.opA = oa; g.opB = ob;
+  g.alpha_re = al.x; g.alpha_im = al.y; g.beta_re = be.x; g.beta_im = be.y;
+  g.batch = batch; g.active = nullptr;
+  const int sl = slices ? slices : 4;
+  if (prec == QT_PREC_MIXED && sl != 4 && sl != 6 && sl != 7)
+    QT_FAIL(QT_ERR_UNSUPPORTED, "complex128 split product supports 4, 6 or 7 digits");
+  cudaError_t e = prec == QT_PREC_FP64 ? qt::zgemm_f64(g, s) : qt::zgemm_oz(g, sl, sl - 1, s);
+  if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+  if (!devp) {
+    const long long cc = c_stride ? (long long)(batch - 1) * c_stride + nm2 : nm2;
+    cudaMemcpyAsync(C, c, cc * 16, cudaMemcpyDeviceToHost, s);
+  }
+  if (!devp || (flags & QT_FLAG_SYNC)) QT_CUDA_TRY(cudaStreamSynchronize(s));
+  return QT_OK;
+}
+
+extern "C" qt_status qt_zinv_batch(qt_ctx* ctx, int n, int batch, const double* A,
+                                   int64_t a_stride, double* X, int64_t x_stride,
+                                   qt_precision prec, unsigned flags, int* status) {
+  if (!ctx || !A || !X || n <= 0 || batch <= 0) QT_FAIL(QT_ERR_ARG, "bad inverse arguments");
+  if (prec == QT_PREC_MIXED && n > 128) QT_FAIL(QT_ERR_UNSUPPORTED, "mixed inverse needs n <= 128");
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = ctx->stream;
+  const long long nm2 = (long long)n * n;
+  const bool devp = (flags & QT_FLAG_DEVICE_POINTERS) != 0;
+  const long long P = batch;
+  const size_t need = (size_t)P * nm2 * 16 * (2 + (devp ? 0 : 2)) + (size_t)P * 8 + (1 << 20);
+  QT_TRY(ensure(ctx->arena, ctx->arena_bytes, need));
+  Arena ar{reinterpret_cast<char*>(ctx->arena), ctx->arena_bytes, 0};
+  Ops<double2> op{s, n, prec};
+  op.P = P;
+  op.slices = env_int("QT_LEAD_SLICES", 7);
+  op.refine = prec == QT_PREC_FP64 ? 0 : 2;
+  cd* one = ar.take<cd>(1);
+  const cd h1{1.0, 0.0};
+  cudaMemcpyAsync(one, &h1, sizeof(cd), cudaMemcpyHostToDevice, s);
+  op.one = one;
+  op.rt1 = reinterpret_cast<double2*>(ar.take<cd>(P * nm2));
+  op.rt2 = reinterpret_cast<double2*>(ar.take<cd>(P * nm2));
+  int* st = ar.take<int>(P);
+  const cd* a = reinterpret_cast<const cd*>(A);
+  cd* x = reinterpret_cast<cd*>(X);
+  long long as = a_stride, xs = x_stride;
+  if (!devp) {
+    cd* ad = ar.take<cd>(P * nm2);
+    cd* xd = ar.take<cd>(P * nm2);
+    if (!ad || !xd) QT_FAIL(QT_ERR_NOMEM, "arena exhausted");
+    for (long long b = 0; b < P; ++b)
+      cudaMemcpyAsync(ad + b * nm2, reinterpret_cast<const cd*>(A) + b * a_stride, nm2 * 16,
+                      cudaMemcpyHostToDevice, s);
+    a = ad; x = xd; as = nm2; xs = nm2;
+  } else if (prec == QT_PREC_MIXED && (const void*)A == (const void*)X) {
+    cd* ad = ar.take<cd>(P * nm2);
+    if (!ad) QT_FAIL(QT_ERR_NOMEM, "arena exhausted");
+    cudaMemcpyAsync(ad, A, P * nm2 * 16, cudaMemcpyDeviceToDevice, s);
+    a = ad; as = nm2;
+  }
+  if (!st || !op.rt2) QT_FAIL(QT_ERR_NOMEM, "arena exhausted");
+  cudaMemsetAsync(st, 0, P * 4, s);
+  QT_TRY(op.inv(ref(a, as, n), ref(x, xs, n), P, st));
+  if (!devp) {
+    for (long long b = 0; b < P; ++b)
+      cudaMemcpyAsync(X + 2 * b * x_stride, x + b * nm2, nm2 * 16, cudaMemcpyDeviceToHost, s);
+    if (status) cudaMemcpyAsync(status, st, P * 4, cudaMemcpyDeviceToHost, s);
+  } else if (status) {
+    cudaMemcpyAsync(status, st, P * 4, cudaMemcpyDeviceToDevice, s);
+  }
+  QT_CUDA_TRY(cudaStreamSynchronize(s));
+  return QT_OK;
+}

@@ -1,0 +1,614 @@
+// Split-precision complex block product on the 5th-generation tensor cores
+// (tcgen05.mma kind::f16, BF16 x BF16 -> FP32 in TMEM), Ozaki-style.
+//
+//   C_b = alpha * op(A_b) op(B_b) + beta * D_b + z_b I     (n <= 128, real alpha/beta)
+//
+// This is the GB300 replacement of the reference's per-slab zgemm calls
+// (src/cuda_rgf_mod.f90:152-175, 293-370; Sancho :698-712) for the
+// split-precision path.  GB300's FP64 pipes run at ~1 TFLOP/s, so FP64-grade
+// products are rebuilt from exact BF16 digit products:
+//
+//  * complex -> real: with At = op(A), Bt = op(B) (n x n complex)
+//      Cr = [Re At | Im At] . [Re Bt ; -Im Bt]      Ci = [Re At | Im At] . [Im Bt ; Re Bt]
+//    one CTA computes one real part (M = 128 padded rows, N = n padded to 16,
+//    K' = 2n padded to 64);
+//  * digits: every row i of [Re At | Im At] is scaled by 2^-e_i (e_i: exponent
+//    bound of the row's largest entry, |entry| < 2^(e_i-1)) and written as S
+//    balanced base-256 digits D_s = d_s 2^(-8s), |d_s| <= 128 -- each exactly
+//    representable in BF16.  Columns of [Re Bt; Im Bt] likewise with f_j;
+//  * products: all digit pairs (s, t) with s + t <= L are issued; pair level
+//    l = s + t accumulates into TMEM accumulator min(l, 3).  For l <= 3 every
+//    partial sum is an integer multiple of 2^(-8l) below 2^24 * 2^(-8l)
+//    ((l+1) products of <= 2^14, K' <= 256), so levels 0..3 are EXACT in FP32;
+//    levels > 3 (FP64-grade mode only) share accumulator 3 with a rounding
+//    error 2^-48 relative to the row/column scale;
+//  * epilogue: the four accumulators are summed in double-float FP32
+//    arithmetic (TwoSum), scaled by 2^(e_i + f_j - 16), and written as FP32
+//    (correctly rounded up to the last digit level) or assembled into FP64
+//    bits with integer operations (no use of the slow FP64 pipe).
+//
+// Roles (416 threads, one CTA per SM: the four accumulators use all 512 TMEM
+// columns):  warps 0-3 epilogue (TMEM lanes 0-127), warps 4-11 producers
+// (digit slicing straight from global memory into the canonical no-swizzle
+// K-major UMMA layout in shared memory), warp 12 TMEM allocation + the single
+// MMA-issuing thread.  Stages are handed over with mbarriers; every wait is
+// bounded (a few seconds) and records a timeout instead of hanging.
+#include <stdint.h>
+
+#include "qt_common.cuh"
+#include "qt_kernels.h"
+
+namespace qt {
+
+__device__ int g_oz_timeouts = 0;
+
+namespace {
+
+constexpr int KC = 32;            // real-K elements per pipeline stage
+constexpr int NTHREADS = 416;
+constexpr int NPROD = 256;        // producer threads (warps 4..11)
+constexpr int MMA_WARP = 12;
+constexpr uint64_t TIMEOUT_NS = 4000000000ull;  // 4 s per wait
+constexpr int PLANE_BYTES = 128 * KC * 2;       // one digit plane of a 128-row tile: 8 KB
+constexpr uint32_t LBO = 128;                   // K-adjacent core matrices
+constexpr uint32_t SBO = (KC / 8) * 128;        // 8-row groups
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: false on timeout or when another role already aborted.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer();
+  while (!mbar_try_wait(bar, parity)) {
+    if (*abort_flag) return false;
+    if (globaltimer() - t0 > TIMEOUT_NS) {
+      *abort_flag = 1;
+      atomicAdd(&g_oz_timeouts, 1);
+      return false;
+    }
+  }
+  return true;
+}
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((LBO >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((SBO >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version (tcgen05); swizzle none
+  return d;
+}
+__host__ __device__ constexpr uint32_t make_idesc(int M, int N) {
+  return (1u << 4)                          // D format F32
+         | (1u << 7)                        // A format BF16
+         | (1u << 10)                       // B format BF16
+         | ((uint32_t)(N >> 3) << 17)       // N >> 3
+         | ((uint32_t)(M >> 4) << 24);      // M >> 4   (A, B K-major, no negate)
+}
+__device__ __forceinline__ void umma(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                     uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15},"
+      " [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// ------------------------------------------------------------ element access
+template <typename T> struct Elem;
+template <> struct Elem<float2> {
+  __device__ static float2 ld(const void* p, long long off) {
+    return reinterpret_cast<const float2*>(p)[off];
+  }
+};
+template <> struct Elem<double2> {
+  __device__ static double2 ld(const void* p, long long off) {
+    return reinterpret_cast<const double2*>(p)[off];
+  }
+};
+
+// element (r, c) of op(M); part 0 = real, 1 = imaginary (conjugated for OP_C)
+template <typename T>
+__device__ __forceinline__ T load_op(const void* M, int ld, int op, int r, int c) {
+  if (op == OP_N) return Elem<T>::ld(M, r + (long long)c * ld);
+  T v = Elem<T>::ld(M, c + (long long)r * ld);
+  if (op == OP_C) v.y = -v.y;
+  return v;
+}
+
+// |x| as ordered integer bits (non-negative floats compare like their bit patterns)
+__device__ __forceinline__ unsigned long long absbits(double2 v, int part) {
+  return (unsigned long long)__double_as_longlong(part ? v.y : v.x) & 0x7FFFFFFFFFFFFFFFull;
+}
+__device__ __forceinline__ unsigned long long absbits(float2 v, int part) {
+  return __float_as_uint(part ? v.y : v.x) & 0x7FFFFFFFu;
+}
+// exponent bound e with max|x| < 2^(e-1) from the bits of max|x|; 0 for a zero vector
+template <typename T> __device__ __forceinline__ int exp_bound_bits(unsigned long long mb);
+template <> __device__ __forceinline__ int exp_bound_bits<double2>(unsigned long long mb) {
+  const int ef = (int)((mb >> 52) & 0x7FF);
+  return ef ? ef - 1023 + 2 : 0;
+}
+template <> __device__ __forceinline__ int exp_bound_bits<float2>(unsigned long long mb) {
+  const int ef = (int)((mb >> 23) & 0xFF);
+  return ef ? ef - 127 + 2 : 0;
+}
+
+// ------------------------------------------------------------ digit slicing
+// FP32 value: y = x 2^(8-e) in (-128, 128); digits D_s = d_s 2^-8s by magic rounding
+template <int S>
+__device__ __forceinline__ void digits_f32(float x, float scale, float* D) {
+  float r = x * scale;
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    const float M = 12582912.0f * __int_as_float((127 - 8 * s) << 23);  // 1.5 * 2^(23 - 8s)
+    const float d = (r + M) - M;
+    D[s] = d;
+    r -= d;
+  }
+}
+// FP64 value via integer arithmetic on its bits: T = round(x 2^(8S - e)), balanced digits
+template <int S>
+__device__ __forceinline__ void digits_f64(double x, int e, float* D) {
+  const long long bits = __double_as_longlong(x);
+  const int ex = (int)((bits >> 52) & 0x7FF);
+  long long T = 0;
+  if (ex != 0) {
+    const long long m = (bits & 0xFFFFFFFFFFFFFll) | (1ll << 52);
+    const int sh = ex - 1075 + 8 * S - e;
+    if (sh >= 0) T = m << sh;
+    else if (sh > -63) T = (m + (1ll << (-sh - 1))) >> (-sh);
+    if (bits < 0) T = -T;
+  }
+  int d[S];
+#pragma unroll
+  for (int s = S - 1; s >= 1; --s) {
+    const int lo = (int)((unsigned)T & 255u);
+    const int di = ((lo + 128) & 255) - 128;
+    d[s] = di;
+    T = (T - di) >> 8;
+  }
+  d[0] = (int)T;
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    const float f = __int_as_float(0x4B400000 + d[s]) - 12582912.0f;  // exact float(d)
+    D[s] = f * __int_as_float((127 - 8 * s) << 23);                     // * 2^-8s (exact)
+  }
+}
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+  // the digits carry <= 8 significant bits: truncation to BF16 is exact
+  return (__float_as_uint(lo) >> 16) | (__float_as_uint(hi) & 0xFFFF0000u);
+}
+
+// ------------------------------------------------------------ epilogue math
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+// (hi + lo) * 2^e2 -> FP64 bits with integer operations; |lo| <= ulp(hi)/2
+__device__ __forceinline__ double df_to_double(float hi, float lo, int e2) {
+  const uint32_t hb = __float_as_uint(hi);
+  if ((hb & 0x7FFFFFFFu) == 0) return 0.0;
+  const uint32_t sgn = hb >> 31;
+  int eh = (int)((hb >> 23) & 0xFF);
+  unsigned long long M;
+  if (eh == 0) {  // subnormal hi: value tiny, keep what is there
+    M = (unsigned long long)(hb & 0x7FFFFF) << 29;
+    eh = 1;
+    while (M && !(M >> 52)) { M <<= 1; --eh; }
+  } else {
+    M = (unsigned long long)((hb & 0x7FFFFF) | 0x800000) << 29;
+  }
+  const uint32_t lb = __float_as_uint(lo);
+  if ((lb & 0x7FFFFFFFu) != 0) {
+    int el = (int)((lb >> 23) & 0xFF);
+    unsigned long long ml = (lb & 0x7FFFFF) | (el ? 0x800000u : 0u);
+    if (!el) el = 1;
+    const int s = 29 - (eh - el);
+    unsigned long long L = 0;
+    if (s >= 0) L = ml << s;
+    else if (s > -63) L = (ml + (1ull << (-s - 1))) >> (-s);
+    if ((lb >> 31) == sgn) M += L; else M -= L;
+    if (M >> 53) { M = (M + 1) >> 1; ++eh; }
+    while (M && !(M >> 52)) { M <<= 1; --eh; }
+  }
+  const int E = eh - 127 + 1023 + e2;
+  if (E <= 0 || M == 0) return sgn ? -0.0 : 0.0;
+  if (E >= 2047) return __longlong_as_double(((long long)sgn << 63) | 0x7FF0000000000000ll);
+  const unsigned long long out = ((unsigned long long)sgn << 63) | ((unsigned long long)E << 52) |
+                                 (M & 0xFFFFFFFFFFFFFull);
+  return __longlong_as_double((long long)out);
+}
+
+template <typename T> struct Store;
+template <> struct Store<float2> {
+  // acc -> value (already combined as hi/lo), adds beta*D and z on the diagonal
+  __device__ static void put(void* C, long long off, int part, float hi, float lo, int e2,
+                             float alpha, float beta, const void* D, long long doff, bool diag,
+                             double zpart) {
+    float v, w;
+    if (e2 > -126 && e2 < 128) {
+      const float sc = __int_as_float((127 + e2) << 23);  // 2^e2
+      v = alpha * (hi * sc);
+      w = alpha * (lo * sc);
+    } else {
+      v = alpha * ldexpf(hi, e2);
+      w = alpha * ldexpf(lo, e2);
+    }
+    if (D) v = fmaf(beta, reinterpret_cast<const float*>(D)[2 * doff + part], v);
+    if (diag) v += (float)zpart;
+    reinterpret_cast<float*>(C)[2 * off + part] = v + w;
+  }
+};
+template <> struct Store<double2> {
+  __device__ static void put(void* C, long long off, int part, float hi, float lo, int e2,
+                             float alpha, float beta, const void* D, long long doff, bool diag,
+                             double zpart) {
+    double v = df_to_double(alpha * hi, alpha * lo, e2);
+    if (D) v = fma((double)beta, reinterpret_cast<const double*>(D)[2 * doff + part], v);
+    if (diag) v += zpart;
+    reinterpret_cast<double*>(C)[2 * off + part] = v;
+  }
+};
+
+// ------------------------------------------------------------ the kernel
+template <int S, int L, typename TIn, typename TOut>
+__global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int stages) {
+  constexpr int NACC = (L < 3 ? L : 3) + 1;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  // carve: [stages x (A planes | B planes)] [barriers] [exponents] [tmem slot, abort flag]
+  const int stage_bytes = 2 * S * PLANE_BYTES;
+  unsigned char* tiles = smem;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)stages * stage_bytes);
+  uint64_t* full = bars;                 // [stages] producers -> MMA
+  uint64_t* empty = bars + stages;       // [stages] MMA (commit) -> producers
+  uint64_t* tmem_full = bars + 2 * stages;  // MMA (commit) -> epilogue
+  uint64_t* tmem_empty = tmem_full + 1;     // epilogue -> MMA
+  uint64_t* exp_full = tmem_full + 2;       // [2] producers -> epilogue (scale exponents)
+  uint64_t* exp_empty = tmem_full + 4;      // [2] epilogue -> producers
+  uint64_t* drain = tmem_full + 6;          // teardown
+  int* erow = reinterpret_cast<int*>(tmem_full + 8);  // [2][128]
+  int* fcol = erow + 256;                             // [2][128]
+  uint32_t* tmem_base_sm = reinterpret_cast<uint32_t*>(fcol + 256);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_base_sm + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int n = a.m;
+  const int npad = (n + 15) & ~15;
+  const int kp = (n + KC - 1) / KC * KC;  // padded complex K
+  const int nch = 2 * kp / KC;            // real-K chunks (first half: Re parts, second: Im)
+  const long long nitems = 2 * a.batch;   // (batch entry, real/imag part of C)
+
+  if (tid == 0) {
+    for (int s = 0; s < stages; ++s) { mbar_init(&full[s], NPROD); mbar_init(&empty[s], 1); }
+    mbar_init(tmem_full, 1);
+    mbar_init(tmem_empty, 128);
+    for (int q = 0; q < 2; ++q) { mbar_init(&exp_full[q], NPROD); mbar_init(&exp_empty[q], 128); }
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == MMA_WARP) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_base_sm)),
+                 "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_base_sm;
+
+  if (warp >= 4 && warp < 12) {
+    // ======================== producers
+    const int p = tid - 128;  // 0..255
+    const int pw = p >> 5;    // producer warp 0..7
+    uint32_t proc = 0, gchunk = 0;
+    for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
+      const long long b = w >> 1;
+      const int part = (int)(w & 1);
+      if (a.active && !a.active[b]) continue;
+      const int q = proc & 1;
+      if (!mbar_wait(&exp_empty[q], ((proc >> 1) & 1) ^ 1, abort_flag)) break;
+      const void* A = batch_ptr<const char>(a.A, b);
+      const void* B = batch_ptr<const char>(a.B, b);
+      // ---- scale exponents of the rows of op(A) and columns of op(B) (Re and Im)
+      for (int i = pw; i < 128; i += 8) {
+        unsigned long long m = 0;
+        if (i < n)
+          for (int k = lane; k < n; k += 32) {
+            const TIn v = load_op<TIn>(A, a.A.ld, a.opA, i, k);
+            m = max(m, max(absbits(v, 0), absbits(v, 1)));
+          }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) erow[q * 128 + i] = exp_bound_bits<TIn>(m);
+      }
+      for (int j = pw; j < 128; j += 8) {
+        unsigned long long m = 0;
+        if (j < n)
+          for (int k = lane; k < n; k += 32) {
+            const TIn v = load_op<TIn>(B, a.B.ld, a.opB, k, j);
+            m = max(m, max(absbits(v, 0), absbits(v, 1)));
+          }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) fcol[q * 128 + j] = exp_bound_bits<TIn>(m);
+      }
+      asm volatile("bar.sync 1, 256;" ::: "memory");  // producers only
+      mbar_arrive(&exp_full[q]);
+      // ---- pipeline stages
+      for (int c = 0; c < nch; ++c, ++gchunk) {
+        const int st = gchunk % stages;
+        const uint32_t ph = (gchunk / stages) & 1;
+        if (!mbar_wait(&empty[st], ph ^ 1, abort_flag)) break;
+        unsigned char* stA = tiles + (size_t)st * stage_bytes;
+        unsigned char* stB = stA + S * PLANE_BYTES;
+        const int half = c >= nch / 2;               // 0: real parts, 1: imaginary parts
+        const int k0 = (c - half * (nch / 2)) * KC;  // complex k offset of this chunk
+        // Cr = Re(At).Re(Bt) + Im(At).(-Im(Bt)) ;  Ci = Re(At).Im(Bt) + Im(At).Re(Bt)
+        const int bpart = (part == 0) ? half : (1 - half);
+        const bool bneg = (part == 0 && half == 1);
+        for (int item = p; item < 1024; item += NPROD) {  // (row, 8-k group), A then B
+          const bool isA = item < 512;
+          const int it2 = isA ? item : item - 512;
+          const int r = it2 & 127, g = it2 >> 7;
+          const int e = isA ? erow[q * 128 + r] : fcol[q * 128 + r];
+          const int vpart = isA ? half : bpart;
+          uint32_t packed[S][4];
+#pragma unroll
+          for (int t = 0; t < 8; t += 2) {
+            float D0[S], D1[S];
+            const int ka = k0 + g * 8 + t;
+            TIn x0, x1;
+            if constexpr (sizeof(TIn) == 8) { x0 = make_float2(0.f, 0.f); x1 = x0; }
+            else { x0 = make_double2(0.0, 0.0); x1 = x0; }
+            if (r < n) {
+              if (ka < n) x0 = isA ? load_op<TIn>(A, a.A.ld, a.opA, r, ka) : load_op<TIn>(B, a.B.ld, a.opB, ka, r);
+              if (ka + 1 < n) x1 = isA ? load_op<TIn>(A, a.A.ld, a.opA, r, ka + 1) : load_op<TIn>(B, a.B.ld, a.opB, ka + 1, r);
+            }
+            if constexpr (sizeof(TIn) == 8) {
+              const float scale = __int_as_float((127 + 8 - e) << 23);  // 2^(8-e)
+              float v0 = vpart ? x0.y : x0.x, v1 = vpart ? x1.y : x1.x;
+              if (!isA && bneg) { v0 = -v0; v1 = -v1; }
+              digits_f32<S>(v0, scale, D0);
+              digits_f32<S>(v1, scale, D1);
+            } else {
+              double v0 = vpart ? x0.y : x0.x, v1 = vpart ? x1.y : x1.x;
+              if (!isA && bneg) {  // sign flip on the bits (no FP64 arithmetic)
+                v0 = __longlong_as_double(__double_as_longlong(v0) ^ (1ll << 63));
+                v1 = __longlong_as_double(__double_as_longlong(v1) ^ (1ll << 63));
+              }
+              digits_f64<S>(v0, e, D0);
+              digits_f64<S>(v1, e, D1);
+            }
+#pragma unroll
+            for (int s = 0; s < S; ++s) packed[s][t >> 1] = pack_bf16x2(D0[s], D1[s]);
+          }
+          // canonical no-swizzle K-major: (r/8)*SBO + g*LBO + (r%8)*16
+          const uint32_t off = (uint32_t)((r >> 3) * SBO + g * LBO + (r & 7) * 16);
+          unsigned char* base = isA ? stA : stB;
+#pragma unroll
+          for (int s = 0; s < S; ++s)
+            *reinterpret_cast<uint4*>(base + (size_t)s * PLANE_BYTES + off) =
+                make_uint4(packed[s][0], packed[s][1], packed[s][2], packed[s][3]);
+        }
+        fence_proxy_async();
+        mbar_arrive(&full[st]);
+      }
+      ++proc;
+    }
+  } else if (warp == MMA_WARP) {
+    // ======================== MMA issuer (one thread)
+    if (lane == 0) {
+      const uint32_t idesc = make_idesc(128, npad);
+      uint32_t proc = 0, gchunk = 0;
+      for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
+        const long long b = w >> 1;
+        if (a.active && !a.active[b]) continue;
+        if (!mbar_wait(tmem_empty, (proc & 1) ^ 1, abort_flag)) break;
+        tc_fence_after();
+        uint32_t touched = 0;
+        for (int c = 0; c < nch; ++c, ++gchunk) {
+          const int st = gchunk % stages;
+          const uint32_t ph = (gchunk / stages) & 1;
+          if (!mbar_wait(&full[st], ph, abort_flag)) break;
+          tc_fence_after();
+          const uint32_t sA = smem_u32(tiles + (size_t)st * stage_bytes);
+          const uint32_t sB = sA + S * PLANE_BYTES;
+#pragma unroll
+          for (int kk = 0; kk < KC / 16; ++kk) {
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+#pragma unroll
+              for (int t = 0; t < S; ++t) {
+                if (s + t > L) continue;
+                const int acc = (s + t) < 3 ? (s + t) : 3;
+                const uint64_t ad = make_desc(sA + s * PLANE_BYTES + kk * 2 * LBO);
+                const uint64_t bd = make_desc(sB + t * PLANE_BYTES + kk * 2 * LBO);
+                umma(tmem + acc * 128, ad, bd, idesc, (touched >> acc) & 1);
+                touched |= 1u << acc;
+              }
+            }
+          }
+          umma_commit(&empty[st]);
+        }
+        umma_commit(tmem_full);
+        ++proc;
+      }
+      // drain: wait until every MMA issued by this thread has completed
+      umma_commit(drain);
+      int dummy = 0;
+      volatile int* never = &dummy;
+      mbar_wait(drain, 0, never);
+    }
+    __syncwarp();
+  } else {
+    // ======================== epilogue (warps 0..3 own TMEM lanes 0..127)
+    const int row = warp * 32 + lane;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    uint32_t proc = 0;
+    for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
+      const long long b = w >> 1;
+      const int part = (int)(w & 1);
+      if (a.active && !a.active[b]) continue;
+      const int q = proc & 1;
+      if (!mbar_wait(tmem_full, proc & 1, abort_flag)) break;
+      if (!mbar_wait(&exp_full[q], (proc >> 1) & 1, abort_flag)) break;
+      tc_fence_after();
+      void* C = batch_ptr<char>(a.C, b);
+      const void* D = a.D.p ? batch_ptr<const char>(a.D, b) : nullptr;
+      double zpart = 0.0;
+      if (a.Z.p) {
+        const double2 z = *batch_ptr<const double2>(a.Z, b);
+        zpart = part ? z.y : z.x;
+      }
+      const int ei = erow[q * 128 + row];
+      const float alpha = (float)a.alpha_re, beta = (float)a.beta_re;
+      for (int j0 = 0; j0 < npad; j0 += 16) {
+        uint32_t r[4][16];
+#pragma unroll
+        for (int acc = 0; acc < NACC; ++acc) tmem_ld16(lane_base + acc * 128 + j0, r[acc]);
+        tmem_wait_ld();
+        if (row < n) {
+#pragma unroll
+          for (int jj = 0; jj < 16; ++jj) {
+            const int j = j0 + jj;
+            if (j < n) {
+              float hi = __uint_as_float(r[0][jj]), lo = 0.f, e;
+#pragma unroll
+              for (int acc = 1; acc < NACC; ++acc) {
+                float s;
+                two_sum(hi, __uint_as_float(r[acc][jj]), s, e);
+                hi = s;
+                lo += e;
+              }
+              float s2;
+              two_sum(hi, lo, s2, e);  // normalise: |lo| <= ulp(hi)/2
+              const int e2 = ei + fcol[q * 128 + j] - 16;
+              Store<TOut>::put(C, row + (long long)j * a.C.ld, part, s2, e, e2, alpha, beta, D,
+                               row + (long long)j * a.D.ld, row == j && a.Z.p, zpart);
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(tmem_empty);
+      mbar_arrive(&exp_empty[q]);
+      ++proc;
+    }
+  }
+  // ---- teardown: every MMA has completed (drained above); free TMEM
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == MMA_WARP) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+  }
+}
+
+template <int S, int L, typename TIn, typename TOut>
+cudaError_t launch(const GemmArgs& a, cudaStream_t s) {
+  int dev = 0, sms = 0, maxsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const int stage_bytes = 2 * S * PLANE_BYTES;
+  const int extra = 2048 + 8 * 64 + 64;  // barriers + exponents + tmem slot
+  int stages = (maxsm - extra) / stage_bytes;
+  if (stages > 4) stages = 4;
+  if (stages < 2) return cudaErrorInvalidConfiguration;
+  const size_t smem = (size_t)stages * stage_bytes + extra;
+  cudaError_t e = cudaFuncSetAttribute(zgemm_oz_kernel<S, L, TIn, TOut>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const long long items = 2 * a.batch;
+  const int grid = (int)(items < sms ? items : sms);
+  zgemm_oz_kernel<S, L, TIn, TOut><<<grid, NTHREADS, smem, s>>>(a, stages);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t zgemm_oz(const GemmArgs& a, int slices, int levels, cudaStream_t s) {
+  if (a.batch <= 0) return cudaSuccess;
+  if (a.m != a.n || a.m != a.k || a.m > 128 || a.m <= 0) return cudaErrorInvalidValue;
+  if (a.opA == OP_T || a.opB == OP_T || a.alpha_im != 0.0 || a.beta_im != 0.0)
+    return cudaErrorInvalidValue;
+  (void)levels;
+  switch (slices) {
+    case 4: return launch<4, 3, double2, double2>(a, s);
+    case 6: return launch<6, 5, double2, double2>(a, s);
+    case 7: return launch<7, 6, double2, double2>(a, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t zgemm_oz_c64(const GemmArgs& a, int slices, cudaStream_t s) {
+  if (a.batch <= 0) return cudaSuccess;
+  if (a.m != a.n || a.m != a.k || a.m > 128 || a.m <= 0) return cudaErrorInvalidValue;
+  if (a.opA == OP_T || a.opB == OP_T || a.alpha_im != 0.0 || a.beta_im != 0.0)
+    return cudaErrorInvalidValue;
+  switch (slices) {
+    case 3: return launch<3, 2, float2, float2>(a, s);
+    case 4: return launch<4, 3, float2, float2>(a, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+int oz_timeouts_and_reset() {
+  int h = 0, z = 0;
+  cudaMemcpyFromSymbol(&h, g_oz_timeouts, sizeof(int));
+  if (h) cudaMemcpyToSymbol(g_oz_timeouts, &z, sizeof(int));
+  return h;
+}
+
+}  // namespace qt

@@ -1,0 +1,279 @@
+"""Host-side mirror of the reference's RGF interface on top of libqtgpu.so.
+
+Names, argument meaning and error behaviour follow the Fortran routines:
+
+* ``Context``                  cuda_rgf_init / cuda_rgf_finish (src/cuda_rgf_mod.f90:32-51)
+* ``cuda_rgf_constblocksize``  src/cuda_rgf_mod.f90:53-413 (one energy point)
+* ``rgf_solve``                the ``do ie / do ik`` loop of negf_solve
+                               (src/negf_mod.f90:115-127) as one batched call
+* ``negf_solve``               src/negf_mod.f90:41-165 incl. the per-cell spectra of
+                               write_spectrum_summed_over_k (src/output_mod.f90:14-61)
+* ``sancho``                   src/rgf_mod.f90:482 / src/cuda_rgf_mod.f90:657-765
+* ``mul_c``, ``invert``        src/matrix_c.f90:615-660, src/linalg.f90:42-62 (batched)
+
+Arrays are numpy complex128 in mathematical (row, col) indexing; they are
+converted to the column-major layout of the C-ABI here.  torch CUDA tensors
+in column-major layout (i.e. ``X.mT.contiguous()`` of a row-major block) may
+be passed instead and are used in place (device-pointer mode).
+
+Errors: a failing call raises ``QtError``.  Point-level failures (singular
+block, Sancho not converged, NaN) do not raise; they are reported in the
+``status`` array, in contrast to the reference's abort()
+(src/cuda_rgf_mod.f90:180-187).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import QtContacts, QtDevice, QtOutputs, check
+
+PREC = {"fp64": _lib.QT_PREC_FP64, "mixed": _lib.QT_PREC_MIXED}
+
+
+class Context:
+    """GPU context: one CUDA stream + device scratch (cuda_rgf_init/finish)."""
+
+    def __init__(self, device=0):
+        self._lib = _lib.load()
+        h = C.c_void_p()
+        check(self._lib.qt_ctx_create(C.byref(h), int(device)))
+        self.handle = h
+        self.device = device
+
+    def close(self):
+        if self.handle:
+            self._lib.qt_ctx_destroy(self.handle)
+            self.handle = None
+
+    def sync(self):
+        check(self._lib.qt_ctx_sync(self.handle))
+
+    def set_scratch_limit(self, nbytes):
+        check(self._lib.qt_ctx_set_scratch_limit(self.handle, int(nbytes)))
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def colmajor(A):
+    """Row-major numpy blocks (..., n, n) -> contiguous column-major complex128."""
+    return np.ascontiguousarray(np.swapaxes(np.asarray(A, dtype=np.complex128), -1, -2))
+
+
+def from_colmajor(buf):
+    return np.swapaxes(buf, -1, -2)
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return C.c_void_p(a.data_ptr())
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _blocks(H, nk, nslab):
+    """Normalise (nm,nm) | (nk,nm,nm) | (nk,nslab,nm,nm) to column-major + strides."""
+    H = np.asarray(H, dtype=np.complex128)
+    nm = H.shape[-1]
+    nm2 = nm * nm
+    if H.ndim == 2:
+        return colmajor(H), 0, 0, nm
+    if H.ndim == 3:
+        if H.shape[0] != nk:
+            raise ValueError("3-D block array must be (nk, nm, nm)")
+        return colmajor(H), (nm2 if nk > 1 else 0), 0, nm
+    if H.ndim == 4:
+        if H.shape[0] != nk or H.shape[1] != nslab:
+            raise ValueError("4-D block array must be (nk, nslab, nm, nm)")
+        return colmajor(H), nslab * nm2, nm2, nm
+    raise ValueError("bad block array rank")
+
+
+def rgf_solve(ctx, Hii, H1i, E, nx, *, nk=1, mul=0.0, mur=0.0, templ=300.0, tempr=300.0,
+              eta_lead=1e-5, eta_interior=0.0, sancho_tol=1e-100, sancho_max_iter=50,
+              precision="fp64", caroli=False, want_diag=True, want_blocks=False,
+              sigma_r_ph=None, sigma_lesser_ph=None, quirks=0):
+    """Batched RGF over all (E, k) points (points ordered p = ie*nk + ik).
+
+    Returns a dict of numpy arrays: tr, tre (nE, nk); T (nE, nk) if caroli;
+    diag_gr/gl/gg (nE, nk, nx, nm) if want_diag; G_r/G_lesser/G_greater
+    (nE, nk, nx, nm, nm) if want_blocks; status (nE, nk); sancho_iters (nE, nk, 2).
+    """
+    lib = ctx._lib
+    E = np.ascontiguousarray(np.asarray(E, dtype=np.float64).ravel())
+    nE = E.shape[0]
+    hii, hk, hl, nm = _blocks(Hii, nk, nx)
+    h1i, h1k, h1l, nm1 = _blocks(H1i, nk, nx + 1)
+    if nm1 != nm:
+        raise ValueError("Hii and H1i block sizes differ")
+    dev = QtDevice(nm, nx, nk, _ptr(hii), hk, hl, _ptr(h1i), h1k, h1l, None, 0, 0)
+    con = QtContacts(mul, mur, templ, tempr, eta_lead, eta_interior, sancho_tol,
+                     int(sancho_max_iter), int(quirks))
+    npts = nE * nk
+    res = {"tr": np.zeros(npts), "tre": np.zeros(npts),
+           "status": np.zeros(npts, dtype=np.int32),
+           "sancho_iters": np.zeros((npts, 2), dtype=np.int32)}
+    if caroli:
+        res["T"] = np.zeros(npts)
+    if want_diag:
+        for k in ("diag_gr", "diag_gl", "diag_gg"):
+            res[k] = np.zeros((npts, nx, nm), dtype=np.complex128)
+    if want_blocks:
+        for k in ("G_r", "G_lesser", "G_greater"):
+            res[k] = np.zeros((npts, nx, nm, nm), dtype=np.complex128)
+    out = QtOutputs(*[_ptr(res.get(k)) for k in ("tr", "tre", "T", "diag_gr", "diag_gl",
+                                                 "diag_gg", "G_r", "G_lesser", "G_greater",
+                                                 "status", "sancho_iters")])
+    sr = None if sigma_r_ph is None else colmajor(sigma_r_ph)
+    sl = None if sigma_lesser_ph is None else colmajor(sigma_lesser_ph)
+    flags = _lib.QT_FLAG_SYNC | (_lib.QT_FLAG_CAROLI if caroli else 0)
+    check(lib.qt_rgf_solve(ctx.handle, C.byref(dev), _ptr(E), nE, C.byref(con), _ptr(sr),
+                           _ptr(sl), PREC[precision], flags, C.byref(out)), allow_points=True)
+    if want_blocks:
+        for k in ("G_r", "G_lesser", "G_greater"):
+            res[k] = from_colmajor(res[k]).reshape(nE, nk, nx, nm, nm)
+    for k in ("tr", "tre", "T", "status"):
+        if k in res:
+            res[k] = res[k].reshape(nE, nk)
+    for k in ("diag_gr", "diag_gl", "diag_gg"):
+        if k in res:
+            res[k] = res[k].reshape(nE, nk, nx, nm)
+    res["sancho_iters"] = res["sancho_iters"].reshape(nE, nk, 2)
+    return res
+
+
+def cuda_rgf_constblocksize(ctx, nm, nx, En, mul, mur, TEMPl, TEMPr, Hii, H1i, Sii=None,
+                            sigma_lesser_ph=None, sigma_r_ph=None):
+    """One point with the reference's argument list (src/cuda_rgf_mod.f90:53-59).
+
+    Hii (nx, nm, nm), H1i (nx+1, nm, nm), optional Sii / sigmas (nx, nm, nm).
+    mu/T may be scalars or the reference's constant nm x nm matrices.
+    Returns (G_r, G_lesser, G_greater, Jdens, tr, tre); Jdens is all zeros
+    (bond currents are not produced by the batched sweep).
+    """
+    def scalar(x):
+        x = np.asarray(x, dtype=np.float64)
+        if x.ndim and not np.all(x == x.flat[0]):
+            raise ValueError("mu/T matrices must be constant (src/negf_mod.f90:82-85)")
+        return float(x.flat[0])
+
+    lib = ctx._lib
+    hii = colmajor(Hii)
+    h1i = colmajor(H1i)
+    sii = None if Sii is None else colmajor(Sii)
+    sl = None if sigma_lesser_ph is None else colmajor(sigma_lesser_ph)
+    sr = None if sigma_r_ph is None else colmajor(sigma_r_ph)
+    Gr = np.zeros((nx, nm, nm), dtype=np.complex128)
+    Gl = np.zeros_like(Gr)
+    Gg = np.zeros_like(Gr)
+    Jd = np.zeros_like(Gr)
+    tr = C.c_double()
+    tre = C.c_double()
+    check(lib.qt_rgf_constblocksize(ctx.handle, nm, nx, float(En), scalar(mul), scalar(mur),
+                                    scalar(TEMPl), scalar(TEMPr), _ptr(hii), _ptr(h1i), _ptr(sii),
+                                    _ptr(sl), _ptr(sr), _ptr(Gr), _ptr(Gl), _ptr(Gg), _ptr(Jd),
+                                    C.byref(tr), C.byref(tre)), allow_points=True)
+    return (from_colmajor(Gr), from_colmajor(Gl), from_colmajor(Gg), from_colmajor(Jd),
+            tr.value, tre.value)
+
+
+def sancho(ctx, E, H00, H10, *, eta=1e-5, tol=1e-100, max_iter=50, precision="fp64"):
+    """Batched Sancho-Rubio: E (npts,), H00/H10 (nm,nm) shared or (npts,nm,nm).
+
+    Returns (G00, GBB, iters, status) with G00/GBB (npts, nm, nm).
+    """
+    lib = ctx._lib
+    E = np.ascontiguousarray(np.atleast_1d(np.asarray(E, dtype=np.float64)))
+    npts = E.shape[0]
+    H00 = np.asarray(H00, dtype=np.complex128)
+    H10 = np.asarray(H10, dtype=np.complex128)
+    nm = H00.shape[-1]
+    h00, h10 = colmajor(H00), colmajor(H10)
+    G00 = np.zeros((npts, nm, nm), dtype=np.complex128)
+    GBB = np.zeros_like(G00)
+    iters = np.zeros(npts, dtype=np.int32)
+    status = np.zeros(npts, dtype=np.int32)
+    check(lib.qt_sancho_batch(ctx.handle, nm, npts, _ptr(E), _ptr(h00), nm * nm if H00.ndim == 3 else 0,
+                              _ptr(h10), nm * nm if H10.ndim == 3 else 0, None, 0, eta, tol,
+                              int(max_iter), PREC[precision], 0, _ptr(G00), _ptr(GBB), _ptr(iters),
+                              _ptr(status)))
+    return from_colmajor(G00), from_colmajor(GBB), iters, status
+
+
+def mul_c(ctx, A, B, opA="N", opB="N", alpha=1.0, beta=0.0, D=None, precision="fp64", slices=0):
+    """Batched C = alpha op(A) op(B) + beta D for (batch, n, n) arrays (or shared (n, n))."""
+    lib = ctx._lib
+    A = np.asarray(A, dtype=np.complex128)
+    B = np.asarray(B, dtype=np.complex128)
+    n = A.shape[-1]
+    batch = max(A.shape[0] if A.ndim == 3 else 1, B.shape[0] if B.ndim == 3 else 1)
+    a, b = colmajor(A), colmajor(B)
+    d = None if D is None else colmajor(D)
+    Cm = np.zeros((batch, n, n), dtype=np.complex128)
+    al = np.array([complex(alpha).real, complex(alpha).imag])
+    be = np.array([complex(beta).real, complex(beta).imag])
+    st = lambda X: (n * n if X is not None and X.ndim == 3 else 0)
+    check(lib.qt_zgemm_batch(ctx.handle, n, batch, opA.encode(), _ptr(a), st(A), opB.encode(),
+                             _ptr(b), st(B), _ptr(al), _ptr(be), _ptr(d),
+                             st(None if D is None else np.asarray(D)), _ptr(Cm), n * n,
+                             PREC[precision], int(slices), 0))
+    return from_colmajor(Cm)
+
+
+def invert(ctx, A, precision="fp64"):
+    """Batched block inverse of (batch, n, n); returns (X, status)."""
+    lib = ctx._lib
+    A = np.asarray(A, dtype=np.complex128)
+    if A.ndim == 2:
+        A = A[None]
+    batch, n = A.shape[0], A.shape[-1]
+    a = colmajor(A)
+    X = np.zeros_like(a)
+    status = np.zeros(batch, dtype=np.int32)
+    check(lib.qt_zinv_batch(ctx.handle, n, batch, _ptr(a), n * n, _ptr(X), n * n,
+                            PREC[precision], 0, _ptr(status)))
+    return from_colmajor(X), status
+
+
+def cell_spectra(diag, nbnd, nslab, nk_axis=1):
+    """write_spectrum_summed_over_k's per-cell traces (src/output_mod.f90:37-59).
+
+    diag: (nE, nk, nx, nm) diagonals.  Returns (nE, nx*nslab) complex traces
+    averaged over k.
+    """
+    nE, nk, nx, nm = diag.shape
+    t = diag.reshape(nE, nk, nx, nslab, nbnd).sum(axis=4).mean(axis=1)
+    return t.reshape(nE, nx * nslab)
+
+
+def negf_solve(ctx, Hii, H1i, nx, nen, emin, emax, temp, mu, nbnd, nslab, *, nk=1,
+               precision="fp64", **kw):
+    """Ballistic NEGF driver (src/negf_mod.f90:41-165).
+
+    Energy grid E_ie = emin + ie (emax-emin)/(nen-1) (src/negf_mod.f90:100-101).
+    Returns dict with E, tr, tre (nen, nk) and the ldos/ndos/pdos spectra
+    (nen, nx*nslab, 2) = (Re*c1, Im*c2) columns with the reference coefficients
+    (1,-2), (1,1), (1,-1) (src/negf_mod.f90:142-149).
+    """
+    E = emin + np.arange(nen) * ((emax - emin) / (nen - 1))
+    r = rgf_solve(ctx, Hii, H1i, E, nx, nk=nk, mul=mu[0], mur=mu[1], templ=temp[0],
+                  tempr=temp[1], precision=precision, **kw)
+    out = {"E": E, "tr": r["tr"], "tre": r["tre"], "status": r["status"]}
+    for name, key, c in (("ldos", "diag_gr", (1.0, -2.0)), ("ndos", "diag_gl", (1.0, 1.0)),
+                         ("pdos", "diag_gg", (1.0, -1.0))):
+        t = cell_spectra(r[key], nbnd, nslab)
+        out[name] = np.stack([t.real * c[0], t.imag * c[1]], axis=-1)
+    return out

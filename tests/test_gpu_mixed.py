@@ -1,0 +1,88 @@
+"""Split-precision (tcgen05 Ozaki-digit) path against FP64 references."""
+import numpy as np
+import pytest
+
+from oracle import rgf as orc
+from quantum_transport_gb300 import rgf
+from quantum_transport_gb300.devices import make_chain_device
+from tests.goldutil import printed_match
+
+pytestmark = pytest.mark.gpu
+
+# normwise error bound per digit count, relative to (|op(A)| |op(B)|)_ij:
+# S digits keep 8S-1 bits of each row/column-aligned operand
+TOL = {4: 2.0 ** -29, 6: 2.0 ** -45, 7: 2.0 ** -53}
+
+
+def rand_blocks(rng, b, n, scale=1.0):
+    return scale * (rng.normal(size=(b, n, n)) + 1j * rng.normal(size=(b, n, n)))
+
+
+@pytest.mark.parametrize("slices", [4, 6, 7])
+@pytest.mark.parametrize("n", [16, 33, 96, 128])
+@pytest.mark.parametrize("ops", ["NN", "NC", "CN", "CC"])
+def test_zgemm_split(ctx, slices, n, ops):
+    rng = np.random.default_rng(100 * n + slices)
+    A = rand_blocks(rng, 3, n)
+    B = rand_blocks(rng, 3, n, scale=1e-3)  # scales differ per operand
+    A[:, 0, :] *= 1e4                       # rows of very different magnitude
+    op = {"N": lambda X: X, "C": lambda X: np.conj(np.swapaxes(X, -1, -2))}
+    C = rgf.mul_c(ctx, A, B, ops[0], ops[1], precision="mixed", slices=slices)
+    ref = op[ops[0]](A) @ op[ops[1]](B)
+    bound = np.abs(op[ops[0]](A)) @ np.abs(op[ops[1]](B))
+    err = np.abs(C - ref)
+    assert (err <= 4 * n * TOL[slices] * bound + 1e-300).all(), (err / bound).max()
+
+
+def test_zgemm_split_alpha_beta(ctx):
+    rng = np.random.default_rng(9)
+    n = 64
+    A, B, D = rand_blocks(rng, 2, n), rand_blocks(rng, 2, n), rand_blocks(rng, 2, n)
+    C = rgf.mul_c(ctx, A, B, "N", "C", alpha=-1.0, beta=1.0, D=D, precision="mixed", slices=7)
+    ref = -A @ np.conj(np.swapaxes(B, -1, -2)) + D
+    np.testing.assert_allclose(C, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
+
+
+def test_zinv_split(ctx):
+    rng = np.random.default_rng(3)
+    A = rand_blocks(rng, 5, 96) + 4 * np.eye(96)
+    X, st = rgf.invert(ctx, A, precision="mixed")
+    assert (st == 0).all()
+    np.testing.assert_allclose(X @ A, np.broadcast_to(np.eye(96), A.shape), atol=1e-11)
+
+
+def test_sancho_split_cnt_golden(ctx, cnt):
+    """FP64-grade digits reproduce the reference's lead traces (file precision ~1e-12)."""
+    idx = np.arange(0, 200, 7)
+    E = cnt["E"][idx]
+    for j, h in enumerate((cnt["H10"].conj().T, cnt["H10"])):
+        G00, GBB, it, st = rgf.sancho(ctx, E, cnt["H00"], h, precision="mixed")
+        assert (st == 0).all()
+        np.testing.assert_allclose(-np.trace(G00, axis1=1, axis2=2).imag,
+                                   cnt["sancho_g00"][idx, j], rtol=1e-8)
+
+
+def test_rgf_split_cnt_golden(ctx, cnt):
+    """The test_cnt run through the split-precision path: ldos/ndos/pdos0000.dat digits."""
+    nx = int(cnt["nx"])
+    r = rgf.negf_solve(ctx, cnt["H00"], cnt["H10"], nx, 200, -6.0, -1.0, (300.0, 300.0),
+                       (-3.7, -3.7), int(cnt["nb"]), int(cnt["ns"]), precision="mixed")
+    assert (r["status"] == 0).all()
+    for name, col in (("ldos", 0), ("ldos", 1), ("ndos", 1), ("pdos", 1)):
+        ok = printed_match(r[name][:, :, col], cnt[name][:, :, col], full=cnt[name][:, :, col])
+        assert ok.mean() > 0.995, (name, col, np.argwhere(~ok)[:5])
+
+
+def test_rgf_split_vs_fp64_transmission(ctx):
+    """T(E) of the split path within 1e-6 (relative) of the FP64 path."""
+    dev = make_chain_device(24, 64, 16, -2.0, 2.0, seed=2024, nk=4)
+    kw = dict(nk=dev.nk, mul=0.1, mur=-0.1, templ=290.1, tempr=290.1, sancho_tol=1e-10,
+              caroli=True)
+    r64 = rgf.rgf_solve(ctx, dev.H00, dev.H10, dev.E, dev.nx, **kw)
+    rmx = rgf.rgf_solve(ctx, dev.H00, dev.H10, dev.E, dev.nx, precision="mixed", **kw)
+    assert (rmx["status"] == 0).all()
+    rel = np.abs(rmx["T"] - r64["T"]) / np.abs(r64["T"])
+    assert rel.max() <= 1e-6, rel.max()
+    for key in ("diag_gr", "diag_gl"):
+        err = np.abs(rmx[key] - r64[key]).max() / np.abs(r64[key]).max()
+        assert err <= 1e-5, (key, err)
