@@ -1,0 +1,342 @@
+"""Benchmark: batched RGF E-points/s on one GB300 (split-precision tensor-core path).
+
+Workload (the batched configuration): a seeded synthetic device of 100 slabs x
+128 orbitals with transverse dispersion over 16 k-points and 4096 energies on
+[-2, 2] eV -- 65,536 independent (E, k) solves.  One STEP solves one batch of
+``--batch-energies`` energies x 16 k through the whole hot path (both
+Sancho-Rubio leads, forward and backward sweeps, Caroli T(E), tr/tre, LDOS
+and G^< diagonals); successive steps walk through the 4096-energy grid.
+
+Reported (one JSON line on rank 0):
+  value        E-points/s with inputs resident in HBM (device-pointer call)
+  e2e          the same through the host-pointer C-ABI call (H blocks and the
+               energy slice copied in, all outputs copied out, inside the timer)
+  roofline     the dominant kernel (complex64 split product) timed live with
+               CUDA events on the library's stream
+  cpu_baseline the C restatement of the sweep timed on the host cores
+  fp64         the plain-FP64 GPU path on a small sample of the same points
+               and the T(E) error of the split path against it
+
+``--impl reference`` times the CPU restatement (the reference's Fortran
+cannot be built on this machine or the GPU machine: no Fortran compiler).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "E-points/s (RGF) and GW-SCBA time-to-converge at 1e-6 err, vs plain FP64 GPU"
+NX, NM, NK, NE = 100, 128, 16, 4096
+SEED = 2024
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch-energies", type=int, default=64,
+                    help="energies per step (x 16 k-points)")
+    ap.add_argument("--fp64-energies", type=int, default=2)
+    ap.add_argument("--cpu-points", type=int, default=16)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def device():
+    from quantum_transport_gb300.devices import config_batched
+    return config_batched(seed=SEED, nE=NE, nk=NK, nx=NX, nm=NM)
+
+
+def config_dict(a, extra=None):
+    c = {"workload": "batched RGF, 100 slabs x 128 orbitals, 16 k x 4096 E "
+                     "(65,536 (E,k) solves), seeded synthetic chain",
+         "slabs": NX, "orbitals_per_slab": NM, "k_points": NK, "energies": NE,
+         "points_per_step": a.batch_energies * NK,
+         "outputs": "T(E) Caroli, tr, tre, diag G^R (LDOS), diag G^<",
+         "sancho_tol": 1e-10, "eta_lead": 1e-5,
+         "l2": "no flush: per-step working set (g_l, g^<_l per point x slabs) >> 129 MB L2"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (SM clock, throttle reasons)."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) > 8
+                          for i, v in enumerate(r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def cpu_baseline(dev, npts, threads):
+    """The C restatement on the host cores: npts points of the same workload."""
+    from oracle import cref
+    cref.build()
+    ne = max(1, npts // NK)
+    t0 = time.perf_counter()
+    r = cref.rgf(dev.H00, dev.H10, dev.E[:ne], NX, mul=0.1, mur=-0.1, templ=300.0, tempr=300.0,
+                 sancho_tol=1e-10, threads=threads, want_diag=True)
+    dt = time.perf_counter() - t0
+    return ne * NK / dt, dt, r
+
+
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    dev = device()
+    threads = os.cpu_count() or 1
+    npts = max(NK, (threads // NK) * NK) if threads >= NK else NK
+    for _ in range(a.warmup):
+        cpu_baseline(dev, npts, threads)
+    times = []
+    for _ in range(a.steps):
+        _, dt, _ = cpu_baseline(dev, npts, threads)
+        times.append(dt)
+    ms = 1e3 * sum(times) / len(times)
+    v = npts / (ms / 1e3)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "E-points/s",
+            "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+            "data": "synthetic (seeded)",
+            "config": config_dict(a, {"points_per_step": npts}),
+            "cpu_baseline": {"value": v, "unit": "E-points/s", "cores": threads, "kind": "port",
+                             "sample": f"{npts} points (one energy x 16 k) per step of the same "
+                                       "workload; C99+OpenMP restatement of the reference sweep "
+                                       "(no Fortran compiler on the box)"},
+            "e2e": {"value": v, "unit": "E-points/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(a):
+    import torch
+    import torch.distributed as dist
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl", rank=rank, world_size=world)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    from quantum_transport_gb300.build import build
+    build()
+    from quantum_transport_gb300 import rgf
+
+    dev = device()
+    ctx = rgf.Context(local)
+    B = a.batch_energies
+    P = B * NK
+    nblk = NE // B
+    cm = lambda x: torch.from_numpy(rgf.colmajor(x)).cuda()
+    H00 = cm(dev.H00)                 # (16, 128, 128) complex128, column-major per block
+    H10 = cm(dev.H10)
+    E = torch.from_numpy(dev.E).cuda()
+    nm2 = NM * NM
+    out = {"T": torch.zeros(P, dtype=torch.float64, device="cuda"),
+           "tr": torch.zeros(P, dtype=torch.float64, device="cuda"),
+           "tre": torch.zeros(P, dtype=torch.float64, device="cuda"),
+           "diag_gr": torch.zeros(P * NX * NM, dtype=torch.complex128, device="cuda"),
+           "diag_gl": torch.zeros(P * NX * NM, dtype=torch.complex128, device="cuda"),
+           "status": torch.zeros(P, dtype=torch.int32, device="cuda")}
+    kw = dict(mul=0.1, mur=-0.1, templ=300.0, tempr=300.0, sancho_tol=1e-10, caroli=True)
+
+    def step(i, precision="mixed", o=out, nE=B):
+        blk = (rank * 7919 + i) % nblk
+        rgf.rgf_solve_device(ctx, H00, nm2, 0, H10, 0, 0, NM, NX, NK, E[blk * B:], nE, o,
+                             precision=precision, **kw)
+
+    torch.cuda.synchronize()
+    for i in range(a.warmup):
+        step(i)
+    ctx.sync()
+    stream = torch.cuda.ExternalStream(ctx.stream_ptr)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = Clocks(local)
+    ctx.profile_read()  # drop warm-up entries
+    ctx.profile(True)
+    n0 = rgf.kernel_launches()
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0.record(stream)
+    for i in range(a.steps):
+        step(a.warmup + i)
+    ev1.record(stream)
+    ev1.synchronize()
+    ctx.sync()
+    clk = clocks.stop()
+    launches = rgf.kernel_launches() - n0
+    ctx.profile(False)
+    prof = ctx.profile_read()
+    ms = ev0.elapsed_time(ev1) / a.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    status_bad = int((out["status"] != 0).sum().item())
+    value = world * P / (ms / 1e3)
+
+    pk, pk_kind = peaks()
+    tot_ms = sum(v[1] for v in prof.values()) or 1.0
+    dom = prof.get("zgemm_oz_c64", (0, 0.0, 0.0, 0.0))
+    alg_tf = dom[2] / (dom[1] / 1e3) / 1e12 if dom[1] else 0.0
+    exe_tf = dom[3] / (dom[1] / 1e3) / 1e12 if dom[1] else 0.0
+    peak = pk.get("bf16_tflops_sustained", pk.get("bf16_tflops"))
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp) and dom[0]:
+        with open(tp) as f:
+            bpp = json.load(f).get("zgemm_oz_c64_dram_bytes_per_product")
+        if bpp:
+            traffic = bpp * (dom[2] / (8.0 * NM ** 3)) / dom[0]
+    roofline = {"kernel": "zgemm_oz_kernel<4,3,float2,float2> (complex64 split product)",
+                "bound": "tensor", "achieved": alg_tf, "peak": peak, "unit": "TFLOP/s",
+                "frac": alg_tf / peak if peak else None, "traffic": traffic,
+                "peak_source": f"bf16_tflops_sustained of {pk_kind}",
+                "achieved_is": "algorithmic 8 n^3 flops per complex block product / event time",
+                "executed_tensor_tflops": exe_tf,
+                "executed_frac": exe_tf / peak if peak else None,
+                "launches": dom[0], "avg_launch_ms": dom[1] / dom[0] if dom[0] else None,
+                "time_share": {k: round(v[1] / tot_ms, 4) for k, v in prof.items()}}
+    line = {"metric": METRIC, "value": value, "unit": "E-points/s", "n_gpus": world,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16-digit split (c64 sweep, "
+            "FP64-grade c128 leads)", "data": "synthetic (seeded, no dataset)",
+            "config": config_dict(a, {"parallelism": f"points sharded over {world} GPU(s)",
+                                      "points_bad_status": status_bad}),
+            "roofline": roofline, "clocks": clk, "gpu_launches": launches}
+
+    if rank == 0:
+        # ---- plain-FP64 GPU path on a small sample of the same points; T(E) error
+        Bf = a.fp64_energies
+        Pf = Bf * NK
+        of = {k: torch.zeros(Pf * (NX * NM if k.startswith("diag") else 1),
+                             dtype=v.dtype, device="cuda") for k, v in out.items()}
+        om = {k: torch.zeros_like(v) for k, v in of.items()}
+        Es = E[:Bf]
+        rgf.rgf_solve_device(ctx, H00, nm2, 0, H10, 0, 0, NM, NX, NK, Es, Bf, om, **kw)
+        ctx.sync()
+        t0 = time.perf_counter()
+        rgf.rgf_solve_device(ctx, H00, nm2, 0, H10, 0, 0, NM, NX, NK, Es, Bf, of,
+                             precision="fp64", **kw)
+        ctx.sync()
+        t64 = time.perf_counter() - t0
+        T64, Tmx = of["T"].cpu().numpy(), om["T"].cpu().numpy()
+        d64, dmx = of["diag_gr"].cpu().numpy(), om["diag_gr"].cpu().numpy()
+        l64, lmx = of["diag_gl"].cpu().numpy(), om["diag_gl"].cpu().numpy()
+        fp64 = {"value": Pf / t64, "unit": "E-points/s", "sample_points": Pf,
+                "speedup_split_vs_fp64": value / world / (Pf / t64),
+                "T_rel_err_max": float(np.max(np.abs(Tmx - T64) / np.abs(T64))),
+                "ldos_rel_err_max": float(np.max(np.abs(dmx.imag - d64.imag)) /
+                                          np.max(np.abs(d64.imag))),
+                "diag_glesser_rel_err_max": float(np.max(np.abs(lmx - l64)) /
+                                                  max(np.max(np.abs(l64)), 1e-300))}
+        line["fp64_gpu"] = fp64
+        if world == 1 and not a.no_cpu:
+            threads = os.cpu_count() or 1
+            v, dt, r = cpu_baseline(dev, a.cpu_points, threads)
+            line["cpu_baseline"] = {"value": v, "unit": "E-points/s", "cores": threads,
+                                    "kind": "port",
+                                    "sample": f"{max(1, a.cpu_points // NK) * NK} points (one "
+                                              f"energy x 16 k) of the same workload, {dt:.1f} s; "
+                                              "C99+OpenMP restatement of the reference sweep"}
+            Tc = r["T"].ravel()
+            line["cpu_baseline"]["T_rel_err_vs_fp64_gpu"] = float(
+                np.max(np.abs(Tc - T64[:Tc.size]) / np.abs(T64[:Tc.size])))
+        if not a.no_e2e:
+            # ---- end to end through the host-pointer C-ABI call
+            Eh = dev.E
+            rgf.rgf_solve(ctx, dev.H00, dev.H10, Eh[:B], NX, nk=NK, precision="mixed",
+                          want_diag=True, **kw)
+            t0 = time.perf_counter()
+            ne = max(1, min(a.steps, 3))
+            for i in range(ne):
+                blk = (i + 1) % nblk
+                r = rgf.rgf_solve(ctx, dev.H00, dev.H10, Eh[blk * B:(blk + 1) * B], NX, nk=NK,
+                                  precision="mixed", want_diag=True, **kw)
+            te = (time.perf_counter() - t0) / ne
+            h2d = dev.H00.nbytes + dev.H10.nbytes + B * 8
+            d2h = P * (3 * 8 + 4 + 8) + 3 * P * NX * NM * 16
+            line["e2e"] = {"value": P / te, "unit": "E-points/s", "h2d_bytes_per_step": h2d,
+                           "d2h_bytes_per_step": d2h, "steps": ne,
+                           "points_bad_status": int((r["status"] != 0).sum())}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -72,6 +72,22 @@ const char* qt_last_error(void);
 /* Library version string.                                                   */
 const char* qt_version(void);
 
+/* Instrumentation (no counterpart in the reference, which only prints
+ * omp_get_wtime phase times, src/cuda_rgf_mod.f90:87-412).
+ * qt_kernel_launches: kernels launched by this library since load.
+ * qt_ctx_profile(enable): record CUDA events around every block product and
+ *   inverse on the context's stream.
+ * qt_ctx_profile_read(kind): launches, summed device time (ms) and the
+ *   algorithmic / executed-tensor flops of one kind since the last read:
+ *   0 complex64 split product, 1 complex128 split product, 2 FP64 product,
+ *   3 FP32 inverse, 4 FP64 inverse.
+ * qt_ctx_stream: the context's cudaStream_t (as void*).                    */
+int64_t qt_kernel_launches(void);
+qt_status qt_ctx_profile(qt_ctx* ctx, int enable);
+qt_status qt_ctx_profile_read(qt_ctx* ctx, int kind, int64_t* launches, double* ms,
+                              double* alg_flops, double* tensor_flops);
+qt_status qt_ctx_stream(qt_ctx* ctx, void** stream);
+
 /* Block-tridiagonal device of nx slabs of constant block size nm at nk
  * transverse k-points (cuda_rgf_constblocksize's Hii(nx), H1i(nx+1), Sii(nx),
  * src/cuda_rgf_mod.f90:55; built per k by devH_build_fromWannierFile,
@@ -180,6 +196,45 @@ qt_status qt_zgemm_batch(qt_ctx* ctx, int n, int batch, char opA, const double* 
 qt_status qt_zinv_batch(qt_ctx* ctx, int n, int batch, const double* A, int64_t a_stride,
                         double* X, int64_t x_stride, qt_precision prec, unsigned flags,
                         int* status);
+
+/* ---- GW / SCBA (one k-point; device pointers: QT_FLAG_DEVICE_POINTERS required).
+ * Energy-resolved arrays are [nE][nx][nm*nm] complex128 column-major
+ * slab-diagonal blocks; the energy grid E must be uniform (dE = E[1]-E[0]) and
+ * nE <= 2048 (zero-padded FFT length 4096).  V: the nm x nm slab-diagonal
+ * Coulomb block (the reference passes Vii/V1i, src/gw_mod.f90:84,597-600;
+ * only the diagonal block enters the per-slab W restatement).                */
+
+/* One evaluation of the SCBA map Sigma -> Sigma_new of gw_ephoton_3d_ijs
+ * (src/gw_mod.f90:368-749 and :950-959): G by the batched RGF with
+ * sigma_r/sigma_lesser (green_RGF_RS, :1131-1345), P by energy correlation of
+ * the Re-zeroed G (:444-519), W = (I - V P^R)^-1 V and W^<> = W P^<> W^+ per
+ * slab block (green_rgf_calc_w, called at :597, is absent from the
+ * reference), Sigma by energy convolution (:646-698), Re/Im recombination,
+ * symmetrisation (:698, :731-743) and the edge-block copy (:950-959).      */
+qt_status qt_gw_step(qt_ctx* ctx, const qt_device* dev, const double* E, int nE,
+                     const qt_contacts* contacts, const double* V, double spindeg,
+                     qt_precision prec, unsigned flags, const double* sigma_r,
+                     const double* sigma_lesser, double* new_r, double* new_lesser,
+                     double* new_greater);
+
+/* Plain linear-mixing SCBA (src/gw_mod.f90:349-749) iterated until the
+ * residual ||S_new - S||_F / ||S_new||_F over Sigma^< and Sigma^> is <= tol
+ * or max_iter maps were evaluated (the reference has no convergence test and
+ * runs a fixed niter).  sigma_* are the start values on input and the mixed
+ * result on output; residuals [max_iter]; *iters = maps evaluated.          */
+qt_status qt_scba_solve(qt_ctx* ctx, const qt_device* dev, const double* E, int nE,
+                        const qt_contacts* contacts, const double* V, double spindeg,
+                        double alpha, double tol, int max_iter, qt_precision prec,
+                        unsigned flags, double* sigma_r, double* sigma_lesser,
+                        double* sigma_greater, double* residuals, int* iters);
+
+/* Batched energy correlation (mode 0) / convolution (mode 1) of corr1d2 /
+ * conv1d2 (src/fft_mod.f90:58-168) on n-point series stored energy-major,
+ * element (e, s) at 2*(e*nseries + s) doubles:
+ *   mode 0: Z[m] = sum_e X[e] Y[e - (m - n/2)]
+ *   mode 1: Z[e] = sum_m X[e - (m - n/2)] Y[m]          n <= 2048.          */
+qt_status qt_corr_batch(qt_ctx* ctx, int n, int64_t nseries, const double* X, const double* Y,
+                        double* Z, int mode, unsigned flags);
 
 #ifdef __cplusplus
 }

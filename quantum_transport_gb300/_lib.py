@@ -22,7 +22,9 @@ QT_PT_SINGULAR, QT_PT_SANCHO_NOT_CONVERGED, QT_PT_NONFINITE = 1, 2, 4
 EXPORTS = [
     "qt_ctx_create", "qt_ctx_destroy", "qt_ctx_sync", "qt_ctx_set_scratch_limit",
     "qt_last_error", "qt_version", "qt_rgf_solve", "qt_rgf_constblocksize",
-    "qt_sancho_batch", "qt_zgemm_batch", "qt_zinv_batch",
+    "qt_sancho_batch", "qt_zgemm_batch", "qt_zinv_batch", "qt_kernel_launches",
+    "qt_ctx_profile", "qt_ctx_profile_read", "qt_ctx_stream", "qt_gw_step", "qt_scba_solve",
+    "qt_corr_batch",
 ]
 
 
@@ -77,9 +79,20 @@ def load(path=LIB_PATH):
     lib.qt_zgemm_batch.argtypes = [vp, ci, ci, C.c_char, vp, i64, C.c_char, vp, i64, vp, vp, vp,
                                    i64, vp, i64, ci, ci, C.c_uint]
     lib.qt_zinv_batch.argtypes = [vp, ci, ci, vp, i64, vp, i64, ci, C.c_uint, vp]
+    lib.qt_kernel_launches.argtypes = []
+    lib.qt_kernel_launches.restype = C.c_int64
+    lib.qt_ctx_profile.argtypes = [vp, ci]
+    lib.qt_ctx_profile_read.argtypes = [vp, ci, C.POINTER(C.c_int64), C.POINTER(dbl),
+                                        C.POINTER(dbl), C.POINTER(dbl)]
+    lib.qt_ctx_stream.argtypes = [vp, C.POINTER(vp)]
+    lib.qt_gw_step.argtypes = [vp, C.POINTER(QtDevice), vp, ci, C.POINTER(QtContacts), vp, dbl,
+                               ci, C.c_uint, vp, vp, vp, vp, vp]
+    lib.qt_scba_solve.argtypes = [vp, C.POINTER(QtDevice), vp, ci, C.POINTER(QtContacts), vp,
+                                  dbl, dbl, dbl, ci, ci, C.c_uint, vp, vp, vp, vp, vp]
+    lib.qt_corr_batch.argtypes = [vp, ci, i64, vp, vp, vp, ci, C.c_uint]
     for name in EXPORTS:
         f = getattr(lib, name)
-        if name not in ("qt_last_error", "qt_version"):
+        if name not in ("qt_last_error", "qt_version", "qt_kernel_launches"):
             f.restype = C.c_int
     _lib = lib
     return lib

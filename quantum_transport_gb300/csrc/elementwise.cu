@@ -265,6 +265,7 @@ cudaError_t zaxpby(int n, long long batch, BatchRef X, double ar, double ai, Bat
                    double bi, BatchRef Z, BatchRef Y, const unsigned char* active, cudaStream_t s) {
   if (batch <= 0) return cudaSuccess;
   zaxpby_kernel<TC><<<grid_for(batch), NT, 0, s>>>(n, batch, X, ar, ai, W, br, bi, Z, Y, active);
+  count_launch();
   return cudaGetLastError();
 }
 template <typename TC>
@@ -272,12 +273,14 @@ cudaError_t zantiherm(int n, long long batch, BatchRef X, double cr, double ci, 
                       BatchRef Y, cudaStream_t s) {
   if (batch <= 0) return cudaSuccess;
   zantiherm_kernel<TC><<<grid_for(batch), NT, 0, s>>>(n, batch, X, cr, ci, W, Y);
+  count_launch();
   return cudaGetLastError();
 }
 template <typename TC>
 cudaError_t zdagger(int n, long long batch, BatchRef X, BatchRef Y, cudaStream_t s) {
   if (batch <= 0) return cudaSuccess;
   zdagger_kernel<TC><<<grid_for(batch), NT, 0, s>>>(n, batch, X, Y);
+  count_launch();
   return cudaGetLastError();
 }
 template <typename TC>
@@ -285,6 +288,7 @@ cudaError_t zabssum(int n, long long batch, BatchRef X, double* out, const unsig
                     cudaStream_t s) {
   if (batch <= 0) return cudaSuccess;
   zabssum_kernel<TC><<<grid_for(batch), NT, 0, s>>>(n, batch, X, out, active);
+  count_launch();
   return cudaGetLastError();
 }
 template <typename TC>
@@ -292,6 +296,7 @@ cudaError_t ztrace_current(int n, long long batch, BatchRef X, BatchRef Y1, Batc
                            double sign, const double* fermi, double* out, cudaStream_t s) {
   if (batch <= 0) return cudaSuccess;
   ztrace_current_kernel<TC><<<grid_for(batch), NT, 0, s>>>(n, batch, X, Y1, Y2, sign, fermi, out);
+  count_launch();
   return cudaGetLastError();
 }
 template <typename TC>
@@ -299,6 +304,7 @@ cudaError_t ztrace_prod(int n, long long batch, BatchRef X, BatchRef Y, double s
                         cudaStream_t s) {
   if (batch <= 0) return cudaSuccess;
   ztrace_prod_kernel<TC><<<grid_for(batch), NT, 0, s>>>(n, batch, X, Y, scale, out);
+  count_launch();
   return cudaGetLastError();
 }
 template <typename TC>
@@ -306,6 +312,7 @@ cudaError_t zscale_add(int n, long long batch, BatchRef X, const double* f, Batc
                        cudaStream_t s) {
   if (batch <= 0) return cudaSuccess;
   zscale_add_kernel<TC><<<grid_for(batch), NT, 0, s>>>(n, batch, X, f, W, Y);
+  count_launch();
   return cudaGetLastError();
 }
 template <typename TC>
@@ -313,6 +320,7 @@ cudaError_t zdiag(int n, long long batch, BatchRef X, double* out, long long ost
                   long long ooff, cudaStream_t s) {
   if (batch <= 0) return cudaSuccess;
   zdiag_kernel<TC><<<gdiag(batch * n), NT, 0, s>>>(n, batch, X, out, ostride, ooff);
+  count_launch();
   return cudaGetLastError();
 }
 template <typename TC>
@@ -320,24 +328,28 @@ cudaError_t zdiag_greater(int n, long long batch, BatchRef X, BatchRef Y, double
                           long long ostride, long long ooff, cudaStream_t s) {
   if (batch <= 0) return cudaSuccess;
   zdiag_greater_kernel<TC><<<gdiag(batch * n), NT, 0, s>>>(n, batch, X, Y, out, ostride, ooff);
+  count_launch();
   return cudaGetLastError();
 }
 template <typename TC>
 cudaError_t zcopy(int n, long long batch, BatchRef X, BatchRef Y, cudaStream_t s) {
   if (batch <= 0) return cudaSuccess;
   zconvert_kernel<TC, TC><<<grid_for(batch), NT, 0, s>>>(n, batch, X, Y);
+  count_launch();
   return cudaGetLastError();
 }
 template <typename TS, typename TD>
 cudaError_t zconvert(int n, long long batch, BatchRef X, BatchRef Y, cudaStream_t s) {
   if (batch <= 0) return cudaSuccess;
   zconvert_kernel<TS, TD><<<grid_for(batch), NT, 0, s>>>(n, batch, X, Y);
+  count_launch();
   return cudaGetLastError();
 }
 template <typename TC>
 cudaError_t zcheck_finite(int n, long long batch, BatchRef X, int* status, cudaStream_t s) {
   if (batch <= 0) return cudaSuccess;
   zcheck_finite_kernel<TC><<<grid_for(batch), NT, 0, s>>>(n, batch, X, status);
+  count_launch();
   return cudaGetLastError();
 }
 

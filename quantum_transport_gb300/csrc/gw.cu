@@ -1,0 +1,226 @@
+// GW/SCBA self-energy loop on the GPU (rows of gw_ephoton_3d_ijs,
+// src/gw_mod.f90:444-749, restated for one k-point).
+//
+// Data layout: every energy-resolved quantity (G^{R,<,>}, P, W, Sigma) is an
+// array [nE][nx][nm*nm] of complex128 column-major slab-diagonal blocks -- the
+// block layout qt_rgf_solve reads (sigmas) and writes (full G blocks).  An
+// energy SERIES is one matrix element (i, j) of one slab followed through the
+// energy grid: element stride nx*nm*nm.
+//
+//  * zcorrconv: batched energy correlation / convolution through zero-padded
+//    radix-2 FFTs in shared memory (one CTA per series, L = 2^ceil(log2 2n)),
+//    replacing corr1d2 / conv1d2 + MKL DFTI (src/fft_mod.f90:58-190), which
+//    created a new DFTI descriptor for every series:
+//      corr(X, Y)[m] = sum_e X[e] Y[e - (m - n/2)]
+//      conv(X, W)[e] = sum_m X[e - (m - n/2)] W[m]
+//    FP64 arithmetic: the SCBA residual target (1e-8) is below FP32 resolution.
+//  * sigma_post: Sigma^R <- Re Sigma^R + i Im(Sigma^> - Sigma^<)/2 and the
+//    symmetrisation (Sigma + Sigma^T)/2 (src/gw_mod.f90:698, 731-743).
+//  * mix_residual: linear mixing (:747-749) with the residual norms.
+#include <cmath>
+
+#include "qt_common.cuh"
+#include "qt_kernels.h"
+
+namespace qt {
+
+namespace {
+
+constexpr int FFT_NT = 256;
+constexpr int LMAX = 4096;
+
+__device__ __forceinline__ double2 dmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+__global__ void twiddle_kernel(double2* tw) {
+  // tw[k] = exp(-2 pi i k / LMAX), k < LMAX/2
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < LMAX / 2; k += gridDim.x * blockDim.x) {
+    double s, c;
+    sincospi(-2.0 * k / LMAX, &s, &c);
+    tw[k] = make_double2(c, s);
+  }
+}
+
+// in-place iterative radix-2 DIT on bit-reversed input; sign -1 forward, +1 inverse
+__device__ void fft_smem(double2* a, int L, int logL, const double2* tw, bool inverse) {
+  for (int s = 1; s <= logL; ++s) {
+    const int m = 1 << s, h = m >> 1, step = LMAX / m;
+    for (int t = threadIdx.x; t < L / 2; t += blockDim.x) {
+      const int grp = t >> (s - 1), k = t & (h - 1);
+      const int i0 = grp * m + k, i1 = i0 + h;
+      double2 w = tw[k * step];
+      if (inverse) w.y = -w.y;
+      const double2 u = a[i0], v = dmul(a[i1], w);
+      a[i0] = make_double2(u.x + v.x, u.y + v.y);
+      a[i1] = make_double2(u.x - v.x, u.y - v.y);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(FFT_NT) zcorrconv_kernel(CorrConvArgs a, const double2* tw) {
+  extern __shared__ double2 sm[];
+  const int n = a.n, L = a.L, logL = a.logL;
+  double2* x = sm;
+  double2* y = sm + L;
+  const long long nm2 = (long long)a.nm * a.nm;
+  const double2* X = reinterpret_cast<const double2*>(a.X);
+  const double2* Y = reinterpret_cast<const double2*>(a.Y);
+  double2* Z = reinterpret_cast<double2*>(a.Z);
+  for (long long s = blockIdx.x; s < a.nseries; s += gridDim.x) {
+    const long long ix = s / nm2, ij = s % nm2;
+    const int i = (int)(ij % a.nm), j = (int)(ij / a.nm);
+    const long long sx = ix * nm2 + ij;
+    const long long sy = a.transY ? ix * nm2 + i * (long long)a.nm + j : sx;
+    for (int t = threadIdx.x; t < L; t += blockDim.x) {
+      double2 vx = make_double2(0.0, 0.0), vy = vx;
+      if (t < n) {
+        vx = X[(long long)t * a.estride + sx];
+        if (a.imagX) vx.x = 0.0;
+        const int ty = a.corr ? (n - 1 - t) : t;  // correlation: reversed Y
+        vy = Y[(long long)ty * a.estride + sy];
+        if (a.imagY) vy.x = 0.0;
+        if (a.conjY) vy.y = -vy.y;
+      }
+      const int r = (int)(__brev((unsigned)t) >> (32 - logL));
+      x[r] = vx;
+      y[r] = vy;
+    }
+    __syncthreads();
+    fft_smem(x, L, logL, tw, false);
+    fft_smem(y, L, logL, tw, false);
+    // pointwise product, bit-reversed into y for the inverse transform
+    for (int t = threadIdx.x; t < L; t += blockDim.x) {
+      const double2 p = dmul(x[t], y[t]);
+      x[t] = p;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < L; t += blockDim.x)
+      y[(int)(__brev((unsigned)t) >> (32 - logL))] = x[t];
+    __syncthreads();
+    fft_smem(y, L, logL, tw, true);
+    const double inv = 1.0 / L;
+    const double2 sc = make_double2(a.scale_re * inv, a.scale_im * inv);
+    for (int m = threadIdx.x; m < n; m += blockDim.x) {
+      const int t = a.corr ? (m - n / 2 + n - 1) : (m + n / 2);
+      const double2 v = dmul(y[t], sc);
+      double2* zp = &Z[(long long)m * a.estride + sx];
+      if (a.accumulate) {
+        const double2 o = *zp;
+        *zp = make_double2(o.x + v.x, o.y + v.y);
+      } else {
+        *zp = v;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Sigma^R <- Re Sigma^R + i Im(Sigma^> - Sigma^<)/2, then (S + S^T)/2 for all three,
+// one CTA per (energy, slab) block (src/gw_mod.f90:698, 731-743)
+__global__ void sigma_post_kernel(int nm, long long nblocks, double2* SR, double2* SL,
+                                  double2* SG) {
+  const long long nm2 = (long long)nm * nm;
+  for (long long b = blockIdx.x; b < nblocks; b += gridDim.x) {
+    double2 *r = SR + b * nm2, *l = SL + b * nm2, *g = SG + b * nm2;
+    for (int e = threadIdx.x; e < nm * nm; e += blockDim.x) {
+      const int i = e % nm, j = e / nm;
+      if (i > j) continue;  // the thread owning (i<=j) writes both (i,j) and (j,i)
+      const long long a1 = i + (long long)j * nm, a2 = j + (long long)i * nm;
+      const double2 r1 = r[a1], r2 = r[a2], l1 = l[a1], l2 = l[a2], g1 = g[a1], g2 = g[a2];
+      const double2 rr1 = make_double2(r1.x, 0.5 * (g1.y - l1.y));
+      const double2 rr2 = make_double2(r2.x, 0.5 * (g2.y - l2.y));
+      const double2 rs = make_double2(0.5 * (rr1.x + rr2.x), 0.5 * (rr1.y + rr2.y));
+      const double2 ls = make_double2(0.5 * (l1.x + l2.x), 0.5 * (l1.y + l2.y));
+      const double2 gs = make_double2(0.5 * (g1.x + g2.x), 0.5 * (g1.y + g2.y));
+      r[a1] = rs; r[a2] = rs;
+      l[a1] = ls; l[a2] = ls;
+      g[a1] = gs; g[a2] = gs;
+    }
+  }
+}
+
+// sums[0] += |new - old|^2, sums[1] += |new|^2 over count elements (Sigma^< and Sigma^>)
+__global__ void residual_kernel(long long count, const double2* nl, const double2* ol,
+                                const double2* ng, const double2* og, double* sums) {
+  double d = 0.0, m = 0.0;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < count;
+       t += (long long)gridDim.x * blockDim.x) {
+    const double2 a = nl[t], b = ol[t], c = ng[t], e = og[t];
+    d += (a.x - b.x) * (a.x - b.x) + (a.y - b.y) * (a.y - b.y) + (c.x - e.x) * (c.x - e.x) +
+         (c.y - e.y) * (c.y - e.y);
+    m += a.x * a.x + a.y * a.y + c.x * c.x + c.y * c.y;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    d += __shfl_down_sync(0xffffffffu, d, o);
+    m += __shfl_down_sync(0xffffffffu, m, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&sums[0], d);
+    atomicAdd(&sums[1], m);
+  }
+}
+
+// S <- S + alpha (N - S)   (linear mixing, src/gw_mod.f90:747-749)
+__global__ void mix_kernel(long long count, double alpha, double2* S, const double2* N) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < count;
+       t += (long long)gridDim.x * blockDim.x) {
+    const double2 s = S[t], v = N[t];
+    S[t] = make_double2(s.x + alpha * (v.x - s.x), s.y + alpha * (v.y - s.y));
+  }
+}
+
+inline unsigned g1(long long n) {
+  long long g = (n + 255) / 256;
+  return (unsigned)(g < 1 ? 1 : (g > 65535LL * 8 ? 65535LL * 8 : g));
+}
+
+}  // namespace
+
+cudaError_t gw_twiddles(double2* tw, cudaStream_t s) {
+  twiddle_kernel<<<8, 256, 0, s>>>(tw);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t zcorrconv(CorrConvArgs a, const double2* tw, cudaStream_t s) {
+  if (a.nseries <= 0) return cudaSuccess;
+  int L = 1, logL = 0;
+  while (L < 2 * a.n) { L <<= 1; ++logL; }
+  if (L > LMAX) return cudaErrorInvalidValue;
+  a.L = L;
+  a.logL = logL;
+  const size_t smem = (size_t)2 * L * sizeof(double2);
+  cudaError_t e = cudaFuncSetAttribute(zcorrconv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  const long long g = a.nseries < 65535LL * 16 ? a.nseries : 65535LL * 16;
+  zcorrconv_kernel<<<(unsigned)g, FFT_NT, smem, s>>>(a, tw);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t gw_sigma_post(int nm, long long nblocks, double2* SR, double2* SL, double2* SG,
+                          cudaStream_t s) {
+  const long long g = nblocks < 65535LL * 8 ? nblocks : 65535LL * 8;
+  sigma_post_kernel<<<(unsigned)g, 256, 0, s>>>(nm, nblocks, SR, SL, SG);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t gw_residual(long long count, const double2* nl, const double2* ol, const double2* ng,
+                        const double2* og, double* sums, cudaStream_t s) {
+  residual_kernel<<<g1(count) > 1024 ? 1024 : g1(count), 256, 0, s>>>(count, nl, ol, ng, og, sums);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t gw_mix(long long count, double alpha, double2* S, const double2* N, cudaStream_t s) {
+  mix_kernel<<<g1(count), 256, 0, s>>>(count, alpha, S, N);
+  count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace qt

@@ -6,6 +6,9 @@ namespace qt {
 
 enum { OP_N = 0, OP_C = 1, OP_T = 2 };
 
+// every kernel launch of the library is counted (reported by qt_kernel_launches)
+void count_launch(long long n = 1);
+
 // C_b = alpha * op(A_b) op(B_b) + beta * D_b + z_b * I   (m x n result, inner k)
 struct GemmArgs {
   int m, n, k;
@@ -14,6 +17,7 @@ struct GemmArgs {
   double alpha_re, alpha_im, beta_re, beta_im;
   long long batch;
   const unsigned char* active;  // optional per-batch mask: skip entry when 0
+  int* scales;  // split-precision scratch: batch x 256 ints (row / column exponents)
 };
 
 cudaError_t zgemm_f64(const GemmArgs& a, cudaStream_t s);
@@ -87,5 +91,29 @@ cudaError_t zconvert(int n, long long batch, BatchRef X, BatchRef Y, cudaStream_
 // status_b |= PT_NONFINITE if any element of X_b is not finite
 template <typename TC>
 cudaError_t zcheck_finite(int n, long long batch, BatchRef X, int* status, cudaStream_t s);
+
+// ---- GW/SCBA (gw.cu): energy series of element (i,j) of slab ix, arrays [nE][nx][nm*nm]
+struct CorrConvArgs {
+  int n;              // energies per series
+  int nm;             // block size
+  long long nseries;  // nx * nm * nm
+  long long estride;  // element stride between consecutive energies (nx * nm * nm)
+  const void* X;
+  const void* Y;
+  void* Z;
+  int corr;           // 1: correlation (Y reversed), 0: convolution
+  int transY;         // Y series is the transposed element (j, i)
+  int conjY, imagX, imagY;  // conj(Y); Re(X) := 0; Re(Y) := 0 (applied before conj)
+  int accumulate;     // Z += result
+  double scale_re, scale_im;
+  int L, logL;        // set by the launcher
+};
+cudaError_t gw_twiddles(double2* tw, cudaStream_t s);  // 2048 entries exp(-2 pi i k / 4096)
+cudaError_t zcorrconv(CorrConvArgs a, const double2* tw, cudaStream_t s);
+cudaError_t gw_sigma_post(int nm, long long nblocks, double2* SR, double2* SL, double2* SG,
+                          cudaStream_t s);
+cudaError_t gw_residual(long long count, const double2* nl, const double2* ol, const double2* ng,
+                        const double2* og, double* sums, cudaStream_t s);
+cudaError_t gw_mix(long long count, double alpha, double2* S, const double2* N, cudaStream_t s);
 
 }  // namespace qt

@@ -18,6 +18,7 @@
 //   6. left-contact current tre (src/cuda_rgf_mod.f90:387-407)
 //   7. optional Caroli T(E) from the left-connected chain G_{N1}.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -42,6 +43,12 @@ extern "C" void qt_set_last_error(const char* msg, const char* file, int line) {
 }
 
 extern "C" const char* qt_last_error(void) { return g_last_error.c_str(); }
+
+namespace {
+std::atomic<long long> g_launches{0};
+}
+void qt::count_launch(long long n) { g_launches += n; }
+extern "C" int64_t qt_kernel_launches(void) { return g_launches.load(); }
 extern "C" const char* qt_version(void) { return "qtgpu 0.1 sm_103a"; }
 
 #define QT_FAIL(code, msg)                             \
@@ -56,7 +63,32 @@ extern "C" const char* qt_version(void) { return "qtgpu 0.1 sm_103a"; }
     if (_s != QT_OK) return _s;                        \
   } while (0)
 
+// Optional CUDA-event timing of the block products and inverses on the
+// context's stream (qt_ctx_profile): kinds 0 complex64 split product,
+// 1 complex128 split product, 2 FP64 product, 3 FP32 inverse, 4 FP64 inverse.
+struct Prof {
+  struct Entry {
+    int kind;
+    cudaEvent_t a, b;
+    double alg, tensor;
+  };
+  bool on = false;
+  std::vector<Entry> v;
+  std::vector<cudaEvent_t> pool;
+  cudaEvent_t get() {
+    if (!pool.empty()) {
+      cudaEvent_t e = pool.back();
+      pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+  }
+};
+
 struct qt_ctx {
+  Prof prof;
   int device = 0;
   cudaStream_t stream = nullptr;
   int64_t scratch_limit = 48LL << 30;
@@ -171,6 +203,8 @@ struct Ops {
   int slices = 4;
   int refine = 1;
   const cd* one = nullptr;  // device scalar (1, 0)
+  Prof* prof = nullptr;     // optional launch timing
+  int* scales = nullptr;    // P * 256 ints: exponent scratch of the split product
   TC* rt1 = nullptr;        // P * n*n refinement scratch
   TC* rt2 = nullptr;
   long long P = 0;
@@ -185,13 +219,36 @@ struct Ops {
     g.alpha_re = alpha.x; g.alpha_im = alpha.y; g.beta_re = beta.x; g.beta_im = beta.y;
     g.batch = batch;
     g.active = active;
+    g.scales = scales;
+    if (prec != QT_PREC_FP64 && (!scales || batch > P)) QT_FAIL(QT_ERR_ARG, "split product scratch too small");
     cudaError_t e;
+    const bool timed = prof && prof->on;
+    cudaEvent_t ea = nullptr, eb = nullptr;
+    if (timed) { ea = prof->get(); eb = prof->get(); cudaEventRecord(ea, s); }
+    int kind;
     if constexpr (sizeof(TC) == 16) {
+      kind = prec == QT_PREC_FP64 ? 2 : 1;
       e = prec == QT_PREC_FP64 ? qt::zgemm_f64(g, s) : qt::zgemm_oz(g, slices, slices - 1, s);
     } else {
+      kind = 0;
       e = qt::zgemm_oz_c64(g, slices, s);
     }
     if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+    if (timed) {
+      cudaEventRecord(eb, s);
+      // algorithmic: 8 n^3 real flops per complex block product; executed on the tensor
+      // pipe: 2 real parts x digit pairs x 2 x 128 x npad x K'
+      const double alg = 8.0 * n * (double)n * n * batch;
+      double tens = 0.0;
+      if (kind != 2) {
+        const int L = slices - 1, npad = (n + 15) / 16 * 16, kp = (n + 31) / 32 * 32;
+        int pairs = 0;
+        for (int a = 0; a < slices; ++a)
+          for (int b = 0; b < slices; ++b) pairs += (a + b <= L);
+        tens = 2.0 * pairs * 2.0 * 128.0 * npad * (2.0 * kp) * batch;
+      }
+      prof->v.push_back({kind, ea, eb, alg, tens});
+    }
     return QT_OK;
   }
   // X = inv(A); A is preserved (X must differ from A in the split path)
@@ -200,15 +257,21 @@ struct Ops {
     qt::InvArgs a;
     a.n = n; a.A = A; a.X = X; a.batch = batch; a.status = status; a.active = active;
     cudaError_t e;
+    const bool timed = prof && prof->on;
+    cudaEvent_t ea = nullptr, eb = nullptr;
+    if (timed) { ea = prof->get(); eb = prof->get(); cudaEventRecord(ea, s); }
+    const double alg = 8.0 * n * (double)n * n * batch;  // inversion counted as one n^3 product
     if (prec == QT_PREC_FP64) {
       if constexpr (sizeof(TC) == 16) e = qt::zinv_f64(a, s);
       else e = cudaErrorInvalidValue;
       if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+      if (timed) { cudaEventRecord(eb, s); prof->v.push_back({4, ea, eb, alg, 0.0}); }
       return QT_OK;
     }
     if (X.p == A.p) QT_FAIL(QT_ERR_ARG, "split-precision inverse needs X != A");
     e = qt::zinv_f32<TC>(a, s);
     if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+    if (timed) { cudaEventRecord(eb, s); prof->v.push_back({3, ea, eb, alg, 0.0}); }
     if (refine > 0 && (batch > P || !rt1 || !rt2)) QT_FAIL(QT_ERR_ARG, "refinement scratch too small");
     const BatchRef R = ref(rt1, (long long)n * n, n), T = ref(rt2, (long long)n * n, n);
     for (int it = 0; it < refine; ++it) {
@@ -249,7 +312,7 @@ size_t wave_bytes(const Problem& pb, long long P) {
   const size_t tc = pb.prec == QT_PREC_FP64 ? 16 : 8;
   const size_t sweep = (2 * (size_t)pb.nx + 14 + 2) * tc;  // g_l, g^<_l, temporaries, refinement
   const size_t lead = (7 + 2 + 6) * 16;                     // Sancho state + refinement + contact
-  return (sweep + lead) * nm2 * P + (size_t)P * 512 + (512 << 10);
+  return (sweep + lead) * nm2 * P + (size_t)P * (512 + 2048) + (512 << 10);
 }
 
 // Batched Sancho-Rubio on the wave (complex128 state).  H00 per point, H_10 the
@@ -271,6 +334,7 @@ qt_status sancho_wave(const Ops<double2>& op0, Arena& ar, long long P, BatchRef 
   if (op.prec != QT_PREC_FP64) {
     op.rt1 = reinterpret_cast<double2*>(ar.take<cd>((size_t)P * nm2));
     op.rt2 = reinterpret_cast<double2*>(ar.take<cd>((size_t)P * nm2));
+    if (!op.scales || op.P < P) op.scales = ar.take<int>((size_t)P * 256);
     op.P = P;
     if (!op.rt1 || !op.rt2) QT_FAIL(QT_ERR_NOMEM, "wave arena exhausted (sancho refinement)");
   }
@@ -313,6 +377,7 @@ qt_status sancho_wave(const Ops<double2>& op0, Arena& ar, long long P, BatchRef 
     qt::zabssum<double2>(n, P, H01, err, active, s);
     cudaMemsetAsync(nact, 0, sizeof(int), s);
     sancho_update_kernel<<<g1d(P), 256, 0, s>>>(P, err, tol, it, active, iters, nact);
+    qt::count_launch();
     if ((it % 4) == 0 || it == max_iter) {
       int h = 0;
       cudaMemcpyAsync(&h, nact, sizeof(int), cudaMemcpyDeviceToHost, s);
@@ -322,6 +387,7 @@ qt_status sancho_wave(const Ops<double2>& op0, Arena& ar, long long P, BatchRef 
     }
   }
   flag_unconverged_kernel<<<g1d(P), 256, 0, s>>>(P, active, status);
+  qt::count_launch();
   // G00 = (z S - H_SS)^-1 ; GBB = (z S - H_BB)^-1    (:740-761)
   qt::zaxpby<double2>(n, P, HSS, -1, 0, nullref(), 0, 0, Zl, C, nullptr, s);
   QT_TRY(op.inv(C, G00, P, status));
@@ -370,33 +436,43 @@ qt_status solve_wave(qt_ctx* ctx, const Problem& pb, long long p0, long long P, 
   TC* rt1 = ar.take<TC>((size_t)P * nm2);
   TC* rt2 = ar.take<TC>((size_t)P * nm2);
   cd* cbuf = ar.take<cd>((size_t)6 * P * nm2);      // complex128 contact scratch
+  int* scales = ar.take<int>((size_t)P * 256);       // split-product exponent scratch
   if (!zint || !zlead || !fl || !fr || !fe || !one || !status || !gl_all || !gln_all || !tmp ||
-      !rt1 || !rt2 || !cbuf)
+      !rt1 || !rt2 || !cbuf || !scales)
     QT_FAIL(QT_ERR_NOMEM, "wave arena exhausted");
   // sweep operations on TC, contact operations on complex128
   Ops<TC> op{s, n, pb.prec};
   op.slices = pb.sweep_slices;
   op.refine = split ? 1 : 0;
-  op.one = one; op.rt1 = rt1; op.rt2 = rt2; op.P = P;
+  op.one = one; op.rt1 = rt1; op.rt2 = rt2; op.P = P; op.scales = scales;
+  op.prof = &ctx->prof;
   Ops<double2> cop{s, n, pb.prec};
+  cop.prof = &ctx->prof;
   cop.slices = pb.lead_slices;
   cop.refine = split ? 2 : 0;
   cop.one = one;
+  cop.scales = scales;
+  cop.P = P;
 
   const cd h1{1.0, 0.0};
   cudaMemcpyAsync(one, &h1, sizeof(cd), cudaMemcpyHostToDevice, s);
   cudaMemsetAsync(status, 0, P * sizeof(int), s);
   make_z_kernel<<<g1d(P), 256, 0, s>>>(pb.E, p0, P, nk, pb.c.eta_interior, zint);
+  qt::count_launch();
   make_z_kernel<<<g1d(P), 256, 0, s>>>(pb.E, p0, P, nk, pb.c.eta_lead, zlead);
+  qt::count_launch();
   // Contact Fermi pairings: GPU routine src/cuda_rgf_mod.f90:113 (mul,TEMPl), :242 (mur,TEMPl),
   // :388 (mul,TEMPr); CPU routine src/rgf_mod.f90:100 (mur,TEMPr), :182 (mul,TEMPl), :258 (mur,TEMPr).
   const bool cpu = (q & QT_QUIRK_CPU_FERMI) != 0;
   make_fermi_kernel<<<g1d(P), 256, 0, s>>>(pb.E, p0, P, nk, cpu ? pb.c.mur : pb.c.mul,
                                            cpu ? pb.c.tempr : pb.c.templ, fl);
+  qt::count_launch();
   make_fermi_kernel<<<g1d(P), 256, 0, s>>>(pb.E, p0, P, nk, cpu ? pb.c.mul : pb.c.mur, pb.c.templ,
                                            fr);
+  qt::count_launch();
   make_fermi_kernel<<<g1d(P), 256, 0, s>>>(pb.E, p0, P, nk, cpu ? pb.c.mur : pb.c.mul, pb.c.tempr,
                                            fe);
+  qt::count_launch();
   const double tr_sign = cpu ? 1.0 : -1.0;
 
   const bool c64 = sizeof(TC) == 8;
@@ -630,6 +706,9 @@ extern "C" qt_status qt_ctx_destroy(qt_ctx* c) {
   cudaStreamSynchronize(c->stream);
   if (c->arena) cudaFree(c->arena);
   if (c->io) cudaFree(c->io);
+  if (c->conv) cudaFree(c->conv);
+  for (auto& e : c->prof.v) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
+  for (auto e : c->prof.pool) cudaEventDestroy(e);
   cudaStreamDestroy(c->stream);
   delete c;
   return QT_OK;
@@ -644,6 +723,41 @@ extern "C" qt_status qt_ctx_sync(qt_ctx* c) {
 extern "C" qt_status qt_ctx_set_scratch_limit(qt_ctx* c, int64_t bytes) {
   if (!c || bytes <= 0) QT_FAIL(QT_ERR_ARG, "bad scratch limit");
   c->scratch_limit = bytes;
+  return QT_OK;
+}
+
+extern "C" qt_status qt_ctx_profile(qt_ctx* c, int enable) {
+  if (!c) QT_FAIL(QT_ERR_ARG, "null ctx");
+  c->prof.on = enable != 0;
+  return QT_OK;
+}
+
+extern "C" qt_status qt_ctx_profile_read(qt_ctx* c, int kind, int64_t* launches, double* ms,
+                                         double* alg_flops, double* tensor_flops) {
+  if (!c) QT_FAIL(QT_ERR_ARG, "null ctx");
+  QT_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  int64_t nl = 0;
+  double t = 0.0, fa = 0.0, ft = 0.0;
+  std::vector<Prof::Entry> keep;
+  for (auto& e : c->prof.v) {
+    if (e.kind != kind) { keep.push_back(e); continue; }
+    float x = 0.f;
+    cudaEventElapsedTime(&x, e.a, e.b);
+    ++nl; t += x; fa += e.alg; ft += e.tensor;
+    c->prof.pool.push_back(e.a);
+    c->prof.pool.push_back(e.b);
+  }
+  c->prof.v.swap(keep);
+  if (launches) *launches = nl;
+  if (ms) *ms = t;
+  if (alg_flops) *alg_flops = fa;
+  if (tensor_flops) *tensor_flops = ft;
+  return QT_OK;
+}
+
+extern "C" qt_status qt_ctx_stream(qt_ctx* c, void** stream) {
+  if (!c || !stream) QT_FAIL(QT_ERR_ARG, "null argument");
+  *stream = (void*)c->stream;
   return QT_OK;
 }
 
@@ -672,6 +786,7 @@ qt_status run_problem(qt_ctx* ctx, Problem& pb, long long hii_n, long long h1i_n
     auto conv = [&](const cd* src, long long count) -> const float2* {
       if (!src) return nullptr;
       flat_d2f_kernel<<<g1d(count), 256, 0, s>>>(reinterpret_cast<const double2*>(src), c, count);
+      qt::count_launch();
       const float2* r = c;
       c += count;
       return r;
@@ -852,7 +967,7 @@ extern "C" qt_status qt_sancho_batch(qt_ctx* ctx, int nm, int npts, const double
   // scratch: z, status, iters, 2 refinement blocks + Sancho state (7 blocks)
   const size_t need = (size_t)P * nm2 * sizeof(cd) * (9 + (devp ? 0 : 2)) + (size_t)P * 64 +
                       (h00_stride ? P : 1) * nm2 * 16 + (h10_stride ? P : 1) * nm2 * 16 +
-                      (size_t)P * 8 + (1 << 20);
+                      (size_t)P * 1100 + (1 << 20);
   QT_TRY(ensure(ctx->arena, ctx->arena_bytes, need));
   Arena ar{reinterpret_cast<char*>(ctx->arena), ctx->arena_bytes, 0};
   cudaStream_t s = ctx->stream;
@@ -884,6 +999,7 @@ extern "C" qt_status qt_sancho_batch(qt_ctx* ctx, int nm, int npts, const double
   }
   if (!one || !z || !st || !it || !g00) QT_FAIL(QT_ERR_NOMEM, "arena exhausted");
   make_z_kernel<<<g1d(P), 256, 0, s>>>(Ed, 0, P, 1, eta, z);
+  qt::count_launch();
   cudaMemsetAsync(st, 0, P * 4, s);
   QT_TRY(sancho_wave(op, ar, P, ref(h00, h00_stride ? nm2 : 0, nm), ref(h10, h10_stride ? nm2 : 0, nm),
                      false, z, tol, max_iter, ref(g00, nm2, nm), gbb ? ref(gbb, nm2, nm) : nullref(),
@@ -950,6 +1066,11 @@ extern "C" qt_status qt_zgemm_batch(qt_ctx* ctx, int n, int batch, char opA, con
   g.opA = oa; g.opB = ob;
   g.alpha_re = al.x; g.alpha_im = al.y; g.beta_re = be.x; g.beta_im = be.y;
   g.batch = batch; g.active = nullptr;
+  g.scales = nullptr;
+  if (prec == QT_PREC_MIXED) {
+    QT_TRY(ensure(ctx->arena, ctx->arena_bytes, (size_t)batch * 1024 + 4096));
+    g.scales = reinterpret_cast<int*>(ctx->arena);
+  }
   const int sl = slices ? slices : 4;
   if (prec == QT_PREC_MIXED && sl != 4 && sl != 6 && sl != 7)
     QT_FAIL(QT_ERR_UNSUPPORTED, "complex128 split product supports 4, 6 or 7 digits");
@@ -973,7 +1094,7 @@ extern "C" qt_status qt_zinv_batch(qt_ctx* ctx, int n, int batch, const double* 
   const long long nm2 = (long long)n * n;
   const bool devp = (flags & QT_FLAG_DEVICE_POINTERS) != 0;
   const long long P = batch;
-  const size_t need = (size_t)P * nm2 * 16 * (2 + (devp ? 0 : 2)) + (size_t)P * 8 + (1 << 20);
+  const size_t need = (size_t)P * nm2 * 16 * (3 + (devp ? 0 : 2)) + (size_t)P * 1100 + (1 << 20);
   QT_TRY(ensure(ctx->arena, ctx->arena_bytes, need));
   Arena ar{reinterpret_cast<char*>(ctx->arena), ctx->arena_bytes, 0};
   Ops<double2> op{s, n, prec};
@@ -986,6 +1107,7 @@ extern "C" qt_status qt_zinv_batch(qt_ctx* ctx, int n, int batch, const double* 
   op.one = one;
   op.rt1 = reinterpret_cast<double2*>(ar.take<cd>(P * nm2));
   op.rt2 = reinterpret_cast<double2*>(ar.take<cd>(P * nm2));
+  op.scales = ar.take<int>(P * 256);
   int* st = ar.take<int>(P);
   const cd* a = reinterpret_cast<const cd*>(A);
   cd* x = reinterpret_cast<cd*>(X);
@@ -1004,7 +1126,7 @@ extern "C" qt_status qt_zinv_batch(qt_ctx* ctx, int n, int batch, const double* 
     cudaMemcpyAsync(ad, A, P * nm2 * 16, cudaMemcpyDeviceToDevice, s);
     a = ad; as = nm2;
   }
-  if (!st || !op.rt2) QT_FAIL(QT_ERR_NOMEM, "arena exhausted");
+  if (!st || !op.rt2 || !op.scales) QT_FAIL(QT_ERR_NOMEM, "arena exhausted");
   cudaMemsetAsync(st, 0, P * 4, s);
   QT_TRY(op.inv(ref(a, as, n), ref(x, xs, n), P, st));
   if (!devp) {
@@ -1015,5 +1137,252 @@ extern "C" qt_status qt_zinv_batch(qt_ctx* ctx, int n, int batch, const double* 
     cudaMemcpyAsync(status, st, P * 4, cudaMemcpyDeviceToDevice, s);
   }
   QT_CUDA_TRY(cudaStreamSynchronize(s));
+  return QT_OK;
+}
+
+// ================================================================ GW / SCBA
+// One evaluation of the SCBA map Sigma -> Sigma_new for one k-point
+// (gw_ephoton_3d_ijs, src/gw_mod.f90:368-749): G by the batched RGF with the
+// scattering self-energies (green_RGF_RS, :1131-1345), P by energy
+// correlations of the Re-zeroed G (:444-519), W per slab-diagonal block
+// (green_rgf_calc_w is absent from the reference; restated as
+// W^R = (I - V P^R)^-1 V, W^{<,>} = W^R P^{<,>} W^R^+), Sigma by energy
+// convolutions (:646-698), recombination + symmetrisation (:698, 731-743) and
+// the edge-block copy (:950-959).
+namespace {
+
+struct GwBuffers {
+  cd *GR, *GL, *GG, *PR, *PL, *PG, *T1, *T2, *NR, *NL, *NG;
+  double2* tw;
+  double* sums;
+};
+
+qt_status gw_map(qt_ctx* ctx, Problem pb, const cd* V, double spindeg, const cd* SR,
+                 const cd* SL, GwBuffers& w, long long hii_n, long long h1i_n) {
+  cudaStream_t s = ctx->stream;
+  const int nm = pb.nm, nx = pb.nx;
+  const long long nE = pb.npts;  // nk == 1
+  const long long nm2 = (long long)nm * nm, nblk = nE * nx, cnt = nblk * nm2;
+  // ---- G with the current self-energies
+  pb.sigr = SR;
+  pb.sigl = SL;
+  pb.tr = pb.tre = pb.T = pb.dgr = pb.dgl = pb.dgg = nullptr;
+  pb.Gr = w.GR; pb.Gl = w.GL; pb.Gg = w.GG;
+  pb.flags &= ~QT_FLAG_CAROLI;
+  QT_TRY(run_problem(ctx, pb, hii_n, h1i_n));
+  // ---- polarisation: energy correlations of Re-zeroed G, x -i dE/(2 pi) spindeg
+  double dE = 0.0;
+  {
+    double e2[2] = {0, 0};
+    cudaMemcpyAsync(e2, pb.E, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
+    QT_CUDA_TRY(cudaStreamSynchronize(s));
+    dE = e2[1] - e2[0];
+  }
+  const double pf = dE / (2.0 * M_PI) * spindeg;  // P scale = -i * pf
+  qt::CorrConvArgs c{};
+  c.n = (int)nE; c.nm = nm; c.nseries = nx * nm2; c.estride = nx * nm2;
+  auto cc = [&](const cd* X, const cd* Y, cd* Z, int corr, int transY, int conjY, int imX,
+                int imY, int acc, double sr, double si) -> qt_status {
+    qt::CorrConvArgs a = c;
+    a.X = X; a.Y = Y; a.Z = Z; a.corr = corr; a.transY = transY; a.conjY = conjY;
+    a.imagX = imX; a.imagY = imY; a.accumulate = acc; a.scale_re = sr; a.scale_im = si;
+    cudaError_t e = qt::zcorrconv(a, w.tw, s);
+    if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+    return QT_OK;
+  };
+  QT_TRY(cc(w.GL, w.GG, w.PL, 1, 1, 0, 1, 1, 0, 0.0, -pf));        // P^< = corr(G^<_ij, G^>_ji)
+  QT_TRY(cc(w.GG, w.GL, w.PG, 1, 1, 0, 1, 1, 0, 0.0, -pf));        // P^> = corr(G^>_ij, G^<_ji)
+  QT_TRY(cc(w.GL, w.GR, w.PR, 1, 0, 1, 1, 1, 0, 0.0, -pf));        // corr(G^<_ij, conj G^R_ij)
+  QT_TRY(cc(w.GR, w.GL, w.PR, 1, 1, 0, 1, 1, 1, 0.0, -pf));        //   + corr(G^R_ij, G^<_ji)
+  // ---- screened interaction per (w, slab) block
+  Ops<double2> op{s, nm, pb.prec};
+  op.slices = pb.lead_slices;
+  op.refine = pb.prec == QT_PREC_FP64 ? 0 : 2;
+  op.prof = &ctx->prof;
+  {
+    const size_t need_extra = (size_t)nblk * 1024 + 2 * (size_t)nblk * nm2 * 16 + 4096;
+    QT_TRY(ensure(ctx->arena, ctx->arena_bytes, need_extra));
+    Arena ar{reinterpret_cast<char*>(ctx->arena), ctx->arena_bytes, 0};
+    cd* one = ar.take<cd>(1);
+    const cd h1{1.0, 0.0};
+    cudaMemcpyAsync(one, &h1, sizeof(cd), cudaMemcpyHostToDevice, s);
+    op.one = one;
+    op.scales = ar.take<int>((size_t)nblk * 256);
+    op.rt1 = reinterpret_cast<double2*>(ar.take<cd>((size_t)nblk * nm2));
+    op.rt2 = reinterpret_cast<double2*>(ar.take<cd>((size_t)nblk * nm2));
+    op.P = nblk;
+    if (!op.scales || !op.rt2) QT_FAIL(QT_ERR_NOMEM, "arena exhausted (W)");
+    const BatchRef Vr = ref(V, 0, nm), B = ref(nullptr, nm2, nm);
+    auto blk = [&](const cd* p) { BatchRef r = B; r.p = const_cast<cd*>(p); return r; };
+    // T1 = I - V P^R ; T2 = T1^-1 ; W^R (-> NR scratch) = T2 V
+    QT_TRY(op.gemm(Vr, qt::OP_N, blk(w.PR), qt::OP_N, blk(w.T1), nblk, {-1, 0}, nullref(),
+                   {0, 0}, ref(one, 0, 1)));
+    QT_TRY(op.inv(blk(w.T1), blk(w.T2), nblk, nullptr));
+    QT_TRY(op.gemm(blk(w.T2), qt::OP_N, Vr, qt::OP_N, blk(w.NR), nblk));
+    // W^< = W^R P^< W^R^+ (-> PL), W^> (-> PG)
+    QT_TRY(op.gemm(blk(w.NR), qt::OP_N, blk(w.PL), qt::OP_N, blk(w.T1), nblk));
+    QT_TRY(op.gemm(blk(w.T1), qt::OP_N, blk(w.NR), qt::OP_C, blk(w.PL), nblk));
+    QT_TRY(op.gemm(blk(w.NR), qt::OP_N, blk(w.PG), qt::OP_N, blk(w.T1), nblk));
+    QT_TRY(op.gemm(blk(w.T1), qt::OP_N, blk(w.NR), qt::OP_C, blk(w.PG), nblk));
+    qt::zcopy<double2>(nm, nblk, blk(w.NR), blk(w.PR), s);  // W^R -> PR
+  }
+  // ---- self-energy: energy convolutions x i dE / (2 pi)
+  const double sf = dE / (2.0 * M_PI);
+  QT_TRY(cc(w.GL, w.PL, w.NL, 0, 0, 0, 1, 0, 0, 0.0, sf));  // Sigma^< = conv(G^<, W^<)
+  QT_TRY(cc(w.GG, w.PG, w.NG, 0, 0, 0, 1, 0, 0, 0.0, sf));  // Sigma^> = conv(G^>, W^>)
+  QT_TRY(cc(w.GL, w.PR, w.NR, 0, 0, 0, 1, 0, 0, 0.0, sf));  // Sigma^R = conv(G^<, W^R)
+  QT_TRY(cc(w.GR, w.PL, w.NR, 0, 0, 0, 1, 0, 1, 0.0, sf));  //   + conv(G^R, W^<)
+  QT_TRY(cc(w.GR, w.PR, w.NR, 0, 0, 0, 1, 0, 1, 0.0, sf));  //   + conv(G^R, W^R)
+  cudaError_t e = qt::gw_sigma_post(nm, nblk, reinterpret_cast<double2*>(w.NR),
+                                    reinterpret_cast<double2*>(w.NL),
+                                    reinterpret_cast<double2*>(w.NG), s);
+  if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+  // ---- edge blocks 1,2 <- 3 and nx-1,nx <- nx-2 (src/gw_mod.f90:950-959)
+  if (nx >= 5) {
+    for (cd* S : {w.NR, w.NL, w.NG}) {
+      auto slab = [&](int l) { return ref(S + l * nm2, nx * nm2, nm); };
+      qt::zcopy<double2>(nm, nE, slab(2), slab(0), s);
+      qt::zcopy<double2>(nm, nE, slab(2), slab(1), s);
+      qt::zcopy<double2>(nm, nE, slab(nx - 3), slab(nx - 1), s);
+      qt::zcopy<double2>(nm, nE, slab(nx - 3), slab(nx - 2), s);
+    }
+  }
+  (void)cnt;
+  return QT_OK;
+}
+
+qt_status gw_setup(qt_ctx* ctx, const qt_device* dev, const double* E, int nE,
+                   const qt_contacts* c, qt_precision prec, unsigned flags, Problem& pb,
+                   long long& hii_n, long long& h1i_n) {
+  if (!ctx || !dev || !E || !c) QT_FAIL(QT_ERR_ARG, "null argument");
+  if (!(flags & QT_FLAG_DEVICE_POINTERS)) QT_FAIL(QT_ERR_UNSUPPORTED, "GW entry points take device pointers");
+  if (dev->nk != 1) QT_FAIL(QT_ERR_UNSUPPORTED, "GW path: one k-point");
+  if (dev->nm <= 0 || dev->nx < 2 || nE < 2) QT_FAIL(QT_ERR_ARG, "need nm > 0, nx >= 2, nE >= 2");
+  if (2 * nE > 4096) QT_FAIL(QT_ERR_UNSUPPORTED, "GW path: nE <= 2048 (FFT length 4096)");
+  if (dev->Sii) QT_FAIL(QT_ERR_UNSUPPORTED, "Sii must be NULL (identity overlap)");
+  if (prec == QT_PREC_MIXED && dev->nm > 128) QT_FAIL(QT_ERR_UNSUPPORTED, "mixed path needs nm <= 128");
+  cudaSetDevice(ctx->device);
+  pb = Problem{};
+  pb.nm = dev->nm; pb.nx = dev->nx; pb.nk = 1; pb.npts = nE;
+  pb.Hii = reinterpret_cast<const cd*>(dev->Hii); pb.hk = 0; pb.hl = dev->hii_lstride;
+  pb.H1i = reinterpret_cast<const cd*>(dev->H1i); pb.h1k = 0; pb.h1l = dev->h1i_lstride;
+  pb.E = E; pb.c = *c; pb.prec = prec; pb.flags = flags;
+  const long long nm2 = (long long)dev->nm * dev->nm;
+  hii_n = (pb.hl ? (dev->nx - 1) * pb.hl : 0) + nm2;
+  h1i_n = (pb.h1l ? dev->nx * pb.h1l : 0) + nm2;
+  return QT_OK;
+}
+
+struct GwAlloc {
+  void* p = nullptr;
+  ~GwAlloc() { if (p) cudaFree(p); }
+};
+
+qt_status gw_alloc(qt_ctx* ctx, long long cnt, GwBuffers& w, GwAlloc& hold) {
+  const size_t blk = (size_t)cnt * sizeof(cd);
+  const size_t need = 11 * blk + 2048 * sizeof(double2) + 64;
+  if (cudaMalloc(&hold.p, need) != cudaSuccess) {
+    cudaGetLastError();
+    QT_FAIL(QT_ERR_NOMEM, "GW buffers");
+  }
+  char* b = reinterpret_cast<char*>(hold.p);
+  cd** slots[] = {&w.GR, &w.GL, &w.GG, &w.PR, &w.PL, &w.PG, &w.T1, &w.T2, &w.NR, &w.NL, &w.NG};
+  for (int i = 0; i < 11; ++i) *slots[i] = reinterpret_cast<cd*>(b + i * blk);
+  w.tw = reinterpret_cast<double2*>(b + 11 * blk);
+  w.sums = reinterpret_cast<double*>(b + 11 * blk + 2048 * sizeof(double2));
+  cudaError_t e = qt::gw_twiddles(w.tw, ctx->stream);
+  if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+  return QT_OK;
+}
+
+}  // namespace
+
+extern "C" qt_status qt_gw_step(qt_ctx* ctx, const qt_device* dev, const double* E, int nE,
+                                const qt_contacts* c, const double* V, double spindeg,
+                                qt_precision prec, unsigned flags, const double* sigma_r,
+                                const double* sigma_lesser, double* new_r, double* new_lesser,
+                                double* new_greater) {
+  Problem pb;
+  long long hn, h1n;
+  QT_TRY(gw_setup(ctx, dev, E, nE, c, prec, flags, pb, hn, h1n));
+  if (!V || !sigma_r || !sigma_lesser || !new_r || !new_lesser || !new_greater)
+    QT_FAIL(QT_ERR_ARG, "null GW array");
+  const long long cnt = (long long)nE * dev->nx * dev->nm * dev->nm;
+  GwBuffers w{};
+  GwAlloc hold;
+  QT_TRY(gw_alloc(ctx, cnt, w, hold));
+  QT_TRY(gw_map(ctx, pb, reinterpret_cast<const cd*>(V), spindeg,
+                reinterpret_cast<const cd*>(sigma_r), reinterpret_cast<const cd*>(sigma_lesser),
+                w, hn, h1n));
+  cudaStream_t s = ctx->stream;
+  cudaMemcpyAsync(new_r, w.NR, cnt * 16, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(new_lesser, w.NL, cnt * 16, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(new_greater, w.NG, cnt * 16, cudaMemcpyDeviceToDevice, s);
+  QT_CUDA_TRY(cudaStreamSynchronize(s));
+  if (prec != QT_PREC_FP64 && qt::oz_timeouts_and_reset())
+    QT_FAIL(QT_ERR_CUDA, "tensor-core kernel wait timed out");
+  return QT_OK;
+}
+
+extern "C" qt_status qt_scba_solve(qt_ctx* ctx, const qt_device* dev, const double* E, int nE,
+                                   const qt_contacts* c, const double* V, double spindeg,
+                                   double alpha, double tol, int max_iter, qt_precision prec,
+                                   unsigned flags, double* sigma_r, double* sigma_lesser,
+                                   double* sigma_greater, double* residuals, int* iters) {
+  Problem pb;
+  long long hn, h1n;
+  QT_TRY(gw_setup(ctx, dev, E, nE, c, prec, flags, pb, hn, h1n));
+  if (!V || !sigma_r || !sigma_lesser || !sigma_greater || max_iter <= 0)
+    QT_FAIL(QT_ERR_ARG, "bad SCBA arguments");
+  const long long cnt = (long long)nE * dev->nx * dev->nm * dev->nm;
+  GwBuffers w{};
+  GwAlloc hold;
+  QT_TRY(gw_alloc(ctx, cnt, w, hold));
+  cudaStream_t s = ctx->stream;
+  double2* SR = reinterpret_cast<double2*>(sigma_r);
+  double2* SL = reinterpret_cast<double2*>(sigma_lesser);
+  double2* SG = reinterpret_cast<double2*>(sigma_greater);
+  int it = 0;
+  for (; it < max_iter; ++it) {
+    QT_TRY(gw_map(ctx, pb, reinterpret_cast<const cd*>(V), spindeg, reinterpret_cast<cd*>(SR),
+                  reinterpret_cast<cd*>(SL), w, hn, h1n));
+    cudaMemsetAsync(w.sums, 0, 2 * sizeof(double), s);
+    qt::gw_residual(cnt, reinterpret_cast<double2*>(w.NL), SL, reinterpret_cast<double2*>(w.NG),
+                    SG, w.sums, s);
+    double h[2];
+    cudaMemcpyAsync(h, w.sums, sizeof(h), cudaMemcpyDeviceToHost, s);
+    QT_CUDA_TRY(cudaStreamSynchronize(s));
+    const double r = std::sqrt(h[0]) / std::max(std::sqrt(h[1]), 1e-300);
+    if (residuals) residuals[it] = r;
+    // linear mixing (src/gw_mod.f90:747-749)
+    qt::gw_mix(cnt, alpha, SR, reinterpret_cast<double2*>(w.NR), s);
+    qt::gw_mix(cnt, alpha, SL, reinterpret_cast<double2*>(w.NL), s);
+    qt::gw_mix(cnt, alpha, SG, reinterpret_cast<double2*>(w.NG), s);
+    if (r <= tol) { ++it; break; }
+  }
+  if (iters) *iters = it;
+  QT_CUDA_TRY(cudaStreamSynchronize(s));
+  if (prec != QT_PREC_FP64 && qt::oz_timeouts_and_reset())
+    QT_FAIL(QT_ERR_CUDA, "tensor-core kernel wait timed out");
+  return QT_OK;
+}
+
+extern "C" qt_status qt_corr_batch(qt_ctx* ctx, int n, int64_t nseries, const double* X,
+                                   const double* Y, double* Z, int mode, unsigned flags) {
+  if (!ctx || !X || !Y || !Z || n <= 0 || nseries <= 0 || (mode != 0 && mode != 1))
+    QT_FAIL(QT_ERR_ARG, "bad correlation arguments");
+  if (!(flags & QT_FLAG_DEVICE_POINTERS)) QT_FAIL(QT_ERR_UNSUPPORTED, "device pointers required");
+  if (2 * n > 4096) QT_FAIL(QT_ERR_UNSUPPORTED, "n <= 2048");
+  cudaSetDevice(ctx->device);
+  QT_TRY(ensure(ctx->arena, ctx->arena_bytes, 2048 * sizeof(double2) + 256));
+  double2* tw = reinterpret_cast<double2*>(ctx->arena);
+  cudaError_t e = qt::gw_twiddles(tw, ctx->stream);
+  if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+  qt::CorrConvArgs a{};
+  a.n = n; a.nm = 1; a.nseries = nseries; a.estride = nseries;
+  a.X = X; a.Y = Y; a.Z = Z; a.corr = mode == 0; a.scale_re = 1.0;
+  e = qt::zcorrconv(a, tw, ctx->stream);
+  if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+  if (flags & QT_FLAG_SYNC) QT_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return QT_OK;
 }

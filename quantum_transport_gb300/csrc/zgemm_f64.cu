@@ -98,6 +98,7 @@ cudaError_t zgemm_f64(const GemmArgs& a, cudaStream_t s) {
   const int tiles = ((a.m + BM - 1) / BM) * ((a.n + BN - 1) / BN);
   const long long by = a.batch < 65535 ? a.batch : 65535;
   zgemm_f64_kernel<<<dim3(tiles, (unsigned)by), NT, 0, s>>>(a);
+  count_launch();
   return cudaGetLastError();
 }
 

@@ -137,6 +137,12 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r) {
         "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
 }
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t* r) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                 "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+}
 __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
@@ -299,25 +305,79 @@ template <> struct Store<double2> {
   }
 };
 
+// ------------------------------------------------------------ scale prologue
+// scales[b][0..127]   = e_i: exponent bound of row i of op(A)   over Re and Im parts
+// scales[b][128..255] = f_j: exponent bound of column j of op(B)
+// One CTA per (batch entry, operand).  A vector is either contiguous in memory
+// (warp per vector, lanes along it) or strided (threads along consecutive
+// vectors, which coalesces the loads across the warp); loads are unrolled so
+// many are in flight.
+template <typename TIn>
+__global__ void __launch_bounds__(256) oz_scales_kernel(GemmArgs a) {
+  __shared__ unsigned long long part_max[256];
+  const int which = blockIdx.y;
+  const int n = a.m, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (long long b = blockIdx.x; b < a.batch; b += gridDim.x) {
+    int* out = a.scales + b * 256 + which * 128;
+    if (a.active && !a.active[b]) continue;
+    const int op = which ? a.opB : a.opA;
+    const BatchRef& R = which ? a.B : a.A;
+    const TIn* M = batch_ptr<const TIn>(R, b);
+    const int ld = R.ld;
+    // row of op(A) = storage row (OP_N) / storage column (else); column of op(B) = storage
+    // column (OP_N) / storage row (else)
+    const bool contiguous = which ? (op == OP_N) : (op != OP_N);
+    if (contiguous) {
+      for (int v = warp; v < 128; v += 8) {
+        unsigned long long m = 0;
+        if (v < n) {
+#pragma unroll 4
+          for (int e = lane; e < n; e += 32) {
+            const TIn x = M[e + (long long)v * ld];
+            m = max(m, max(absbits(x, 0), absbits(x, 1)));
+          }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) out[v] = v < n ? exp_bound_bits<TIn>(m) : 0;
+      }
+    } else {
+      const int v = tid & 127, h = tid >> 7;  // two threads per vector
+      unsigned long long m = 0;
+      if (v < n) {
+#pragma unroll 8
+        for (int e = h; e < n; e += 2) {
+          const TIn x = M[v + (long long)e * ld];
+          m = max(m, max(absbits(x, 0), absbits(x, 1)));
+        }
+      }
+      part_max[tid] = m;
+      __syncthreads();
+      if (h == 0) out[v] = v < n ? exp_bound_bits<TIn>(max(m, part_max[tid + 128])) : 0;
+      __syncthreads();
+    }
+  }
+}
+
 // ------------------------------------------------------------ the kernel
-template <int S, int L, typename TIn, typename TOut>
+template <int S, int L, int NT, typename TIn, typename TOut>
 __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int stages) {
-  constexpr int NACC = (L < 3 ? L : 3) + 1;
+  // NT output columns per CTA; the 512 TMEM columns hold 512/NT accumulators.  With
+  // NT = 64 every digit level up to 7 has its own (exact) accumulator.
+  constexpr int NACC_MAX = 512 / NT;
+  constexpr int NACC = (L + 1 < NACC_MAX) ? L + 1 : NACC_MAX;
+  constexpr int BPLANE = NT * KC * 2;  // one B digit plane of an NT-row tile
   extern __shared__ __align__(1024) unsigned char smem[];
-  // carve: [stages x (A planes | B planes)] [barriers] [exponents] [tmem slot, abort flag]
-  const int stage_bytes = 2 * S * PLANE_BYTES;
+  // carve: [stages x (A planes | B planes)] [barriers] [tmem slot, abort flag]
+  const int stage_bytes = S * (PLANE_BYTES + BPLANE);
   unsigned char* tiles = smem;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)stages * stage_bytes);
   uint64_t* full = bars;                 // [stages] producers -> MMA
   uint64_t* empty = bars + stages;       // [stages] MMA (commit) -> producers
   uint64_t* tmem_full = bars + 2 * stages;  // MMA (commit) -> epilogue
   uint64_t* tmem_empty = tmem_full + 1;     // epilogue -> MMA
-  uint64_t* exp_full = tmem_full + 2;       // [2] producers -> epilogue (scale exponents)
-  uint64_t* exp_empty = tmem_full + 4;      // [2] epilogue -> producers
-  uint64_t* drain = tmem_full + 6;          // teardown
-  int* erow = reinterpret_cast<int*>(tmem_full + 8);  // [2][128]
-  int* fcol = erow + 256;                             // [2][128]
-  uint32_t* tmem_base_sm = reinterpret_cast<uint32_t*>(fcol + 256);
+  uint64_t* drain = tmem_full + 2;          // teardown
+  uint32_t* tmem_base_sm = reinterpret_cast<uint32_t*>(tmem_full + 4);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_base_sm + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -325,13 +385,14 @@ __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int s
   const int npad = (n + 15) & ~15;
   const int kp = (n + KC - 1) / KC * KC;  // padded complex K
   const int nch = 2 * kp / KC;            // real-K chunks (first half: Re parts, second: Im)
-  const long long nitems = 2 * a.batch;   // (batch entry, real/imag part of C)
+  const int ntile = (npad + NT - 1) / NT;  // column tiles per real part
+  // work item: (batch entry, real/imag part of C, column tile)
+  const long long nitems = 2LL * ntile * a.batch;
 
   if (tid == 0) {
     for (int s = 0; s < stages; ++s) { mbar_init(&full[s], NPROD); mbar_init(&empty[s], 1); }
     mbar_init(tmem_full, 1);
     mbar_init(tmem_empty, 128);
-    for (int q = 0; q < 2; ++q) { mbar_init(&exp_full[q], NPROD); mbar_init(&exp_empty[q], 128); }
     mbar_init(drain, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -350,41 +411,16 @@ __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int s
   if (warp >= 4 && warp < 12) {
     // ======================== producers
     const int p = tid - 128;  // 0..255
-    const int pw = p >> 5;    // producer warp 0..7
     uint32_t proc = 0, gchunk = 0;
     for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
-      const long long b = w >> 1;
-      const int part = (int)(w & 1);
+      const long long b = w / (2 * ntile);
+      const int part = (int)((w / ntile) & 1), ct = (int)(w % ntile);
       if (a.active && !a.active[b]) continue;
-      const int q = proc & 1;
-      if (!mbar_wait(&exp_empty[q], ((proc >> 1) & 1) ^ 1, abort_flag)) break;
-      const void* A = batch_ptr<const char>(a.A, b);
-      const void* B = batch_ptr<const char>(a.B, b);
-      // ---- scale exponents of the rows of op(A) and columns of op(B) (Re and Im)
-      for (int i = pw; i < 128; i += 8) {
-        unsigned long long m = 0;
-        if (i < n)
-          for (int k = lane; k < n; k += 32) {
-            const TIn v = load_op<TIn>(A, a.A.ld, a.opA, i, k);
-            m = max(m, max(absbits(v, 0), absbits(v, 1)));
-          }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (lane == 0) erow[q * 128 + i] = exp_bound_bits<TIn>(m);
-      }
-      for (int j = pw; j < 128; j += 8) {
-        unsigned long long m = 0;
-        if (j < n)
-          for (int k = lane; k < n; k += 32) {
-            const TIn v = load_op<TIn>(B, a.B.ld, a.opB, k, j);
-            m = max(m, max(absbits(v, 0), absbits(v, 1)));
-          }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (lane == 0) fcol[q * 128 + j] = exp_bound_bits<TIn>(m);
-      }
-      asm volatile("bar.sync 1, 256;" ::: "memory");  // producers only
-      mbar_arrive(&exp_full[q]);
+      // batch strides are in complex elements: address through the element type
+      const void* A = batch_ptr<const TIn>(a.A, b);
+      const void* B = batch_ptr<const TIn>(a.B, b);
+      const int* erow = a.scales + b * 256;  // row exponents of op(A) (prologue kernel)
+      const int* fcol = erow + 128;          // column exponents of op(B)
       // ---- pipeline stages
       for (int c = 0; c < nch; ++c, ++gchunk) {
         const int st = gchunk % stages;
@@ -397,11 +433,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int s
         // Cr = Re(At).Re(Bt) + Im(At).(-Im(Bt)) ;  Ci = Re(At).Im(Bt) + Im(At).Re(Bt)
         const int bpart = (part == 0) ? half : (1 - half);
         const bool bneg = (part == 0 && half == 1);
-        for (int item = p; item < 1024; item += NPROD) {  // (row, 8-k group), A then B
+        for (int item = p; item < 512 + 4 * NT; item += NPROD) {  // (row, 8-k group), A then B
           const bool isA = item < 512;
           const int it2 = isA ? item : item - 512;
-          const int r = it2 & 127, g = it2 >> 7;
-          const int e = isA ? erow[q * 128 + r] : fcol[q * 128 + r];
+          const int r = isA ? (it2 & 127) : (it2 % NT), g = isA ? (it2 >> 7) : (it2 / NT);
+          const int rg = isA ? r : ct * NT + r;  // row of op(A) / column of op(B)
+          const int e = isA ? erow[r] : (rg < n ? fcol[rg] : 0);
           const int vpart = isA ? half : bpart;
           uint32_t packed[S][4];
 #pragma unroll
@@ -411,9 +448,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int s
             TIn x0, x1;
             if constexpr (sizeof(TIn) == 8) { x0 = make_float2(0.f, 0.f); x1 = x0; }
             else { x0 = make_double2(0.0, 0.0); x1 = x0; }
-            if (r < n) {
-              if (ka < n) x0 = isA ? load_op<TIn>(A, a.A.ld, a.opA, r, ka) : load_op<TIn>(B, a.B.ld, a.opB, ka, r);
-              if (ka + 1 < n) x1 = isA ? load_op<TIn>(A, a.A.ld, a.opA, r, ka + 1) : load_op<TIn>(B, a.B.ld, a.opB, ka + 1, r);
+            if (rg < n) {
+              if (ka < n) x0 = isA ? load_op<TIn>(A, a.A.ld, a.opA, rg, ka) : load_op<TIn>(B, a.B.ld, a.opB, ka, rg);
+              if (ka + 1 < n) x1 = isA ? load_op<TIn>(A, a.A.ld, a.opA, rg, ka + 1) : load_op<TIn>(B, a.B.ld, a.opB, ka + 1, rg);
             }
             if constexpr (sizeof(TIn) == 8) {
               const float scale = __int_as_float((127 + 8 - e) << 23);  // 2^(8-e)
@@ -436,9 +473,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int s
           // canonical no-swizzle K-major: (r/8)*SBO + g*LBO + (r%8)*16
           const uint32_t off = (uint32_t)((r >> 3) * SBO + g * LBO + (r & 7) * 16);
           unsigned char* base = isA ? stA : stB;
+          const int pstride = isA ? PLANE_BYTES : BPLANE;
 #pragma unroll
           for (int s = 0; s < S; ++s)
-            *reinterpret_cast<uint4*>(base + (size_t)s * PLANE_BYTES + off) =
+            *reinterpret_cast<uint4*>(base + (size_t)s * pstride + off) =
                 make_uint4(packed[s][0], packed[s][1], packed[s][2], packed[s][3]);
         }
         fence_proxy_async();
@@ -449,10 +487,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int s
   } else if (warp == MMA_WARP) {
     // ======================== MMA issuer (one thread)
     if (lane == 0) {
-      const uint32_t idesc = make_idesc(128, npad);
+      const uint32_t idesc = make_idesc(128, NT);
       uint32_t proc = 0, gchunk = 0;
       for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
-        const long long b = w >> 1;
+        const long long b = w / (2 * ntile);
         if (a.active && !a.active[b]) continue;
         if (!mbar_wait(tmem_empty, (proc & 1) ^ 1, abort_flag)) break;
         tc_fence_after();
@@ -471,10 +509,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int s
 #pragma unroll
               for (int t = 0; t < S; ++t) {
                 if (s + t > L) continue;
-                const int acc = (s + t) < 3 ? (s + t) : 3;
+                const int acc = (s + t) < NACC - 1 ? (s + t) : NACC - 1;
                 const uint64_t ad = make_desc(sA + s * PLANE_BYTES + kk * 2 * LBO);
-                const uint64_t bd = make_desc(sB + t * PLANE_BYTES + kk * 2 * LBO);
-                umma(tmem + acc * 128, ad, bd, idesc, (touched >> acc) & 1);
+                const uint64_t bd = make_desc(sB + t * BPLANE + kk * 2 * LBO);
+                umma(tmem + acc * NT, ad, bd, idesc, (touched >> acc) & 1);
                 touched |= 1u << acc;
               }
             }
@@ -497,31 +535,35 @@ __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int s
     const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
     uint32_t proc = 0;
     for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
-      const long long b = w >> 1;
-      const int part = (int)(w & 1);
+      const long long b = w / (2 * ntile);
+      const int part = (int)((w / ntile) & 1), ct = (int)(w % ntile);
       if (a.active && !a.active[b]) continue;
-      const int q = proc & 1;
       if (!mbar_wait(tmem_full, proc & 1, abort_flag)) break;
-      if (!mbar_wait(&exp_full[q], (proc >> 1) & 1, abort_flag)) break;
+      const int* erow = a.scales + b * 256;
+      const int* fcol = erow + 128;
       tc_fence_after();
-      void* C = batch_ptr<char>(a.C, b);
-      const void* D = a.D.p ? batch_ptr<const char>(a.D, b) : nullptr;
+      void* C = batch_ptr<TOut>(a.C, b);
+      const void* D = a.D.p ? batch_ptr<const TOut>(a.D, b) : nullptr;
       double zpart = 0.0;
       if (a.Z.p) {
         const double2 z = *batch_ptr<const double2>(a.Z, b);
         zpart = part ? z.y : z.x;
       }
-      const int ei = erow[q * 128 + row];
+      const int ei = erow[row];
       const float alpha = (float)a.alpha_re, beta = (float)a.beta_re;
-      for (int j0 = 0; j0 < npad; j0 += 16) {
-        uint32_t r[4][16];
+      constexpr int CW = NACC > 4 ? 8 : 16;  // columns per TMEM read (register budget)
+      for (int j0 = 0; j0 < NT; j0 += CW) {
+        uint32_t r[NACC][16];
 #pragma unroll
-        for (int acc = 0; acc < NACC; ++acc) tmem_ld16(lane_base + acc * 128 + j0, r[acc]);
+        for (int acc = 0; acc < NACC; ++acc) {
+          if constexpr (CW == 16) tmem_ld16(lane_base + acc * NT + j0, r[acc]);
+          else tmem_ld8(lane_base + acc * NT + j0, r[acc]);
+        }
         tmem_wait_ld();
         if (row < n) {
 #pragma unroll
-          for (int jj = 0; jj < 16; ++jj) {
-            const int j = j0 + jj;
+          for (int jj = 0; jj < CW; ++jj) {
+            const int j = ct * NT + j0 + jj;
             if (j < n) {
               float hi = __uint_as_float(r[0][jj]), lo = 0.f, e;
 #pragma unroll
@@ -533,7 +575,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int s
               }
               float s2;
               two_sum(hi, lo, s2, e);  // normalise: |lo| <= ulp(hi)/2
-              const int e2 = ei + fcol[q * 128 + j] - 16;
+              const int e2 = ei + fcol[j] - 16;
               Store<TOut>::put(C, row + (long long)j * a.C.ld, part, s2, e, e2, alpha, beta, D,
                                row + (long long)j * a.D.ld, row == j && a.Z.p, zpart);
             }
@@ -542,7 +584,6 @@ __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int s
       }
       tc_fence_before();
       mbar_arrive(tmem_empty);
-      mbar_arrive(&exp_empty[q]);
       ++proc;
     }
   }
@@ -555,24 +596,30 @@ __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int s
   }
 }
 
-template <int S, int L, typename TIn, typename TOut>
+template <int S, int L, int NT, typename TIn, typename TOut>
 cudaError_t launch(const GemmArgs& a, cudaStream_t s) {
   int dev = 0, sms = 0, maxsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const int stage_bytes = 2 * S * PLANE_BYTES;
+  const int stage_bytes = S * (PLANE_BYTES + NT * KC * 2);
   const int extra = 2048 + 8 * 64 + 64;  // barriers + exponents + tmem slot
   int stages = (maxsm - extra) / stage_bytes;
   if (stages > 4) stages = 4;
   if (stages < 2) return cudaErrorInvalidConfiguration;
   const size_t smem = (size_t)stages * stage_bytes + extra;
-  cudaError_t e = cudaFuncSetAttribute(zgemm_oz_kernel<S, L, TIn, TOut>,
+  cudaError_t e = cudaFuncSetAttribute(zgemm_oz_kernel<S, L, NT, TIn, TOut>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  const long long items = 2 * a.batch;
+  const int ntile = (((a.m + 15) & ~15) + NT - 1) / NT;
+  const long long items = 2LL * ntile * a.batch;
   const int grid = (int)(items < sms ? items : sms);
-  zgemm_oz_kernel<S, L, TIn, TOut><<<grid, NTHREADS, smem, s>>>(a, stages);
+  if (!a.scales) return cudaErrorInvalidValue;
+  const long long gb = a.batch < 65535 ? a.batch : 65535;
+  oz_scales_kernel<TIn><<<dim3((unsigned)gb, 2), 256, 0, s>>>(a);
+  count_launch();
+  zgemm_oz_kernel<S, L, NT, TIn, TOut><<<grid, NTHREADS, smem, s>>>(a, stages);
+  count_launch();
   return cudaGetLastError();
 }
 
@@ -585,9 +632,9 @@ cudaError_t zgemm_oz(const GemmArgs& a, int slices, int levels, cudaStream_t s) 
     return cudaErrorInvalidValue;
   (void)levels;
   switch (slices) {
-    case 4: return launch<4, 3, double2, double2>(a, s);
-    case 6: return launch<6, 5, double2, double2>(a, s);
-    case 7: return launch<7, 6, double2, double2>(a, s);
+    case 4: return launch<4, 3, 128, double2, double2>(a, s);
+    case 6: return launch<6, 5, 64, double2, double2>(a, s);   // one exact accumulator per level
+    case 7: return launch<7, 6, 64, double2, double2>(a, s);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -598,8 +645,8 @@ cudaError_t zgemm_oz_c64(const GemmArgs& a, int slices, cudaStream_t s) {
   if (a.opA == OP_T || a.opB == OP_T || a.alpha_im != 0.0 || a.beta_im != 0.0)
     return cudaErrorInvalidValue;
   switch (slices) {
-    case 3: return launch<3, 2, float2, float2>(a, s);
-    case 4: return launch<4, 3, float2, float2>(a, s);
+    case 3: return launch<3, 2, 128, float2, float2>(a, s);
+    case 4: return launch<4, 3, 128, float2, float2>(a, s);
     default: return cudaErrorInvalidValue;
   }
 }

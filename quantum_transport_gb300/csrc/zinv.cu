@@ -234,6 +234,7 @@ cudaError_t zinv_f64(const InvArgs& a, cudaStream_t s) {
   if (a.batch <= 0) return cudaSuccess;
   const size_t sm = (size_t)a.n * 2 * sizeof(cd) + (size_t)a.n * sizeof(int);
   zinv_f64_kernel<<<(unsigned)grid_for(a.batch), NT64, sm, s>>>(a);
+  count_launch();
   return cudaGetLastError();
 }
 
@@ -247,6 +248,7 @@ cudaError_t zinv_f32(const InvArgs& a, cudaStream_t s) {
                                        (int)sm);
   if (e != cudaSuccess) return e;
   zinv_f32_kernel<TC><<<(unsigned)grid_for(a.batch), NT32, sm, s>>>(a);
+  count_launch();
   return cudaGetLastError();
 }
 template cudaError_t zinv_f32<double2>(const InvArgs&, cudaStream_t);

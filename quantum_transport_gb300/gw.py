@@ -1,0 +1,98 @@
+"""GW/SCBA self-energy loop on the GPU (host-side mirror of gw_ephoton_3d_ijs).
+
+* ``corr`` / ``conv``  corr1d2 / conv1d2 (src/fft_mod.f90:58-168), batched
+* ``gw_step``          one evaluation Sigma -> Sigma_new of the SCBA map
+                       (src/gw_mod.f90:368-749, 950-959)
+* ``scba``             the plain linear-mixing loop (src/gw_mod.f90:349-749)
+                       run to a residual tolerance
+
+All arrays are torch CUDA tensors (device pointers); energy-resolved blocks
+are complex128 tensors of shape (nE, nx, nm, nm) stored column-major per
+block (``to_dev`` / ``from_dev`` convert from/to row-major numpy).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import QtContacts, QtDevice, check
+from .rgf import PREC, _ptr, colmajor
+
+
+def to_dev(A):
+    import torch
+    return torch.from_numpy(colmajor(A)).cuda()
+
+
+def from_dev(T):
+    return np.swapaxes(T.cpu().numpy(), -1, -2)
+
+
+def corr(ctx, X, Y, mode="corr"):
+    """Z = corr/conv of energy-major series X, Y: tensors (n, nseries) complex128 on the GPU."""
+    import torch
+    n, ns = X.shape
+    Z = torch.empty_like(X)
+    check(ctx._lib.qt_corr_batch(ctx.handle, n, ns, _ptr(X), _ptr(Y), _ptr(Z),
+                                 0 if mode == "corr" else 1,
+                                 _lib.QT_FLAG_DEVICE_POINTERS | _lib.QT_FLAG_SYNC))
+    return Z
+
+
+class GwSystem:
+    """Device, energy grid, contacts and Coulomb block of one SCBA problem (nk = 1)."""
+
+    def __init__(self, ctx, H00, H10, E, nx, V, *, mu=(0.0, 0.0), temp=(300.0, 300.0),
+                 eta_lead=1e-3, sancho_max_iter=100, sancho_tol=1e-100, spindeg=2.0,
+                 precision="fp64"):
+        import torch
+        self.ctx = ctx
+        self.nm = H00.shape[-1]
+        self.nx = nx
+        self.nE = len(E)
+        self.H00 = to_dev(H00)
+        self.H10 = to_dev(H10)
+        self.E = torch.from_numpy(np.ascontiguousarray(E, dtype=np.float64)).cuda()
+        self.V = to_dev(V)
+        self.spindeg = spindeg
+        self.prec = PREC[precision]
+        self.dev = QtDevice(self.nm, nx, 1, _ptr(self.H00), 0, 0, _ptr(self.H10), 0, 0,
+                            None, 0, 0)
+        self.con = QtContacts(mu[0], mu[1], temp[0], temp[1], eta_lead, 0.0, sancho_tol,
+                              int(sancho_max_iter), 0)
+
+    def zeros(self):
+        import torch
+        return torch.zeros((self.nE, self.nx, self.nm, self.nm), dtype=torch.complex128,
+                           device="cuda")
+
+    def step(self, SR, SL):
+        """Sigma_new (R, <, >) from Sigma (R, <): one SCBA map evaluation."""
+        NR, NL, NG = self.zeros(), self.zeros(), self.zeros()
+        check(self.ctx._lib.qt_gw_step(self.ctx.handle, C.byref(self.dev), _ptr(self.E), self.nE,
+                                       C.byref(self.con), _ptr(self.V), self.spindeg, self.prec,
+                                       _lib.QT_FLAG_DEVICE_POINTERS, _ptr(SR), _ptr(SL),
+                                       _ptr(NR), _ptr(NL), _ptr(NG)))
+        return NR, NL, NG
+
+    def scba(self, alpha=0.3, tol=1e-8, max_iter=60, start=None):
+        """Plain linear mixing to tol; returns (SR, SL, SG, residuals)."""
+        SR, SL, SG = start if start is not None else (self.zeros(), self.zeros(), self.zeros())
+        res = np.zeros(max_iter)
+        it = C.c_int()
+        check(self.ctx._lib.qt_scba_solve(self.ctx.handle, C.byref(self.dev), _ptr(self.E),
+                                          self.nE, C.byref(self.con), _ptr(self.V), self.spindeg,
+                                          alpha, tol, max_iter, self.prec,
+                                          _lib.QT_FLAG_DEVICE_POINTERS, _ptr(SR), _ptr(SL),
+                                          _ptr(SG), res.ctypes.data_as(C.c_void_p), C.byref(it)))
+        return SR, SL, SG, res[:it.value]
+
+
+def residual(NL, NG, SL, SG):
+    """||S_new - S||_F / ||S_new||_F over Sigma^< and Sigma^> (the SCBA stopping measure)."""
+    import torch
+    num = torch.sqrt(torch.sum(torch.abs(NL - SL) ** 2) + torch.sum(torch.abs(NG - SG) ** 2))
+    den = torch.sqrt(torch.sum(torch.abs(NL) ** 2) + torch.sum(torch.abs(NG) ** 2))
+    return float(num / den.clamp_min(1e-300))

@@ -54,6 +54,31 @@ class Context:
     def set_scratch_limit(self, nbytes):
         check(self._lib.qt_ctx_set_scratch_limit(self.handle, int(nbytes)))
 
+    def profile(self, enable=True):
+        """Event-time every block product / inverse launch on this context's stream."""
+        check(self._lib.qt_ctx_profile(self.handle, int(bool(enable))))
+
+    PROFILE_KINDS = {0: "zgemm_oz_c64", 1: "zgemm_oz_c128", 2: "zgemm_f64", 3: "zinv_f32",
+                     4: "zinv_f64"}
+
+    def profile_read(self):
+        """{kind name: (launches, ms, algorithmic flops, executed tensor flops)} since last read."""
+        out = {}
+        for k, name in self.PROFILE_KINDS.items():
+            nl, ms, fa, ft = C.c_int64(), C.c_double(), C.c_double(), C.c_double()
+            check(self._lib.qt_ctx_profile_read(self.handle, k, C.byref(nl), C.byref(ms),
+                                                C.byref(fa), C.byref(ft)))
+            if nl.value:
+                out[name] = (nl.value, ms.value, fa.value, ft.value)
+        return out
+
+    @property
+    def stream_ptr(self):
+        p = C.c_void_p()
+        check(self._lib.qt_ctx_stream(self.handle, C.byref(p)))
+        return p.value or 0
+
+
     def __enter__(self):
         return self
 
@@ -65,6 +90,11 @@ class Context:
             self.close()
         except Exception:
             pass
+
+
+def kernel_launches():
+    """Kernels launched by libqtgpu.so in this process."""
+    return int(_lib.load().qt_kernel_launches())
 
 
 def colmajor(A):
@@ -277,3 +307,28 @@ def negf_solve(ctx, Hii, H1i, nx, nen, emin, emax, temp, mu, nbnd, nslab, *, nk=
         t = cell_spectra(r[key], nbnd, nslab)
         out[name] = np.stack([t.real * c[0], t.imag * c[1]], axis=-1)
     return out
+
+
+def rgf_solve_device(ctx, Hii, hk, hl, H1i, h1k, h1l, nm, nx, nk, E, nE, out, *, mul=0.0,
+                     mur=0.0, templ=300.0, tempr=300.0, eta_lead=1e-5, eta_interior=0.0,
+                     sancho_tol=1e-100, sancho_max_iter=50, precision="mixed", caroli=True,
+                     quirks=0, sync=False):
+    """Device-pointer form of ``rgf_solve`` (no host copies; asynchronous on ctx's stream).
+
+    Hii/H1i/E: torch CUDA tensors (column-major complex128 blocks, float64
+    energies); ``out``: dict of torch CUDA tensors for any of tr, tre, T,
+    diag_gr, diag_gl, diag_gg, status, sancho_iters.  Strides in complex elements.
+    Returns the status code (QT_OK or QT_ERR_POINTS when synchronised).
+    """
+    lib = ctx._lib
+    dev = QtDevice(nm, nx, nk, _ptr(Hii), hk, hl, _ptr(H1i), h1k, h1l, None, 0, 0)
+    con = QtContacts(mul, mur, templ, tempr, eta_lead, eta_interior, sancho_tol,
+                     int(sancho_max_iter), int(quirks))
+    o = QtOutputs(*[_ptr(out.get(k)) for k in ("tr", "tre", "T", "diag_gr", "diag_gl",
+                                               "diag_gg", "G_r", "G_lesser", "G_greater",
+                                               "status", "sancho_iters")])
+    flags = _lib.QT_FLAG_DEVICE_POINTERS | (_lib.QT_FLAG_CAROLI if caroli else 0) | \
+        (_lib.QT_FLAG_SYNC if sync else 0)
+    return check(lib.qt_rgf_solve(ctx.handle, C.byref(dev), _ptr(E), int(nE), C.byref(con),
+                                  None, None, PREC[precision], flags, C.byref(o)),
+                 allow_points=True)

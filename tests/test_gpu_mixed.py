@@ -9,9 +9,10 @@ from tests.goldutil import printed_match
 
 pytestmark = pytest.mark.gpu
 
-# normwise error bound per digit count, relative to (|op(A)| |op(B)|)_ij:
-# S digits keep 8S-1 bits of each row/column-aligned operand
-TOL = {4: 2.0 ** -29, 6: 2.0 ** -45, 7: 2.0 ** -53}
+# S digits keep 8S-1 bits of each operand row (column) relative to its largest entry, and
+# every digit level is accumulated exactly, so the error of C_ij is bounded by
+#   2^(4-8S) * (max_k |A_ik| sum_k |B_kj| + sum_k |A_ik| max_k |B_kj|)
+TOL = {4: 2.0 ** -28, 6: 2.0 ** -44, 7: 2.0 ** -52}
 
 
 def rand_blocks(rng, b, n, scale=1.0):
@@ -29,9 +30,11 @@ def test_zgemm_split(ctx, slices, n, ops):
     op = {"N": lambda X: X, "C": lambda X: np.conj(np.swapaxes(X, -1, -2))}
     C = rgf.mul_c(ctx, A, B, ops[0], ops[1], precision="mixed", slices=slices)
     ref = op[ops[0]](A) @ op[ops[1]](B)
-    bound = np.abs(op[ops[0]](A)) @ np.abs(op[ops[1]](B))
+    a, b = np.abs(op[ops[0]](A)), np.abs(op[ops[1]](B))
+    bound = (a.max(axis=-1, keepdims=True) * b.sum(axis=-2, keepdims=True)
+             + a.sum(axis=-1, keepdims=True) * b.max(axis=-2, keepdims=True))
     err = np.abs(C - ref)
-    assert (err <= 4 * n * TOL[slices] * bound + 1e-300).all(), (err / bound).max()
+    assert (err <= TOL[slices] * bound).all(), (err / bound).max()
 
 
 def test_zgemm_split_alpha_beta(ctx):
@@ -48,7 +51,7 @@ def test_zinv_split(ctx):
     A = rand_blocks(rng, 5, 96) + 4 * np.eye(96)
     X, st = rgf.invert(ctx, A, precision="mixed")
     assert (st == 0).all()
-    np.testing.assert_allclose(X @ A, np.broadcast_to(np.eye(96), A.shape), atol=1e-11)
+    np.testing.assert_allclose(X @ A, np.broadcast_to(np.eye(96), A.shape), atol=1e-12)
 
 
 def test_sancho_split_cnt_golden(ctx, cnt):
