@@ -449,7 +449,7 @@ qt_status solve_wave(qt_ctx* ctx, const Problem& pb, long long p0, long long P, 
   Ops<double2> cop{s, n, pb.prec};
   cop.prof = &ctx->prof;
   cop.slices = pb.lead_slices;
-  cop.refine = split ? 2 : 0;
+  cop.refine = split ? 3 : 0;  // FP32 elimination: (kappa 2^-24)^(r+1), kappa ~ 1e5 at lead band edges
   cop.one = one;
   cop.scales = scales;
   cop.P = P;
@@ -973,7 +973,7 @@ extern "C" qt_status qt_sancho_batch(qt_ctx* ctx, int nm, int npts, const double
   cudaStream_t s = ctx->stream;
   Ops<double2> op{s, nm, prec};
   op.slices = env_int("QT_LEAD_SLICES", 7);
-  op.refine = prec == QT_PREC_FP64 ? 0 : 2;
+  op.refine = prec == QT_PREC_FP64 ? 0 : 3;
   cd* one = ar.take<cd>(1);
   const cd h1{1.0, 0.0};
   cudaMemcpyAsync(one, &h1, sizeof(cd), cudaMemcpyHostToDevice, s);
@@ -1100,7 +1100,7 @@ extern "C" qt_status qt_zinv_batch(qt_ctx* ctx, int n, int batch, const double* 
   Ops<double2> op{s, n, prec};
   op.P = P;
   op.slices = env_int("QT_LEAD_SLICES", 7);
-  op.refine = prec == QT_PREC_FP64 ? 0 : 2;
+  op.refine = prec == QT_PREC_FP64 ? 0 : 3;
   cd* one = ar.take<cd>(1);
   const cd h1{1.0, 0.0};
   cudaMemcpyAsync(one, &h1, sizeof(cd), cudaMemcpyHostToDevice, s);

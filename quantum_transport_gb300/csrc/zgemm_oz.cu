@@ -367,6 +367,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int s
   constexpr int NACC_MAX = 512 / NT;
   constexpr int NACC = (L + 1 < NACC_MAX) ? L + 1 : NACC_MAX;
   constexpr int BPLANE = NT * KC * 2;  // one B digit plane of an NT-row tile
+  constexpr int ITEMS = (512 + 4 * NT) / NPROD;  // (row, 8-K group) items per producer thread
+  static_assert((512 + 4 * NT) % NPROD == 0, "item split");
   extern __shared__ __align__(1024) unsigned char smem[];
   // carve: [stages x (A planes | B planes)] [barriers] [tmem slot, abort flag]
   const int stage_bytes = S * (PLANE_BYTES + BPLANE);
@@ -383,8 +385,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int s
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int n = a.m;
   const int npad = (n + 15) & ~15;
-  const int kp = (n + KC - 1) / KC * KC;  // padded complex K
-  const int nch = 2 * kp / KC;            // real-K chunks (first half: Re parts, second: Im)
+  const int nch = (n + KC / 2 - 1) / (KC / 2);  // stages: KC real K = KC/2 complex k each
   const int ntile = (npad + NT - 1) / NT;  // column tiles per real part
   // work item: (batch entry, real/imag part of C, column tile)
   const long long nitems = 2LL * ntile * a.batch;
@@ -421,63 +422,78 @@ __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int s
       const void* B = batch_ptr<const TIn>(a.B, b);
       const int* erow = a.scales + b * 256;  // row exponents of op(A) (prologue kernel)
       const int* fcol = erow + 128;          // column exponents of op(B)
-      // ---- pipeline stages
+      // ---- pipeline stages.  The real K axis interleaves (Re, Im) of each complex k:
+      //   A' row i:      Re At[i,k], Im At[i,k]
+      //   B' (C real):   Re Bt[k,j], -Im Bt[k,j]      B' (C imag): Im Bt[k,j], Re Bt[k,j]
+      // so every complex element is loaded once; all loads of a stage are issued
+      // before any digit arithmetic (memory-level parallelism).
       for (int c = 0; c < nch; ++c, ++gchunk) {
         const int st = gchunk % stages;
         const uint32_t ph = (gchunk / stages) & 1;
         if (!mbar_wait(&empty[st], ph ^ 1, abort_flag)) break;
         unsigned char* stA = tiles + (size_t)st * stage_bytes;
         unsigned char* stB = stA + S * PLANE_BYTES;
-        const int half = c >= nch / 2;               // 0: real parts, 1: imaginary parts
-        const int k0 = (c - half * (nch / 2)) * KC;  // complex k offset of this chunk
-        // Cr = Re(At).Re(Bt) + Im(At).(-Im(Bt)) ;  Ci = Re(At).Im(Bt) + Im(At).Re(Bt)
-        const int bpart = (part == 0) ? half : (1 - half);
-        const bool bneg = (part == 0 && half == 1);
-        for (int item = p; item < 512 + 4 * NT; item += NPROD) {  // (row, 8-k group), A then B
+        const int kc0 = c * (KC / 2);  // complex k offset of this stage
+        TIn xv[ITEMS][4];
+#pragma unroll
+        for (int q = 0; q < ITEMS; ++q) {
+          const int item = p + q * NPROD;
+          const bool isA = item < 512;
+          const int it2 = isA ? item : item - 512;
+          const int r = isA ? (it2 & 127) : (it2 % NT), g = isA ? (it2 >> 7) : (it2 / NT);
+          const int rg = isA ? r : ct * NT + r;
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int k = kc0 + 4 * g + u;
+            TIn x;
+            x.x = 0; x.y = 0;
+            if (rg < n && k < n)
+              x = isA ? load_op<TIn>(A, a.A.ld, a.opA, rg, k) : load_op<TIn>(B, a.B.ld, a.opB, k, rg);
+            xv[q][u] = x;
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < ITEMS; ++q) {
+          const int item = p + q * NPROD;
           const bool isA = item < 512;
           const int it2 = isA ? item : item - 512;
           const int r = isA ? (it2 & 127) : (it2 % NT), g = isA ? (it2 >> 7) : (it2 / NT);
           const int rg = isA ? r : ct * NT + r;  // row of op(A) / column of op(B)
           const int e = isA ? erow[r] : (rg < n ? fcol[rg] : 0);
-          const int vpart = isA ? half : bpart;
           uint32_t packed[S][4];
 #pragma unroll
-          for (int t = 0; t < 8; t += 2) {
+          for (int u = 0; u < 4; ++u) {
             float D0[S], D1[S];
-            const int ka = k0 + g * 8 + t;
-            TIn x0, x1;
-            if constexpr (sizeof(TIn) == 8) { x0 = make_float2(0.f, 0.f); x1 = x0; }
-            else { x0 = make_double2(0.0, 0.0); x1 = x0; }
-            if (rg < n) {
-              if (ka < n) x0 = isA ? load_op<TIn>(A, a.A.ld, a.opA, rg, ka) : load_op<TIn>(B, a.B.ld, a.opB, ka, rg);
-              if (ka + 1 < n) x1 = isA ? load_op<TIn>(A, a.A.ld, a.opA, rg, ka + 1) : load_op<TIn>(B, a.B.ld, a.opB, ka + 1, rg);
-            }
+            const TIn x = xv[q][u];
             if constexpr (sizeof(TIn) == 8) {
               const float scale = __int_as_float((127 + 8 - e) << 23);  // 2^(8-e)
-              float v0 = vpart ? x0.y : x0.x, v1 = vpart ? x1.y : x1.x;
-              if (!isA && bneg) { v0 = -v0; v1 = -v1; }
+              float v0 = x.x, v1 = x.y;
+              if (!isA) {
+                if (part == 0) v1 = -v1;
+                else { v0 = x.y; v1 = x.x; }
+              }
               digits_f32<S>(v0, scale, D0);
               digits_f32<S>(v1, scale, D1);
             } else {
-              double v0 = vpart ? x0.y : x0.x, v1 = vpart ? x1.y : x1.x;
-              if (!isA && bneg) {  // sign flip on the bits (no FP64 arithmetic)
-                v0 = __longlong_as_double(__double_as_longlong(v0) ^ (1ll << 63));
-                v1 = __longlong_as_double(__double_as_longlong(v1) ^ (1ll << 63));
+              double v0 = x.x, v1 = x.y;
+              if (!isA) {
+                if (part == 0) v1 = __longlong_as_double(__double_as_longlong(v1) ^ (1ll << 63));
+                else { v0 = x.y; v1 = x.x; }
               }
               digits_f64<S>(v0, e, D0);
               digits_f64<S>(v1, e, D1);
             }
 #pragma unroll
-            for (int s = 0; s < S; ++s) packed[s][t >> 1] = pack_bf16x2(D0[s], D1[s]);
+            for (int s2 = 0; s2 < S; ++s2) packed[s2][u] = pack_bf16x2(D0[s2], D1[s2]);
           }
           // canonical no-swizzle K-major: (r/8)*SBO + g*LBO + (r%8)*16
           const uint32_t off = (uint32_t)((r >> 3) * SBO + g * LBO + (r & 7) * 16);
           unsigned char* base = isA ? stA : stB;
           const int pstride = isA ? PLANE_BYTES : BPLANE;
 #pragma unroll
-          for (int s = 0; s < S; ++s)
-            *reinterpret_cast<uint4*>(base + (size_t)s * pstride + off) =
-                make_uint4(packed[s][0], packed[s][1], packed[s][2], packed[s][3]);
+          for (int s2 = 0; s2 < S; ++s2)
+            *reinterpret_cast<uint4*>(base + (size_t)s2 * pstride + off) =
+                make_uint4(packed[s2][0], packed[s2][1], packed[s2][2], packed[s2][3]);
         }
         fence_proxy_async();
         mbar_arrive(&full[st]);

@@ -226,6 +226,128 @@ __global__ __launch_bounds__(NT32) void zinv_f32_kernel(InvArgs a) {
   }
 }
 
+// Register-blocked FP32 Gauss-Jordan for 64 < n <= 128 (blocks padded to 128 with the
+// identity).  Warp w owns columns 8w..8w+7, lane l owns rows 4l..4l+3: 32 complex
+// entries per thread stay in registers for the whole elimination.  Pivoting is implicit
+// (no row swaps): step k picks the unused row p with the largest |re|+|im| in column k
+// (warp-local search in the warp owning column k), and at the end the inverse is
+// X[k][j] = M[P[k]][P^-1[j]].  One __syncthreads per step (pivot column and index are
+// double-buffered in shared memory).
+template <typename TC>
+__global__ __launch_bounds__(512, 1) void zinv_f32_rb_kernel(InvArgs a) {
+  __shared__ float2 colbuf[2][128];
+  __shared__ int pbuf[2];
+  __shared__ int perm[128], pinv[128];
+  __shared__ int badflag;
+  const int n = a.n;
+  const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
+  for (long long b = blockIdx.x; b < a.batch; b += gridDim.x) {
+    if (a.active && !a.active[b]) continue;
+    const TC* A = batch_ptr<const TC>(a.A, b);
+    TC* X = batch_ptr<TC>(a.X, b);
+    const int lda = a.A.ld, ld = a.X.ld;
+    float2 M[4][8];
+#pragma unroll
+    for (int rr = 0; rr < 4; ++rr)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int r = 4 * l + rr, c = 8 * w + j;
+        if (r < n && c < n) M[rr][j] = to_f2(A[r + (long long)c * lda]);
+        else M[rr][j] = make_float2(r == c ? 1.f : 0.f, 0.f);
+      }
+    unsigned used = 0;
+    if (tid == 0) badflag = 0;
+    for (int k = 0; k < 128; ++k) {
+      const int q = k & 1, wk = k >> 3, ck = k & 7;
+      if (w == wk) {
+        float best = -1.f;
+        int bi = 0x7fffffff;
+#pragma unroll
+        for (int rr = 0; rr < 4; ++rr) {
+          float2 v = M[rr][0];
+#pragma unroll
+          for (int j = 1; j < 8; ++j)
+            if (j == ck) v = M[rr][j];
+          colbuf[q][4 * l + rr] = v;
+          float m = fabsf(v.x) + fabsf(v.y);
+          if (!(m == m)) m = 0.f;  // NaN: still selectable (flagged below), never skipped
+          if (!((used >> rr) & 1u) && (m > best || (m == best && 4 * l + rr < bi))) {
+            best = m;
+            bi = 4 * l + rr;
+          }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+          const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+          if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+        }
+        if (bi > 127) bi = 0;  // unreachable: 128 - k >= 1 unused rows always compete
+        if (l == 0) {
+          pbuf[q] = bi;
+          if (!(best > 0.f) || !isfinite(best)) badflag = 1;
+        }
+      }
+      __syncthreads();
+      const int p = pbuf[q];
+      const int lp = p >> 2, rp = p & 3;
+      const float2 piv = colbuf[q][p];
+      const float d = piv.x * piv.x + piv.y * piv.y;
+      const float2 inv = d > 0.f ? make_float2(piv.x / d, -piv.y / d) : make_float2(0.f, 0.f);
+      // pivot row (my 8 columns), broadcast from the owning lane, normalised
+      float2 rowp[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        float2 v;
+        v.x = (rp == 0) ? M[0][j].x : (rp == 1) ? M[1][j].x : (rp == 2) ? M[2][j].x : M[3][j].x;
+        v.y = (rp == 0) ? M[0][j].y : (rp == 1) ? M[1][j].y : (rp == 2) ? M[2][j].y : M[3][j].y;
+        v.x = __shfl_sync(0xffffffffu, v.x, lp);
+        v.y = __shfl_sync(0xffffffffu, v.y, lp);
+        rowp[j] = make_float2(v.x * inv.x - v.y * inv.y, v.x * inv.y + v.y * inv.x);
+        if (w == wk && j == ck) rowp[j] = inv;
+      }
+#pragma unroll
+      for (int rr = 0; rr < 4; ++rr) {
+        const int r = 4 * l + rr;
+        if (r == p) {
+#pragma unroll
+          for (int j = 0; j < 8; ++j) M[rr][j] = rowp[j];
+        } else {
+          const float2 f = colbuf[q][r];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            if (w == wk && j == ck) {
+              M[rr][j] = make_float2(-(f.x * inv.x - f.y * inv.y), -(f.x * inv.y + f.y * inv.x));
+            } else {
+              float2 m = M[rr][j];
+              m.x = fmaf(-f.x, rowp[j].x, m.x); m.x = fmaf(f.y, rowp[j].y, m.x);
+              m.y = fmaf(-f.x, rowp[j].y, m.y); m.y = fmaf(-f.y, rowp[j].x, m.y);
+              M[rr][j] = m;
+            }
+          }
+        }
+      }
+      if (l == lp) used |= 1u << rp;
+      if (tid == 0) perm[k] = p;
+    }
+    __syncthreads();
+    if (tid < 128) pinv[tid] = -1;
+    __syncthreads();
+    if (tid < 128) pinv[perm[tid] & 127] = tid;
+    __syncthreads();
+#pragma unroll
+    for (int rr = 0; rr < 4; ++rr)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int orow = pinv[4 * l + rr], ocol = perm[8 * w + j];
+        if (orow >= 0 && orow < n && ocol >= 0 && ocol < n)
+          X[orow + (long long)ocol * ld] = from_f2<TC>(M[rr][j]);
+      }
+    if (tid == 0 && badflag && a.status) atomicOr(&a.status[b], PT_SINGULAR);
+    __syncthreads();
+  }
+}
+
 long long grid_for(long long batch) { return batch < 65535 * 4 ? batch : 65535 * 4; }
 
 }  // namespace
@@ -242,6 +364,11 @@ template <typename TC>
 cudaError_t zinv_f32(const InvArgs& a, cudaStream_t s) {
   if (a.batch <= 0) return cudaSuccess;
   if (a.n > 128) return cudaErrorInvalidValue;
+  if (a.n > 64) {  // register-blocked elimination
+    zinv_f32_rb_kernel<TC><<<(unsigned)grid_for(a.batch), 512, 0, s>>>(a);
+    count_launch();
+    return cudaGetLastError();
+  }
   const size_t sm = (size_t)a.n * a.n * sizeof(float2) + (size_t)a.n * 2 * sizeof(float2) +
                     (size_t)a.n * sizeof(int);
   cudaError_t e = cudaFuncSetAttribute(zinv_f32_kernel<TC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
