@@ -197,6 +197,27 @@ qt_status qt_zinv_batch(qt_ctx* ctx, int n, int batch, const double* A, int64_t 
                         double* X, int64_t x_stride, qt_precision prec, unsigned flags,
                         int* status);
 
+/* Allocation-free split-precision block product.  No counterpart in the
+ * reference: it exists for callers that must not allocate device memory --
+ * hosts whose device memory belongs to another allocator (a framework's caching
+ * pool, a Fortran code's OpenMP `target enter data` buffers) and latency-
+ * critical loops where cudaMalloc/cudaFree would implicitly synchronise the
+ * device.  Same product as qt_zgemm_batch with QT_PREC_MIXED (device pointers,
+ * op 'N'/'C', real alpha/beta, n <= 128, slices 0 (=4), 4, 6 or 7), but its
+ * scratch (256 scale exponents per batch entry) lives in a file-scope device
+ * array of QT_NOALLOC_MAX_BATCH x 256 ints (512 KiB per GPU, held until the
+ * process exits), and it needs no context: work goes on `stream`.
+ *   - batch > QT_NOALLOC_MAX_BATCH is rejected with QT_ERR_ARG;
+ *   - the first call on a device fetches the array's device address with
+ *     cudaGetSymbolAddress; make it before any stream capture;
+ *   - all calls share the array, so calls overlapping on the GPU race;
+ *   - it calls no cudaMalloc, cudaFree or other allocating routine.         */
+#define QT_NOALLOC_MAX_BATCH 512
+qt_status qt_zgemm_batch_noalloc(int n, int batch, char opA, const double* A, int64_t a_stride,
+                                 char opB, const double* B, int64_t b_stride, const double* alpha,
+                                 const double* beta, const double* D, int64_t d_stride, double* C,
+                                 int64_t c_stride, int slices, void* stream);
+
 /* ---- GW / SCBA (one k-point; device pointers: QT_FLAG_DEVICE_POINTERS required).
  * Energy-resolved arrays are [nE][nx][nm*nm] complex128 column-major
  * slab-diagonal blocks; the energy grid E must be uniform (dE = E[1]-E[0]) and

@@ -24,7 +24,7 @@ EXPORTS = [
     "qt_last_error", "qt_version", "qt_rgf_solve", "qt_rgf_constblocksize",
     "qt_sancho_batch", "qt_zgemm_batch", "qt_zinv_batch", "qt_kernel_launches",
     "qt_ctx_profile", "qt_ctx_profile_read", "qt_ctx_stream", "qt_gw_step", "qt_scba_solve",
-    "qt_corr_batch",
+    "qt_corr_batch", "qt_zgemm_batch_noalloc",
 ]
 
 
@@ -90,6 +90,8 @@ def load(path=LIB_PATH):
     lib.qt_scba_solve.argtypes = [vp, C.POINTER(QtDevice), vp, ci, C.POINTER(QtContacts), vp,
                                   dbl, dbl, dbl, ci, ci, C.c_uint, vp, vp, vp, vp, vp]
     lib.qt_corr_batch.argtypes = [vp, ci, i64, vp, vp, vp, ci, C.c_uint]
+    lib.qt_zgemm_batch_noalloc.argtypes = [ci, ci, C.c_char, vp, i64, C.c_char, vp, i64, vp, vp,
+                                           vp, i64, vp, i64, ci, vp]
     for name in EXPORTS:
         f = getattr(lib, name)
         if name not in ("qt_last_error", "qt_version", "qt_kernel_launches"):
