@@ -49,7 +49,10 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--batch-energies", type=int, default=64,
                     help="energies per step (x 16 k-points)")
-    ap.add_argument("--fp64-energies", type=int, default=2)
+    ap.add_argument("--fp64-energies", type=int, default=8,
+                    help="energies (x 16 k) of the FP64-pipe sample; 0 skips it")
+    ap.add_argument("--hi-energies", type=int, default=16,
+                    help="energies (x 16 k) of the complex128 split-path sample")
     ap.add_argument("--cpu-points", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -185,6 +188,7 @@ def run_ours(a):
     from quantum_transport_gb300.build import build
     build()
     from quantum_transport_gb300 import rgf
+    from quantum_transport_gb300.shard import energy_range, max_over_ranks
 
     dev = device()
     ctx = rgf.Context(local)
@@ -204,9 +208,13 @@ def run_ours(a):
            "status": torch.zeros(P, dtype=torch.int32, device="cuda")}
     kw = dict(mul=0.1, mur=-0.1, templ=300.0, tempr=300.0, sancho_tol=1e-10, caroli=True)
 
+    # each rank owns a contiguous block of the energy grid and cycles through it
+    lo, hi = energy_range(NE, world, rank)
+    nblk_r = max(1, (hi - lo) // B)
+
     def step(i, precision="mixed", o=out, nE=B):
-        blk = (rank * 7919 + i) % nblk
-        rgf.rgf_solve_device(ctx, H00, nm2, 0, H10, 0, 0, NM, NX, NK, E[blk * B:], nE, o,
+        e0 = min(lo + (i % nblk_r) * B, NE - B)
+        rgf.rgf_solve_device(ctx, H00, nm2, 0, H10, 0, 0, NM, NX, NK, E[e0:], nE, o,
                              precision=precision, **kw)
 
     torch.cuda.synchronize()
@@ -233,10 +241,7 @@ def run_ours(a):
     ctx.profile(False)
     prof = ctx.profile_read()
     ms = ev0.elapsed_time(ev1) / a.steps
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms)
     status_bad = int((out["status"] != 0).sum().item())
     value = world * P / (ms / 1e3)
 
@@ -270,7 +275,7 @@ def run_ours(a):
                                       "points_bad_status": status_bad}),
             "roofline": roofline, "clocks": clk, "gpu_launches": launches}
 
-    if rank == 0:
+    if rank == 0 and a.fp64_energies > 0:
         # ---- plain-FP64 GPU path on a small sample of the same points; T(E) error
         Bf = a.fp64_energies
         Pf = Bf * NK
@@ -295,7 +300,30 @@ def run_ours(a):
                                           np.max(np.abs(d64.imag))),
                 "diag_glesser_rel_err_max": float(np.max(np.abs(lmx - l64)) /
                                                   max(np.max(np.abs(l64)), 1e-300))}
+        if a.hi_energies > 0:
+            # ---- complex128 split path (FP64-grade): throughput and error on its own sample
+            Bh = min(a.hi_energies, B)
+            oh = {k: torch.zeros(Bh * NK * (NX * NM if k.startswith("diag") else 1),
+                                 dtype=v.dtype, device="cuda") for k, v in out.items()}
+            rgf.rgf_solve_device(ctx, H00, nm2, 0, H10, 0, 0, NM, NX, NK, E, 1, oh,
+                                 precision="mixed-fp64", **kw)  # first-call set-up
+            ctx.sync()
+            t0 = time.perf_counter()
+            rgf.rgf_solve_device(ctx, H00, nm2, 0, H10, 0, 0, NM, NX, NK, E, Bh, oh,
+                                 precision="mixed-fp64", **kw)
+            ctx.sync()
+            th = time.perf_counter() - t0
+            m = min(Bh, Bf) * NK
+            Th = oh["T"].cpu().numpy()[:m]
+            dh = oh["diag_gr"].cpu().numpy()[:m * NX * NM]
+            fp64["mixed_fp64"] = {
+                "value": Bh * NK / th, "unit": "E-points/s", "sample_points": Bh * NK,
+                "speedup_vs_fp64": (Bh * NK / th) / (Pf / t64),
+                "T_rel_err_max": float(np.max(np.abs(Th - T64[:m]) / np.abs(T64[:m]))),
+                "ldos_rel_err_max": float(np.max(np.abs(dh.imag - d64[:m * NX * NM].imag)) /
+                                          np.max(np.abs(d64[:m * NX * NM].imag)))}
         line["fp64_gpu"] = fp64
+    if rank == 0:
         if world == 1 and not a.no_cpu:
             threads = os.cpu_count() or 1
             v, dt, r = cpu_baseline(dev, a.cpu_points, threads)
@@ -305,8 +333,9 @@ def run_ours(a):
                                               f"energy x 16 k) of the same workload, {dt:.1f} s; "
                                               "C99+OpenMP restatement of the reference sweep"}
             Tc = r["T"].ravel()
-            line["cpu_baseline"]["T_rel_err_vs_fp64_gpu"] = float(
-                np.max(np.abs(Tc - T64[:Tc.size]) / np.abs(T64[:Tc.size])))
+            if "fp64_gpu" in line:
+                line["cpu_baseline"]["T_rel_err_vs_fp64_gpu"] = float(
+                    np.max(np.abs(Tc - T64[:Tc.size]) / np.abs(T64[:Tc.size])))
         if not a.no_e2e:
             # ---- end to end through the host-pointer C-ABI call
             Eh = dev.E

@@ -37,9 +37,16 @@ typedef enum {
 
 typedef enum {
   QT_PREC_FP64 = 0,  /* complex128 on the FP64 pipes (plain path)                 */
-  QT_PREC_MIXED = 1  /* Ozaki-split bf16 tensor-core GEMMs (tcgen05, FP32 TMEM
+  QT_PREC_MIXED = 1, /* Ozaki-split bf16 tensor-core GEMMs (tcgen05, FP32 TMEM
                         accumulation, exact leading digit levels), FP32 block LU +
-                        one residual refinement; Sancho at FP64-grade digits     */
+                        one residual refinement; Sancho at FP64-grade digits.
+                        The sweep stores complex64 blocks: H is resolved to
+                        2^-24 relative, which near band edges (η -> 0) moves
+                        spectra by up to ~1e-4 of their maximum               */
+  QT_PREC_MIXED_FP64 = 2 /* the same tensor-core products with complex128
+                        storage everywhere: 6-digit products (2^-44 relative)
+                        in the sweep, 7 in the leads, FP32 block LU + three
+                        refinements.  FP64-grade results at tensor-core rate  */
 } qt_precision;
 
 #define QT_FLAG_DEVICE_POINTERS 1u /* all arrays are device pointers            */
@@ -256,6 +263,69 @@ qt_status qt_scba_solve(qt_ctx* ctx, const qt_device* dev, const double* E, int 
  *   mode 1: Z[e] = sum_m X[e - (m - n/2)] Y[m]          n <= 2048.          */
 qt_status qt_corr_batch(qt_ctx* ctx, int n, int64_t nseries, const double* X, const double* Y,
                         double* Z, int mode, unsigned flags);
+
+/* ---------------------------------------------------------------------------
+ * Learned SCBA mixing: the multilayer perceptron that proposes the next
+ * self-energy iterate.  No counterpart in the reference, whose SCBA loop mixes
+ * linearly (src/gw_mod.f90:747-749).
+ *
+ * Network: n_in -> width -> ... -> width -> n_out with `depth` GELU hidden
+ * layers; BF16 weights and activations, FP32 accumulation on the tensor cores,
+ * FP32 master parameters, AdamW (beta1 0.9, beta2 0.999, eps 1e-8, weight decay
+ * decoupled and applied to every parameter), loss = mean squared error over all
+ * outputs.  Parameters are one flat FP32 array: for each layer l, W_l
+ * (dout x din, row-major) followed by b_l (dout).
+ * Inputs X [batch][n_in], targets T and outputs Y [batch][n_out], row-major
+ * FP32; device pointers with QT_FLAG_DEVICE_POINTERS, host pointers otherwise.
+ * ------------------------------------------------------------------------- */
+typedef struct qt_mlp qt_mlp;
+
+/* init_params: host array of qt_mlp_num_params floats, or NULL for
+ * Glorot-uniform weights (seeded) and zero biases.  Runs on ctx's stream.   */
+qt_status qt_mlp_create(qt_ctx* ctx, int n_in, int width, int depth, int n_out, int max_batch,
+                        const float* init_params, uint64_t seed, qt_mlp** out);
+qt_status qt_mlp_destroy(qt_mlp* net);
+qt_status qt_mlp_num_params(const qt_mlp* net, int64_t* count);
+qt_status qt_mlp_get_params(qt_mlp* net, float* host_params);
+qt_status qt_mlp_set_params(qt_mlp* net, const float* host_params);
+/* Y = net(X) */
+qt_status qt_mlp_infer(qt_mlp* net, int batch, const float* X, float* Y, unsigned flags);
+/* gradient of the loss at the current parameters (host output, flat like the
+ * parameters) and the loss; no update                                      */
+qt_status qt_mlp_grad(qt_mlp* net, int batch, const float* X, const float* T, float* grad_host,
+                      double* loss, unsigned flags);
+/* one AdamW step on the batch; loss (host, nullable) is the loss before the
+ * step.  Asynchronous when loss is NULL and QT_FLAG_SYNC is not set.       */
+qt_status qt_mlp_train_step(qt_mlp* net, int batch, const float* X, const float* T, float lr,
+                            float weight_decay, double* loss, unsigned flags);
+
+/* Mixing kernels (device pointers; QT_FLAG_SYNC synchronises).  Self-energies
+ * are [nE][nx][nm*nm] complex128 column-major blocks; orbital o = l*nm + i.
+ * No counterpart in the reference (linear mixing only).
+ *
+ * qt_mix_diag:     out[q][e][o] = Im X_q[e][l][i,i], q = 0 (XL), 1 (XG)
+ * qt_mix_features: network input rows feats[o][2*nhist*64 + 2] from a ring
+ *                  [h][q][e][o] of nhist (<= 3) diagonal residual series,
+ *                  newest first: 64 Chebyshev coefficients per series
+ *                  (Qt: [nE][64] projector) scaled by the newest pair's norm,
+ *                  then log10(residual)/8 and the orbital's log10 decay
+ * qt_mix_apply:    out = S + a_ij R + b_ij (S - S_prev), a_ij = (a_i + a_j)/2,
+ *                  b_ij likewise; ab[o] = (a_o, b_o) clamped to [0, alpha_max]
+ *                  and [beta_min, beta_max]; S_prev may be NULL; out may be S
+ * qt_mix_gram:     G[i][j] = Re <XL_i, XL_j> + Re <XG_i, XG_j> (host k x k)
+ * qt_mix_combine:  out = sum_i coef_i (X_i + alpha R_i)  (k <= 8 vectors)   */
+qt_status qt_mix_diag(qt_ctx* ctx, int nE, int nx, int nm, const double* XL, const double* XG,
+                      double* out, unsigned flags);
+qt_status qt_mix_features(qt_ctx* ctx, int nE, int64_t norb, int nhist, const double* ring,
+                          const double* Qt, double log_residual, float* feats, unsigned flags);
+qt_status qt_mix_apply(qt_ctx* ctx, int nE, int nx, int nm, const float* ab, double alpha_max,
+                       double beta_min, double beta_max, const double* S, const double* R,
+                       const double* S_prev, double* out, unsigned flags);
+qt_status qt_mix_gram(qt_ctx* ctx, int64_t count, int k, const double* const* XL,
+                      const double* const* XG, double* G_host);
+qt_status qt_mix_combine(qt_ctx* ctx, int64_t count, int k, const double* coef,
+                         const double* const* X, const double* const* R, double alpha,
+                         double* out, unsigned flags);
 
 #ifdef __cplusplus
 }

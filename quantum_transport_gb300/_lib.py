@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libqtgpu.so")
 
 QT_OK, QT_ERR_ARG, QT_ERR_CUDA, QT_ERR_NOMEM, QT_ERR_UNSUPPORTED, QT_ERR_POINTS = range(6)
-QT_PREC_FP64, QT_PREC_MIXED = 0, 1
+QT_PREC_FP64, QT_PREC_MIXED, QT_PREC_MIXED_FP64 = 0, 1, 2
 QT_FLAG_DEVICE_POINTERS, QT_FLAG_CAROLI, QT_FLAG_SYNC = 1, 2, 4
 QT_QUIRK_CPU_FERMI, QT_QUIRK_GLP_ZERO, QT_QUIRK_BACK_H1I_NEXT = 1, 2, 4
 QT_PT_SINGULAR, QT_PT_SANCHO_NOT_CONVERGED, QT_PT_NONFINITE = 1, 2, 4
@@ -25,6 +25,9 @@ EXPORTS = [
     "qt_sancho_batch", "qt_zgemm_batch", "qt_zinv_batch", "qt_kernel_launches",
     "qt_ctx_profile", "qt_ctx_profile_read", "qt_ctx_stream", "qt_gw_step", "qt_scba_solve",
     "qt_corr_batch", "qt_zgemm_batch_noalloc",
+    "qt_mlp_create", "qt_mlp_destroy", "qt_mlp_num_params", "qt_mlp_get_params",
+    "qt_mlp_set_params", "qt_mlp_infer", "qt_mlp_grad", "qt_mlp_train_step",
+    "qt_mix_diag", "qt_mix_features", "qt_mix_apply", "qt_mix_gram", "qt_mix_combine",
 ]
 
 
@@ -92,6 +95,21 @@ def load(path=LIB_PATH):
     lib.qt_corr_batch.argtypes = [vp, ci, i64, vp, vp, vp, ci, C.c_uint]
     lib.qt_zgemm_batch_noalloc.argtypes = [ci, ci, C.c_char, vp, i64, C.c_char, vp, i64, vp, vp,
                                            vp, i64, vp, i64, ci, vp]
+    flt = C.c_float
+    lib.qt_mlp_create.argtypes = [vp, ci, ci, ci, ci, ci, vp, C.c_uint64, C.POINTER(vp)]
+    lib.qt_mlp_destroy.argtypes = [vp]
+    lib.qt_mlp_num_params.argtypes = [vp, C.POINTER(C.c_int64)]
+    lib.qt_mlp_get_params.argtypes = [vp, vp]
+    lib.qt_mlp_set_params.argtypes = [vp, vp]
+    lib.qt_mlp_infer.argtypes = [vp, ci, vp, vp, C.c_uint]
+    lib.qt_mlp_grad.argtypes = [vp, ci, vp, vp, vp, C.POINTER(dbl), C.c_uint]
+    lib.qt_mlp_train_step.argtypes = [vp, ci, vp, vp, flt, flt, C.POINTER(dbl), C.c_uint]
+    pvp = C.POINTER(vp)
+    lib.qt_mix_diag.argtypes = [vp, ci, ci, ci, vp, vp, vp, C.c_uint]
+    lib.qt_mix_features.argtypes = [vp, ci, i64, ci, vp, vp, dbl, vp, C.c_uint]
+    lib.qt_mix_apply.argtypes = [vp, ci, ci, ci, vp, dbl, dbl, dbl, vp, vp, vp, vp, C.c_uint]
+    lib.qt_mix_gram.argtypes = [vp, i64, ci, pvp, pvp, vp]
+    lib.qt_mix_combine.argtypes = [vp, i64, ci, vp, pvp, pvp, dbl, vp, C.c_uint]
     for name in EXPORTS:
         f = getattr(lib, name)
         if name not in ("qt_last_error", "qt_version", "qt_kernel_launches"):

@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "../../include/qt_rgf.h"
+#include "qt_abi.h"
 #include "qt_common.cuh"
 #include "qt_kernels.h"
 
@@ -50,18 +51,6 @@ std::atomic<long long> g_launches{0};
 void qt::count_launch(long long n) { g_launches += n; }
 extern "C" int64_t qt_kernel_launches(void) { return g_launches.load(); }
 extern "C" const char* qt_version(void) { return "qtgpu 0.1 sm_103a"; }
-
-#define QT_FAIL(code, msg)                             \
-  do {                                                 \
-    qt_set_last_error((msg), __FILE__, __LINE__);      \
-    return (code);                                     \
-  } while (0)
-
-#define QT_TRY(expr)                                   \
-  do {                                                 \
-    qt_status _s = (expr);                             \
-    if (_s != QT_OK) return _s;                        \
-  } while (0)
 
 // Optional CUDA-event timing of the block products and inverses on the
 // context's stream (qt_ctx_profile): kinds 0 complex64 split product,
@@ -99,6 +88,9 @@ struct qt_ctx {
   void* conv = nullptr;  // complex64 copies of H / sigma for the split-precision sweep
   size_t conv_bytes = 0;
 };
+
+int qt::ctx_device(const qt_ctx* c) { return c->device; }
+cudaStream_t qt::ctx_stream(const qt_ctx* c) { return c->stream; }
 
 namespace {
 
@@ -309,7 +301,7 @@ struct Problem {
 
 size_t wave_bytes(const Problem& pb, long long P) {
   const size_t nm2 = (size_t)pb.nm * pb.nm;
-  const size_t tc = pb.prec == QT_PREC_FP64 ? 16 : 8;
+  const size_t tc = pb.prec == QT_PREC_MIXED ? 8 : 16;  // complex64 sweep only in MIXED
   const size_t sweep = (2 * (size_t)pb.nx + 14 + 2) * tc;  // g_l, g^<_l, temporaries, refinement
   const size_t lead = (7 + 2 + 6) * 16;                     // Sancho state + refinement + contact
   return (sweep + lead) * nm2 * P + (size_t)P * (512 + 2048) + (512 << 10);
@@ -443,7 +435,9 @@ qt_status solve_wave(qt_ctx* ctx, const Problem& pb, long long p0, long long P, 
   // sweep operations on TC, contact operations on complex128
   Ops<TC> op{s, n, pb.prec};
   op.slices = pb.sweep_slices;
-  op.refine = split ? 1 : 0;
+  // complex64 sweep: one refinement reaches its storage resolution; complex128 sweep
+  // (MIXED_FP64): three, as for the leads
+  op.refine = split ? (sizeof(TC) == 8 ? 1 : 3) : 0;
   op.one = one; op.rt1 = rt1; op.rt2 = rt2; op.P = P; op.scales = scales;
   op.prof = &ctx->prof;
   Ops<double2> cop{s, n, pb.prec};
@@ -763,22 +757,31 @@ extern "C" qt_status qt_ctx_stream(qt_ctx* c, void** stream) {
 
 namespace {
 
+bool valid_prec(qt_precision p) {
+  return p == QT_PREC_FP64 || p == QT_PREC_MIXED || p == QT_PREC_MIXED_FP64;
+}
+
 int env_int(const char* name, int dflt) {
   const char* v = getenv(name);
   return v && *v ? atoi(v) : dflt;
 }
 
 qt_status run_problem(qt_ctx* ctx, Problem& pb, long long hii_n, long long h1i_n) {
-  // digits of the split-precision products: 4 for the complex64 sweep, 7 (FP64 grade) for
-  // the lead decimation; QT_SWEEP_SLICES / QT_LEAD_SLICES override for accuracy studies
-  pb.sweep_slices = env_int("QT_SWEEP_SLICES", 4);
+  // digits of the split-precision products: 4 for the complex64 sweep (MIXED), 6 for the
+  // complex128 sweep (MIXED_FP64), 7 (FP64 grade) for the lead decimation;
+  // QT_SWEEP_SLICES / QT_LEAD_SLICES override for accuracy studies
+  const bool c64 = pb.prec == QT_PREC_MIXED;
+  pb.sweep_slices = env_int("QT_SWEEP_SLICES", c64 ? 4 : 6);
   pb.lead_slices = env_int("QT_LEAD_SLICES", 7);
-  if (pb.sweep_slices != 3 && pb.sweep_slices != 4) QT_FAIL(QT_ERR_ARG, "QT_SWEEP_SLICES in {3,4}");
+  if (c64 && pb.sweep_slices != 3 && pb.sweep_slices != 4)
+    QT_FAIL(QT_ERR_ARG, "QT_SWEEP_SLICES in {3,4} for the complex64 sweep");
+  if (!c64 && pb.sweep_slices != 4 && pb.sweep_slices != 6 && pb.sweep_slices != 7)
+    QT_FAIL(QT_ERR_ARG, "QT_SWEEP_SLICES in {4,6,7} for the complex128 sweep");
   if (pb.lead_slices != 4 && pb.lead_slices != 6 && pb.lead_slices != 7)
     QT_FAIL(QT_ERR_ARG, "QT_LEAD_SLICES in {4,6,7}");
   cudaStream_t s = ctx->stream;
   const bool split = pb.prec != QT_PREC_FP64;
-  if (split) {
+  if (c64) {
     const long long blk = pb.npts * pb.nx * (long long)pb.nm * pb.nm;
     const long long cnt = hii_n + h1i_n + (pb.sigr ? blk : 0) + (pb.sigl ? blk : 0);
     QT_TRY(ensure(ctx->conv, ctx->conv_bytes, (size_t)cnt * sizeof(float2) + 4096));
@@ -801,7 +804,7 @@ qt_status run_problem(qt_ctx* ctx, Problem& pb, long long hii_n, long long h1i_n
   for (long long p0 = 0; p0 < pb.npts; p0 += P) {
     const long long Pw = std::min(P, pb.npts - p0);
     Arena ar{reinterpret_cast<char*>(ctx->arena), ctx->arena_bytes, 0};
-    if (split) QT_TRY(solve_wave<float2>(ctx, pb, p0, Pw, ar));
+    if (c64) QT_TRY(solve_wave<float2>(ctx, pb, p0, Pw, ar));
     else QT_TRY(solve_wave<double2>(ctx, pb, p0, Pw, ar));
   }
   if (split) {
@@ -822,7 +825,8 @@ extern "C" qt_status qt_rgf_solve(qt_ctx* ctx, const qt_device* dev, const doubl
     QT_FAIL(QT_ERR_ARG, "need nm > 0, nx >= 2, nk > 0, nE > 0");
   if (!dev->Hii || !dev->H1i) QT_FAIL(QT_ERR_ARG, "Hii/H1i required");
   if (dev->Sii) QT_FAIL(QT_ERR_UNSUPPORTED, "Sii must be NULL (identity overlap)");
-  if (prec == QT_PREC_MIXED && dev->nm > 128) QT_FAIL(QT_ERR_UNSUPPORTED, "mixed path needs nm <= 128");
+  if (!valid_prec(prec)) QT_FAIL(QT_ERR_ARG, "unknown precision");
+  if (prec != QT_PREC_FP64 && dev->nm > 128) QT_FAIL(QT_ERR_UNSUPPORTED, "mixed path needs nm <= 128");
   if (c->sancho_max_iter <= 0) QT_FAIL(QT_ERR_ARG, "sancho_max_iter must be > 0");
   cudaSetDevice(ctx->device);
   const int nm = dev->nm, nx = dev->nx, nk = dev->nk;
@@ -959,6 +963,8 @@ extern "C" qt_status qt_sancho_batch(qt_ctx* ctx, int nm, int npts, const double
   if (!ctx || !E || !H00 || !H10 || !G00 || nm <= 0 || npts <= 0 || max_iter <= 0)
     QT_FAIL(QT_ERR_ARG, "bad sancho arguments");
   if (S00) QT_FAIL(QT_ERR_UNSUPPORTED, "S00 must be NULL (identity overlap)");
+  if (!valid_prec(prec)) QT_FAIL(QT_ERR_ARG, "unknown precision");
+  if (prec == QT_PREC_MIXED_FP64) prec = QT_PREC_MIXED;  // blocks are complex128 in both
   if (prec == QT_PREC_MIXED && nm > 128) QT_FAIL(QT_ERR_UNSUPPORTED, "mixed path needs nm <= 128");
   cudaSetDevice(ctx->device);
   const long long nm2 = (long long)nm * nm;
@@ -1038,6 +1044,8 @@ extern "C" qt_status qt_zgemm_batch(qt_ctx* ctx, int n, int batch, char opA, con
   const int oa = parse_op(opA), ob = parse_op(opB);
   if (!ctx || !A || !B || !C || n <= 0 || batch <= 0 || oa < 0 || ob < 0)
     QT_FAIL(QT_ERR_ARG, "bad gemm arguments");
+  if (!valid_prec(prec)) QT_FAIL(QT_ERR_ARG, "unknown precision");
+  if (prec == QT_PREC_MIXED_FP64) prec = QT_PREC_MIXED;  // blocks are complex128 in both
   if (prec == QT_PREC_MIXED && (n > 128 || oa == qt::OP_T || ob == qt::OP_T))
     QT_FAIL(QT_ERR_UNSUPPORTED, "mixed gemm: n <= 128 and op in {N, C}");
   if (slices < 0 || slices > 8) QT_FAIL(QT_ERR_ARG, "slices in 0..8");
@@ -1088,6 +1096,8 @@ extern "C" qt_status qt_zinv_batch(qt_ctx* ctx, int n, int batch, const double* 
                                    int64_t a_stride, double* X, int64_t x_stride,
                                    qt_precision prec, unsigned flags, int* status) {
   if (!ctx || !A || !X || n <= 0 || batch <= 0) QT_FAIL(QT_ERR_ARG, "bad inverse arguments");
+  if (!valid_prec(prec)) QT_FAIL(QT_ERR_ARG, "unknown precision");
+  if (prec == QT_PREC_MIXED_FP64) prec = QT_PREC_MIXED;  // blocks are complex128 in both
   if (prec == QT_PREC_MIXED && n > 128) QT_FAIL(QT_ERR_UNSUPPORTED, "mixed inverse needs n <= 128");
   cudaSetDevice(ctx->device);
   cudaStream_t s = ctx->stream;
@@ -1260,7 +1270,8 @@ qt_status gw_setup(qt_ctx* ctx, const qt_device* dev, const double* E, int nE,
   if (dev->nm <= 0 || dev->nx < 2 || nE < 2) QT_FAIL(QT_ERR_ARG, "need nm > 0, nx >= 2, nE >= 2");
   if (2 * nE > 4096) QT_FAIL(QT_ERR_UNSUPPORTED, "GW path: nE <= 2048 (FFT length 4096)");
   if (dev->Sii) QT_FAIL(QT_ERR_UNSUPPORTED, "Sii must be NULL (identity overlap)");
-  if (prec == QT_PREC_MIXED && dev->nm > 128) QT_FAIL(QT_ERR_UNSUPPORTED, "mixed path needs nm <= 128");
+  if (!valid_prec(prec)) QT_FAIL(QT_ERR_ARG, "unknown precision");
+  if (prec != QT_PREC_FP64 && dev->nm > 128) QT_FAIL(QT_ERR_UNSUPPORTED, "mixed path needs nm <= 128");
   cudaSetDevice(ctx->device);
   pb = Problem{};
   pb.nm = dev->nm; pb.nx = dev->nx; pb.nk = 1; pb.npts = nE;

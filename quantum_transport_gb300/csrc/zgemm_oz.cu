@@ -8,26 +8,29 @@
 // split-precision path.  GB300's FP64 pipes run at ~1 TFLOP/s, so FP64-grade
 // products are rebuilt from exact BF16 digit products:
 //
-//  * complex -> real: with At = op(A), Bt = op(B) (n x n complex)
-//      Cr = [Re At | Im At] . [Re Bt ; -Im Bt]      Ci = [Re At | Im At] . [Im Bt ; Re Bt]
-//    one CTA computes one real part (M = 128 padded rows, N = n padded to 16,
-//    K' = 2n padded to 64);
-//  * digits: every row i of [Re At | Im At] is scaled by 2^-e_i (e_i: exponent
-//    bound of the row's largest entry, |entry| < 2^(e_i-1)) and written as S
-//    balanced base-256 digits D_s = d_s 2^(-8s), |d_s| <= 128 -- each exactly
-//    representable in BF16.  Columns of [Re Bt; Im Bt] likewise with f_j;
+//  * complex -> real: with At = op(A), Bt = op(B) (n x n complex), the real K
+//    axis interleaves the real and imaginary parts of each complex k:
+//      A' row i = (Re At[i,k], Im At[i,k])_k
+//      Cr: B' column j = (Re Bt[k,j], -Im Bt[k,j])_k    Ci: (Im Bt[k,j], Re Bt[k,j])_k
+//    so each complex element is loaded once per stage.  One CTA work item is one
+//    real part of one NT-column tile (M = 128 padded rows, K' = 2n);
+//  * digits: every row i of A' is scaled by 2^-e_i (e_i: exponent bound of the
+//    row's largest entry, |entry| < 2^(e_i-1), from the prologue kernel) and
+//    written as S balanced base-256 digits D_s = d_s 2^(-8s), |d_s| <= 128 --
+//    each exactly representable in BF16.  Columns of B' likewise with f_j;
 //  * products: all digit pairs (s, t) with s + t <= L are issued; pair level
-//    l = s + t accumulates into TMEM accumulator min(l, 3).  For l <= 3 every
-//    partial sum is an integer multiple of 2^(-8l) below 2^24 * 2^(-8l)
-//    ((l+1) products of <= 2^14, K' <= 256), so levels 0..3 are EXACT in FP32;
-//    levels > 3 (FP64-grade mode only) share accumulator 3 with a rounding
-//    error 2^-48 relative to the row/column scale;
-//  * epilogue: the four accumulators are summed in double-float FP32
-//    arithmetic (TwoSum), scaled by 2^(e_i + f_j - 16), and written as FP32
-//    (correctly rounded up to the last digit level) or assembled into FP64
-//    bits with integer operations (no use of the slow FP64 pipe).
+//    l = s + t accumulates into TMEM accumulator min(l, NACC - 1), where the 512
+//    TMEM columns hold NACC = 512 / NT accumulators (4 for NT = 128, 8 for
+//    NT = 64).  A level-l partial sum is an integer multiple of 2^(-8l) below
+//    (l+1) 2^14 K' 2^(-8l), so levels l <= 3 are EXACT in FP32 for K' <= 256;
+//    a higher level on its own accumulator rounds at 2^(-24-8l) <= 2^-56 of
+//    the row/column scale;
+//  * epilogue: the accumulators are summed in double-float FP32 arithmetic
+//    (TwoSum), scaled by 2^(e_i + f_j - 16), and written as FP32 (complex64
+//    output) or assembled into FP64 bits with integer operations (complex128
+//    output, no use of the FP64 pipe).
 //
-// Roles (416 threads, one CTA per SM: the four accumulators use all 512 TMEM
+// Roles (416 threads, one CTA per SM: the accumulators use all 512 TMEM
 // columns):  warps 0-3 epilogue (TMEM lanes 0-127), warps 4-11 producers
 // (digit slicing straight from global memory into the canonical no-swizzle
 // K-major UMMA layout in shared memory), warp 12 TMEM allocation + the single
@@ -37,6 +40,7 @@
 
 #include "qt_common.cuh"
 #include "qt_kernels.h"
+#include "tc_ptx.cuh"
 
 namespace qt {
 
@@ -53,99 +57,24 @@ constexpr int PLANE_BYTES = 128 * KC * 2;       // one digit plane of a 128-row 
 constexpr uint32_t LBO = 128;                   // K-adjacent core matrices
 constexpr uint32_t SBO = (KC / 8) * 128;        // 8-row groups
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ uint64_t globaltimer() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait: false on timeout or when another role already aborted.
+using tc::fence_proxy_async;
+using tc::make_idesc;
+using tc::mbar_arrive;
+using tc::mbar_init;
+using tc::smem_u32;
+using tc::tmem_ld16;
+using tc::tmem_ld8;
+using tc::tmem_wait_ld;
+using tc::umma;
+using tc::umma_commit;
+
+// bounded wait (4 s); a timeout raises the CTA's abort flag and counts in g_oz_timeouts
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const uint64_t t0 = globaltimer();
-  while (!mbar_try_wait(bar, parity)) {
-    if (*abort_flag) return false;
-    if (globaltimer() - t0 > TIMEOUT_NS) {
-      *abort_flag = 1;
-      atomicAdd(&g_oz_timeouts, 1);
-      return false;
-    }
-  }
-  return true;
+  return tc::mbar_wait(bar, parity, abort_flag, &g_oz_timeouts, TIMEOUT_NS);
 }
-__device__ __forceinline__ void fence_proxy_async() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-__device__ __forceinline__ void tc_fence_before() {
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tc_fence_after() {
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
-  d |= (uint64_t)((LBO >> 4) & 0x3FFFu) << 16;
-  d |= (uint64_t)((SBO >> 4) & 0x3FFFu) << 32;
-  d |= (uint64_t)1 << 46;  // descriptor version (tcgen05); swizzle none
-  return d;
-}
-__host__ __device__ constexpr uint32_t make_idesc(int M, int N) {
-  return (1u << 4)                          // D format F32
-         | (1u << 7)                        // A format BF16
-         | (1u << 10)                       // B format BF16
-         | ((uint32_t)(N >> 3) << 17)       // N >> 3
-         | ((uint32_t)(M >> 4) << 24);      // M >> 4   (A, B K-major, no negate)
-}
-__device__ __forceinline__ void umma(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                     uint32_t acc) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
-}
-__device__ __forceinline__ void umma_commit(uint64_t* bar) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-          smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15},"
-      " [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-}
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t* r) {
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
-                 "=r"(r[6]), "=r"(r[7])
-               : "r"(taddr));
-}
-__device__ __forceinline__ void tmem_wait_ld() {
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
+__device__ __forceinline__ void tc_fence_before() { tc::fence_before(); }
+__device__ __forceinline__ void tc_fence_after() { tc::fence_after(); }
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) { return tc::make_desc(saddr, LBO, SBO); }
 
 // ------------------------------------------------------------ element access
 template <typename T> struct Elem;
@@ -399,10 +328,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int s
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == MMA_WARP) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                     smem_u32(tmem_base_sm)),
-                 "r"(512));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    tc::tmem_alloc(tmem_base_sm, 512);
   }
   tc_fence_before();
   __syncthreads();
@@ -608,7 +534,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int s
   __syncthreads();
   tc_fence_after();
   if (warp == MMA_WARP) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+    tc::tmem_dealloc(tmem, 512);
   }
 }
 

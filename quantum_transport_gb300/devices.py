@@ -81,3 +81,41 @@ def config_ballistic_small(seed=1234):
 def config_batched(seed=2024, nE=4096, nk=16, nx=100, nm=128):
     """100 slabs x 128 orbitals, 4096 energies on [-2, 2] eV x 16 k in [-pi, pi)."""
     return make_chain_device(nx, nm, nE, -2.0, 2.0, seed, nk=nk)
+
+
+@dataclasses.dataclass
+class GwDevice:
+    """A GW/SCBA problem: per-slab on-site blocks ``H00`` (nx, nm, nm), coupling
+    ``H10``, energies ``E`` and the Coulomb block ``V`` (nm, nm)."""
+    H00: np.ndarray
+    H10: np.ndarray
+    E: np.ndarray
+    V: np.ndarray
+
+    @property
+    def nx(self):
+        return self.H00.shape[0]
+
+    @property
+    def nm(self):
+        return self.H00.shape[-1]
+
+
+def coulomb_block(nm, spacing_nm=0.25, strength=14.4):
+    """V_ij = 14.4 / (|r_i - r_j| + 1) eV, orbitals on a 1-D grid of 0.25 nm."""
+    r = np.arange(nm) * spacing_nm
+    return strength / (np.abs(r[:, None] - r[None, :]) + 1.0)
+
+
+def disordered_gw_device(seed, nx=6, nm=8, nE=64, emin=-4.0, emax=4.0, sigma=None,
+                         base_seed=3):
+    """One disorder realisation of the GW device family: the seeded chain of
+    ``make_chain_device(seed=base_seed)`` plus on-site disorder N(0, sigma) on
+    every orbital of every slab, sigma ~ U[0.05, 0.3] eV drawn from ``seed``
+    unless given."""
+    base = make_chain_device(nx, nm, nE, emin, emax, seed=base_seed)
+    rng = np.random.default_rng(seed)
+    s = rng.uniform(0.05, 0.3) if sigma is None else sigma
+    H = np.repeat(base.H00[:1], nx, axis=0).copy()
+    H[:, np.arange(nm), np.arange(nm)] += rng.normal(0.0, s, (nx, nm))
+    return GwDevice(H00=H, H10=base.H10, E=base.E, V=coulomb_block(nm))

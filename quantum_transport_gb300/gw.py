@@ -42,7 +42,10 @@ def corr(ctx, X, Y, mode="corr"):
 
 
 class GwSystem:
-    """Device, energy grid, contacts and Coulomb block of one SCBA problem (nk = 1)."""
+    """Device, energy grid, contacts and Coulomb block of one SCBA problem (nk = 1).
+
+    ``H00``: one on-site block shared by all slabs (nm, nm), or one per slab
+    (nx, nm, nm); the leads continue the first and last slab."""
 
     def __init__(self, ctx, H00, H10, E, nx, V, *, mu=(0.0, 0.0), temp=(300.0, 300.0),
                  eta_lead=1e-3, sancho_max_iter=100, sancho_tol=1e-100, spindeg=2.0,
@@ -52,13 +55,17 @@ class GwSystem:
         self.nm = H00.shape[-1]
         self.nx = nx
         self.nE = len(E)
+        H00 = np.asarray(H00)
+        if H00.ndim == 3 and H00.shape[0] != nx:
+            raise ValueError("per-slab H00 must have nx blocks")
+        hl = self.nm * self.nm if H00.ndim == 3 else 0  # per-slab blocks or one shared block
         self.H00 = to_dev(H00)
         self.H10 = to_dev(H10)
         self.E = torch.from_numpy(np.ascontiguousarray(E, dtype=np.float64)).cuda()
         self.V = to_dev(V)
         self.spindeg = spindeg
         self.prec = PREC[precision]
-        self.dev = QtDevice(self.nm, nx, 1, _ptr(self.H00), 0, 0, _ptr(self.H10), 0, 0,
+        self.dev = QtDevice(self.nm, nx, 1, _ptr(self.H00), 0, hl, _ptr(self.H10), 0, 0,
                             None, 0, 0)
         self.con = QtContacts(mu[0], mu[1], temp[0], temp[1], eta_lead, 0.0, sancho_tol,
                               int(sancho_max_iter), 0)

@@ -1,0 +1,339 @@
+"""Learned SCBA mixing: a network proposes the next self-energy iterate.
+
+The reference iterates Sigma <- Sigma + alpha (F(Sigma) - Sigma) with a fixed
+alpha (src/gw_mod.f90:747-749), F being one GW evaluation (G by RGF, P, W,
+Sigma; ``GwSystem.step``).  Here, once three residuals R = F(Sigma) - Sigma
+are known, a multilayer perceptron reads, for every orbital o (row i of slab
+l), the Chebyshev coefficients of the diagonal residual series Im R^<_ii(E),
+Im R^>_ii(E) of the last three iterates plus the residual norms.  For each
+orbital it returns a step a_o and a momentum b_o.  The proposal is
+
+    Sigma_new = Sigma + a_ij R + b_ij (Sigma - Sigma_prev),   a_ij = (a_i + a_j)/2,
+
+applied to Sigma^R, Sigma^< and Sigma^> (b_ij likewise).  At a fixed point
+R = 0 and Sigma = Sigma_prev, so no proposal can move the fixed point.  A
+proposal is kept only if the residual F evaluates for it is below the last
+accepted one; otherwise it is discarded and a Pulay (DIIS) step over the
+accepted history is taken instead.
+
+Training data come from the method itself: plain-mixing runs on seeded
+disorder realisations give iterate histories and their converged fixed point
+Sigma*.  For each iterate and orbital the target (a*, b*) minimises
+|| diag(Sigma + a R + b D - Sigma*) || over both series, D = Sigma - Sigma_prev.
+Further rounds add the learned loop's own iterates with the same targets.
+The network is trained on the GPU by the library's own kernels (``mlp.Mlp``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import time
+
+import numpy as np
+
+from ._lib import check
+from .mlp import Mlp
+
+NCOEF = 64
+NHIST = 3
+N_IN = 2 * NHIST * NCOEF + 2
+N_OUT = 2
+ALPHA_MAX, BETA_MIN, BETA_MAX = 4.0, -0.5, 0.95
+
+
+def chebyshev_projector(nE, ncoef=NCOEF):
+    """Qt (nE, ncoef): least-squares Chebyshev coefficients c = Qt^T s of a series
+    s sampled on a uniform grid mapped to [-1, 1]."""
+    x = np.linspace(-1.0, 1.0, nE)
+    V = np.polynomial.chebyshev.chebvander(x, ncoef - 1)
+    return np.ascontiguousarray(np.linalg.pinv(V).T)
+
+
+def _vp(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def _plist(ts):
+    arr = (C.c_void_p * len(ts))(*[t.data_ptr() for t in ts])
+    return C.cast(arr, C.POINTER(C.c_void_p)), arr
+
+
+class MixOps:
+    """Self-energy arithmetic on the device through the mixing kernels."""
+
+    def __init__(self, system):
+        self.sys = system
+        self.ctx = system.ctx
+        self.lib = system.ctx._lib
+        self.count = system.nE * system.nx * system.nm * system.nm
+
+    def combine(self, coef, X, R, alpha, out):
+        px, kx = _plist(X)
+        pr, kr = _plist(R)
+        c = np.ascontiguousarray(coef, dtype=np.float64)
+        check(self.lib.qt_mix_combine(self.ctx.handle, self.count, len(X),
+                                      c.ctypes.data_as(C.c_void_p), px, pr, float(alpha),
+                                      _vp(out), 0))
+        return out
+
+    def diff(self, N, S, out):
+        """out = N - S"""
+        return self.combine([1.0], [N], [S], -1.0, out)
+
+    def gram(self, XL, XG):
+        k = len(XL)
+        G = np.zeros((k, k))
+        pl, kl = _plist(XL)
+        pg, kg = _plist(XG)
+        check(self.lib.qt_mix_gram(self.ctx.handle, self.count, k, pl, pg,
+                                   G.ctypes.data_as(C.c_void_p)))
+        return G
+
+    def residual(self, R, N):
+        """||R^<, R^>|| / ||N^<, N^>|| (the SCBA stopping measure)"""
+        G = self.gram([R[1], N[1]], [R[2], N[2]])
+        return float(np.sqrt(G[0, 0]) / max(np.sqrt(G[1, 1]), 1e-300))
+
+    def diag(self, XL, XG, out):
+        s = self.sys
+        check(self.lib.qt_mix_diag(self.ctx.handle, s.nE, s.nx, s.nm, _vp(XL), _vp(XG),
+                                   _vp(out), 0))
+        return out
+
+
+def pulay_coefficients(G):
+    """DIIS: minimise || sum c_i R_i || with sum c_i = 1 (G: residual Gram matrix)."""
+    k = G.shape[0]
+    scale = max(np.abs(np.diag(G)).max(), 1e-300)
+    A = np.zeros((k + 1, k + 1))
+    A[:k, :k] = G / scale
+    A[k, :k] = A[:k, k] = 1.0
+    b = np.zeros(k + 1)
+    b[k] = 1.0
+    return np.linalg.lstsq(A, b, rcond=None)[0][:k]
+
+
+@dataclasses.dataclass
+class ScbaResult:
+    sigma: tuple          # (Sigma^R, Sigma^<, Sigma^>) device tensors
+    residuals: list       # residual of every evaluation of F
+    evaluations: int      # GW evaluations (iterations), rejected proposals included
+    seconds: float
+    accepted: int = 0     # learned proposals kept
+    rejected: int = 0     # learned proposals discarded (Pulay step taken instead)
+    pulay: int = 0        # Pulay steps
+    plain: int = 0        # linear-mixing steps
+
+
+class Recorder:
+    """Collects network inputs and diagonal series of the iterates of one run,
+    from which training targets follow once the fixed point is known."""
+
+    def __init__(self):
+        self.feats, self.s, self.r, self.d = [], [], [], []
+
+    def add(self, feats, s_diag, r_diag, d_diag):
+        self.feats.append(feats)
+        self.s.append(s_diag)
+        self.r.append(r_diag)
+        self.d.append(d_diag)
+
+    def targets(self, s_star, lam=1e-9):
+        """(X, T): network inputs and the (a*, b*) that bring each orbital's diagonal
+        closest to the fixed point's (least squares over both series)."""
+        if not self.feats:
+            return np.zeros((0, N_IN), np.float32), np.zeros((0, N_OUT), np.float32)
+        X, T = [], []
+        for f, s, r, d in zip(self.feats, self.s, self.r, self.d):
+            u = (s_star - s).reshape(-1, s.shape[-1])  # [2 nE][norb]
+            r = r.reshape(u.shape)
+            d = d.reshape(u.shape)
+            a11, a12, a22 = (r * r).sum(0), (r * d).sum(0), (d * d).sum(0)
+            b1, b2 = (r * u).sum(0), (d * u).sum(0)
+            reg = lam * (a11 + a22) + 1e-300
+            det = (a11 + reg) * (a22 + reg) - a12 * a12
+            a = ((a22 + reg) * b1 - a12 * b2) / det
+            b = ((a11 + reg) * b2 - a12 * b1) / det
+            T.append(np.stack([np.clip(a, 0.0, ALPHA_MAX), np.clip(b, BETA_MIN, BETA_MAX)], 1))
+            X.append(f)
+        return np.concatenate(X).astype(np.float32), np.concatenate(T).astype(np.float32)
+
+
+class LearnedMixer:
+    """The network and the Chebyshev projector for one energy grid."""
+
+    def __init__(self, ctx, nE, *, width=512, depth=4, max_batch=1 << 16, seed=0, params=None):
+        import torch
+        self.ctx = ctx
+        self.nE = nE
+        self.Qt = torch.from_numpy(chebyshev_projector(nE)).cuda()
+        self.net = Mlp(ctx, N_IN, width, depth, N_OUT, max_batch, params=params, seed=seed)
+
+    def features(self, ring, log_residual, out):
+        norb = ring.shape[-1]
+        check(self.ctx._lib.qt_mix_features(self.ctx.handle, self.nE, norb, NHIST, _vp(ring),
+                                            _vp(self.Qt), float(log_residual), _vp(out), 0))
+        return out
+
+
+def _pulay_step(ops, hist, alpha):
+    import torch
+    G = ops.gram([h[1][1] for h in hist], [h[1][2] for h in hist])
+    c = pulay_coefficients(G)
+    return tuple(ops.combine(c, [h[0][q] for h in hist], [h[1][q] for h in hist], alpha,
+                             torch.empty_like(hist[-1][0][q])) for q in range(3))
+
+
+def run_scba(system, *, method="learned", mixer=None, alpha=0.3, tol=1e-8, max_iter=60,
+             pulay_depth=3, recorder=None):
+    """SCBA to ||R|| / ||F(Sigma)|| <= tol with plain, Pulay or learned mixing.
+
+    ``method``: "plain" (the reference's linear mixing), "pulay" (DIIS over the
+    last ``pulay_depth`` iterates) or "learned" (network proposals, Pulay
+    fallback).  Returns a ``ScbaResult``; the converged self-energy is
+    Sigma + alpha R of the last evaluation, as in the plain loop.
+    """
+    import torch
+    if method == "learned" and mixer is None:
+        raise ValueError("learned mixing needs a LearnedMixer")
+    ops = MixOps(system)
+    norb = system.nx * system.nm
+    S = (system.zeros(), system.zeros(), system.zeros())
+    hist = []
+    ring = torch.zeros((NHIST, 2, system.nE, norb), dtype=torch.float64, device="cuda")
+    nring = 0
+    feats = torch.empty((norb, N_IN), dtype=torch.float32, device="cuda")
+    ab = torch.empty((norb, N_OUT), dtype=torch.float32, device="cuda")
+    res = ScbaResult(sigma=None, residuals=[], evaluations=0, seconds=0.0)
+    r_acc, last, final = np.inf, None, None
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(max_iter):
+        N = system.step(S[0], S[1])
+        R = tuple(ops.diff(N[q], S[q], torch.empty_like(S[q])) for q in range(3))
+        r = ops.residual(R, N)
+        res.residuals.append(r)
+        if r <= tol:
+            final = tuple(ops.combine([1.0], [S[q]], [R[q]], alpha, torch.empty_like(S[q]))
+                          for q in range(3))
+            if last == "learned":
+                res.accepted += 1
+            break
+        if last == "learned" and r >= r_acc:
+            res.rejected += 1
+            S = _pulay_step(ops, hist[-pulay_depth:], alpha)
+            res.pulay += 1
+            last = "pulay"
+            continue
+        if last == "learned":
+            res.accepted += 1
+        hist = (hist + [(S, R)])[-max(pulay_depth, 2):]
+        r_acc = r
+        ring[1:] = ring[:-1].clone()
+        ops.diag(R[1], R[2], ring[0])
+        nring = min(nring + 1, NHIST)
+        ready = nring == NHIST and len(hist) >= 2
+        if ready and (mixer is not None or recorder is not None):
+            (mixer.features if mixer is not None else _features_only(system))(
+                ring, np.log10(max(r, 1e-300)), feats)
+        if ready and recorder is not None:
+            Sp = hist[-2][0]
+            D = tuple(ops.diff(S[q], Sp[q], torch.empty_like(S[q])) for q in (1, 2))
+            sd = ops.diag(S[1], S[2], torch.empty_like(ring[0]))
+            dd = ops.diag(D[0], D[1], torch.empty_like(ring[0]))
+            recorder.add(feats.cpu().numpy(), sd.cpu().numpy(), ring[0].cpu().numpy(),
+                         dd.cpu().numpy())
+        if method == "learned" and ready:
+            mixer.net.infer(feats, out=ab)
+            Sp = hist[-2][0]
+            newS = []
+            for q in range(3):
+                o = torch.empty_like(S[q])
+                check(system.ctx._lib.qt_mix_apply(
+                    system.ctx.handle, system.nE, system.nx, system.nm, _vp(ab), ALPHA_MAX,
+                    BETA_MIN, BETA_MAX, _vp(S[q]), _vp(R[q]), _vp(Sp[q]), _vp(o), 0))
+                newS.append(o)
+            S = tuple(newS)
+            last = "learned"
+        elif method == "pulay" and len(hist) >= 2:
+            S = _pulay_step(ops, hist[-pulay_depth:], alpha)
+            res.pulay += 1
+            last = "pulay"
+        else:
+            S = tuple(ops.combine([1.0], [S[q]], [R[q]], alpha, torch.empty_like(S[q]))
+                      for q in range(3))
+            res.plain += 1
+            last = "plain"
+    torch.cuda.synchronize()
+    res.seconds = time.perf_counter() - t0
+    res.sigma = final if final is not None else S
+    res.evaluations = len(res.residuals)
+    return res
+
+
+_FEATURE_CACHE = {}
+
+
+def _features_only(system):
+    """Feature extraction without a network (recording plain runs)."""
+    import torch
+    key = (id(system.ctx), system.nE)
+    if key not in _FEATURE_CACHE:
+        Qt = torch.from_numpy(chebyshev_projector(system.nE)).cuda()
+
+        def f(ring, log_residual, out, Qt=Qt, ctx=system.ctx, nE=system.nE):
+            check(ctx._lib.qt_mix_features(ctx.handle, nE, ring.shape[-1], NHIST, _vp(ring),
+                                           _vp(Qt), float(log_residual), _vp(out), 0))
+            return out
+        _FEATURE_CACHE[key] = f
+    return _FEATURE_CACHE[key]
+
+
+def fixed_point_diag(system, result):
+    """Diagonal series [2][nE][norb] of a converged result's Sigma^<, Sigma^>."""
+    import torch
+    ops = MixOps(system)
+    out = torch.empty((2, system.nE, system.nx * system.nm), dtype=torch.float64, device="cuda")
+    return ops.diag(result.sigma[1], result.sigma[2], out).cpu().numpy()
+
+
+def collect(systems, *, mixer=None, alpha=0.3, tol=1e-8, max_iter=200, fixed_points=None):
+    """Training pairs from SCBA runs on ``systems`` (a list of GwSystem).
+
+    Without ``mixer``: plain-mixing runs, whose converged result is the fixed point.
+    With ``mixer``: learned runs, targets taken against ``fixed_points`` (one diagonal
+    series per system, from the plain runs).  Returns (X, T, fixed_points, results).
+    """
+    Xs, Ts, fps, results = [], [], [], []
+    for i, s in enumerate(systems):
+        rec = Recorder()
+        r = run_scba(s, method="plain" if mixer is None else "learned", mixer=mixer,
+                     alpha=alpha, tol=tol, max_iter=max_iter, recorder=rec)
+        fp = fixed_point_diag(s, r) if mixer is None else fixed_points[i]
+        X, T = rec.targets(fp)
+        Xs.append(X)
+        Ts.append(T)
+        fps.append(fp)
+        results.append(r)
+    return np.concatenate(Xs), np.concatenate(Ts), fps, results
+
+
+def train(mixer, X, T, *, steps=1500, batch=4096, lr=1e-3, weight_decay=1e-4, seed=0,
+          log_every=0):
+    """AdamW on the GPU with the library's kernels; returns the loss trace (host)."""
+    import torch
+    Xd = torch.from_numpy(np.ascontiguousarray(X, np.float32)).cuda()
+    Td = torch.from_numpy(np.ascontiguousarray(T, np.float32)).cuda()
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    n = Xd.shape[0]
+    b = min(batch, n, mixer.net.max_batch)
+    losses = []
+    for step in range(steps):
+        idx = torch.randint(0, n, (b,), device="cuda", generator=g)
+        want = log_every and (step % log_every == 0 or step == steps - 1)
+        loss = mixer.net.train_step(Xd[idx].contiguous(), Td[idx].contiguous(), lr=lr,
+                                    weight_decay=weight_decay, want_loss=bool(want))
+        if want:
+            losses.append((step, loss))
+    return losses

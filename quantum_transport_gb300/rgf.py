@@ -30,7 +30,8 @@ import numpy as np
 from . import _lib
 from ._lib import QtContacts, QtDevice, QtOutputs, check
 
-PREC = {"fp64": _lib.QT_PREC_FP64, "mixed": _lib.QT_PREC_MIXED}
+PREC = {"fp64": _lib.QT_PREC_FP64, "mixed": _lib.QT_PREC_MIXED,
+        "mixed-fp64": _lib.QT_PREC_MIXED_FP64}
 
 
 class Context:
@@ -141,6 +142,10 @@ def rgf_solve(ctx, Hii, H1i, E, nx, *, nk=1, mul=0.0, mur=0.0, templ=300.0, temp
     Returns a dict of numpy arrays: tr, tre (nE, nk); T (nE, nk) if caroli;
     diag_gr/gl/gg (nE, nk, nx, nm) if want_diag; G_r/G_lesser/G_greater
     (nE, nk, nx, nm, nm) if want_blocks; status (nE, nk); sancho_iters (nE, nk, 2).
+
+    ``precision``: "fp64" (FP64 pipes), "mixed" (tensor-core split products,
+    complex64 sweep storage) or "mixed-fp64" (the same products with complex128
+    storage, FP64-grade results).
     """
     lib = ctx._lib
     E = np.ascontiguousarray(np.asarray(E, dtype=np.float64).ravel())

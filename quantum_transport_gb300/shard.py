@@ -1,0 +1,63 @@
+"""Sharding the (E, k) points over ranks: one process per GPU, no data-path collective.
+
+Every (E, k) point of the RGF sweep is independent.  As in the reference, each
+rank takes a contiguous block of the energy grid (src/main.f90:100-101,
+src/negf_mod.f90:100-103).  It solves all k-points of its energies and
+exchanges nothing until the final gather of the per-point results.  The
+reference gives every rank nen / comm_size energies and drops the remaining
+nen mod comm_size; ``energy_range`` spreads them over the first ranks instead,
+and reproduces the reference's split with ``drop_remainder=True``.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def energy_range(nE, world, rank, drop_remainder=False):
+    """[lo, hi) of the energies of ``rank`` among ``world`` ranks."""
+    if world <= 0 or not 0 <= rank < world:
+        raise ValueError("need 0 <= rank < world")
+    base, extra = divmod(nE, world)
+    if drop_remainder:
+        return base * rank, base * (rank + 1)
+    lo = base * rank + min(rank, extra)
+    return lo, lo + base + (1 if rank < extra else 0)
+
+
+def gather_points(local, nE, world, rank, group=None):
+    """All ranks' per-energy results, concatenated in energy order.
+
+    ``local``: numpy array whose first axis is this rank's energies; returns the
+    (nE, ...) array on every rank.  Uses torch.distributed.all_gather: gloo for
+    host ranks, NCCL for GPU ranks (CPU tensors are moved to the rank's device).
+    """
+    import torch
+    import torch.distributed as dist
+    if world == 1:
+        return np.asarray(local)
+    local = np.ascontiguousarray(local)
+    counts = [energy_range(nE, world, r)[1] - energy_range(nE, world, r)[0] for r in range(world)]
+    if local.shape[0] != counts[rank]:
+        raise ValueError("local block does not match energy_range")
+    cuda = dist.get_backend(group) == "nccl"
+    dev = torch.device("cuda", torch.cuda.current_device()) if cuda else torch.device("cpu")
+    width = max(counts)
+    buf = np.zeros((width,) + local.shape[1:], dtype=local.dtype)
+    buf[:local.shape[0]] = local
+    t = torch.from_numpy(buf).to(dev)
+    outs = [torch.empty_like(t) for _ in range(world)]
+    dist.all_gather(outs, t, group=group)
+    return np.concatenate([o.cpu().numpy()[:c] for o, c in zip(outs, counts)])
+
+
+def max_over_ranks(x, group=None):
+    """The maximum of a host scalar over all ranks (e.g. the slowest rank's time)."""
+    import torch
+    import torch.distributed as dist
+    if not dist.is_initialized() or dist.get_world_size(group) == 1:
+        return float(x)
+    cuda = dist.get_backend(group) == "nccl"
+    t = torch.tensor([float(x)], dtype=torch.float64,
+                     device=torch.device("cuda", torch.cuda.current_device()) if cuda else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX, group=group)
+    return float(t.item())
