@@ -72,6 +72,13 @@ typedef struct qt_ctx qt_ctx;
 qt_status qt_ctx_create(qt_ctx** ctx, int device);
 qt_status qt_ctx_destroy(qt_ctx* ctx);
 qt_status qt_ctx_sync(qt_ctx* ctx);
+/* Launch on `stream` (a cudaStream_t, e.g. the caller framework's current
+ * stream, 0 = the legacy default stream) instead of the context's own stream,
+ * so that the caller's work on its buffers is ordered with the library's;
+ * use_own != 0 returns to the context's own stream.  Synchronises the stream
+ * in use before switching.  Networks (qt_mlp) launch on their context's
+ * current stream and must be destroyed before their context.               */
+qt_status qt_ctx_set_stream(qt_ctx* ctx, void* stream, int use_own);
 /* Bound (bytes) on the per-wave device scratch; default 48 GiB.            */
 qt_status qt_ctx_set_scratch_limit(qt_ctx* ctx, int64_t bytes);
 /* Message of the last error on this thread ("" if none).                   */
@@ -163,6 +170,35 @@ qt_status qt_rgf_solve(qt_ctx* ctx, const qt_device* dev, const double* E, int n
                        const qt_contacts* contacts, const double* sigma_r_ph,
                        const double* sigma_lesser_ph, qt_precision prec, unsigned flags,
                        qt_outputs* out);
+
+/* Slabs with different orbital counts: rgf_variableblock_forward
+ * (src/rgf_mod.f90:46-269) over all nE x nk points.  Block l (0-based) has
+ * nm[l] orbitals.
+ *   Hii + hii_off[l]  H_ll, nm[l] x nm[l], column-major (+ ik * hii_kstride per k)
+ *   H1i + h1i_off[l]  H1i[l] = H_{l,l-1}, nm[l] x nm[l-1], for 1 <= l < nx;
+ *                     H1i[0], H1i[nx]: the left / right lead's own coupling
+ *                     (nm[0] x nm[0], nm[nx-1] x nm[nx-1]) (+ ik * h1i_kstride)
+ * Offsets in complex elements; nm, hii_off, h1i_off are host arrays.  The
+ * backward step couples slabs l and l+1 through H_{l+1,l}: the reference's
+ * H1i(l) (src/rgf_mod.f90:215-245) only fits equal neighbouring blocks.  The
+ * right lead is decimated with H1i[nx] as in src/rgf_mod.f90:153.
+ * Outputs: tr, tre, T [npts]; diag_gr / diag_gl / diag_gg packed
+ * [npts][sum nm[l]] complex128; full blocks are not returned (must be NULL).
+ * The split precisions need nm[l] <= 128.                                  */
+typedef struct {
+  int nx, nk;
+  const int* nm;
+  const double* Hii;
+  const int64_t* hii_off;
+  int64_t hii_kstride;
+  const double* H1i;
+  const int64_t* h1i_off;
+  int64_t h1i_kstride;
+} qt_device_vb;
+
+qt_status qt_rgf_solve_vb(qt_ctx* ctx, const qt_device_vb* dev, const double* E, int nE,
+                          const qt_contacts* contacts, qt_precision prec, unsigned flags,
+                          qt_outputs* out);
 
 /* Single-point drop-in with the argument list of cuda_rgf_constblocksize
  * (src/cuda_rgf_mod.f90:53-59): contiguous (nm, nm, nx) arrays for Hii, Sii,
@@ -307,7 +343,8 @@ qt_status qt_mlp_train_step(qt_mlp* net, int batch, const float* X, const float*
  * qt_mix_features: network input rows feats[o][2*nhist*64 + 2] from a ring
  *                  [h][q][e][o] of nhist (<= 3) diagonal residual series,
  *                  newest first: 64 Chebyshev coefficients per series
- *                  (Qt: [nE][64] projector) scaled by the newest pair's norm,
+ *                  (Qt: [nE][64] projector) scaled by the newest pair's norm
+ *                  and clamped to +-8,
  *                  then log10(residual)/8 and the orbital's log10 decay
  * qt_mix_apply:    out = S + a_ij R + b_ij (S - S_prev), a_ij = (a_i + a_j)/2,
  *                  b_ij likewise; ab[o] = (a_o, b_o) clamped to [0, alpha_max]

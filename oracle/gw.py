@@ -133,14 +133,16 @@ def copy_edges(S):
 
 
 def green(E, H00, H10, nx, SR, SL, *, mu, temp, eta_lead=1e-3, sancho_nmax=100):
-    """G^{R,<,>} diagonal blocks (nE, nx, nm, nm) for self-energies SR, SL (green_RGF_RS)."""
+    """G^{R,<,>} diagonal blocks (nE, nx, nm, nm) for self-energies SR, SL (green_RGF_RS).
+    ``H00``: one on-site block (nm, nm) for every slab, or one per slab (nx, nm, nm)."""
     nE = len(E)
-    nm = H00.shape[0]
+    nm = H00.shape[-1]
+    Hii = list(H00) if H00.ndim == 3 else [H00] * nx
     GR = np.zeros((nE, nx, nm, nm), dtype=np.complex128)
     GL = np.zeros_like(GR)
     GG = np.zeros_like(GR)
     for ie, e in enumerate(E):
-        o = orc.rgf_constblocksize(e, [H00] * nx, [H10] * (nx + 1), None, list(SL[ie]),
+        o = orc.rgf_constblocksize(e, Hii, [H10] * (nx + 1), None, list(SL[ie]),
                                    list(SR[ie]), mul=mu[0], mur=mu[1], templ=temp[0],
                                    tempr=temp[1], eta_lead=eta_lead, sancho_nmax=sancho_nmax,
                                    sancho_tol=1e-100)

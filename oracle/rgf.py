@@ -129,7 +129,18 @@ QUIRKS_CPU = dict(
     greater_from_glp=False,  # G^> = G^< + G - G^+ in every slab    src/rgf_mod.f90:249
     back_coupling="l",     # backward step at slab l uses H1i(l)    src/rgf_mod.f90:215-245
     jdens="cpu",           # Jdens = -2 H10^+ (...)                 src/rgf_mod.f90:215-221
+    right_coupling="nx+1",  # right lead decimated with H1i(nx+1)   src/rgf_mod.f90:153
 )
+# Physically consistent conventions for blocks of different sizes: the backward step
+# couples slab l to l+1 through H_{l+1,l} = H1i[l+1] (the reference's H1i(l) only fits
+# when neighbouring blocks have equal size), each lead through its own coupling block.
+QUIRKS_VARIABLE = dict(QUIRKS_CPU, back_coupling="next")
+
+
+def _diags(blocks):
+    """(nx, nm) diagonals for equal blocks; packed (sum n_l,) when sizes vary."""
+    d = [np.diag(x) for x in blocks]
+    return np.stack(d) if len({len(x) for x in d}) == 1 else np.concatenate(d)
 
 
 def _coupling(H1i, l, mode):
@@ -151,15 +162,14 @@ def rgf_constblocksize(E, Hii, H1i, Sii=None, sigma_lesser_ph=None, sigma_r_ph=N
     """
     q = dict(QUIRKS_GOLDEN if quirks is None else quirks)
     nx = len(Hii)
-    nm = Hii[0].shape[0]
-    I = np.eye(nm, dtype=np.complex128)
+    sizes = [h.shape[0] for h in Hii]  # block sizes may vary along the device
     if Sii is None:
-        Sii = [I] * nx
-    zero = np.zeros((nm, nm), dtype=np.complex128)
+        Sii = [np.eye(n, dtype=np.complex128) for n in sizes]
+    zeros = [np.zeros((n, n), dtype=np.complex128) for n in sizes]
     if sigma_lesser_ph is None:
-        sigma_lesser_ph = [zero] * nx
+        sigma_lesser_ph = zeros
     if sigma_r_ph is None:
-        sigma_r_ph = [zero] * nx
+        sigma_r_ph = zeros
     z = complex(E, interior_eta)
 
     def fermi(which):
@@ -198,11 +208,14 @@ def rgf_constblocksize(E, Hii, H1i, Sii=None, sigma_lesser_ph=None, sigma_r_ph=N
     # ---- right contact (src/cuda_rgf_mod.f90:192-277)
     S00 = Sii[nx - 1]
     H00 = Hii[nx - 1] + sigma_r_ph[nx - 1] @ S00
-    H10 = H1i[nx - 1] if q.get("right_coupling", "nx") == "nx" else H1i[nx]
-    G00R, GBBR, itR, errR, inf = sancho(E, S00, H00, H10, eta=eta_lead,
+    # lead coupling: H1i(nx) in the GPU routine (src/cuda_rgf_mod.f90:157-159), the lead's
+    # own H1i(nx+1) in the CPU routine (src/rgf_mod.f90:153); device coupling H1i(nx)
+    Hlead = H1i[nx - 1] if q.get("right_coupling", "nx") == "nx" else H1i[nx]
+    G00R, GBBR, itR, errR, inf = sancho(E, S00, H00, Hlead, eta=eta_lead,
                                         nmax=sancho_nmax, tol=sancho_tol)
     info = info or inf
-    sigmar = dag(H10) @ G00R @ H10
+    sigmar = dag(Hlead) @ G00R @ Hlead
+    H10 = H1i[nx - 1]
     C = H10 @ Gl[nx - 2] @ dag(H10)
     GNN, inf = invert(z * S00 - H00 - sigmar - C)
     info = info or inf
@@ -221,7 +234,7 @@ def rgf_constblocksize(E, Hii, H1i, Sii=None, sigma_lesser_ph=None, sigma_r_ph=N
     G_r[nx - 1] = GNN
     G_l[nx - 1] = Gn
     G_g[nx - 1] = Gp
-    Jd[nx - 1] = (B - Cc) if q["jdens"] == "cpu" else zero
+    Jd[nx - 1] = (B - Cc) if q["jdens"] == "cpu" else zeros[nx - 1]
     # ---- backward sweep (src/cuda_rgf_mod.f90:283-381)
     G00 = GNN
     for l in range(nx - 2, -1, -1):
@@ -253,9 +266,7 @@ def rgf_constblocksize(E, Hii, H1i, Sii=None, sigma_lesser_ph=None, sigma_r_ph=N
     tre = float(np.real(np.trace(B - Cc)))
     out = dict(tr=tr, tre=tre, info=info,
                sancho_left=(G00L, GBBL, itL, errL), sancho_right=(G00R, GBBR, itR, errR),
-               diag_Gr=np.stack([np.diag(x) for x in G_r]),
-               diag_Gl=np.stack([np.diag(x) for x in G_l]),
-               diag_Gg=np.stack([np.diag(x) for x in G_g]))
+               diag_Gr=_diags(G_r), diag_Gl=_diags(G_l), diag_Gg=_diags(G_g))
     if want_blocks:
         out.update(G_r=G_r, G_lesser=G_l, G_greater=G_g, Jdens=Jd, Gl=Gl, Gln=Gln)
     return out

@@ -28,6 +28,7 @@ EXPORTS = [
     "qt_mlp_create", "qt_mlp_destroy", "qt_mlp_num_params", "qt_mlp_get_params",
     "qt_mlp_set_params", "qt_mlp_infer", "qt_mlp_grad", "qt_mlp_train_step",
     "qt_mix_diag", "qt_mix_features", "qt_mix_apply", "qt_mix_gram", "qt_mix_combine",
+    "qt_rgf_solve_vb", "qt_ctx_set_stream",
 ]
 
 
@@ -36,6 +37,12 @@ class QtDevice(C.Structure):
                 ("Hii", C.c_void_p), ("hii_kstride", C.c_int64), ("hii_lstride", C.c_int64),
                 ("H1i", C.c_void_p), ("h1i_kstride", C.c_int64), ("h1i_lstride", C.c_int64),
                 ("Sii", C.c_void_p), ("sii_kstride", C.c_int64), ("sii_lstride", C.c_int64)]
+
+
+class QtDeviceVB(C.Structure):
+    _fields_ = [("nx", C.c_int), ("nk", C.c_int), ("nm", C.c_void_p),
+                ("Hii", C.c_void_p), ("hii_off", C.c_void_p), ("hii_kstride", C.c_int64),
+                ("H1i", C.c_void_p), ("h1i_off", C.c_void_p), ("h1i_kstride", C.c_int64)]
 
 
 class QtContacts(C.Structure):
@@ -72,6 +79,7 @@ def load(path=LIB_PATH):
     lib.qt_ctx_destroy.argtypes = [vp]
     lib.qt_ctx_sync.argtypes = [vp]
     lib.qt_ctx_set_scratch_limit.argtypes = [vp, i64]
+    lib.qt_ctx_set_stream.argtypes = [vp, vp, ci]
     lib.qt_last_error.restype = C.c_char_p
     lib.qt_version.restype = C.c_char_p
     lib.qt_rgf_solve.argtypes = [vp, C.POINTER(QtDevice), vp, ci, C.POINTER(QtContacts), vp, vp,
@@ -105,6 +113,8 @@ def load(path=LIB_PATH):
     lib.qt_mlp_grad.argtypes = [vp, ci, vp, vp, vp, C.POINTER(dbl), C.c_uint]
     lib.qt_mlp_train_step.argtypes = [vp, ci, vp, vp, flt, flt, C.POINTER(dbl), C.c_uint]
     pvp = C.POINTER(vp)
+    lib.qt_rgf_solve_vb.argtypes = [vp, C.POINTER(QtDeviceVB), vp, ci, C.POINTER(QtContacts), ci,
+                                    C.c_uint, C.POINTER(QtOutputs)]
     lib.qt_mix_diag.argtypes = [vp, ci, ci, ci, vp, vp, vp, C.c_uint]
     lib.qt_mix_features.argtypes = [vp, ci, i64, ci, vp, vp, dbl, vp, C.c_uint]
     lib.qt_mix_apply.argtypes = [vp, ci, ci, ci, vp, dbl, dbl, dbl, vp, vp, vp, vp, C.c_uint]

@@ -10,8 +10,8 @@
 //  * mix_diag:     Im of the diagonal series of X^< and X^> -> [2][nE][norb]
 //  * mix_features: per orbital, 64 Chebyshev coefficients of each of the
 //                  last nhist residual series (< and >), scaled by the norm of
-//                  the newest pair, plus the global residual and the orbital's
-//                  residual decay: the network's input row
+//                  the newest pair and clamped to +-8, plus the global residual
+//                  and the orbital's residual decay: the network's input row
 //  * mix_apply:    S + a_ij R + b_ij (S - S_prev) with a_ij = (a_i + a_j)/2,
 //                  b_ij = (b_i + b_j)/2 from the per-orbital network outputs
 //  * mix_gram / mix_combine: Pulay's residual Gram matrix and the affine
@@ -71,7 +71,8 @@ __global__ void mix_features_kernel(int nE, long long norb, int nhist, const dou
     __syncthreads();
     const double n0 = red[2 * nhist * NCOEF], n1 = red[2 * nhist * NCOEF + 1];
     float* f = feats + o * n_in;
-    if (s < 2 * nhist) f[t] = (float)(c / (n0 + 1e-300));
+    // an orbital whose newest residual vanishes would blow its older ones up: clamp to +-8
+    if (s < 2 * nhist) f[t] = (float)fmax(-8.0, fmin(8.0, c / (n0 + 1e-300)));
     if (t == 0) {
       f[2 * nhist * NCOEF] = (float)(log_residual / 8.0);
       const double decay = (nhist > 1 && n1 > 0.0 && n0 > 0.0) ? log10(n0 / n1) : 0.0;

@@ -353,7 +353,6 @@ using qt::MlpGemm;
 struct qt_mlp {
   qt_ctx* ctx = nullptr;
   int device = 0;
-  cudaStream_t s = nullptr;
   int n_in = 0, width = 0, depth = 0, n_out = 0, max_batch = 0;
   std::vector<int> din, dout;         // per linear layer
   std::vector<long long> woff, boff;  // offsets of W_l (dout x din, row-major) and b_l
@@ -395,6 +394,7 @@ qt_status gemm_call(cudaError_t e) {
 
 // forward pass of `batch` rows of X (device, [batch][n_in]) into n->y
 qt_status forward(qt_mlp* n, int batch, const float* X) {
+  cudaStream_t s = qt::ctx_stream(n->ctx);
   const int L = n->depth + 1;
   const long long BW = (long long)n->max_batch * n->width;
   for (int l = 0; l < L; ++l) {
@@ -421,15 +421,15 @@ qt_status forward(qt_mlp* n, int batch, const float* X) {
       g.scm = n->n_out;
       g.scn = 1;
     }
-    QT_TRY(gemm_call(l == 0 ? qt::gemm<float, uint16_t>(g, n->s)
-                            : qt::gemm<uint16_t, uint16_t>(g, n->s)));
+    QT_TRY(gemm_call(l == 0 ? qt::gemm<float, uint16_t>(g, s)
+                            : qt::gemm<uint16_t, uint16_t>(g, s)));
   }
   return QT_OK;
 }
 
 // loss and gradients (n->grad, flat like the parameters) after forward() on the same X
 qt_status backward(qt_mlp* n, int batch, const float* X, const float* T) {
-  cudaStream_t s = n->s;
+  cudaStream_t s = qt::ctx_stream(n->ctx);
   const int L = n->depth + 1;
   const long long BW = (long long)n->max_batch * n->width;
   const long long cnt = (long long)batch * n->n_out;
@@ -489,7 +489,8 @@ qt_status backward(qt_mlp* n, int batch, const float* X, const float* T) {
 }
 
 qt_status sync_and_check(qt_mlp* n) {
-  QT_CUDA_TRY(cudaStreamSynchronize(n->s));
+  cudaStream_t s = qt::ctx_stream(n->ctx);
+  QT_CUDA_TRY(cudaStreamSynchronize(s));
   if (qt::mlp_timeouts_and_reset()) QT_FAIL(QT_ERR_CUDA, "tensor-core kernel wait timed out");
   return QT_OK;
 }
@@ -499,16 +500,17 @@ qt_status inputs(qt_mlp* n, int batch, const float* X, const float* T, unsigned 
                  const float** Xd, const float** Td) {
   if (!n || !X || batch <= 0 || batch > n->max_batch) QT_FAIL(QT_ERR_ARG, "bad batch or input");
   cudaSetDevice(n->device);
+  cudaStream_t s = qt::ctx_stream(n->ctx);
   if (flags & QT_FLAG_DEVICE_POINTERS) {
     *Xd = X;
     if (Td) *Td = T;
     return QT_OK;
   }
-  cudaMemcpyAsync(n->xin, X, (size_t)batch * n->n_in * sizeof(float), cudaMemcpyHostToDevice, n->s);
+  cudaMemcpyAsync(n->xin, X, (size_t)batch * n->n_in * sizeof(float), cudaMemcpyHostToDevice, s);
   *Xd = n->xin;
   if (Td && T) {
     cudaMemcpyAsync(n->tin, T, (size_t)batch * n->n_out * sizeof(float), cudaMemcpyHostToDevice,
-                    n->s);
+                    s);
     *Td = n->tin;
   }
   return QT_OK;
@@ -524,7 +526,6 @@ extern "C" qt_status qt_mlp_create(qt_ctx* ctx, int n_in, int width, int depth, 
   qt_mlp* n = new qt_mlp();
   n->ctx = ctx;
   n->device = qt::ctx_device(ctx);
-  n->s = qt::ctx_stream(ctx);
   n->n_in = n_in; n->width = width; n->depth = depth; n->n_out = n_out;
   n->max_batch = max_batch;
   for (int l = 0; l <= depth; ++l) {
@@ -574,12 +575,13 @@ extern "C" qt_status qt_mlp_create(qt_ctx* ctx, int n_in, int width, int depth, 
       }
     }
   }
-  cudaMemcpyAsync(n->w, h.data(), P * sizeof(float), cudaMemcpyHostToDevice, n->s);
-  cudaMemsetAsync(n->m, 0, P * sizeof(float), n->s);
-  cudaMemsetAsync(n->v, 0, P * sizeof(float), n->s);
-  qt::to_bf16_kernel<<<qt::grid_for((long long)P), 256, 0, n->s>>>((long long)P, n->w, n->wb);
+  cudaStream_t s = qt::ctx_stream(ctx);
+  cudaMemcpyAsync(n->w, h.data(), P * sizeof(float), cudaMemcpyHostToDevice, s);
+  cudaMemsetAsync(n->m, 0, P * sizeof(float), s);
+  cudaMemsetAsync(n->v, 0, P * sizeof(float), s);
+  qt::to_bf16_kernel<<<qt::grid_for((long long)P), 256, 0, s>>>((long long)P, n->w, n->wb);
   qt::count_launch();
-  if (cudaStreamSynchronize(n->s) != cudaSuccess) {
+  if (cudaStreamSynchronize(s) != cudaSuccess) {
     const char* msg = cudaGetErrorString(cudaGetLastError());
     cudaFree(n->mem);
     delete n;
@@ -592,7 +594,8 @@ extern "C" qt_status qt_mlp_create(qt_ctx* ctx, int n_in, int width, int depth, 
 extern "C" qt_status qt_mlp_destroy(qt_mlp* n) {
   if (!n) return QT_OK;
   cudaSetDevice(n->device);
-  cudaStreamSynchronize(n->s);
+  cudaStream_t s = qt::ctx_stream(n->ctx);
+  cudaStreamSynchronize(s);
   cudaFree(n->mem);
   delete n;
   return QT_OK;
@@ -607,16 +610,18 @@ extern "C" qt_status qt_mlp_num_params(const qt_mlp* n, int64_t* count) {
 extern "C" qt_status qt_mlp_get_params(qt_mlp* n, float* host) {
   if (!n || !host) QT_FAIL(QT_ERR_ARG, "null argument");
   cudaSetDevice(n->device);
-  cudaMemcpyAsync(host, n->w, (size_t)n->nparams * sizeof(float), cudaMemcpyDeviceToHost, n->s);
+  cudaStream_t s = qt::ctx_stream(n->ctx);
+  cudaMemcpyAsync(host, n->w, (size_t)n->nparams * sizeof(float), cudaMemcpyDeviceToHost, s);
   return sync_and_check(n);
 }
 
 extern "C" qt_status qt_mlp_set_params(qt_mlp* n, const float* host) {
   if (!n || !host) QT_FAIL(QT_ERR_ARG, "null argument");
   cudaSetDevice(n->device);
+  cudaStream_t s = qt::ctx_stream(n->ctx);
   const long long P = n->nparams;
-  cudaMemcpyAsync(n->w, host, (size_t)P * sizeof(float), cudaMemcpyHostToDevice, n->s);
-  qt::to_bf16_kernel<<<qt::grid_for(P), 256, 0, n->s>>>(P, n->w, n->wb);
+  cudaMemcpyAsync(n->w, host, (size_t)P * sizeof(float), cudaMemcpyHostToDevice, s);
+  qt::to_bf16_kernel<<<qt::grid_for(P), 256, 0, s>>>(P, n->w, n->wb);
   qt::count_launch();
   return sync_and_check(n);
 }
@@ -626,9 +631,10 @@ extern "C" qt_status qt_mlp_infer(qt_mlp* n, int batch, const float* X, float* Y
   QT_TRY(inputs(n, batch, X, nullptr, flags, &Xd, nullptr));
   if (!Y) QT_FAIL(QT_ERR_ARG, "null output");
   QT_TRY(forward(n, batch, Xd));
+  cudaStream_t s = qt::ctx_stream(n->ctx);
   const size_t yb = (size_t)batch * n->n_out * sizeof(float);
   const bool devp = (flags & QT_FLAG_DEVICE_POINTERS) != 0;
-  cudaMemcpyAsync(Y, n->y, yb, devp ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, n->s);
+  cudaMemcpyAsync(Y, n->y, yb, devp ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s);
   if (!devp || (flags & QT_FLAG_SYNC)) return sync_and_check(n);
   return QT_OK;
 }
@@ -640,9 +646,10 @@ extern "C" qt_status qt_mlp_grad(qt_mlp* n, int batch, const float* X, const flo
   QT_TRY(inputs(n, batch, X, T, flags, &Xd, &Td));
   QT_TRY(forward(n, batch, Xd));
   QT_TRY(backward(n, batch, Xd, Td));
+  cudaStream_t s = qt::ctx_stream(n->ctx);
   cudaMemcpyAsync(grad_host, n->grad, (size_t)n->nparams * sizeof(float), cudaMemcpyDeviceToHost,
-                  n->s);
-  if (loss) cudaMemcpyAsync(loss, n->loss, sizeof(double), cudaMemcpyDeviceToHost, n->s);
+                  s);
+  if (loss) cudaMemcpyAsync(loss, n->loss, sizeof(double), cudaMemcpyDeviceToHost, s);
   return sync_and_check(n);
 }
 
@@ -658,12 +665,13 @@ extern "C" qt_status qt_mlp_train_step(qt_mlp* n, int batch, const float* X, con
   const float bc1 = 1.0f - (float)std::pow((double)ADAM_B1, n->step);
   const float bc2 = 1.0f - (float)std::pow((double)ADAM_B2, n->step);
   const long long P = n->nparams;
-  qt::adamw_kernel<<<qt::grid_for(P), 256, 0, n->s>>>(P, n->w, n->grad, n->m, n->v, lr, ADAM_B1,
-                                                      ADAM_B2, ADAM_EPS, weight_decay, bc1, bc2,
-                                                      n->wb);
+  cudaStream_t s = qt::ctx_stream(n->ctx);
+  qt::adamw_kernel<<<qt::grid_for(P), 256, 0, s>>>(P, n->w, n->grad, n->m, n->v, lr, ADAM_B1,
+                                                   ADAM_B2, ADAM_EPS, weight_decay, bc1, bc2,
+                                                   n->wb);
   qt::count_launch();
   if (loss) {
-    cudaMemcpyAsync(loss, n->loss, sizeof(double), cudaMemcpyDeviceToHost, n->s);
+    cudaMemcpyAsync(loss, n->loss, sizeof(double), cudaMemcpyDeviceToHost, s);
     return sync_and_check(n);
   }
   if (flags & QT_FLAG_SYNC) return sync_and_check(n);

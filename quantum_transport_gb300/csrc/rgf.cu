@@ -79,7 +79,8 @@ struct Prof {
 struct qt_ctx {
   Prof prof;
   int device = 0;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;      // where every launch of this context goes
+  cudaStream_t own_stream = nullptr;  // created with the context, destroyed with it
   int64_t scratch_limit = 48LL << 30;
   void* arena = nullptr;
   size_t arena_bytes = 0;
@@ -168,6 +169,18 @@ __global__ void flag_unconverged_kernel(long long P, const unsigned char* active
     if (active[b]) status[b] |= qt::PT_SANCHO_NOT_CONVERGED;
 }
 
+// status[b] |= NONFINITE when any of the `row` doubles of point b's output is NaN/Inf
+// (one warp per point; the outputs are what the caller reads)
+__global__ void check_outputs_kernel(long long P, long long row, const double* data, int* status) {
+  const int lane = threadIdx.x & 31;
+  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long b = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; b < P; b += warps) {
+    bool bad = false;
+    for (long long i = lane; i < row; i += 32) bad |= !isfinite(data[b * row + i]);
+    if (__any_sync(0xffffffffu, bad) && lane == 0) status[b] |= qt::PT_NONFINITE;
+  }
+}
+
 inline unsigned g1d(long long n) {
   long long g = (n + 255) / 256;
   if (g < 1) g = 1;
@@ -204,8 +217,16 @@ struct Ops {
   qt_status gemm(BatchRef A, int opA, BatchRef B, int opB, BatchRef C, long long batch,
                  cd alpha = {1, 0}, BatchRef D = nullref(), cd beta = {0, 0},
                  BatchRef Z = nullref(), const unsigned char* active = nullptr) {
+    return gemm3(n, n, n, A, opA, B, opB, C, batch, alpha, D, beta, Z, active);
+  }
+  // C (m x nn) = alpha op(A) op(B) + beta D + z I, op(A) m x k, op(B) k x nn
+  qt_status gemm3(int m, int nn, int k, BatchRef A, int opA, BatchRef B, int opB, BatchRef C,
+                  long long batch, cd alpha = {1, 0}, BatchRef D = nullref(), cd beta = {0, 0},
+                  BatchRef Z = nullref(), const unsigned char* active = nullptr) {
     qt::GemmArgs g;
-    g.m = g.n = g.k = n;
+    g.m = m;
+    g.n = nn;
+    g.k = k;
     g.A = A; g.B = B; g.C = C; g.D = D; g.Z = Z;
     g.opA = opA; g.opB = opB;
     g.alpha_re = alpha.x; g.alpha_im = alpha.y; g.beta_re = beta.x; g.beta_im = beta.y;
@@ -228,12 +249,12 @@ struct Ops {
     if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
     if (timed) {
       cudaEventRecord(eb, s);
-      // algorithmic: 8 n^3 real flops per complex block product; executed on the tensor
+      // algorithmic: 8 m n k real flops per complex block product; executed on the tensor
       // pipe: 2 real parts x digit pairs x 2 x 128 x npad x K'
-      const double alg = 8.0 * n * (double)n * n * batch;
+      const double alg = 8.0 * m * (double)nn * k * batch;
       double tens = 0.0;
       if (kind != 2) {
-        const int L = slices - 1, npad = (n + 15) / 16 * 16, kp = (n + 31) / 32 * 32;
+        const int L = slices - 1, npad = (nn + 15) / 16 * 16, kp = (k + 15) / 16 * 16;
         int pairs = 0;
         for (int a = 0; a < slices; ++a)
           for (int b = 0; b < slices; ++b) pairs += (a + b <= L);
@@ -245,14 +266,15 @@ struct Ops {
   }
   // X = inv(A); A is preserved (X must differ from A in the split path)
   qt_status inv(BatchRef A, BatchRef X, long long batch, int* status,
-                const unsigned char* active = nullptr) {
+                const unsigned char* active = nullptr, int nn = 0) {
+    if (nn <= 0) nn = n;
     qt::InvArgs a;
-    a.n = n; a.A = A; a.X = X; a.batch = batch; a.status = status; a.active = active;
+    a.n = nn; a.A = A; a.X = X; a.batch = batch; a.status = status; a.active = active;
     cudaError_t e;
     const bool timed = prof && prof->on;
     cudaEvent_t ea = nullptr, eb = nullptr;
     if (timed) { ea = prof->get(); eb = prof->get(); cudaEventRecord(ea, s); }
-    const double alg = 8.0 * n * (double)n * n * batch;  // inversion counted as one n^3 product
+    const double alg = 8.0 * nn * (double)nn * nn * batch;  // inversion counted as one n^3 product
     if (prec == QT_PREC_FP64) {
       if constexpr (sizeof(TC) == 16) e = qt::zinv_f64(a, s);
       else e = cudaErrorInvalidValue;
@@ -265,12 +287,14 @@ struct Ops {
     if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
     if (timed) { cudaEventRecord(eb, s); prof->v.push_back({3, ea, eb, alg, 0.0}); }
     if (refine > 0 && (batch > P || !rt1 || !rt2)) QT_FAIL(QT_ERR_ARG, "refinement scratch too small");
-    const BatchRef R = ref(rt1, (long long)n * n, n), T = ref(rt2, (long long)n * n, n);
+    // refinement scratch holds batch blocks of the widest size (stride n*n)
+    const BatchRef R = ref(rt1, (long long)n * n, nn), T = ref(rt2, (long long)n * n, nn);
     for (int it = 0; it < refine; ++it) {
-      QT_TRY(gemm(A, qt::OP_N, X, qt::OP_N, R, batch, cd{-1, 0}, nullref(), cd{0, 0},
-                  ref(one, 0, 1), active));  // R = I - A X
-      QT_TRY(gemm(X, qt::OP_N, R, qt::OP_N, T, batch, cd{1, 0}, X, cd{1, 0}, nullref(), active));
-      qt::zcopy<TC>(n, batch, T, X, s);
+      QT_TRY(gemm3(nn, nn, nn, A, qt::OP_N, X, qt::OP_N, R, batch, cd{-1, 0}, nullref(),
+                   cd{0, 0}, ref(one, 0, 1), active));  // R = I - A X
+      QT_TRY(gemm3(nn, nn, nn, X, qt::OP_N, R, qt::OP_N, T, batch, cd{1, 0}, X, cd{1, 0},
+                   nullref(), active));
+      qt::zcopy<TC>(nn, batch, T, X, s);
     }
     return QT_OK;
   }
@@ -293,6 +317,7 @@ struct Problem {
   qt_precision prec;
   unsigned flags;
   int sweep_slices, lead_slices;
+  int sweep_refine;  // refinement steps of the sweep's FP32 inverses (split paths)
   // device outputs (may be null)
   double *tr, *tre, *T, *dgr, *dgl, *dgg;
   cd *Gr, *Gl, *Gg;
@@ -396,6 +421,23 @@ qt_status sancho_wave(const Ops<double2>& op0, Arena& ar, long long P, BatchRef 
   return QT_OK;
 }
 
+// non-finite outputs of a wave: diagonals (diag complex values per point) and traces
+void check_wave_outputs(long long P, long long diag, long long p0, const double* dgr,
+                        const double* dgl, const double* dgg, const double* T, const double* tr,
+                        const double* tre, int* status, cudaStream_t s) {
+  const unsigned grid = (unsigned)std::min<long long>((P + 7) / 8, 4096);
+  for (const double* d : {dgr, dgl, dgg})
+    if (d) {
+      check_outputs_kernel<<<grid, 256, 0, s>>>(P, 2 * diag, d + 2 * p0 * diag, status);
+      qt::count_launch();
+    }
+  for (const double* d : {T, tr, tre})
+    if (d) {
+      check_outputs_kernel<<<grid, 256, 0, s>>>(P, 1, d + p0, status);
+      qt::count_launch();
+    }
+}
+
 template <typename TC>
 void zconvert_or_copy(int n, long long P, BatchRef X, BatchRef Y, cudaStream_t s) {
   if constexpr (sizeof(TC) == 16) qt::zcopy<double2>(n, P, X, Y, s);
@@ -435,9 +477,7 @@ qt_status solve_wave(qt_ctx* ctx, const Problem& pb, long long p0, long long P, 
   // sweep operations on TC, contact operations on complex128
   Ops<TC> op{s, n, pb.prec};
   op.slices = pb.sweep_slices;
-  // complex64 sweep: one refinement reaches its storage resolution; complex128 sweep
-  // (MIXED_FP64): three, as for the leads
-  op.refine = split ? (sizeof(TC) == 8 ? 1 : 3) : 0;
+  op.refine = split ? pb.sweep_refine : 0;
   op.one = one; op.rt1 = rt1; op.rt2 = rt2; op.P = P; op.scales = scales;
   op.prof = &ctx->prof;
   Ops<double2> cop{s, n, pb.prec};
@@ -639,6 +679,245 @@ qt_status solve_wave(qt_ctx* ctx, const Problem& pb, long long p0, long long P, 
     qt::ztrace_current<TC>(n, P, SigL, T(0), Gncur, 1.0, fe, pb.tre + p0, s);
   }
   qt::zcheck_finite<TC>(n, P, Gcur, status, s);  // canary on the last block touched
+  check_wave_outputs(P, (long long)nx * n, p0, pb.dgr, pb.dgl, pb.dgg, pb.T, pb.tr, pb.tre,
+                     status, s);
+  if (pb.status)
+    cudaMemcpyAsync(pb.status + p0, status, P * sizeof(int), cudaMemcpyDeviceToDevice, s);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+  return QT_OK;
+}
+
+// ------------------------------------------------- variable block sizes
+// Slabs of different orbital counts n_l (rgf_variableblock_forward,
+// src/rgf_mod.f90:46-269).  H1i[l] = H_{l,l-1} is n_l x n_{l-1}; H1i[0] and
+// H1i[nx] are the leads' own couplings (n_0 x n_0, n_{nx-1} x n_{nx-1}).  The
+// backward step couples slab l to l+1 through H_{l+1,l} = H1i[l+1] (the
+// reference's H1i(l) only fits equal neighbouring blocks), and the right lead is
+// decimated with H1i[nx] as in the CPU routine (src/rgf_mod.f90:153).
+struct ProblemVB {
+  int nx, nk, nmax;
+  long long npts, dsum;             // points; sum of n_l (diagonal output stride)
+  std::vector<int> n;               // [nx]
+  std::vector<long long> hoff, h1off, doff, goff;  // H / H1i offsets, diagonal and g offsets
+  long long gsum;                   // sum of n_l^2
+  const cd* Hii; long long hk;
+  const cd* H1i; long long h1k;
+  const float2* Hii32;
+  const float2* H1i32;
+  const double* E;
+  qt_contacts c;
+  qt_precision prec;
+  unsigned flags;
+  int sweep_slices, lead_slices, sweep_refine;
+  double *tr, *tre, *T, *dgr, *dgl, *dgg;
+  int *status, *iters;
+};
+
+size_t wave_bytes_vb(const ProblemVB& pb, long long P) {
+  const size_t m2 = (size_t)pb.nmax * pb.nmax;
+  const size_t tc = pb.prec == QT_PREC_MIXED ? 8 : 16;
+  const size_t sweep = (2 * (size_t)pb.gsum + 16 * m2) * tc;
+  const size_t lead = (7 + 2 + 6) * 16 * m2;
+  return (sweep + lead) * P + (size_t)P * (512 + 2048) + (512 << 10);
+}
+
+template <typename TC>
+qt_status solve_wave_vb(qt_ctx* ctx, const ProblemVB& pb, long long p0, long long P, Arena& ar) {
+  const int nx = pb.nx, nk = pb.nk, nm = pb.nmax;
+  const long long m2 = (long long)nm * nm;
+  cudaStream_t s = ctx->stream;
+  const unsigned q = pb.c.quirks;
+  const bool split = pb.prec != QT_PREC_FP64;
+  const bool c64 = sizeof(TC) == 8;
+  const std::vector<int>& n = pb.n;
+
+  cd* zint = ar.take<cd>(P);
+  cd* zlead = ar.take<cd>(P);
+  double* fl = ar.take<double>(P);
+  double* fr = ar.take<double>(P);
+  double* fe = ar.take<double>(P);
+  cd* one = ar.take<cd>(1);
+  int* status = ar.take<int>(P);
+  TC* gl_all = ar.take<TC>((size_t)pb.gsum * P);   // g_l   [l][b][n_l^2]
+  TC* gln_all = ar.take<TC>((size_t)pb.gsum * P);  // g^<_l
+  TC* tmp = ar.take<TC>((size_t)14 * P * m2);
+  TC* rt1 = ar.take<TC>((size_t)P * m2);
+  TC* rt2 = ar.take<TC>((size_t)P * m2);
+  cd* cbuf = ar.take<cd>((size_t)6 * P * m2);
+  int* scales = ar.take<int>((size_t)P * 256);
+  if (!zint || !zlead || !fl || !fr || !fe || !one || !status || !gl_all || !gln_all || !tmp ||
+      !rt1 || !rt2 || !cbuf || !scales)
+    QT_FAIL(QT_ERR_NOMEM, "wave arena exhausted");
+  Ops<TC> op{s, nm, pb.prec};
+  op.slices = pb.sweep_slices;
+  op.refine = split ? pb.sweep_refine : 0;
+  op.one = one; op.rt1 = rt1; op.rt2 = rt2; op.P = P; op.scales = scales;
+  op.prof = &ctx->prof;
+  Ops<double2> cop{s, nm, pb.prec};
+  cop.prof = &ctx->prof;
+  cop.slices = pb.lead_slices;
+  cop.refine = split ? 3 : 0;
+  cop.one = one; cop.scales = scales; cop.P = P;
+
+  const cd h1{1.0, 0.0};
+  cudaMemcpyAsync(one, &h1, sizeof(cd), cudaMemcpyHostToDevice, s);
+  cudaMemsetAsync(status, 0, P * sizeof(int), s);
+  make_z_kernel<<<g1d(P), 256, 0, s>>>(pb.E, p0, P, nk, pb.c.eta_interior, zint);
+  qt::count_launch();
+  make_z_kernel<<<g1d(P), 256, 0, s>>>(pb.E, p0, P, nk, pb.c.eta_lead, zlead);
+  qt::count_launch();
+  const bool cpu = (q & QT_QUIRK_CPU_FERMI) != 0;
+  make_fermi_kernel<<<g1d(P), 256, 0, s>>>(pb.E, p0, P, nk, cpu ? pb.c.mur : pb.c.mul,
+                                           cpu ? pb.c.tempr : pb.c.templ, fl);
+  qt::count_launch();
+  make_fermi_kernel<<<g1d(P), 256, 0, s>>>(pb.E, p0, P, nk, cpu ? pb.c.mul : pb.c.mur, pb.c.templ,
+                                           fr);
+  qt::count_launch();
+  make_fermi_kernel<<<g1d(P), 256, 0, s>>>(pb.E, p0, P, nk, cpu ? pb.c.mur : pb.c.mul, pb.c.tempr,
+                                           fe);
+  qt::count_launch();
+  const double tr_sign = cpu ? 1.0 : -1.0;
+
+  // temporaries hold up to nmax x nmax per point; ld = rows of what they hold
+  auto T = [&](int i, int ld) { return ref(tmp + (size_t)i * P * m2, m2, ld); };
+  auto C8 = [&](int i, int ld) { return ref(cbuf + (size_t)i * P * m2, m2, ld); };
+  auto GL = [&](int l) {
+    return ref(gl_all + (size_t)pb.goff[l] * P, (long long)n[l] * n[l], n[l]);
+  };
+  auto GLN = [&](int l) {
+    return ref(gln_all + (size_t)pb.goff[l] * P, (long long)n[l] * n[l], n[l]);
+  };
+  auto HII8 = [&](int l) { return ref(pb.Hii + pb.hoff[l], pb.hk, n[l], pb.hk ? nk : 0); };
+  auto HII = [&](int l) {
+    return c64 ? ref(pb.Hii32 + pb.hoff[l], pb.hk, n[l], pb.hk ? nk : 0) : HII8(l);
+  };
+  // coupling l: rows n_l (n_0 / n_{nx-1} for the leads' own couplings)
+  auto rows1 = [&](int l) { return l == 0 ? n[0] : (l == nx ? n[nx - 1] : n[l]); };
+  auto H1I8 = [&](int l) { return ref(pb.H1i + pb.h1off[l], pb.h1k, rows1(l), pb.h1k ? nk : 0); };
+  auto H1I = [&](int l) {
+    return c64 ? ref(pb.H1i32 + pb.h1off[l], pb.h1k, rows1(l), pb.h1k ? nk : 0) : H1I8(l);
+  };
+  const BatchRef Zi = ref(zint, 1, 1);
+  const cd one_c{1, 0}, mone{-1, 0};
+  const bool caroli = (pb.flags & QT_FLAG_CAROLI) && pb.T;
+  const int n0 = n[0], N = nx - 1, nN = n[N];
+  auto emit = [&](int l, BatchRef G, BatchRef Gn) {
+    const long long os = pb.dsum, oo = pb.doff[l];
+    if (pb.dgr) qt::zdiag<TC>(n[l], P, G, pb.dgr + 2 * p0 * pb.dsum, os, oo, s);
+    if (pb.dgl) qt::zdiag<TC>(n[l], P, Gn, pb.dgl + 2 * p0 * pb.dsum, os, oo, s);
+    if (pb.dgg) qt::zdiag_greater<TC>(n[l], P, G, Gn, pb.dgg + 2 * p0 * pb.dsum, os, oo, s);
+  };
+
+  // ---------------- left contact: lead block n_0 with its own coupling H1i[0]
+  {
+    Ops<double2> lop = cop;
+    lop.n = n0;
+    QT_TRY(sancho_wave(lop, ar, P, HII8(0), H1I8(0), true, zlead, pb.c.sancho_tol,
+                       pb.c.sancho_max_iter, C8(1, n0), nullref(), status,
+                       pb.iters ? pb.iters + p0 * 2 : nullptr, 2));
+    QT_TRY(cop.gemm3(n0, n0, n0, H1I8(0), qt::OP_N, C8(1, n0), qt::OP_N, C8(2, n0), P));
+    QT_TRY(cop.gemm3(n0, n0, n0, C8(2, n0), qt::OP_N, H1I8(0), qt::OP_C, C8(3, n0), P));
+  }
+  const BatchRef SigL = T(13, n0), Pch = T(12, nm);
+  zconvert_or_copy<TC>(n0, P, C8(3, n0), SigL, s);
+  qt::zaxpby<TC>(n0, P, HII(0), -1, 0, SigL, -1, 0, Zi, T(3, n0), nullptr, s);
+  QT_TRY(op.inv(T(3, n0), GL(0), P, status, nullptr, n0));
+  qt::zantiherm<TC>(n0, P, SigL, -1, 0, nullref(), T(4, n0), s);
+  qt::zscale_add<TC>(n0, P, T(4, n0), fl, nullref(), T(4, n0), s);
+  QT_TRY(op.gemm3(n0, n0, n0, GL(0), qt::OP_N, T(4, n0), qt::OP_N, T(5, n0), P));
+  QT_TRY(op.gemm3(n0, n0, n0, T(5, n0), qt::OP_N, GL(0), qt::OP_C, GLN(0), P));
+  // Caroli chain P_l (n_l x n_0), ld n_l
+  if (caroli) qt::zcopy<TC>(n0, P, GL(0), ref(tmp + (size_t)12 * P * m2, m2, n0), s);
+
+  // ---------------- forward sweep
+  for (int l = 1; l <= N - 1; ++l) {
+    const int nl = n[l], np = n[l - 1];
+    const BatchRef H10 = H1I(l);  // n_l x n_{l-1}
+    QT_TRY(op.gemm3(nl, np, np, H10, qt::OP_N, GL(l - 1), qt::OP_N, T(0, nl), P));
+    QT_TRY(op.gemm3(nl, nl, np, T(0, nl), qt::OP_N, H10, qt::OP_C, T(1, nl), P, mone, HII(l),
+                    mone, Zi));
+    QT_TRY(op.inv(T(1, nl), GL(l), P, status, nullptr, nl));
+    QT_TRY(op.gemm3(nl, np, np, H10, qt::OP_N, GLN(l - 1), qt::OP_N, T(0, nl), P));
+    QT_TRY(op.gemm3(nl, nl, np, T(0, nl), qt::OP_N, H10, qt::OP_C, T(1, nl), P));
+    QT_TRY(op.gemm3(nl, nl, nl, GL(l), qt::OP_N, T(1, nl), qt::OP_N, T(0, nl), P));
+    QT_TRY(op.gemm3(nl, nl, nl, T(0, nl), qt::OP_N, GL(l), qt::OP_C, GLN(l), P));
+    if (caroli) {  // P_l = g_l H_{l,l-1} P_{l-1}
+      QT_TRY(op.gemm3(nl, n0, np, H10, qt::OP_N, ref(tmp + (size_t)12 * P * m2, m2, np),
+                      qt::OP_N, T(0, nl), P));
+      QT_TRY(op.gemm3(nl, n0, nl, GL(l), qt::OP_N, T(0, nl), qt::OP_N,
+                      ref(tmp + (size_t)12 * P * m2, m2, nl), P));
+    }
+  }
+
+  // ---------------- right contact: lead block n_N, decimated with its own H1i[nx]
+  {
+    Ops<double2> lop = cop;
+    lop.n = nN;
+    QT_TRY(sancho_wave(lop, ar, P, HII8(N), H1I8(nx), false, zlead, pb.c.sancho_tol,
+                       pb.c.sancho_max_iter, C8(1, nN), nullref(), status,
+                       pb.iters ? pb.iters + p0 * 2 + 1 : nullptr, 2));
+    QT_TRY(cop.gemm3(nN, nN, nN, H1I8(nx), qt::OP_C, C8(1, nN), qt::OP_N, C8(2, nN), P));
+    QT_TRY(cop.gemm3(nN, nN, nN, C8(2, nN), qt::OP_N, H1I8(nx), qt::OP_N, C8(3, nN), P));
+  }
+  const BatchRef SigR = T(2, nN);
+  zconvert_or_copy<TC>(nN, P, C8(3, nN), SigR, s);
+  const int np = n[N - 1];
+  const BatchRef Hd = H1I(N);  // device coupling n_N x n_{N-1}
+  QT_TRY(op.gemm3(nN, np, np, Hd, qt::OP_N, GL(N - 1), qt::OP_N, T(3, nN), P));
+  qt::zaxpby<TC>(nN, P, HII(N), -1, 0, SigR, -1, 0, Zi, T(4, nN), nullptr, s);
+  QT_TRY(op.gemm3(nN, nN, np, T(3, nN), qt::OP_N, Hd, qt::OP_C, T(5, nN), P, mone, T(4, nN),
+                  one_c));
+  int ig = 6, ign = 7, inew = 3, innew = 4;  // rotating temporaries for G, G^<
+  QT_TRY(op.inv(T(5, nN), T(ig, nN), P, status, nullptr, nN));
+  const BatchRef GamR = T(9, nN);
+  qt::zantiherm<TC>(nN, P, SigR, -1, 0, nullref(), GamR, s);
+  QT_TRY(op.gemm3(nN, np, np, Hd, qt::OP_N, GLN(N - 1), qt::OP_N, T(0, nN), P));
+  QT_TRY(op.gemm3(nN, nN, np, T(0, nN), qt::OP_N, Hd, qt::OP_C, T(5, nN), P));
+  qt::zscale_add<TC>(nN, P, GamR, fr, T(5, nN), T(5, nN), s);
+  QT_TRY(op.gemm3(nN, nN, nN, T(ig, nN), qt::OP_N, T(5, nN), qt::OP_N, T(0, nN), P));
+  QT_TRY(op.gemm3(nN, nN, nN, T(0, nN), qt::OP_N, T(ig, nN), qt::OP_C, T(ign, nN), P));
+  qt::zantiherm<TC>(nN, P, T(ig, nN), 1, 0, T(ign, nN), T(8, nN), s);  // G^>_NN
+  if (pb.tr) qt::ztrace_current<TC>(nN, P, SigR, T(8, nN), T(ign, nN), tr_sign, fr, pb.tr + p0, s);
+  if (caroli) {
+    // G_N1 = G_NN H_{N,N-1} P_{N-1} (n_N x n_0); T = -Re Tr[Gam'_R G_N1 Gam'_L G_N1^+]
+    QT_TRY(op.gemm3(nN, n0, np, Hd, qt::OP_N, ref(tmp + (size_t)12 * P * m2, m2, np), qt::OP_N,
+                    T(0, nN), P));
+    QT_TRY(op.gemm3(nN, n0, nN, T(ig, nN), qt::OP_N, T(0, nN), qt::OP_N, T(10, nN), P));
+    qt::zantiherm<TC>(n0, P, SigL, -1, 0, nullref(), T(5, n0), s);
+    QT_TRY(op.gemm3(n0, nN, n0, T(5, n0), qt::OP_N, T(10, nN), qt::OP_C, T(0, n0), P));
+    QT_TRY(op.gemm3(nN, nN, n0, T(10, nN), qt::OP_N, T(0, n0), qt::OP_N, T(5, nN), P));
+    qt::ztrace_prod<TC>(nN, P, GamR, T(5, nN), -1.0, pb.T + p0, s);
+  }
+  emit(N, T(ig, nN), T(ign, nN));
+
+  // ---------------- backward sweep, coupling H_{l+1,l} = H1i[l+1] (n_{l+1} x n_l)
+  for (int l = N - 1; l >= 0; --l) {
+    const int nl = n[l], nq = n[l + 1];
+    const BatchRef Hc = H1I(l + 1);
+    // X = g H^+ (nl x nq); GN0 = X G_{l+1}; Y = H g (nq x nl); G_l = g + GN0 Y
+    QT_TRY(op.gemm3(nl, nq, nl, GL(l), qt::OP_N, Hc, qt::OP_C, T(0, nl), P));
+    QT_TRY(op.gemm3(nl, nq, nq, T(0, nl), qt::OP_N, T(ig, nq), qt::OP_N, T(1, nl), P));
+    QT_TRY(op.gemm3(nq, nl, nl, Hc, qt::OP_N, GL(l), qt::OP_N, T(2, nq), P));
+    QT_TRY(op.gemm3(nl, nl, nq, T(1, nl), qt::OP_N, T(2, nq), qt::OP_N, T(inew, nl), P, one_c,
+                    GL(l), one_c));
+    // G^<_l = g^< + X G^<_{l+1} X^+ + W - W^+,  W = (GN0 H) g^<
+    QT_TRY(op.gemm3(nl, nq, nq, T(0, nl), qt::OP_N, T(ign, nq), qt::OP_N, T(5, nl), P));
+    QT_TRY(op.gemm3(nl, nl, nq, T(5, nl), qt::OP_N, T(0, nl), qt::OP_C, T(innew, nl), P, one_c,
+                    GLN(l), one_c));
+    QT_TRY(op.gemm3(nl, nl, nq, T(1, nl), qt::OP_N, Hc, qt::OP_N, T(2, nl), P));
+    QT_TRY(op.gemm3(nl, nl, nl, T(2, nl), qt::OP_N, GLN(l), qt::OP_N, T(10, nl), P));
+    qt::zantiherm<TC>(nl, P, T(10, nl), 1, 0, T(innew, nl), T(innew, nl), s);
+    std::swap(ig, inew);
+    std::swap(ign, innew);
+    emit(l, T(ig, nl), T(ign, nl));
+  }
+  if (pb.tre) {
+    qt::zantiherm<TC>(n0, P, T(ig, n0), 1, 0, T(ign, n0), T(0, n0), s);
+    qt::ztrace_current<TC>(n0, P, SigL, T(0, n0), T(ign, n0), 1.0, fe, pb.tre + p0, s);
+  }
+  qt::zcheck_finite<TC>(n0, P, T(ig, n0), status, s);
+  check_wave_outputs(P, pb.dsum, p0, pb.dgr, pb.dgl, pb.dgg, pb.T, pb.tr, pb.tre, status, s);
   if (pb.status)
     cudaMemcpyAsync(pb.status + p0, status, P * sizeof(int), cudaMemcpyDeviceToDevice, s);
   cudaError_t e = cudaGetLastError();
@@ -686,10 +965,11 @@ extern "C" qt_status qt_ctx_create(qt_ctx** out, int device) {
   qt_ctx* c = new qt_ctx();
   c->device = device;
   cudaSetDevice(device);
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;
     QT_FAIL(QT_ERR_CUDA, "stream creation failed");
   }
+  c->stream = c->own_stream;
   *out = c;
   return QT_OK;
 }
@@ -703,7 +983,7 @@ extern "C" qt_status qt_ctx_destroy(qt_ctx* c) {
   if (c->conv) cudaFree(c->conv);
   for (auto& e : c->prof.v) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
   for (auto e : c->prof.pool) cudaEventDestroy(e);
-  cudaStreamDestroy(c->stream);
+  cudaStreamDestroy(c->own_stream);
   delete c;
   return QT_OK;
 }
@@ -749,6 +1029,14 @@ extern "C" qt_status qt_ctx_profile_read(qt_ctx* c, int kind, int64_t* launches,
   return QT_OK;
 }
 
+extern "C" qt_status qt_ctx_set_stream(qt_ctx* c, void* stream, int use_own) {
+  if (!c) QT_FAIL(QT_ERR_ARG, "null ctx");
+  cudaSetDevice(c->device);
+  QT_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  c->stream = use_own ? c->own_stream : reinterpret_cast<cudaStream_t>(stream);
+  return QT_OK;
+}
+
 extern "C" qt_status qt_ctx_stream(qt_ctx* c, void** stream) {
   if (!c || !stream) QT_FAIL(QT_ERR_ARG, "null argument");
   *stream = (void*)c->stream;
@@ -773,6 +1061,10 @@ qt_status run_problem(qt_ctx* ctx, Problem& pb, long long hii_n, long long h1i_n
   const bool c64 = pb.prec == QT_PREC_MIXED;
   pb.sweep_slices = env_int("QT_SWEEP_SLICES", c64 ? 4 : 6);
   pb.lead_slices = env_int("QT_LEAD_SLICES", 7);
+  // complex64 sweep: one refinement reaches its storage resolution; complex128 sweep
+  // (MIXED_FP64): three, as for the leads.  QT_SWEEP_REFINE overrides.
+  pb.sweep_refine = env_int("QT_SWEEP_REFINE", c64 ? 1 : 3);
+  if (pb.sweep_refine < 0 || pb.sweep_refine > 8) QT_FAIL(QT_ERR_ARG, "QT_SWEEP_REFINE in 0..8");
   if (c64 && pb.sweep_slices != 3 && pb.sweep_slices != 4)
     QT_FAIL(QT_ERR_ARG, "QT_SWEEP_SLICES in {3,4} for the complex64 sweep");
   if (!c64 && pb.sweep_slices != 4 && pb.sweep_slices != 6 && pb.sweep_slices != 7)
@@ -808,6 +1100,49 @@ qt_status run_problem(qt_ctx* ctx, Problem& pb, long long hii_n, long long h1i_n
     else QT_TRY(solve_wave<double2>(ctx, pb, p0, Pw, ar));
   }
   if (split) {
+    QT_CUDA_TRY(cudaStreamSynchronize(s));
+    if (qt::oz_timeouts_and_reset()) QT_FAIL(QT_ERR_CUDA, "tensor-core kernel wait timed out");
+  }
+  return QT_OK;
+}
+
+qt_status run_problem_vb(qt_ctx* ctx, ProblemVB& pb, long long hii_n, long long h1i_n) {
+  const bool c64 = pb.prec == QT_PREC_MIXED;
+  pb.sweep_slices = env_int("QT_SWEEP_SLICES", c64 ? 4 : 6);
+  pb.lead_slices = env_int("QT_LEAD_SLICES", 7);
+  pb.sweep_refine = env_int("QT_SWEEP_REFINE", c64 ? 1 : 3);
+  if (pb.sweep_refine < 0 || pb.sweep_refine > 8) QT_FAIL(QT_ERR_ARG, "QT_SWEEP_REFINE in 0..8");
+  if (c64 && pb.sweep_slices != 3 && pb.sweep_slices != 4)
+    QT_FAIL(QT_ERR_ARG, "QT_SWEEP_SLICES in {3,4} for the complex64 sweep");
+  if (!c64 && pb.sweep_slices != 4 && pb.sweep_slices != 6 && pb.sweep_slices != 7)
+    QT_FAIL(QT_ERR_ARG, "QT_SWEEP_SLICES in {4,6,7} for the complex128 sweep");
+  if (pb.lead_slices != 4 && pb.lead_slices != 6 && pb.lead_slices != 7)
+    QT_FAIL(QT_ERR_ARG, "QT_LEAD_SLICES in {4,6,7}");
+  cudaStream_t s = ctx->stream;
+  if (c64) {
+    QT_TRY(ensure(ctx->conv, ctx->conv_bytes, (size_t)(hii_n + h1i_n) * sizeof(float2) + 4096));
+    float2* c = reinterpret_cast<float2*>(ctx->conv);
+    flat_d2f_kernel<<<g1d(hii_n), 256, 0, s>>>(reinterpret_cast<const double2*>(pb.Hii), c, hii_n);
+    qt::count_launch();
+    flat_d2f_kernel<<<g1d(h1i_n), 256, 0, s>>>(reinterpret_cast<const double2*>(pb.H1i),
+                                                c + hii_n, h1i_n);
+    qt::count_launch();
+    pb.Hii32 = c;
+    pb.H1i32 = c + hii_n;
+  }
+  const size_t per = wave_bytes_vb(pb, 1);
+  long long P = (long long)((size_t)ctx->scratch_limit / (per + 1));
+  P = std::min<long long>(P, std::max<long long>(152 * 4, pb.nk));
+  P = std::min<long long>(P, pb.npts);
+  P = std::max<long long>(P / pb.nk, 1) * pb.nk;
+  QT_TRY(ensure(ctx->arena, ctx->arena_bytes, wave_bytes_vb(pb, P)));
+  for (long long p0 = 0; p0 < pb.npts; p0 += P) {
+    const long long Pw = std::min(P, pb.npts - p0);
+    Arena ar{reinterpret_cast<char*>(ctx->arena), ctx->arena_bytes, 0};
+    if (c64) QT_TRY(solve_wave_vb<float2>(ctx, pb, p0, Pw, ar));
+    else QT_TRY(solve_wave_vb<double2>(ctx, pb, p0, Pw, ar));
+  }
+  if (pb.prec != QT_PREC_FP64) {
     QT_CUDA_TRY(cudaStreamSynchronize(s));
     if (qt::oz_timeouts_and_reset()) QT_FAIL(QT_ERR_CUDA, "tensor-core kernel wait timed out");
   }
@@ -913,6 +1248,101 @@ extern "C" qt_status qt_rgf_solve(qt_ctx* ctx, const qt_device* dev, const doubl
       }
       for (long long p = 0; p < npts; ++p)
         if (st_h[p]) return QT_ERR_POINTS;
+    }
+  }
+  return QT_OK;
+}
+
+extern "C" qt_status qt_rgf_solve_vb(qt_ctx* ctx, const qt_device_vb* dev, const double* E,
+                                     int nE, const qt_contacts* c, qt_precision prec,
+                                     unsigned flags, qt_outputs* out) {
+  if (!ctx || !dev || !E || !c || !out) QT_FAIL(QT_ERR_ARG, "null argument");
+  if (dev->nx < 2 || dev->nk <= 0 || nE <= 0 || !dev->nm || !dev->hii_off || !dev->h1i_off)
+    QT_FAIL(QT_ERR_ARG, "need nx >= 2, nk > 0, nE > 0 and the block tables");
+  if (!dev->Hii || !dev->H1i) QT_FAIL(QT_ERR_ARG, "Hii/H1i required");
+  if (!valid_prec(prec)) QT_FAIL(QT_ERR_ARG, "unknown precision");
+  if (c->sancho_max_iter <= 0) QT_FAIL(QT_ERR_ARG, "sancho_max_iter must be > 0");
+  if (c->quirks & QT_QUIRK_GLP_ZERO) QT_FAIL(QT_ERR_UNSUPPORTED, "QT_QUIRK_GLP_ZERO needs equal blocks");
+  if (out->G_r || out->G_lesser || out->G_greater)
+    QT_FAIL(QT_ERR_UNSUPPORTED, "variable blocks: diagonal outputs only");
+  cudaSetDevice(ctx->device);
+  ProblemVB pb{};
+  pb.nx = dev->nx; pb.nk = dev->nk;
+  pb.npts = (long long)nE * dev->nk;
+  pb.c = *c; pb.prec = prec; pb.flags = flags;
+  pb.hk = dev->hii_kstride; pb.h1k = dev->h1i_kstride;
+  long long hii_n = 0, h1i_n = 0;
+  for (int l = 0; l < dev->nx; ++l) {
+    const int nl = dev->nm[l];
+    if (nl <= 0) QT_FAIL(QT_ERR_ARG, "block sizes must be > 0");
+    pb.n.push_back(nl);
+    pb.nmax = std::max(pb.nmax, nl);
+    pb.hoff.push_back(dev->hii_off[l]);
+    pb.doff.push_back(pb.dsum);
+    pb.dsum += nl;
+    pb.goff.push_back(pb.gsum);
+    pb.gsum += (long long)nl * nl;
+    hii_n = std::max(hii_n, (long long)dev->hii_off[l] + (long long)nl * nl);
+  }
+  for (int l = 0; l <= dev->nx; ++l) {
+    const int rows = l == 0 ? pb.n[0] : (l == dev->nx ? pb.n[dev->nx - 1] : pb.n[l]);
+    const int cols = l == 0 ? pb.n[0] : (l == dev->nx ? pb.n[dev->nx - 1] : pb.n[l - 1]);
+    pb.h1off.push_back(dev->h1i_off[l]);
+    h1i_n = std::max(h1i_n, (long long)dev->h1i_off[l] + (long long)rows * cols);
+  }
+  if (prec != QT_PREC_FP64 && pb.nmax > 128) QT_FAIL(QT_ERR_UNSUPPORTED, "mixed path needs blocks <= 128");
+  hii_n += pb.hk ? (dev->nk - 1) * pb.hk : 0;
+  h1i_n += pb.h1k ? (dev->nk - 1) * pb.h1k : 0;
+  const long long npts = pb.npts, diag_n = npts * pb.dsum;
+  const bool devp = (flags & QT_FLAG_DEVICE_POINTERS) != 0;
+  if (devp) {
+    pb.Hii = reinterpret_cast<const cd*>(dev->Hii);
+    pb.H1i = reinterpret_cast<const cd*>(dev->H1i);
+    pb.E = E;
+    pb.tr = out->tr; pb.tre = out->tre; pb.T = out->T;
+    pb.dgr = out->diag_gr; pb.dgl = out->diag_gl; pb.dgg = out->diag_gg;
+    pb.status = out->status; pb.iters = out->sancho_iters;
+    QT_TRY(run_problem_vb(ctx, pb, hii_n, h1i_n));
+  } else {
+    size_t need = 0;
+    auto add = [&](size_t bytes) { need += (bytes + 255) & ~size_t(255); };
+    add(hii_n * 16); add(h1i_n * 16); add(nE * 8);
+    add(npts * 8 * 3); add(diag_n * 16 * 3); add(npts * 4 * 3);
+    QT_TRY(ensure(ctx->io, ctx->io_bytes, need + 4096));
+    HostStage st{ctx, reinterpret_cast<char*>(ctx->io)};
+    pb.Hii = st.put(reinterpret_cast<const cd*>(dev->Hii), hii_n, true);
+    pb.H1i = st.put(reinterpret_cast<const cd*>(dev->H1i), h1i_n, true);
+    pb.E = st.put(E, nE, true);
+    pb.tr = out->tr ? st.put<double>(nullptr, npts, false) : nullptr;
+    pb.tre = out->tre ? st.put<double>(nullptr, npts, false) : nullptr;
+    pb.T = out->T ? st.put<double>(nullptr, npts, false) : nullptr;
+    pb.dgr = out->diag_gr ? st.put<double>(nullptr, 2 * diag_n, false) : nullptr;
+    pb.dgl = out->diag_gl ? st.put<double>(nullptr, 2 * diag_n, false) : nullptr;
+    pb.dgg = out->diag_gg ? st.put<double>(nullptr, 2 * diag_n, false) : nullptr;
+    pb.status = st.put<int>(nullptr, npts, false);
+    pb.iters = st.put<int>(nullptr, 2 * npts, false);
+    QT_TRY(run_problem_vb(ctx, pb, hii_n, h1i_n));
+    auto back = [&](void* dst, const void* src, size_t bytes) {
+      if (dst && src) cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream);
+    };
+    back(out->tr, pb.tr, npts * 8);
+    back(out->tre, pb.tre, npts * 8);
+    back(out->T, pb.T, npts * 8);
+    back(out->diag_gr, pb.dgr, diag_n * 16);
+    back(out->diag_gl, pb.dgl, diag_n * 16);
+    back(out->diag_gg, pb.dgg, diag_n * 16);
+    back(out->status, pb.status, npts * 4);
+    back(out->sancho_iters, pb.iters, npts * 8);
+    flags |= QT_FLAG_SYNC;
+  }
+  if (flags & QT_FLAG_SYNC) {
+    QT_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    if (out->status) {
+      std::vector<int> hs(npts);
+      cudaMemcpy(hs.data(), out->status, npts * sizeof(int),
+                 devp ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost);
+      for (long long p = 0; p < npts; ++p)
+        if (hs[p]) return QT_ERR_POINTS;
     }
   }
   return QT_OK;

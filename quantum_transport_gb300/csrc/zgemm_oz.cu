@@ -30,11 +30,11 @@
 //    output) or assembled into FP64 bits with integer operations (complex128
 //    output, no use of the FP64 pipe).
 //
-// Roles (416 threads, one CTA per SM: the accumulators use all 512 TMEM
-// columns):  warps 0-3 epilogue (TMEM lanes 0-127), warps 4-11 producers
-// (digit slicing straight from global memory into the canonical no-swizzle
-// K-major UMMA layout in shared memory), warp 12 TMEM allocation + the single
-// MMA-issuing thread.  Stages are handed over with mbarriers; every wait is
+// Roles (one CTA per SM: the accumulators use all 512 TMEM columns): warps 0-3
+// epilogue (TMEM lanes 0-127); 16 producer warps for 128-column tiles, 8 for
+// 64-column tiles (digit slicing straight from global memory into the
+// canonical no-swizzle K-major UMMA layout in shared memory); the last warp
+// allocates TMEM and holds the single MMA-issuing thread.  Stages are handed over with mbarriers; every wait is
 // bounded (a few seconds) and records a timeout instead of hanging.
 #include <stdint.h>
 
@@ -49,9 +49,15 @@ __device__ int g_oz_timeouts = 0;
 namespace {
 
 constexpr int KC = 32;            // real-K elements per pipeline stage
-constexpr int NTHREADS = 416;
-constexpr int NPROD = 256;        // producer threads (warps 4..11)
-constexpr int MMA_WARP = 12;
+// Roles per CTA: warps 0-3 epilogue, then the producer warps, then the MMA warp.
+// 128-column tiles get 16 producer warps (more loads in flight per SM), 64-column
+// tiles 8, so that each producer thread stages a whole number of items.
+template <int NT>
+struct Roles {
+  static constexpr int NPROD = NT == 128 ? 512 : 256;
+  static constexpr int NTHREADS = 128 + NPROD + 32;
+  static constexpr int MMA_WARP = 4 + NPROD / 32;
+};
 constexpr uint64_t TIMEOUT_NS = 4000000000ull;  // 4 s per wait
 constexpr int PLANE_BYTES = 128 * KC * 2;       // one digit plane of a 128-row tile: 8 KB
 constexpr uint32_t LBO = 128;                   // K-adjacent core matrices
@@ -245,7 +251,8 @@ template <typename TIn>
 __global__ void __launch_bounds__(256) oz_scales_kernel(GemmArgs a) {
   __shared__ unsigned long long part_max[256];
   const int which = blockIdx.y;
-  const int n = a.m, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nv = which ? a.n : a.m, K = a.k;  // vectors (rows of op(A) / columns of op(B)), length
   for (long long b = blockIdx.x; b < a.batch; b += gridDim.x) {
     int* out = a.scales + b * 256 + which * 128;
     if (a.active && !a.active[b]) continue;
@@ -259,30 +266,30 @@ __global__ void __launch_bounds__(256) oz_scales_kernel(GemmArgs a) {
     if (contiguous) {
       for (int v = warp; v < 128; v += 8) {
         unsigned long long m = 0;
-        if (v < n) {
+        if (v < nv) {
 #pragma unroll 4
-          for (int e = lane; e < n; e += 32) {
+          for (int e = lane; e < K; e += 32) {
             const TIn x = M[e + (long long)v * ld];
             m = max(m, max(absbits(x, 0), absbits(x, 1)));
           }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (lane == 0) out[v] = v < n ? exp_bound_bits<TIn>(m) : 0;
+        if (lane == 0) out[v] = v < nv ? exp_bound_bits<TIn>(m) : 0;
       }
     } else {
       const int v = tid & 127, h = tid >> 7;  // two threads per vector
       unsigned long long m = 0;
-      if (v < n) {
+      if (v < nv) {
 #pragma unroll 8
-        for (int e = h; e < n; e += 2) {
+        for (int e = h; e < K; e += 2) {
           const TIn x = M[v + (long long)e * ld];
           m = max(m, max(absbits(x, 0), absbits(x, 1)));
         }
       }
       part_max[tid] = m;
       __syncthreads();
-      if (h == 0) out[v] = v < n ? exp_bound_bits<TIn>(max(m, part_max[tid + 128])) : 0;
+      if (h == 0) out[v] = v < nv ? exp_bound_bits<TIn>(max(m, part_max[tid + 128])) : 0;
       __syncthreads();
     }
   }
@@ -290,7 +297,8 @@ __global__ void __launch_bounds__(256) oz_scales_kernel(GemmArgs a) {
 
 // ------------------------------------------------------------ the kernel
 template <int S, int L, int NT, typename TIn, typename TOut>
-__global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int stages) {
+__global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int stages) {
+  constexpr int NPROD = Roles<NT>::NPROD, MMA_WARP = Roles<NT>::MMA_WARP;
   // NT output columns per CTA; the 512 TMEM columns hold 512/NT accumulators.  With
   // NT = 64 every digit level up to 7 has its own (exact) accumulator.
   constexpr int NACC_MAX = 512 / NT;
@@ -312,9 +320,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int s
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_base_sm + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int n = a.m;
+  const int m = a.m, n = a.n, K = a.k;         // C is m x n, op(A) m x K, op(B) K x n
   const int npad = (n + 15) & ~15;
-  const int nch = (n + KC / 2 - 1) / (KC / 2);  // stages: KC real K = KC/2 complex k each
+  const int nch = (K + KC / 2 - 1) / (KC / 2);  // stages: KC real K = KC/2 complex k each
   const int ntile = (npad + NT - 1) / NT;  // column tiles per real part
   // work item: (batch entry, real/imag part of C, column tile)
   const long long nitems = 2LL * ntile * a.batch;
@@ -335,9 +343,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int s
   tc_fence_after();
   const uint32_t tmem = *tmem_base_sm;
 
-  if (warp >= 4 && warp < 12) {
+  if (warp >= 4 && warp < MMA_WARP) {
     // ======================== producers
-    const int p = tid - 128;  // 0..255
+    const int p = tid - 128;  // 0 .. NPROD-1
     uint32_t proc = 0, gchunk = 0;
     for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
       const long long b = w / (2 * ntile);
@@ -373,7 +381,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int s
             const int k = kc0 + 4 * g + u;
             TIn x;
             x.x = 0; x.y = 0;
-            if (rg < n && k < n)
+            if (rg < (isA ? m : n) && k < K)
               x = isA ? load_op<TIn>(A, a.A.ld, a.opA, rg, k) : load_op<TIn>(B, a.B.ld, a.opB, k, rg);
             xv[q][u] = x;
           }
@@ -392,8 +400,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int s
             float D0[S], D1[S];
             const TIn x = xv[q][u];
             if constexpr (sizeof(TIn) == 8) {
-              const float scale = __int_as_float((127 + 8 - e) << 23);  // 2^(8-e)
-              float v0 = x.x, v1 = x.y;
+              // 2^(8-e) as pre * scale: rows below 2^-119 would overflow a single FP32
+              // power of two, so they are first lifted by 2^64 (exact)
+              const bool tiny = e < -118;
+              const float pre = tiny ? 18446744073709551616.0f : 1.0f;
+              const float scale = __int_as_float((127 + 8 - (tiny ? e + 64 : e)) << 23);
+              float v0 = x.x * pre, v1 = x.y * pre;
               if (!isA) {
                 if (part == 0) v1 = -v1;
                 else { v0 = x.y; v1 = x.x; }
@@ -493,7 +505,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int s
       }
       const int ei = erow[row];
       const float alpha = (float)a.alpha_re, beta = (float)a.beta_re;
-      constexpr int CW = NACC > 4 ? 8 : 16;  // columns per TMEM read (register budget)
+      // columns per TMEM read (register budget of the wider 128-column CTAs)
+      constexpr int CW = (NACC > 4 || NPROD > 256) ? 8 : 16;
       for (int j0 = 0; j0 < NT; j0 += CW) {
         uint32_t r[NACC][16];
 #pragma unroll
@@ -502,7 +515,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int s
           else tmem_ld8(lane_base + acc * NT + j0, r[acc]);
         }
         tmem_wait_ld();
-        if (row < n) {
+        if (row < m) {
 #pragma unroll
           for (int jj = 0; jj < CW; ++jj) {
             const int j = ct * NT + j0 + jj;
@@ -553,14 +566,14 @@ cudaError_t launch(const GemmArgs& a, cudaStream_t s) {
   cudaError_t e = cudaFuncSetAttribute(zgemm_oz_kernel<S, L, NT, TIn, TOut>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  const int ntile = (((a.m + 15) & ~15) + NT - 1) / NT;
+  const int ntile = (((a.n + 15) & ~15) + NT - 1) / NT;
   const long long items = 2LL * ntile * a.batch;
   const int grid = (int)(items < sms ? items : sms);
   if (!a.scales) return cudaErrorInvalidValue;
   const long long gb = a.batch < 65535 ? a.batch : 65535;
   oz_scales_kernel<TIn><<<dim3((unsigned)gb, 2), 256, 0, s>>>(a);
   count_launch();
-  zgemm_oz_kernel<S, L, NT, TIn, TOut><<<grid, NTHREADS, smem, s>>>(a, stages);
+  zgemm_oz_kernel<S, L, NT, TIn, TOut><<<grid, Roles<NT>::NTHREADS, smem, s>>>(a, stages);
   count_launch();
   return cudaGetLastError();
 }
@@ -569,7 +582,8 @@ cudaError_t launch(const GemmArgs& a, cudaStream_t s) {
 
 cudaError_t zgemm_oz(const GemmArgs& a, int slices, int levels, cudaStream_t s) {
   if (a.batch <= 0) return cudaSuccess;
-  if (a.m != a.n || a.m != a.k || a.m > 128 || a.m <= 0) return cudaErrorInvalidValue;
+  if (a.m <= 0 || a.n <= 0 || a.k <= 0 || a.m > 128 || a.n > 128 || a.k > 128)
+    return cudaErrorInvalidValue;
   if (a.opA == OP_T || a.opB == OP_T || a.alpha_im != 0.0 || a.beta_im != 0.0)
     return cudaErrorInvalidValue;
   (void)levels;
@@ -583,7 +597,8 @@ cudaError_t zgemm_oz(const GemmArgs& a, int slices, int levels, cudaStream_t s) 
 
 cudaError_t zgemm_oz_c64(const GemmArgs& a, int slices, cudaStream_t s) {
   if (a.batch <= 0) return cudaSuccess;
-  if (a.m != a.n || a.m != a.k || a.m > 128 || a.m <= 0) return cudaErrorInvalidValue;
+  if (a.m <= 0 || a.n <= 0 || a.k <= 0 || a.m > 128 || a.n > 128 || a.k > 128)
+    return cudaErrorInvalidValue;
   if (a.opA == OP_T || a.opB == OP_T || a.alpha_im != 0.0 || a.beta_im != 0.0)
     return cudaErrorInvalidValue;
   switch (slices) {

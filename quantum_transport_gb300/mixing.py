@@ -12,9 +12,10 @@ orbital it returns a step a_o and a momentum b_o.  The proposal is
 
 applied to Sigma^R, Sigma^< and Sigma^> (b_ij likewise).  At a fixed point
 R = 0 and Sigma = Sigma_prev, so no proposal can move the fixed point.  A
-proposal is kept only if the residual F evaluates for it is below the last
-accepted one; otherwise it is discarded and a Pulay (DIIS) step over the
-accepted history is taken instead.
+proposal is kept only if the residual F evaluates for it falls below
+ACCEPT_RATIO times the last accepted one; otherwise it is discarded, a Pulay
+(DIIS) step over the accepted history is taken instead, and the next COOLDOWN
+steps are Pulay steps too.
 
 Training data come from the method itself: plain-mixing runs on seeded
 disorder realisations give iterate histories and their converged fixed point
@@ -39,6 +40,8 @@ NHIST = 3
 N_IN = 2 * NHIST * NCOEF + 2
 N_OUT = 2
 ALPHA_MAX, BETA_MIN, BETA_MAX = 4.0, -0.5, 0.95
+ACCEPT_RATIO = 0.8   # a learned proposal is kept only if it cuts the residual by >= 20 %
+COOLDOWN = 2         # Pulay steps after a rejected proposal before the network is asked again
 
 
 def chebyshev_projector(nE, ncoef=NCOEF):
@@ -123,6 +126,7 @@ class ScbaResult:
     rejected: int = 0     # learned proposals discarded (Pulay step taken instead)
     pulay: int = 0        # Pulay steps
     plain: int = 0        # linear-mixing steps
+    kinds: list = dataclasses.field(default_factory=list)  # step that produced each evaluation
 
 
 class Recorder:
@@ -206,6 +210,7 @@ def run_scba(system, *, method="learned", mixer=None, alpha=0.3, tol=1e-8, max_i
     ab = torch.empty((norb, N_OUT), dtype=torch.float32, device="cuda")
     res = ScbaResult(sigma=None, residuals=[], evaluations=0, seconds=0.0)
     r_acc, last, final = np.inf, None, None
+    cool = 0  # Pulay steps left before the network is asked again
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(max_iter):
@@ -213,17 +218,19 @@ def run_scba(system, *, method="learned", mixer=None, alpha=0.3, tol=1e-8, max_i
         R = tuple(ops.diff(N[q], S[q], torch.empty_like(S[q])) for q in range(3))
         r = ops.residual(R, N)
         res.residuals.append(r)
+        res.kinds.append(last or "start")
         if r <= tol:
             final = tuple(ops.combine([1.0], [S[q]], [R[q]], alpha, torch.empty_like(S[q]))
                           for q in range(3))
             if last == "learned":
                 res.accepted += 1
             break
-        if last == "learned" and r >= r_acc:
+        if last == "learned" and r >= ACCEPT_RATIO * r_acc:
             res.rejected += 1
             S = _pulay_step(ops, hist[-pulay_depth:], alpha)
             res.pulay += 1
             last = "pulay"
+            cool = COOLDOWN
             continue
         if last == "learned":
             res.accepted += 1
@@ -243,7 +250,7 @@ def run_scba(system, *, method="learned", mixer=None, alpha=0.3, tol=1e-8, max_i
             dd = ops.diag(D[0], D[1], torch.empty_like(ring[0]))
             recorder.add(feats.cpu().numpy(), sd.cpu().numpy(), ring[0].cpu().numpy(),
                          dd.cpu().numpy())
-        if method == "learned" and ready:
+        if method == "learned" and ready and cool == 0:
             mixer.net.infer(feats, out=ab)
             Sp = hist[-2][0]
             newS = []
@@ -255,7 +262,8 @@ def run_scba(system, *, method="learned", mixer=None, alpha=0.3, tol=1e-8, max_i
                 newS.append(o)
             S = tuple(newS)
             last = "learned"
-        elif method == "pulay" and len(hist) >= 2:
+        elif (method == "pulay" or (method == "learned" and cool > 0)) and len(hist) >= 2:
+            cool = max(cool - 1, 0)
             S = _pulay_step(ops, hist[-pulay_depth:], alpha)
             res.pulay += 1
             last = "pulay"
@@ -320,8 +328,20 @@ def collect(systems, *, mixer=None, alpha=0.3, tol=1e-8, max_iter=200, fixed_poi
 
 def train(mixer, X, T, *, steps=1500, batch=4096, lr=1e-3, weight_decay=1e-4, seed=0,
           log_every=0):
-    """AdamW on the GPU with the library's kernels; returns the loss trace (host)."""
+    """AdamW on the GPU with the library's kernels; returns the loss trace (host).
+
+    A fresh network first gets its output layer set to predict the targets' mean (bias =
+    mean, weights scaled by 0.1), so that training fits the per-orbital variation.
+    """
     import torch
+    if not getattr(mixer, "trained", False):
+        p = mixer.net.params()
+        d = mixer.net.dims  # (n_in, width, depth, n_out)
+        wo = mixer.net.nparams - d[3] - d[1] * d[3]
+        p[wo:wo + d[1] * d[3]] *= 0.1
+        p[wo + d[1] * d[3]:] = np.asarray(T, np.float64).mean(axis=0)
+        mixer.net.set_params(p)
+        mixer.trained = True
     Xd = torch.from_numpy(np.ascontiguousarray(X, np.float32)).cuda()
     Td = torch.from_numpy(np.ascontiguousarray(T, np.float32)).cuda()
     g = torch.Generator(device="cuda")

@@ -35,14 +35,24 @@ PREC = {"fp64": _lib.QT_PREC_FP64, "mixed": _lib.QT_PREC_MIXED,
 
 
 class Context:
-    """GPU context: one CUDA stream + device scratch (cuda_rgf_init/finish)."""
+    """GPU context: device scratch and the stream it launches on (cuda_rgf_init/finish).
 
-    def __init__(self, device=0):
+    By default the library launches on PyTorch's current stream of ``device``, so that
+    torch tensors passed in place (allocated, sliced or zeroed by torch) are ordered with
+    the library's kernels.  ``torch_stream=False`` keeps the context's own stream; callers
+    then order their work with ``sync()``.
+    """
+
+    def __init__(self, device=0, torch_stream=True):
         self._lib = _lib.load()
         h = C.c_void_p()
         check(self._lib.qt_ctx_create(C.byref(h), int(device)))
         self.handle = h
         self.device = device
+        if torch_stream:
+            import torch
+            s = torch.cuda.current_stream(device).cuda_stream
+            check(self._lib.qt_ctx_set_stream(h, C.c_void_p(s), 0))
 
     def close(self):
         if self.handle:
@@ -186,6 +196,63 @@ def rgf_solve(ctx, Hii, H1i, E, nx, *, nk=1, mul=0.0, mur=0.0, templ=300.0, temp
     for k in ("diag_gr", "diag_gl", "diag_gg"):
         if k in res:
             res[k] = res[k].reshape(nE, nk, nx, nm)
+    res["sancho_iters"] = res["sancho_iters"].reshape(nE, nk, 2)
+    return res
+
+
+def rgf_variableblock_forward(ctx, Hii, H1i, E, *, nk=1, mul=0.0, mur=0.0, templ=300.0,
+                              tempr=300.0, eta_lead=1e-5, eta_interior=0.0, sancho_tol=1e-100,
+                              sancho_max_iter=50, precision="fp64", caroli=False, quirks=0):
+    """Batched RGF over slabs of different orbital counts (rgf_variableblock_forward,
+    src/rgf_mod.f90:46-269) for all (E, k) points.
+
+    ``Hii``: nx blocks H_ll, each (n_l, n_l) or (nk, n_l, n_l).  ``H1i``: nx + 1 blocks,
+    H1i[l] = H_{l,l-1} (n_l, n_{l-1}) for 1 <= l < nx, H1i[0] and H1i[nx] the leads' own
+    couplings (square), each optionally per k.  Returns tr, tre (and T) (nE, nk), status,
+    sancho_iters and the diagonals diag_gr / diag_gl / diag_gg as lists of nx arrays
+    (nE, nk, n_l).
+    """
+    lib = ctx._lib
+    E = np.ascontiguousarray(np.asarray(E, dtype=np.float64).ravel())
+    nE, nx = E.shape[0], len(Hii)
+    if len(H1i) != nx + 1:
+        raise ValueError("H1i needs nx + 1 blocks")
+
+    def pack(blocks):
+        blocks = [np.asarray(b, dtype=np.complex128) for b in blocks]
+        per_k = [b if b.ndim == 3 else np.broadcast_to(b, (nk,) + b.shape) for b in blocks]
+        offs = np.cumsum([0] + [b.shape[1] * b.shape[2] for b in per_k])[:-1].astype(np.int64)
+        kstride = int(sum(b.shape[1] * b.shape[2] for b in per_k))
+        flat = np.concatenate([np.swapaxes(b, -1, -2).reshape(nk, -1) for b in per_k], axis=1)
+        return np.ascontiguousarray(flat), offs, kstride
+
+    sizes = np.array([np.shape(h)[-1] for h in Hii], dtype=np.int32)
+    hii, hoff, hk = pack(Hii)
+    h1i, h1off, h1k = pack(H1i)
+    dev = _lib.QtDeviceVB(nx, nk, _ptr(sizes), _ptr(hii), _ptr(hoff), hk if nk > 1 else 0,
+                          _ptr(h1i), _ptr(h1off), h1k if nk > 1 else 0)
+    con = QtContacts(mul, mur, templ, tempr, eta_lead, eta_interior, sancho_tol,
+                     int(sancho_max_iter), int(quirks))
+    npts, dsum = nE * nk, int(sizes.sum())
+    res = {"tr": np.zeros(npts), "tre": np.zeros(npts),
+           "status": np.zeros(npts, dtype=np.int32),
+           "sancho_iters": np.zeros((npts, 2), dtype=np.int32)}
+    if caroli:
+        res["T"] = np.zeros(npts)
+    for k in ("diag_gr", "diag_gl", "diag_gg"):
+        res[k] = np.zeros((npts, dsum), dtype=np.complex128)
+    out = QtOutputs(*[_ptr(res.get(k)) for k in ("tr", "tre", "T", "diag_gr", "diag_gl",
+                                                 "diag_gg", "G_r", "G_lesser", "G_greater",
+                                                 "status", "sancho_iters")])
+    flags = _lib.QT_FLAG_SYNC | (_lib.QT_FLAG_CAROLI if caroli else 0)
+    check(lib.qt_rgf_solve_vb(ctx.handle, C.byref(dev), _ptr(E), nE, C.byref(con),
+                              PREC[precision], flags, C.byref(out)), allow_points=True)
+    for k in ("tr", "tre", "T", "status"):
+        if k in res:
+            res[k] = res[k].reshape(nE, nk)
+    cut = np.cumsum(sizes)[:-1]
+    for k in ("diag_gr", "diag_gl", "diag_gg"):
+        res[k] = [d.reshape(nE, nk, -1) for d in np.split(res[k], cut, axis=1)]
     res["sancho_iters"] = res["sancho_iters"].reshape(nE, nk, 2)
     return res
 

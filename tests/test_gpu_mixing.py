@@ -74,7 +74,7 @@ def test_mix_features_match_numpy(ctx):
     c = np.einsum("em,hqeo->ohqm", Qt, ring)          # coefficients [o][h][q][m]
     n0 = np.sqrt((c[:, 0] ** 2).sum(axis=(1, 2)))
     n1 = np.sqrt((c[:, 1] ** 2).sum(axis=(1, 2)))
-    ref = np.concatenate([(c / n0[:, None, None, None]).reshape(norb, -1),
+    ref = np.concatenate([np.clip(c / n0[:, None, None, None], -8, 8).reshape(norb, -1),
                           np.full((norb, 1), -3.0 / 8.0),
                           np.clip(np.log10(n0 / n1), -4, 4)[:, None]], axis=1)
     np.testing.assert_allclose(f.cpu().numpy(), ref, rtol=2e-6, atol=2e-6)
