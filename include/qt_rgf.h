@@ -347,7 +347,8 @@ qt_status qt_mlp_train_step(qt_mlp* net, int batch, const float* X, const float*
  *                  and clamped to +-8,
  *                  then log10(residual)/8 and the orbital's log10 decay
  * qt_mix_apply:    out = S + a_ij R + b_ij (S - S_prev), a_ij = (a_i + a_j)/2,
- *                  b_ij likewise; ab[o] = (a_o, b_o) clamped to [0, alpha_max]
+ *                  b_ij likewise; row o of ab [norb][ncols] holds a_o (ncols 1,
+ *                  b = 0) or (a_o, b_o) (ncols 2), clamped to [0, alpha_max]
  *                  and [beta_min, beta_max]; S_prev may be NULL; out may be S
  * qt_mix_gram:     G[i][j] = Re <XL_i, XL_j> + Re <XG_i, XG_j> (host k x k)
  * qt_mix_combine:  out = sum_i coef_i (X_i + alpha R_i)  (k <= 8 vectors)   */
@@ -355,9 +356,9 @@ qt_status qt_mix_diag(qt_ctx* ctx, int nE, int nx, int nm, const double* XL, con
                       double* out, unsigned flags);
 qt_status qt_mix_features(qt_ctx* ctx, int nE, int64_t norb, int nhist, const double* ring,
                           const double* Qt, double log_residual, float* feats, unsigned flags);
-qt_status qt_mix_apply(qt_ctx* ctx, int nE, int nx, int nm, const float* ab, double alpha_max,
-                       double beta_min, double beta_max, const double* S, const double* R,
-                       const double* S_prev, double* out, unsigned flags);
+qt_status qt_mix_apply(qt_ctx* ctx, int nE, int nx, int nm, const float* ab, int ncols,
+                       double alpha_max, double beta_min, double beta_max, const double* S,
+                       const double* R, const double* S_prev, double* out, unsigned flags);
 qt_status qt_mix_gram(qt_ctx* ctx, int64_t count, int k, const double* const* XL,
                       const double* const* XG, double* G_host);
 qt_status qt_mix_combine(qt_ctx* ctx, int64_t count, int k, const double* coef,

@@ -117,7 +117,7 @@ def load(path=LIB_PATH):
                                     C.c_uint, C.POINTER(QtOutputs)]
     lib.qt_mix_diag.argtypes = [vp, ci, ci, ci, vp, vp, vp, C.c_uint]
     lib.qt_mix_features.argtypes = [vp, ci, i64, ci, vp, vp, dbl, vp, C.c_uint]
-    lib.qt_mix_apply.argtypes = [vp, ci, ci, ci, vp, dbl, dbl, dbl, vp, vp, vp, vp, C.c_uint]
+    lib.qt_mix_apply.argtypes = [vp, ci, ci, ci, vp, ci, dbl, dbl, dbl, vp, vp, vp, vp, C.c_uint]
     lib.qt_mix_gram.argtypes = [vp, i64, ci, pvp, pvp, vp]
     lib.qt_mix_combine.argtypes = [vp, i64, ci, vp, pvp, pvp, dbl, vp, C.c_uint]
     for name in EXPORTS:

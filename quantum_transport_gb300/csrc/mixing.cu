@@ -82,8 +82,8 @@ __global__ void mix_features_kernel(int nE, long long norb, int nhist, const dou
   }
 }
 
-__global__ void mix_apply_kernel(int nE, int nx, int nm, const float* ab, float amax, float bmin,
-                                 float bmax, const double2* S, const double2* R,
+__global__ void mix_apply_kernel(int nE, int nx, int nm, const float* ab, int ncols, float amax,
+                                 float bmin, float bmax, const double2* S, const double2* R,
                                  const double2* Sp, double2* out) {
   const long long nm2 = (long long)nm * nm, total = (long long)nE * nx * nm2;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
@@ -91,9 +91,10 @@ __global__ void mix_apply_kernel(int nE, int nx, int nm, const float* ab, float 
     const long long blk = t / nm2, w = t % nm2;
     const int l = (int)(blk % nx), i = (int)(w % nm), j = (int)(w / nm);
     const long long oi = (long long)l * nm + i, oj = (long long)l * nm + j;
-    const float ai = fminf(fmaxf(ab[2 * oi], 0.0f), amax), aj = fminf(fmaxf(ab[2 * oj], 0.0f), amax);
-    const float bi = fminf(fmaxf(ab[2 * oi + 1], bmin), bmax);
-    const float bj = fminf(fmaxf(ab[2 * oj + 1], bmin), bmax);
+    const float ai = fminf(fmaxf(ab[ncols * oi], 0.0f), amax);
+    const float aj = fminf(fmaxf(ab[ncols * oj], 0.0f), amax);
+    const float bi = ncols > 1 ? fminf(fmaxf(ab[ncols * oi + 1], bmin), bmax) : 0.0f;
+    const float bj = ncols > 1 ? fminf(fmaxf(ab[ncols * oj + 1], bmin), bmax) : 0.0f;
     const double a = 0.5 * ((double)ai + aj), b = 0.5 * ((double)bi + bj);
     const double2 s = S[t], r = R[t], p = Sp ? Sp[t] : s;
     out[t] = make_double2(s.x + a * r.x + b * (s.x - p.x), s.y + a * r.y + b * (s.y - p.y));
@@ -201,16 +202,17 @@ extern "C" qt_status qt_mix_features(qt_ctx* ctx, int nE, int64_t norb, int nhis
 }
 
 extern "C" qt_status qt_mix_apply(qt_ctx* ctx, int nE, int nx, int nm, const float* ab,
-                                  double alpha_max, double beta_min, double beta_max,
+                                  int ncols, double alpha_max, double beta_min, double beta_max,
                                   const double* S, const double* R, const double* S_prev,
                                   double* out, unsigned flags) {
-  if (!ctx || !ab || !S || !R || !out || nE <= 0 || nx <= 0 || nm <= 0)
+  if (!ctx || !ab || !S || !R || !out || nE <= 0 || nx <= 0 || nm <= 0 || ncols < 1 ||
+      ncols > 2)
     QT_FAIL(QT_ERR_ARG, "bad mix_apply arguments");
   cudaSetDevice(qt::ctx_device(ctx));
   cudaStream_t s = qt::ctx_stream(ctx);
   const long long total = (long long)nE * nx * nm * nm;
   qt::mix_apply_kernel<<<qt::grid_of(total), 256, 0, s>>>(
-      nE, nx, nm, ab, (float)alpha_max, (float)beta_min, (float)beta_max,
+      nE, nx, nm, ab, ncols, (float)alpha_max, (float)beta_min, (float)beta_max,
       reinterpret_cast<const double2*>(S), reinterpret_cast<const double2*>(R),
       reinterpret_cast<const double2*>(S_prev), reinterpret_cast<double2*>(out));
   return qt::launched(s, flags);

@@ -2,27 +2,31 @@
 
 The reference iterates Sigma <- Sigma + alpha (F(Sigma) - Sigma) with a fixed
 alpha (src/gw_mod.f90:747-749), F being one GW evaluation (G by RGF, P, W,
-Sigma; ``GwSystem.step``).  Here, once three residuals R = F(Sigma) - Sigma
-are known, a multilayer perceptron reads, for every orbital o (row i of slab
-l), the Chebyshev coefficients of the diagonal residual series Im R^<_ii(E),
-Im R^>_ii(E) of the last three iterates plus the residual norms.  For each
-orbital it returns a step a_o and a momentum b_o.  The proposal is
+Sigma; ``GwSystem.step``).  Here every accepted iterate enters a short history
+of (Sigma_j, R_j = F(Sigma_j) - Sigma_j).  Pulay's DIIS combination
+(coefficients c, sum c = 1, minimising ||sum c_j R_j||) gives
 
-    Sigma_new = Sigma + a_ij R + b_ij (Sigma - Sigma_prev),   a_ij = (a_i + a_j)/2,
+    Sigma_bar = sum c_j Sigma_j,      R_bar = sum c_j R_j,
 
-applied to Sigma^R, Sigma^< and Sigma^> (b_ij likewise).  At a fixed point
-R = 0 and Sigma = Sigma_prev, so no proposal can move the fixed point.  A
-proposal is kept only if the residual F evaluates for it falls below
-ACCEPT_RATIO times the last accepted one; otherwise it is discarded, a Pulay
-(DIIS) step over the accepted history is taken instead, and the next COOLDOWN
-steps are Pulay steps too.
+and a Pulay step moves to Sigma_bar + alpha R_bar.  The network instead chooses
+the step length per orbital o (row i of slab l):
 
-Training data come from the method itself: plain-mixing runs on seeded
-disorder realisations give iterate histories and their converged fixed point
-Sigma*.  For each iterate and orbital the target (a*, b*) minimises
-|| diag(Sigma + a R + b D - Sigma*) || over both series, D = Sigma - Sigma_prev.
-Further rounds add the learned loop's own iterates with the same targets.
-The network is trained on the GPU by the library's own kernels (``mlp.Mlp``).
+    Sigma_new = Sigma_bar + a_ij R_bar,      a_ij = (a_i + a_j)/2,
+
+applied to Sigma^R, Sigma^< and Sigma^>.  It reads, per orbital, the Chebyshev
+coefficients of the diagonal series Im R^<_ii(E), Im R^>_ii(E) of R_bar and of
+the last two residuals, plus the global residual and the orbital's DIIS
+reduction |R_bar| / |R_k|.  At a fixed point every R_j = 0, so no proposal can
+move the fixed point.  A proposal is kept only if the residual F evaluates for
+it falls below ACCEPT_RATIO times the last accepted one; otherwise it is
+discarded, the Pulay step is taken instead, and so are the next COOLDOWN steps.
+
+Training data come from the method itself: Pulay runs (the loop without the
+network) on seeded disorder realisations give iterate histories and their
+converged fixed point Sigma*.  For each iterate and orbital the target a* is
+the least-squares step along R_bar towards Sigma* over both diagonal series.
+Further rounds add the learned loop's own iterates with the same targets.  The
+network is trained on the GPU by the library's own kernels (``mlp.Mlp``).
 """
 from __future__ import annotations
 
@@ -36,10 +40,10 @@ from ._lib import check
 from .mlp import Mlp
 
 NCOEF = 64
-NHIST = 3
+NHIST = 3            # series per feature row: R_bar, R_k, R_{k-1}
 N_IN = 2 * NHIST * NCOEF + 2
-N_OUT = 2
-ALPHA_MAX, BETA_MIN, BETA_MAX = 4.0, -0.5, 0.95
+N_OUT = 1
+ALPHA_MAX = 4.0      # largest step along R_bar
 ACCEPT_RATIO = 0.8   # a learned proposal is kept only if it cuts the residual by >= 20 %
 COOLDOWN = 2         # Pulay steps after a rejected proposal before the network is asked again
 
@@ -130,35 +134,28 @@ class ScbaResult:
 
 
 class Recorder:
-    """Collects network inputs and diagonal series of the iterates of one run,
+    """Collects network inputs and the diagonal series of (Sigma_bar, R_bar) of one run,
     from which training targets follow once the fixed point is known."""
 
     def __init__(self):
-        self.feats, self.s, self.r, self.d = [], [], [], []
+        self.feats, self.s, self.r = [], [], []
 
-    def add(self, feats, s_diag, r_diag, d_diag):
+    def add(self, feats, s_diag, r_diag):
         self.feats.append(feats)
         self.s.append(s_diag)
         self.r.append(r_diag)
-        self.d.append(d_diag)
 
-    def targets(self, s_star, lam=1e-9):
-        """(X, T): network inputs and the (a*, b*) that bring each orbital's diagonal
-        closest to the fixed point's (least squares over both series)."""
+    def targets(self, s_star):
+        """(X, T): network inputs and the step a* along R_bar that brings each orbital's
+        diagonal closest to the fixed point's (least squares over both series)."""
         if not self.feats:
             return np.zeros((0, N_IN), np.float32), np.zeros((0, N_OUT), np.float32)
         X, T = [], []
-        for f, s, r, d in zip(self.feats, self.s, self.r, self.d):
+        for f, s, r in zip(self.feats, self.s, self.r):
             u = (s_star - s).reshape(-1, s.shape[-1])  # [2 nE][norb]
             r = r.reshape(u.shape)
-            d = d.reshape(u.shape)
-            a11, a12, a22 = (r * r).sum(0), (r * d).sum(0), (d * d).sum(0)
-            b1, b2 = (r * u).sum(0), (d * u).sum(0)
-            reg = lam * (a11 + a22) + 1e-300
-            det = (a11 + reg) * (a22 + reg) - a12 * a12
-            a = ((a22 + reg) * b1 - a12 * b2) / det
-            b = ((a11 + reg) * b2 - a12 * b1) / det
-            T.append(np.stack([np.clip(a, 0.0, ALPHA_MAX), np.clip(b, BETA_MIN, BETA_MAX)], 1))
+            a = (r * u).sum(0) / ((r * r).sum(0) + 1e-300)
+            T.append(np.clip(a, 0.0, ALPHA_MAX)[:, None])
             X.append(f)
         return np.concatenate(X).astype(np.float32), np.concatenate(T).astype(np.float32)
 
@@ -180,12 +177,34 @@ class LearnedMixer:
         return out
 
 
-def _pulay_step(ops, hist, alpha):
+def _diis(ops, hist):
+    """Sigma_bar, R_bar (three tensors each) of the DIIS combination of ``hist``."""
     import torch
     G = ops.gram([h[1][1] for h in hist], [h[1][2] for h in hist])
     c = pulay_coefficients(G)
-    return tuple(ops.combine(c, [h[0][q] for h in hist], [h[1][q] for h in hist], alpha,
-                             torch.empty_like(hist[-1][0][q])) for q in range(3))
+    zero = [h[1][0] for h in hist]  # any tensors: alpha = 0 ignores them
+    Sb = tuple(ops.combine(c, [h[0][q] for h in hist], zero, 0.0, torch.empty_like(hist[-1][0][q]))
+               for q in range(3))
+    Rb = tuple(ops.combine(c, [h[1][q] for h in hist], zero, 0.0, torch.empty_like(hist[-1][1][q]))
+               for q in range(3))
+    return Sb, Rb
+
+
+def _step(system, Sb, Rb, a=None, alpha=0.3):
+    """Sigma_bar + alpha R_bar, or Sigma_bar + a_ij R_bar with per-orbital a (device [norb][1])."""
+    import torch
+    ops = MixOps(system)
+    if a is None:
+        return tuple(ops.combine([1.0], [Sb[q]], [Rb[q]], alpha, torch.empty_like(Sb[q]))
+                     for q in range(3))
+    out = []
+    for q in range(3):
+        o = torch.empty_like(Sb[q])
+        check(system.ctx._lib.qt_mix_apply(
+            system.ctx.handle, system.nE, system.nx, system.nm, _vp(a), 1, ALPHA_MAX, 0.0, 0.0,
+            _vp(Sb[q]), _vp(Rb[q]), None, _vp(o), 0))
+        out.append(o)
+    return tuple(out)
 
 
 def run_scba(system, *, method="learned", mixer=None, alpha=0.3, tol=1e-8, max_iter=60,
@@ -193,21 +212,23 @@ def run_scba(system, *, method="learned", mixer=None, alpha=0.3, tol=1e-8, max_i
     """SCBA to ||R|| / ||F(Sigma)|| <= tol with plain, Pulay or learned mixing.
 
     ``method``: "plain" (the reference's linear mixing), "pulay" (DIIS over the
-    last ``pulay_depth`` iterates) or "learned" (network proposals, Pulay
-    fallback).  Returns a ``ScbaResult``; the converged self-energy is
-    Sigma + alpha R of the last evaluation, as in the plain loop.
+    last ``pulay_depth`` accepted iterates, step alpha along R_bar) or "learned"
+    (network step lengths along R_bar, Pulay fallback).  Returns a ``ScbaResult``;
+    the converged self-energy is Sigma + alpha R of the last evaluation, as in the
+    plain loop.
     """
     import torch
+    if method not in ("plain", "pulay", "learned"):
+        raise ValueError("method is plain, pulay or learned")
     if method == "learned" and mixer is None:
         raise ValueError("learned mixing needs a LearnedMixer")
     ops = MixOps(system)
     norb = system.nx * system.nm
     S = (system.zeros(), system.zeros(), system.zeros())
-    hist = []
+    hist, rdiag = [], []  # accepted (Sigma, R) and their residual diagonal series
     ring = torch.zeros((NHIST, 2, system.nE, norb), dtype=torch.float64, device="cuda")
-    nring = 0
     feats = torch.empty((norb, N_IN), dtype=torch.float32, device="cuda")
-    ab = torch.empty((norb, N_OUT), dtype=torch.float32, device="cuda")
+    a = torch.empty((norb, N_OUT), dtype=torch.float32, device="cuda")
     res = ScbaResult(sigma=None, residuals=[], evaluations=0, seconds=0.0)
     r_acc, last, final = np.inf, None, None
     cool = 0  # Pulay steps left before the network is asked again
@@ -227,51 +248,43 @@ def run_scba(system, *, method="learned", mixer=None, alpha=0.3, tol=1e-8, max_i
             break
         if last == "learned" and r >= ACCEPT_RATIO * r_acc:
             res.rejected += 1
-            S = _pulay_step(ops, hist[-pulay_depth:], alpha)
+            S = _step(system, *_diis(ops, hist[-pulay_depth:]), alpha=alpha)
             res.pulay += 1
             last = "pulay"
             cool = COOLDOWN
             continue
         if last == "learned":
             res.accepted += 1
-        hist = (hist + [(S, R)])[-max(pulay_depth, 2):]
+        hist = (hist + [(S, R)])[-pulay_depth:]
+        rd = torch.empty((2, system.nE, norb), dtype=torch.float64, device="cuda")
+        rdiag = (rdiag + [ops.diag(R[1], R[2], rd)])[-2:]
         r_acc = r
-        ring[1:] = ring[:-1].clone()
-        ops.diag(R[1], R[2], ring[0])
-        nring = min(nring + 1, NHIST)
-        ready = nring == NHIST and len(hist) >= 2
-        if ready and (mixer is not None or recorder is not None):
-            (mixer.features if mixer is not None else _features_only(system))(
-                ring, np.log10(max(r, 1e-300)), feats)
-        if ready and recorder is not None:
-            Sp = hist[-2][0]
-            D = tuple(ops.diff(S[q], Sp[q], torch.empty_like(S[q])) for q in (1, 2))
-            sd = ops.diag(S[1], S[2], torch.empty_like(ring[0]))
-            dd = ops.diag(D[0], D[1], torch.empty_like(ring[0]))
-            recorder.add(feats.cpu().numpy(), sd.cpu().numpy(), ring[0].cpu().numpy(),
-                         dd.cpu().numpy())
-        if method == "learned" and ready and cool == 0:
-            mixer.net.infer(feats, out=ab)
-            Sp = hist[-2][0]
-            newS = []
-            for q in range(3):
-                o = torch.empty_like(S[q])
-                check(system.ctx._lib.qt_mix_apply(
-                    system.ctx.handle, system.nE, system.nx, system.nm, _vp(ab), ALPHA_MAX,
-                    BETA_MIN, BETA_MAX, _vp(S[q]), _vp(R[q]), _vp(Sp[q]), _vp(o), 0))
-                newS.append(o)
-            S = tuple(newS)
-            last = "learned"
-        elif (method == "pulay" or (method == "learned" and cool > 0)) and len(hist) >= 2:
-            cool = max(cool - 1, 0)
-            S = _pulay_step(ops, hist[-pulay_depth:], alpha)
-            res.pulay += 1
-            last = "pulay"
-        else:
+        if method == "plain" or len(hist) < 2:
             S = tuple(ops.combine([1.0], [S[q]], [R[q]], alpha, torch.empty_like(S[q]))
                       for q in range(3))
             res.plain += 1
             last = "plain"
+            continue
+        Sb, Rb = _diis(ops, hist)
+        use_net = method == "learned" and cool == 0
+        if use_net or recorder is not None:
+            ops.diag(Rb[1], Rb[2], ring[0])
+            ring[1].copy_(rdiag[-1])
+            ring[2].copy_(rdiag[-2])
+            (mixer.features if mixer is not None else _features_only(system))(
+                ring, np.log10(max(r, 1e-300)), feats)
+        if recorder is not None:
+            sd = ops.diag(Sb[1], Sb[2], torch.empty_like(ring[0]))
+            recorder.add(feats.cpu().numpy(), sd.cpu().numpy(), ring[0].cpu().numpy())
+        if use_net:
+            mixer.net.infer(feats, out=a)
+            S = _step(system, Sb, Rb, a=a)
+            last = "learned"
+        else:
+            cool = max(cool - 1, 0)
+            S = _step(system, Sb, Rb, alpha=alpha)
+            res.pulay += 1
+            last = "pulay"
     torch.cuda.synchronize()
     res.seconds = time.perf_counter() - t0
     res.sigma = final if final is not None else S
@@ -308,14 +321,15 @@ def fixed_point_diag(system, result):
 def collect(systems, *, mixer=None, alpha=0.3, tol=1e-8, max_iter=200, fixed_points=None):
     """Training pairs from SCBA runs on ``systems`` (a list of GwSystem).
 
-    Without ``mixer``: plain-mixing runs, whose converged result is the fixed point.
-    With ``mixer``: learned runs, targets taken against ``fixed_points`` (one diagonal
-    series per system, from the plain runs).  Returns (X, T, fixed_points, results).
+    Without ``mixer``: Pulay runs (the loop without the network), whose converged
+    result is the fixed point.  With ``mixer``: learned runs, targets taken against
+    ``fixed_points`` (one diagonal series per system, from the Pulay runs).
+    Returns (X, T, fixed_points, results).
     """
     Xs, Ts, fps, results = [], [], [], []
     for i, s in enumerate(systems):
         rec = Recorder()
-        r = run_scba(s, method="plain" if mixer is None else "learned", mixer=mixer,
+        r = run_scba(s, method="pulay" if mixer is None else "learned", mixer=mixer,
                      alpha=alpha, tol=tol, max_iter=max_iter, recorder=rec)
         fp = fixed_point_diag(s, r) if mixer is None else fixed_points[i]
         X, T = rec.targets(fp)

@@ -46,20 +46,22 @@ def test_mix_kernels_match_numpy(ctx):
     o = ops.combine(c, dA[0:3], dA[3:6], 0.3, torch.empty_like(dA[0]))
     np.testing.assert_allclose(gw.from_dev(o), sum(c[i] * (A[i] + 0.3 * A[3 + i]) for i in range(3)),
                                rtol=1e-13, atol=1e-13)
-    # learned update with per-orbital (a, b), clamped
-    ab = rng.uniform(-1.0, 5.0, size=(s.nx * s.nm, 2)).astype(np.float32)
-    abd = torch.from_numpy(ab).cuda()
-    o = torch.empty_like(dA[0])
-    mixing.check(ctx._lib.qt_mix_apply(ctx.handle, s.nE, s.nx, s.nm, mixing._vp(abd),
-                                       mixing.ALPHA_MAX, mixing.BETA_MIN, mixing.BETA_MAX,
-                                       mixing._vp(dA[0]), mixing._vp(dA[1]), mixing._vp(dA[2]),
-                                       mixing._vp(o), 4))
-    a = np.clip(ab[:, 0].astype(np.float64), 0, mixing.ALPHA_MAX).reshape(s.nx, s.nm)
-    b = np.clip(ab[:, 1].astype(np.float64), mixing.BETA_MIN, mixing.BETA_MAX).reshape(s.nx, s.nm)
-    aij = 0.5 * (a[:, :, None] + a[:, None, :])
-    bij = 0.5 * (b[:, :, None] + b[:, None, :])
-    ref = A[0] + aij[None] * A[1] + bij[None] * (A[0] - A[2])
-    np.testing.assert_allclose(gw.from_dev(o), ref, rtol=1e-6, atol=1e-6 * np.abs(ref).max())
+    # learned update with per-orbital (a, b) or a alone, clamped
+    amax, bmin, bmax = 4.0, -0.5, 0.95
+    for ncols in (2, 1):
+        ab = rng.uniform(-1.0, 5.0, size=(s.nx * s.nm, ncols)).astype(np.float32)
+        abd = torch.from_numpy(ab).cuda()
+        o = torch.empty_like(dA[0])
+        mixing.check(ctx._lib.qt_mix_apply(ctx.handle, s.nE, s.nx, s.nm, mixing._vp(abd), ncols,
+                                           amax, bmin, bmax, mixing._vp(dA[0]), mixing._vp(dA[1]),
+                                           mixing._vp(dA[2]), mixing._vp(o), 4))
+        a = np.clip(ab[:, 0].astype(np.float64), 0, amax).reshape(s.nx, s.nm)
+        b = (np.clip(ab[:, 1].astype(np.float64), bmin, bmax) if ncols == 2
+             else np.zeros(s.nx * s.nm)).reshape(s.nx, s.nm)
+        aij = 0.5 * (a[:, :, None] + a[:, None, :])
+        bij = 0.5 * (b[:, :, None] + b[:, None, :])
+        ref = A[0] + aij[None] * A[1] + bij[None] * (A[0] - A[2])
+        np.testing.assert_allclose(gw.from_dev(o), ref, rtol=1e-6, atol=1e-6 * np.abs(ref).max())
 
 
 def test_mix_features_match_numpy(ctx):
@@ -100,27 +102,30 @@ def test_pulay_matches_plain_fixed_point(ctx):
 
 
 def test_learned_mixing_gain(ctx):
-    """Trained on 12 seeded disorder realisations (plain-loop histories, then one round
-    of the learned loop's own iterates), evaluated on 4 held-out seeds: the learned loop
-    needs at most half the GW evaluations of plain mixing and reaches the same fixed
-    point (max |diff| <= 1e-6 of max |Sigma|)."""
+    """Trained on 12 seeded disorder realisations (Pulay-loop histories, then one round of
+    the learned loop's own iterates), evaluated on 4 held-out seeds.  The learned loop
+    needs at most half the GW evaluations of plain mixing, no more than the Pulay loop it
+    falls back to, and reaches the same fixed point (max |diff| <= 1e-6 of max |Sigma|)."""
     train_sys = [_system(ctx, 100 + i) for i in range(12)]
     test_sys = [_system(ctx, 200 + i) for i in range(4)]
     mixer = mixing.LearnedMixer(ctx, train_sys[0].nE, seed=5)
-    X, T, fps, plain_train = mixing.collect(train_sys)
+    X, T, fps, _ = mixing.collect(train_sys)
     mixing.train(mixer, X, T, steps=800, batch=2048, lr=1e-3)
     X2, T2, _, _ = mixing.collect(train_sys, mixer=mixer, fixed_points=fps)
     mixing.train(mixer, np.concatenate([X, X2]), np.concatenate([T, T2]), steps=800,
                  batch=2048, lr=5e-4, seed=1)
-    plain_n, learned_n = [], []
+    plain_n, pulay_n, learned_n = [], [], []
     for s in test_sys:
         p = mixing.run_scba(s, method="plain", tol=1e-8, max_iter=200)
+        u = mixing.run_scba(s, method="pulay", tol=1e-8, max_iter=200)
         q = mixing.run_scba(s, method="learned", mixer=mixer, tol=1e-8, max_iter=200)
-        assert p.residuals[-1] <= 1e-8 and q.residuals[-1] <= 1e-8
+        assert p.residuals[-1] <= 1e-8 and u.residuals[-1] <= 1e-8 and q.residuals[-1] <= 1e-8
         for a, b in zip(q.sigma, p.sigma):
             a, b = gw.from_dev(a), gw.from_dev(b)
             assert np.abs(a - b).max() <= 1e-6 * np.abs(b).max()
         plain_n.append(p.evaluations)
+        pulay_n.append(u.evaluations)
         learned_n.append(q.evaluations)
-    print("plain", plain_n, "learned", learned_n)
+    print("plain", plain_n, "pulay", pulay_n, "learned", learned_n)
     assert np.mean(learned_n) <= 0.5 * np.mean(plain_n), (plain_n, learned_n)
+    assert np.mean(learned_n) <= np.mean(pulay_n), (pulay_n, learned_n)
