@@ -55,6 +55,9 @@ def parse():
                     help="energies (x 16 k) of the complex128 split-path sample")
     ap.add_argument("--cpu-points", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-scba", action="store_true", help="skip the GW-SCBA mixing comparison")
+    ap.add_argument("--scba-size", default="10,16,256",
+                    help="slabs,orbitals,energies of the GW-SCBA device family")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
 
@@ -167,6 +170,50 @@ def run_reference(a):
             "e2e": {"value": v, "unit": "E-points/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def scba_comparison(ctx, a):
+    """GW-SCBA to residual 1e-8 with plain (the reference's linear mixing), Pulay and learned
+    mixing on held-out seeds of the disorder family; the learned mixer is trained here first,
+    on the GPU with the library's kernels, from the method's own iterates."""
+    from quantum_transport_gb300 import gw, mixing
+    from quantum_transport_gb300.devices import disordered_gw_device
+    nx, nm, nE = (int(x) for x in a.scba_size.split(","))
+
+    def system(seed):
+        d = disordered_gw_device(seed, nx=nx, nm=nm, nE=nE)
+        return gw.GwSystem(ctx, d.H00, d.H10, d.E, d.nx, d.V, mu=(0.1, -0.1))
+
+    train_sys = [system(100 + i) for i in range(8)]
+    test_sys = [system(900 + i) for i in range(2)]
+    t0 = time.perf_counter()
+    mixer = mixing.LearnedMixer(ctx, nE, seed=5, max_batch=max(2048, nx * nm))
+    X, T, fps, _ = mixing.collect(train_sys)
+    mixing.train(mixer, X, T, steps=800, batch=2048, lr=1e-3)
+    X2, T2, _, _ = mixing.collect(train_sys, mixer=mixer, fixed_points=fps)
+    mixing.train(mixer, np.concatenate([X, X2]), np.concatenate([T, T2]), steps=800,
+                 batch=2048, lr=5e-4, seed=1)
+    t_train = time.perf_counter() - t0
+    out = {m: {"evaluations": [], "seconds": []} for m in ("plain", "pulay", "learned")}
+    diff = 0.0
+    for s in test_sys:
+        runs = {m: mixing.run_scba(s, method=m, mixer=mixer if m == "learned" else None,
+                                   tol=1e-8, max_iter=200) for m in out}
+        for m, r in runs.items():
+            out[m]["evaluations"].append(r.evaluations)
+            out[m]["seconds"].append(r.seconds)
+        for x, y in zip(runs["learned"].sigma, runs["plain"].sigma):
+            diff = max(diff, float((x - y).abs().max() / y.abs().max()))
+    mean = lambda v: float(np.mean(v))
+    return {"workload": f"GW-SCBA, {nx} slabs x {nm} orbitals x {nE} energies, on-site disorder "
+                        "sigma ~ U[0.05, 0.3] eV, V_ij = 14.4/(|r_i - r_j| + 1) eV, residual <= 1e-8",
+            "train_seeds": len(train_sys), "test_seeds": len(test_sys),
+            "training_seconds": t_train,
+            **{m: {"evaluations": mean(v["evaluations"]), "seconds": mean(v["seconds"])}
+               for m, v in out.items()},
+            "learned_vs_plain_time": mean(out["learned"]["seconds"]) / mean(out["plain"]["seconds"]),
+            "learned_vs_pulay_time": mean(out["learned"]["seconds"]) / mean(out["pulay"]["seconds"]),
+            "fixed_point_max_rel_diff": diff}
 
 
 def run_ours(a):
@@ -323,6 +370,8 @@ def run_ours(a):
                 "ldos_rel_err_max": float(np.max(np.abs(dh.imag - d64[:m * NX * NM].imag)) /
                                           np.max(np.abs(d64[:m * NX * NM].imag)))}
         line["fp64_gpu"] = fp64
+    if rank == 0 and not a.no_scba:
+        line["scba"] = scba_comparison(ctx, a)
     if rank == 0:
         if world == 1 and not a.no_cpu:
             threads = os.cpu_count() or 1

@@ -163,6 +163,13 @@ __global__ void sancho_update_kernel(long long P, const double* err, double tol,
   }
 }
 
+// status[b] |= st2[b] | st2[P + b]: both leads' decimation flags of point b
+__global__ void or_halves_kernel(long long P, const int* st2, int* status) {
+  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < P;
+       b += (long long)gridDim.x * blockDim.x)
+    status[b] |= st2[b] | st2[P + b];
+}
+
 __global__ void flag_unconverged_kernel(long long P, const unsigned char* active, int* status) {
   for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < P;
        b += (long long)gridDim.x * blockDim.x)
@@ -222,7 +229,9 @@ struct Ops {
   // C (m x nn) = alpha op(A) op(B) + beta D + z I, op(A) m x k, op(B) k x nn
   qt_status gemm3(int m, int nn, int k, BatchRef A, int opA, BatchRef B, int opB, BatchRef C,
                   long long batch, cd alpha = {1, 0}, BatchRef D = nullref(), cd beta = {0, 0},
-                  BatchRef Z = nullref(), const unsigned char* active = nullptr) {
+                  BatchRef Z = nullref(), const unsigned char* active = nullptr,
+                  int digits = 0) {
+    const int sl = digits ? digits : slices;
     qt::GemmArgs g;
     g.m = m;
     g.n = nn;
@@ -241,10 +250,10 @@ struct Ops {
     int kind;
     if constexpr (sizeof(TC) == 16) {
       kind = prec == QT_PREC_FP64 ? 2 : 1;
-      e = prec == QT_PREC_FP64 ? qt::zgemm_f64(g, s) : qt::zgemm_oz(g, slices, slices - 1, s);
+      e = prec == QT_PREC_FP64 ? qt::zgemm_f64(g, s) : qt::zgemm_oz(g, sl, sl - 1, s);
     } else {
       kind = 0;
-      e = qt::zgemm_oz_c64(g, slices, s);
+      e = qt::zgemm_oz_c64(g, sl, s);
     }
     if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
     if (timed) {
@@ -254,10 +263,10 @@ struct Ops {
       const double alg = 8.0 * m * (double)nn * k * batch;
       double tens = 0.0;
       if (kind != 2) {
-        const int L = slices - 1, npad = (nn + 15) / 16 * 16, kp = (k + 15) / 16 * 16;
+        const int L = sl - 1, npad = (nn + 15) / 16 * 16, kp = (k + 15) / 16 * 16;
         int pairs = 0;
-        for (int a = 0; a < slices; ++a)
-          for (int b = 0; b < slices; ++b) pairs += (a + b <= L);
+        for (int a = 0; a < sl; ++a)
+          for (int b = 0; b < sl; ++b) pairs += (a + b <= L);
         tens = 2.0 * pairs * 2.0 * 128.0 * npad * (2.0 * kp) * batch;
       }
       prof->v.push_back({kind, ea, eb, alg, tens});
@@ -287,13 +296,15 @@ struct Ops {
     if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
     if (timed) { cudaEventRecord(eb, s); prof->v.push_back({3, ea, eb, alg, 0.0}); }
     if (refine > 0 && (batch > P || !rt1 || !rt2)) QT_FAIL(QT_ERR_ARG, "refinement scratch too small");
-    // refinement scratch holds batch blocks of the widest size (stride n*n)
+    // refinement scratch holds batch blocks of the widest size (stride n*n).  Only the
+    // residual R = I - A X needs the full digits; the update X R is |R| times smaller than X,
+    // so 4 digits (2^-28 of |X||R|) leave X's accuracy to R's.
     const BatchRef R = ref(rt1, (long long)n * n, nn), T = ref(rt2, (long long)n * n, nn);
     for (int it = 0; it < refine; ++it) {
       QT_TRY(gemm3(nn, nn, nn, A, qt::OP_N, X, qt::OP_N, R, batch, cd{-1, 0}, nullref(),
                    cd{0, 0}, ref(one, 0, 1), active));  // R = I - A X
       QT_TRY(gemm3(nn, nn, nn, X, qt::OP_N, R, qt::OP_N, T, batch, cd{1, 0}, X, cd{1, 0},
-                   nullref(), active));
+                   nullref(), active, 4));
       qt::zcopy<TC>(nn, batch, T, X, s);
     }
     return QT_OK;
@@ -328,8 +339,8 @@ size_t wave_bytes(const Problem& pb, long long P) {
   const size_t nm2 = (size_t)pb.nm * pb.nm;
   const size_t tc = pb.prec == QT_PREC_MIXED ? 8 : 16;  // complex64 sweep only in MIXED
   const size_t sweep = (2 * (size_t)pb.nx + 14 + 2) * tc;  // g_l, g^<_l, temporaries, refinement
-  const size_t lead = (7 + 2 + 6) * 16;                     // Sancho state + refinement + contact
-  return (sweep + lead) * nm2 * P + (size_t)P * (512 + 2048) + (512 << 10);
+  const size_t lead = (2 * (7 + 2) + 6) * 16;  // Sancho state + refinement of both leads + contact
+  return (sweep + lead) * nm2 * P + (size_t)P * 4096 + (512 << 10);
 }
 
 // Batched Sancho-Rubio on the wave (complex128 state).  H00 per point, H_10 the
@@ -541,13 +552,39 @@ qt_status solve_wave(qt_ctx* ctx, const Problem& pb, long long p0, long long P, 
   const BatchRef SigL = T(13), Pch = T(12);
   const bool caroli = (pb.flags & QT_FLAG_CAROLI) && pb.T;
 
+  // ---------------- both leads' decimations as one batched wave of 2P entries:
+  // [0, P) the left lead, called with H10^+ (src/cuda_rgf_mod.f90:90-134), and
+  // [P, 2P) the right lead (:192-277); surface Green's functions into C8(4), C8(5)
+  const int N = nx - 1;
+  {
+    const size_t mark = ar.off;
+    cd* z2 = ar.take<cd>(2 * P);
+    int* st2 = ar.take<int>(2 * P);
+    int* it2 = ar.take<int>(2 * P);
+    if (!z2 || !st2 || !it2) QT_FAIL(QT_ERR_NOMEM, "wave arena exhausted (leads)");
+    cudaMemcpyAsync(z2, zlead, P * sizeof(cd), cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(z2 + P, zlead, P * sizeof(cd), cudaMemcpyDeviceToDevice, s);
+    cudaMemsetAsync(st2, 0, 2 * P * sizeof(int), s);
+    qt::zaxpby<double2>(n, P, HII8(0), 1, 0, SIGR8(0), 1, 0, nullref(), C8(0), nullptr, s);
+    qt::zaxpby<double2>(n, P, HII8(N), 1, 0, SIGR8(N), 1, 0, nullref(), C8(1), nullptr, s);
+    qt::zdagger<double2>(n, P, H1I8(0), C8(2), s);
+    qt::zcopy<double2>(n, P, H1I8(N), C8(3), s);
+    QT_TRY(sancho_wave(cop, ar, 2 * P, C8(0), C8(2), false, z2, pb.c.sancho_tol,
+                       pb.c.sancho_max_iter, C8(4), nullref(), st2, it2, 1));
+    or_halves_kernel<<<g1d(P), 256, 0, s>>>(P, st2, status);
+    qt::count_launch();
+    if (pb.iters) {
+      cudaMemcpy2DAsync(pb.iters + p0 * 2, 2 * sizeof(int), it2, sizeof(int), sizeof(int), P,
+                        cudaMemcpyDeviceToDevice, s);
+      cudaMemcpy2DAsync(pb.iters + p0 * 2 + 1, 2 * sizeof(int), it2 + P, sizeof(int),
+                        sizeof(int), P, cudaMemcpyDeviceToDevice, s);
+    }
+    ar.off = mark;
+  }
+
   // ---------------- left contact (src/cuda_rgf_mod.f90:90-134)
-  // lead decimation and Sigma_L = H10 G00 H10^+ at FP64 grade, then stored as TC
-  qt::zaxpby<double2>(n, P, HII8(0), 1, 0, SIGR8(0), 1, 0, nullref(), C8(0), nullptr, s);
-  QT_TRY(sancho_wave(cop, ar, P, C8(0), H1I8(0), true, zlead, pb.c.sancho_tol,
-                     pb.c.sancho_max_iter, C8(1), nullref(), status,
-                     pb.iters ? pb.iters + p0 * 2 : nullptr, 2));
-  QT_TRY(cop.gemm(H1I8(0), qt::OP_N, C8(1), qt::OP_N, C8(2), P));
+  // Sigma_L = H10 G00 H10^+ at FP64 grade, then stored as TC
+  QT_TRY(cop.gemm(H1I8(0), qt::OP_N, C8(4), qt::OP_N, C8(2), P));
   QT_TRY(cop.gemm(C8(2), qt::OP_N, H1I8(0), qt::OP_C, C8(3), P));
   zconvert_or_copy<TC>(n, P, C8(3), SigL, s);
   // H00 = Hii(1) + sigma_r_ph(1) S ;  g_1 = (z S - H00 - Sigma_L)^-1
@@ -586,14 +623,9 @@ qt_status solve_wave(qt_ctx* ctx, const Problem& pb, long long p0, long long P, 
   }
 
   // ---------------- right contact (src/cuda_rgf_mod.f90:192-277)
-  const int N = nx - 1;
   const BatchRef H10 = H1I(N);  // the reference uses H1i(nx) (1-based) for the right lead
-  qt::zaxpby<double2>(n, P, HII8(N), 1, 0, SIGR8(N), 1, 0, nullref(), C8(0), nullptr, s);
-  QT_TRY(sancho_wave(cop, ar, P, C8(0), H1I8(N), false, zlead, pb.c.sancho_tol,
-                     pb.c.sancho_max_iter, C8(1), nullref(), status,
-                     pb.iters ? pb.iters + p0 * 2 + 1 : nullptr, 2));
-  // Sigma_R = H10^+ G00 H10 at FP64 grade
-  QT_TRY(cop.gemm(H1I8(N), qt::OP_C, C8(1), qt::OP_N, C8(2), P));
+  // Sigma_R = H10^+ G00 H10 at FP64 grade (G00 of the right lead: C8(5))
+  QT_TRY(cop.gemm(H1I8(N), qt::OP_C, C8(5), qt::OP_N, C8(2), P));
   QT_TRY(cop.gemm(C8(2), qt::OP_N, H1I8(N), qt::OP_N, C8(3), P));
   const BatchRef SigR = T(2);
   zconvert_or_copy<TC>(n, P, C8(3), SigR, s);
