@@ -200,6 +200,20 @@ qt_status qt_rgf_solve_vb(qt_ctx* ctx, const qt_device_vb* dev, const double* E,
                           const qt_contacts* contacts, qt_precision prec, unsigned flags,
                           qt_outputs* out);
 
+/* Slab blocks of a Wannier90 tight-binding model: w90_MAT_DEF
+ * (src/wannierHam3d.f90:273-301) at nk transverse k-points in one launch.
+ *   Hr     the model's H(R), Fortran Hr(nb, nb, nxr, nyr, nzr) complex128, with
+ *          R ranges range = {xmin, xmax, ymin, ymax, zmin, zmax}
+ *   cell   the cell vectors alpha, beta, gamm (3 x 3 doubles, Angstrom)
+ *   kvec   [nk][3] Cartesian k vectors kx xhat + ky yhat + kz zhat (1/Angstrom)
+ *   H00    [nk][nm*nm] H_ii of a slab of ns cells (nm = nb*ns), column-major
+ *   H10    [nk][nm*nm] H_{i+1,i}
+ * Host pointers unless QT_FLAG_DEVICE_POINTERS.  The outputs feed qt_rgf_solve
+ * with hii_kstride = nm*nm.                                                */
+qt_status qt_w90_blocks(qt_ctx* ctx, int nb, int ns, const int* range, const double* Hr,
+                        const double* cell, int nk, const double* kvec, double* H00,
+                        double* H10, unsigned flags);
+
 /* Single-point drop-in with the argument list of cuda_rgf_constblocksize
  * (src/cuda_rgf_mod.f90:53-59): contiguous (nm, nm, nx) arrays for Hii, Sii,
  * sigma_lesser_ph, sigma_r_ph, G_r, G_lesser, G_greater, Jdens and

@@ -40,12 +40,28 @@ class W90:
             self.Hr[m, nn, int(np.floor(row[0])) - self.xmin,
                     int(np.floor(row[1])) - self.ymin,
                     int(np.floor(row[2])) - self.zmin] = row[5] + 1j * row[6]
+        self._axes()
+
+    def _axes(self):
+        # transport / transverse unit vectors and the cell length, src/wannierHam3d.f90:130-136
         xhat = self.alpha / np.linalg.norm(self.alpha)
         yhat = -np.cross(xhat, self.gamm)
         yhat = yhat / np.linalg.norm(yhat)
         zhat = self.gamm / np.linalg.norm(self.gamm)
         self.xhat, self.yhat, self.zhat = xhat, yhat, zhat
-        self.Lx = abs(np.dot(self.alpha, xhat))  # src/wannierHam3d.f90:136
+        self.Lx = abs(np.dot(self.alpha, xhat))
+
+    @classmethod
+    def from_arrays(cls, Hr, ranges, alpha, beta, gamm):
+        """A model from Hr (nb, nb, nxr, nyr, nzr) and ranges (xmin, xmax, ymin, ymax, zmin,
+        zmax), as stored in the committed fixture."""
+        w = cls.__new__(cls)
+        w.Hr = np.asarray(Hr, dtype=np.complex128)
+        w.nb = w.Hr.shape[0]
+        w.xmin, w.xmax, w.ymin, w.ymax, w.zmin, w.zmax = (int(x) for x in ranges)
+        w.alpha, w.beta, w.gamm = (np.asarray(v, dtype=np.float64) for v in (alpha, beta, gamm))
+        w._axes()
+        return w
 
     def mat_def(self, ns, kx=0.0, ky=0.0, kz=0.0):
         """(H00, H10) slab blocks of ``ns`` cells, src/wannierHam3d.f90:273-301."""

@@ -7,6 +7,7 @@ Reads (only in the build container, where the reference tree is mounted):
 and writes
   cnt_blocks.npz  H00, H10 slab blocks (ns = 3 cells of nb = 32 orbitals, k = 0),
                   built by oracle.w90 (src/wannierHam3d.f90:273-301), plus Lx, nb, ns
+  cnt_hr.npz      the model itself: Hr(nb, nb, nxr, nyr, nzr), R ranges, cell vectors
   cnt_golden.npz  the reference outputs as arrays on the exact energy grid
                   E = -6 + ie*5/199 (src/negf_mod.f90:100-101)
 
@@ -33,6 +34,9 @@ def main(ref):
     H00, H10 = w.mat_def(ns)
     np.savez_compressed(os.path.join(HERE, "cnt_blocks.npz"), H00=H00, H10=H10, Lx=w.Lx,
                         nb=w.nb, ns=ns)
+    np.savez_compressed(os.path.join(HERE, "cnt_hr.npz"), Hr=w.Hr,
+                        ranges=np.array([w.xmin, w.xmax, w.ymin, w.ymax, w.zmin, w.zmax]),
+                        alpha=w.alpha, beta=w.beta, gamm=w.gamm)
     nen = 200
     E = -6.0 + np.arange(nen) * (5.0 / (nen - 1))
     g00 = np.loadtxt(os.path.join(tc, "sancho_g00.dat"))
