@@ -214,6 +214,23 @@ qt_status qt_w90_blocks(qt_ctx* ctx, int nb, int ns, const int* range, const dou
                         const double* cell, int nk, const double* kvec, double* H00,
                         double* H10, unsigned flags);
 
+/* Device blocks from a COO Hamiltonian: the blocksize branch of
+ * devH_build_fromCOOfile (src/deviceHam_mod.f90:168-224), fed by the entries
+ * load_COOmatrix reads (src/deviceHam_mod.f90:40-91).
+ *   row, col    nnz indices, index_base 0 or 1
+ *   h           nnz complex128 values; s the overlap values on the same
+ *               entries, or NULL (then Sii = I)
+ *   Hii, Sii    [nx][bs*bs] column-major; H1i [nx+1][bs*bs]
+ * An entry of slab ix (row div bs) whose column lies in slab ix writes
+ * Hii[mm,nn] = h and Hii[nn,mm] = conj(h); in slab ix+1 it writes
+ * H1i(ix)[mm, nn-bs]; anything else is dropped.  H1i(nx) repeats H1i(nx-1).
+ * Later entries win, as in the reference's serial loop; the result is
+ * bit-exact and independent of thread order.  Host pointers unless
+ * QT_FLAG_DEVICE_POINTERS.                                                 */
+qt_status qt_coo_blocks(qt_ctx* ctx, int nx, int bs, long long nnz, const int* row,
+                        const int* col, int index_base, const double* h, const double* s,
+                        double* Hii, double* H1i, double* Sii, unsigned flags);
+
 /* Single-point drop-in with the argument list of cuda_rgf_constblocksize
  * (src/cuda_rgf_mod.f90:53-59): contiguous (nm, nm, nx) arrays for Hii, Sii,
  * sigma_lesser_ph, sigma_r_ph, G_r, G_lesser, G_greater, Jdens and
