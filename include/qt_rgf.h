@@ -55,9 +55,10 @@ typedef enum {
 
 /* Reference-quirk switches (default 0 = the behaviour that produced the
  * reference's test_cnt/ outputs).                                            */
-#define QT_QUIRK_CPU_FERMI 1u    /* contact Fermi/temperature pairing and tr
-                                    sign of rgf_variableblock_forward
-                                    (src/rgf_mod.f90:100,182,196-202,258)    */
+#define QT_QUIRK_CPU_FERMI 1u    /* contact Fermi/temperature pairing, tr sign
+                                    and bond-current form of
+                                    rgf_variableblock_forward (src/rgf_mod.f90:
+                                    100,182,196-202,215-221,258)             */
 #define QT_QUIRK_GLP_ZERO 2u     /* G^> recursion seeded with Glp == 0 as in
                                     src/cuda_rgf_mod.f90:78,351-372          */
 #define QT_QUIRK_BACK_H1I_NEXT 4u /* backward step couples l,l+1 through
@@ -144,7 +145,15 @@ typedef struct {
  *   G_r, G_lesser, G_greater [npts][nx][nm*nm] full diagonal blocks
  *                     (cuda_rgf_constblocksize's G_r, G_lesser, G_greater)
  *   status    [npts]  QT_PT_* bits
- *   sancho_iters [npts][2] iterations of the left/right decimation          */
+ *   sancho_iters [npts][2] iterations of the left/right decimation
+ *   bond_cur  [npts][nx-1] bond currents J_l = Re Tr Jdens_l between slabs l
+ *                     and l+1 (0-based), Jdens_l = H^+ G^<_{l+1,l} - H G^<_{l,l+1}
+ *                     with H = H_{l+1,l} (src/cuda_rgf_mod.f90:293-318); with
+ *                     QT_QUIRK_CPU_FERMI the CPU routine's
+ *                     Jdens_l = -2 H^+ G^<_{l+1,l} (src/rgf_mod.f90:215-221)
+ *   Jdens     [npts][nx][nm*nm] the full Jdens_l blocks of
+ *                     cuda_rgf_constblocksize; block nx-1 is zero as there
+ *                     (qt_rgf_solve without QT_QUIRK_CPU_FERMI only)        */
 typedef struct {
   double* tr;
   double* tre;
@@ -157,6 +166,8 @@ typedef struct {
   double* G_greater;
   int* status;
   int* sancho_iters;
+  double* bond_cur;
+  double* Jdens;
 } qt_outputs;
 
 /* Batched ballistic/phonon RGF over nE energies x nk k-points: the whole
@@ -316,12 +327,19 @@ qt_status qt_gw_step(qt_ctx* ctx, const qt_device* dev, const double* E, int nE,
  * residual ||S_new - S||_F / ||S_new||_F over Sigma^< and Sigma^> is <= tol
  * or max_iter maps were evaluated (the reference has no convergence test and
  * runs a fixed niter).  sigma_* are the start values on input and the mixed
- * result on output; residuals [max_iter]; *iters = maps evaluated.          */
+ * result on output; residuals [max_iter]; *iters = maps evaluated.
+ * currents [max_iter][2] (host, may be NULL): the two columns of
+ * Id_iteration.dat (src/gw_mod.f90:413-428), the left- and right-contact
+ * currents (A) of each map's RGF, sum_E I(E) dE e0^2 spindeg / (2 pi hbar)
+ * with the reference's constants e0 = 1.6022e-19 C, hbar = 1.0546e-34 J s.
+ * The per-energy currents at any Sigma come from qt_rgf_solve with the
+ * self-energies as sigma_r_ph / sigma_lesser_ph (tr, tre, bond_cur).      */
 qt_status qt_scba_solve(qt_ctx* ctx, const qt_device* dev, const double* E, int nE,
                         const qt_contacts* contacts, const double* V, double spindeg,
                         double alpha, double tol, int max_iter, qt_precision prec,
                         unsigned flags, double* sigma_r, double* sigma_lesser,
-                        double* sigma_greater, double* residuals, int* iters);
+                        double* sigma_greater, double* residuals, int* iters,
+                        double* currents);
 
 /* Batched energy correlation (mode 0) / convolution (mode 1) of corr1d2 /
  * conv1d2 (src/fft_mod.f90:58-168) on n-point series stored energy-major,

@@ -54,7 +54,7 @@ class QtContacts(C.Structure):
 class QtOutputs(C.Structure):
     _fields_ = [(n, C.c_void_p) for n in ("tr", "tre", "T", "diag_gr", "diag_gl", "diag_gg",
                                           "G_r", "G_lesser", "G_greater", "status",
-                                          "sancho_iters")]
+                                          "sancho_iters", "bond_cur", "Jdens")]
 
 
 class QtError(RuntimeError):
@@ -101,7 +101,7 @@ def load(path=LIB_PATH):
     lib.qt_gw_step.argtypes = [vp, C.POINTER(QtDevice), vp, ci, C.POINTER(QtContacts), vp, dbl,
                                ci, C.c_uint, vp, vp, vp, vp, vp]
     lib.qt_scba_solve.argtypes = [vp, C.POINTER(QtDevice), vp, ci, C.POINTER(QtContacts), vp,
-                                  dbl, dbl, dbl, ci, ci, C.c_uint, vp, vp, vp, vp, vp]
+                                  dbl, dbl, dbl, ci, ci, C.c_uint, vp, vp, vp, vp, vp, vp]
     lib.qt_corr_batch.argtypes = [vp, ci, i64, vp, vp, vp, ci, C.c_uint]
     lib.qt_zgemm_batch_noalloc.argtypes = [ci, ci, C.c_char, vp, i64, C.c_char, vp, i64, vp, vp,
                                            vp, i64, vp, i64, ci, vp]

@@ -176,6 +176,33 @@ __global__ void ztrace_prod_kernel(int n, long long batch, BatchRef X, BatchRef 
   }
 }
 
+// Bond current of one slab pair: T1 (nl x nq), H (nq x nl), A (nq x nl);
+// out = scale * 2 (-Re sum_ij T1(i,j) H(j,i) + Re sum_ab conj(H(a,b)) A(a,b)),
+// the first sum skipped when T1 is null.
+template <typename TC>
+__global__ void zbond_trace_kernel(int nl, int nq, long long batch, BatchRef T1, BatchRef H,
+                                   BatchRef A, double scale, double* out, long long ostride,
+                                   long long ooff) {
+  for (long long b = blockIdx.x; b < batch; b += gridDim.x) {
+    const TC* t1 = T1.p ? batch_ptr<const TC>(T1, b) : nullptr;
+    const TC* h = batch_ptr<const TC>(H, b);
+    const TC* a = batch_ptr<const TC>(A, b);
+    double s = 0.0;
+    for (int e = threadIdx.x; e < nl * nq; e += blockDim.x) {
+      if (t1) {
+        const int i = e % nl, j = e / nl;
+        const TC u = t1[i + (long long)j * T1.ld], v = h[j + (long long)i * H.ld];
+        s -= (double)u.x * v.x - (double)u.y * v.y;
+      }
+      const int r = e % nq, c = e / nq;
+      const TC hv = h[r + (long long)c * H.ld], av = a[r + (long long)c * A.ld];
+      s += (double)hv.x * av.x + (double)hv.y * av.y;
+    }
+    s = block_sum(s);
+    if (threadIdx.x == 0) out[b * ostride + ooff] = 2.0 * scale * s;
+  }
+}
+
 template <typename TC>
 __global__ void zdiag_kernel(int n, long long batch, BatchRef X, double* out, long long ostride,
                              long long ooff) {
@@ -308,6 +335,16 @@ cudaError_t ztrace_prod(int n, long long batch, BatchRef X, BatchRef Y, double s
   return cudaGetLastError();
 }
 template <typename TC>
+cudaError_t zbond_trace(int nl, int nq, long long batch, BatchRef T1, BatchRef H, BatchRef A,
+                        double scale, double* out, long long ostride, long long ooff,
+                        cudaStream_t s) {
+  if (batch <= 0) return cudaSuccess;
+  zbond_trace_kernel<TC><<<grid_for(batch), NT, 0, s>>>(nl, nq, batch, T1, H, A, scale, out,
+                                                        ostride, ooff);
+  count_launch();
+  return cudaGetLastError();
+}
+template <typename TC>
 cudaError_t zscale_add(int n, long long batch, BatchRef X, const double* f, BatchRef W, BatchRef Y,
                        cudaStream_t s) {
   if (batch <= 0) return cudaSuccess;
@@ -365,6 +402,8 @@ cudaError_t zcheck_finite(int n, long long batch, BatchRef X, int* status, cudaS
                                           const double*, double*, cudaStream_t);                  \
   template cudaError_t ztrace_prod<TC>(int, long long, BatchRef, BatchRef, double, double*,       \
                                        cudaStream_t);                                             \
+  template cudaError_t zbond_trace<TC>(int, int, long long, BatchRef, BatchRef, BatchRef, double, \
+                                      double*, long long, long long, cudaStream_t);              \
   template cudaError_t zscale_add<TC>(int, long long, BatchRef, const double*, BatchRef,          \
                                       BatchRef, cudaStream_t);                                    \
   template cudaError_t zdiag<TC>(int, long long, BatchRef, double*, long long, long long,         \

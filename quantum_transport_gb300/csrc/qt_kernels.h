@@ -71,6 +71,13 @@ cudaError_t ztrace_current(int n, long long batch, BatchRef X, BatchRef Y1, Batc
 template <typename TC>
 cudaError_t ztrace_prod(int n, long long batch, BatchRef X, BatchRef Y, double scale, double* out,
                         cudaStream_t s);
+// Bond current between slabs l and l+1 from T1 = g H^+ G^<_{l+1} (nl x nq), the
+// coupling H = H_{l+1,l} (nq x nl) and A = G_{l+1} H g^< (nq x nl):
+// out[b*ostride + ooff] = scale * 2 (-Re Tr[T1 H] + Re Tr[H^+ A]); T1 may be null
+template <typename TC>
+cudaError_t zbond_trace(int nl, int nq, long long batch, BatchRef T1, BatchRef H, BatchRef A,
+                        double scale, double* out, long long ostride, long long ooff,
+                        cudaStream_t s);
 // Y_b = f[b] * X_b + W_b   (W may be null)
 template <typename TC>
 cudaError_t zscale_add(int n, long long batch, BatchRef X, const double* f, BatchRef W, BatchRef Y,

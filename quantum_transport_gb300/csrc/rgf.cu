@@ -14,7 +14,8 @@
 //   3. forward sweep  g_l, g^<_l (src/cuda_rgf_mod.f90:140-188)
 //   4. right contact  G_NN, G^<_NN, tr (src/cuda_rgf_mod.f90:192-277)
 //   5. backward sweep G_l, G^<_l (src/cuda_rgf_mod.f90:283-381), with the
-//      minimal 8-product form (see DESIGN notes in the backward loop)
+//      minimal 8-product form (see the notes at the backward loop), and on
+//      request the bond currents (:293-318)
 //   6. left-contact current tre (src/cuda_rgf_mod.f90:387-407)
 //   7. optional Caroli T(E) from the left-connected chain G_{N1}.
 #include <algorithm>
@@ -332,6 +333,8 @@ struct Problem {
   // device outputs (may be null)
   double *tr, *tre, *T, *dgr, *dgl, *dgg;
   cd *Gr, *Gl, *Gg;
+  double* bond;  // [npts][nx-1] bond currents
+  cd* Jd;        // [npts][nx][nm2] bond-current blocks
   int *status, *iters;
 };
 
@@ -678,6 +681,9 @@ qt_status solve_wave(qt_ctx* ctx, const Problem& pb, long long p0, long long P, 
     }
   };
   emit(N, Gcur, Gncur, Gpcur);
+  if (pb.Jd)  // Jdens(nx) keeps its zero initialisation (src/cuda_rgf_mod.f90:84,283)
+    cudaMemset2DAsync(pb.Jd + (p0 * nx + N) * nm2, (size_t)nx * nm2 * sizeof(cd), 0,
+                      (size_t)nm2 * sizeof(cd), P, s);
 
   // ---------------- backward sweep (src/cuda_rgf_mod.f90:283-381)
   //   X = g H^+ ; GN0 = X G_{l+1} ; G_l = g + GN0 (H g)
@@ -696,6 +702,28 @@ qt_status solve_wave(qt_ctx* ctx, const Problem& pb, long long p0, long long P, 
     QT_TRY(op.gemm(GN0, qt::OP_N, Hc, qt::OP_N, Y, P));
     QT_TRY(op.gemm(Y, qt::OP_N, GLN(l), qt::OP_N, W, P));
     qt::zantiherm<TC>(n, P, W, 1, 0, Gnnew, Gnnew, s);
+    if (pb.bond || pb.Jd) {
+      // Bond current l -> l+1 (src/cuda_rgf_mod.f90:293-318):
+      //   cur = H^+ B - H G^<_{l,l+1} = H^+ B + H B^+,  B = G^<_{l+1,l} = G^<_{l+1} X^+ + G_{l+1} U,
+      //   U = H g^<_l, with G^<_{l,l+1} = -B^+ by anti-Hermiticity of G^<.
+      // The CPU routine's form (src/rgf_mod.f90:215-221) is cur = -2 H^+ B.
+      // Its trace only needs A = G_{l+1} U: Re Tr[H^+ G^<_{l+1} H g^+] = -Re Tr[T1 H]
+      // with T1 = X G^<_{l+1} from the G^< update, so Re Tr cur = 2 (-Re Tr[T1 H] + Re Tr[H^+ A]).
+      const double jsign = (q & QT_QUIRK_CPU_FERMI) ? -1.0 : 1.0;
+      const long long bo = (long long)(nx - 1);
+      QT_TRY(op.gemm(Hc, qt::OP_N, GLN(l), qt::OP_N, T(2), P));  // U
+      QT_TRY(op.gemm(Gcur, qt::OP_N, T(2), qt::OP_N, T(1), P));  // A = G_{l+1} U
+      if (pb.Jd) {
+        QT_TRY(op.gemm(Gncur, qt::OP_N, X, qt::OP_C, T(2), P, one_c, T(1), one_c));  // B
+        QT_TRY(op.gemm(Hc, qt::OP_C, T(2), qt::OP_N, W, P));                          // H^+ B
+        QT_TRY(op.gemm(Hc, qt::OP_N, T(2), qt::OP_C, T(1), P, one_c, W, one_c));      // + H B^+
+        to_c128<TC>(n, P, T(1), OUTB(pb.Jd, l), s);
+        if (pb.bond)
+          qt::zbond_trace<TC>(n, n, P, nullref(), Hc, T(2), jsign, pb.bond + p0 * bo, bo, l, s);
+      } else {
+        qt::zbond_trace<TC>(n, n, P, T1, Hc, T(1), jsign, pb.bond + p0 * bo, bo, l, s);
+      }
+    }
     if (glp) {  // G^>_l = X G^>_{l+1} X^+ (Glp never filled, src/cuda_rgf_mod.f90:78,351-372)
       QT_TRY(op.gemm(X, qt::OP_N, Gpcur, qt::OP_N, T1, P));
       QT_TRY(op.gemm(T1, qt::OP_N, X, qt::OP_C, Gpnew, P));
@@ -743,6 +771,7 @@ struct ProblemVB {
   unsigned flags;
   int sweep_slices, lead_slices, sweep_refine;
   double *tr, *tre, *T, *dgr, *dgl, *dgg;
+  double* bond;  // [npts][nx-1] bond currents
   int *status, *iters;
 };
 
@@ -940,6 +969,15 @@ qt_status solve_wave_vb(qt_ctx* ctx, const ProblemVB& pb, long long p0, long lon
     QT_TRY(op.gemm3(nl, nl, nq, T(1, nl), qt::OP_N, Hc, qt::OP_N, T(2, nl), P));
     QT_TRY(op.gemm3(nl, nl, nl, T(2, nl), qt::OP_N, GLN(l), qt::OP_N, T(10, nl), P));
     qt::zantiherm<TC>(nl, P, T(10, nl), 1, 0, T(innew, nl), T(innew, nl), s);
+    if (pb.bond) {
+      // bond current l -> l+1, trace form of the solve path: U = H g^< (nq x nl),
+      // A = G_{l+1} U, out = sign 2 (-Re Tr[T1 H] + Re Tr[H^+ A]), T1 = X G^<_{l+1} (nl x nq)
+      const double jsign = (q & QT_QUIRK_CPU_FERMI) ? -1.0 : 1.0;
+      QT_TRY(op.gemm3(nq, nl, nl, Hc, qt::OP_N, GLN(l), qt::OP_N, T(2, nq), P));
+      QT_TRY(op.gemm3(nq, nl, nq, T(ig, nq), qt::OP_N, T(2, nq), qt::OP_N, T(1, nq), P));
+      qt::zbond_trace<TC>(nl, nq, P, T(5, nl), Hc, T(1, nq), jsign, pb.bond + p0 * (nx - 1),
+                          nx - 1, l, s);
+    }
     std::swap(ig, inew);
     std::swap(ign, innew);
     emit(l, T(ig, nl), T(ign, nl));
@@ -1195,6 +1233,8 @@ extern "C" qt_status qt_rgf_solve(qt_ctx* ctx, const qt_device* dev, const doubl
   if (!valid_prec(prec)) QT_FAIL(QT_ERR_ARG, "unknown precision");
   if (prec != QT_PREC_FP64 && dev->nm > 128) QT_FAIL(QT_ERR_UNSUPPORTED, "mixed path needs nm <= 128");
   if (c->sancho_max_iter <= 0) QT_FAIL(QT_ERR_ARG, "sancho_max_iter must be > 0");
+  if (out->Jdens && (c->quirks & QT_QUIRK_CPU_FERMI))
+    QT_FAIL(QT_ERR_UNSUPPORTED, "Jdens blocks follow cuda_rgf_constblocksize (no QT_QUIRK_CPU_FERMI)");
   cudaSetDevice(ctx->device);
   const int nm = dev->nm, nx = dev->nx, nk = dev->nk;
   const long long npts = (long long)nE * nk;
@@ -1221,6 +1261,7 @@ extern "C" qt_status qt_rgf_solve(qt_ctx* ctx, const qt_device* dev, const doubl
     pb.dgr = out->diag_gr; pb.dgl = out->diag_gl; pb.dgg = out->diag_gg;
     pb.Gr = reinterpret_cast<cd*>(out->G_r); pb.Gl = reinterpret_cast<cd*>(out->G_lesser);
     pb.Gg = reinterpret_cast<cd*>(out->G_greater);
+    pb.bond = out->bond_cur; pb.Jd = reinterpret_cast<cd*>(out->Jdens);
     pb.status = out->status; pb.iters = out->sancho_iters;
     QT_TRY(run_problem(ctx, pb, hii_n, h1i_n));
   } else {
@@ -1233,6 +1274,8 @@ extern "C" qt_status qt_rgf_solve(qt_ctx* ctx, const qt_device* dev, const doubl
     if (out->G_r) add(blk_n * 16);
     if (out->G_lesser) add(blk_n * 16);
     if (out->G_greater) add(blk_n * 16);
+    if (out->Jdens) add(blk_n * 16);
+    if (out->bond_cur) add(npts * (nx - 1) * 8);
     QT_TRY(ensure(ctx->io, ctx->io_bytes, need + 4096));
     st.base = reinterpret_cast<char*>(ctx->io);
     pb.Hii = st.put(reinterpret_cast<const cd*>(dev->Hii), hii_n, true);
@@ -1249,6 +1292,8 @@ extern "C" qt_status qt_rgf_solve(qt_ctx* ctx, const qt_device* dev, const doubl
     pb.Gr = out->G_r ? st.put<cd>(nullptr, blk_n, false) : nullptr;
     pb.Gl = out->G_lesser ? st.put<cd>(nullptr, blk_n, false) : nullptr;
     pb.Gg = out->G_greater ? st.put<cd>(nullptr, blk_n, false) : nullptr;
+    pb.Jd = out->Jdens ? st.put<cd>(nullptr, blk_n, false) : nullptr;
+    pb.bond = out->bond_cur ? st.put<double>(nullptr, npts * (nx - 1), false) : nullptr;
     pb.status = st.put<int>(nullptr, npts, false);
     pb.iters = st.put<int>(nullptr, 2 * npts, false);
     QT_TRY(run_problem(ctx, pb, hii_n, h1i_n));
@@ -1264,6 +1309,8 @@ extern "C" qt_status qt_rgf_solve(qt_ctx* ctx, const qt_device* dev, const doubl
     back(out->G_r, pb.Gr, blk_n * 16);
     back(out->G_lesser, pb.Gl, blk_n * 16);
     back(out->G_greater, pb.Gg, blk_n * 16);
+    back(out->Jdens, pb.Jd, blk_n * 16);
+    back(out->bond_cur, pb.bond, npts * (nx - 1) * 8);
     back(out->status, pb.status, npts * 4);
     back(out->sancho_iters, pb.iters, npts * 8);
     flags |= QT_FLAG_SYNC;
@@ -1295,8 +1342,8 @@ extern "C" qt_status qt_rgf_solve_vb(qt_ctx* ctx, const qt_device_vb* dev, const
   if (!valid_prec(prec)) QT_FAIL(QT_ERR_ARG, "unknown precision");
   if (c->sancho_max_iter <= 0) QT_FAIL(QT_ERR_ARG, "sancho_max_iter must be > 0");
   if (c->quirks & QT_QUIRK_GLP_ZERO) QT_FAIL(QT_ERR_UNSUPPORTED, "QT_QUIRK_GLP_ZERO needs equal blocks");
-  if (out->G_r || out->G_lesser || out->G_greater)
-    QT_FAIL(QT_ERR_UNSUPPORTED, "variable blocks: diagonal outputs only");
+  if (out->G_r || out->G_lesser || out->G_greater || out->Jdens)
+    QT_FAIL(QT_ERR_UNSUPPORTED, "variable blocks: diagonal outputs and bond currents only");
   cudaSetDevice(ctx->device);
   ProblemVB pb{};
   pb.nx = dev->nx; pb.nk = dev->nk;
@@ -1333,6 +1380,7 @@ extern "C" qt_status qt_rgf_solve_vb(qt_ctx* ctx, const qt_device_vb* dev, const
     pb.E = E;
     pb.tr = out->tr; pb.tre = out->tre; pb.T = out->T;
     pb.dgr = out->diag_gr; pb.dgl = out->diag_gl; pb.dgg = out->diag_gg;
+    pb.bond = out->bond_cur;
     pb.status = out->status; pb.iters = out->sancho_iters;
     QT_TRY(run_problem_vb(ctx, pb, hii_n, h1i_n));
   } else {
@@ -1340,6 +1388,7 @@ extern "C" qt_status qt_rgf_solve_vb(qt_ctx* ctx, const qt_device_vb* dev, const
     auto add = [&](size_t bytes) { need += (bytes + 255) & ~size_t(255); };
     add(hii_n * 16); add(h1i_n * 16); add(nE * 8);
     add(npts * 8 * 3); add(diag_n * 16 * 3); add(npts * 4 * 3);
+    if (out->bond_cur) add(npts * (pb.nx - 1) * 8);
     QT_TRY(ensure(ctx->io, ctx->io_bytes, need + 4096));
     HostStage st{ctx, reinterpret_cast<char*>(ctx->io)};
     pb.Hii = st.put(reinterpret_cast<const cd*>(dev->Hii), hii_n, true);
@@ -1351,6 +1400,7 @@ extern "C" qt_status qt_rgf_solve_vb(qt_ctx* ctx, const qt_device_vb* dev, const
     pb.dgr = out->diag_gr ? st.put<double>(nullptr, 2 * diag_n, false) : nullptr;
     pb.dgl = out->diag_gl ? st.put<double>(nullptr, 2 * diag_n, false) : nullptr;
     pb.dgg = out->diag_gg ? st.put<double>(nullptr, 2 * diag_n, false) : nullptr;
+    pb.bond = out->bond_cur ? st.put<double>(nullptr, npts * (pb.nx - 1), false) : nullptr;
     pb.status = st.put<int>(nullptr, npts, false);
     pb.iters = st.put<int>(nullptr, 2 * npts, false);
     QT_TRY(run_problem_vb(ctx, pb, hii_n, h1i_n));
@@ -1363,6 +1413,7 @@ extern "C" qt_status qt_rgf_solve_vb(qt_ctx* ctx, const qt_device_vb* dev, const
     back(out->diag_gr, pb.dgr, diag_n * 16);
     back(out->diag_gl, pb.dgl, diag_n * 16);
     back(out->diag_gg, pb.dgg, diag_n * 16);
+    back(out->bond_cur, pb.bond, npts * (pb.nx - 1) * 8);
     back(out->status, pb.status, npts * 4);
     back(out->sancho_iters, pb.iters, npts * 8);
     flags |= QT_FLAG_SYNC;
@@ -1397,11 +1448,6 @@ extern "C" qt_status qt_rgf_constblocksize(qt_ctx* ctx, int nm, int nx, double E
             QT_FAIL(QT_ERR_UNSUPPORTED, "Sii must be the identity");
         }
   }
-  if (Jdens) {
-    // bond currents are not produced by the batched sweep; report zeros as the
-    // reference does for the last slab (src/cuda_rgf_mod.f90:84)
-    memset(Jdens, 0, sizeof(double) * 2 * (size_t)nm * nm * nx);
-  }
   qt_device dev{};
   dev.nm = nm; dev.nx = nx; dev.nk = 1;
   dev.Hii = Hii; dev.hii_kstride = 0; dev.hii_lstride = (int64_t)nm * nm;
@@ -1412,6 +1458,7 @@ extern "C" qt_status qt_rgf_constblocksize(qt_ctx* ctx, int nm, int nx, double E
   c.quirks = 0;
   qt_outputs o{};
   o.tr = tr; o.tre = tre; o.G_r = G_r; o.G_lesser = G_lesser; o.G_greater = G_greater;
+  o.Jdens = Jdens;
   return qt_rgf_solve(ctx, &dev, &En, 1, &c, sigma_r_ph, sigma_lesser_ph, QT_PREC_FP64, 0, &o);
 }
 
@@ -1629,8 +1676,15 @@ struct GwBuffers {
   double* sums;
 };
 
+// Optional per-energy currents of the map's RGF (green_RGF_RS's tr, tre, cur): device [nE],
+// [nE], [nE][nx-1]
+struct GwCurrents {
+  double *tr = nullptr, *tre = nullptr, *bond = nullptr;
+};
+
 qt_status gw_map(qt_ctx* ctx, Problem pb, const cd* V, double spindeg, const cd* SR,
-                 const cd* SL, GwBuffers& w, long long hii_n, long long h1i_n) {
+                 const cd* SL, GwBuffers& w, long long hii_n, long long h1i_n,
+                 const GwCurrents& cur = GwCurrents{}) {
   cudaStream_t s = ctx->stream;
   const int nm = pb.nm, nx = pb.nx;
   const long long nE = pb.npts;  // nk == 1
@@ -1638,7 +1692,8 @@ qt_status gw_map(qt_ctx* ctx, Problem pb, const cd* V, double spindeg, const cd*
   // ---- G with the current self-energies
   pb.sigr = SR;
   pb.sigl = SL;
-  pb.tr = pb.tre = pb.T = pb.dgr = pb.dgl = pb.dgg = nullptr;
+  pb.T = pb.dgr = pb.dgl = pb.dgg = nullptr;
+  pb.tr = cur.tr; pb.tre = cur.tre; pb.bond = cur.bond; pb.Jd = nullptr;
   pb.Gr = w.GR; pb.Gl = w.GL; pb.Gg = w.GG;
   pb.flags &= ~QT_FLAG_CAROLI;
   QT_TRY(run_problem(ctx, pb, hii_n, h1i_n));
@@ -1753,7 +1808,8 @@ struct GwAlloc {
 
 qt_status gw_alloc(qt_ctx* ctx, long long cnt, GwBuffers& w, GwAlloc& hold) {
   const size_t blk = (size_t)cnt * sizeof(cd);
-  const size_t need = 11 * blk + 2048 * sizeof(double2) + 64;
+  // 11 block arrays, FFT twiddles, then 64 B of sums and 2 x 2048 doubles of currents
+  const size_t need = 11 * blk + 2048 * sizeof(double2) + 64 + 2 * 2048 * sizeof(double);
   if (cudaMalloc(&hold.p, need) != cudaSuccess) {
     cudaGetLastError();
     QT_FAIL(QT_ERR_NOMEM, "GW buffers");
@@ -1801,7 +1857,8 @@ extern "C" qt_status qt_scba_solve(qt_ctx* ctx, const qt_device* dev, const doub
                                    const qt_contacts* c, const double* V, double spindeg,
                                    double alpha, double tol, int max_iter, qt_precision prec,
                                    unsigned flags, double* sigma_r, double* sigma_lesser,
-                                   double* sigma_greater, double* residuals, int* iters) {
+                                   double* sigma_greater, double* residuals, int* iters,
+                                   double* currents) {
   Problem pb;
   long long hn, h1n;
   QT_TRY(gw_setup(ctx, dev, E, nE, c, prec, flags, pb, hn, h1n));
@@ -1815,10 +1872,38 @@ extern "C" qt_status qt_scba_solve(qt_ctx* ctx, const qt_device* dev, const doub
   double2* SR = reinterpret_cast<double2*>(sigma_r);
   double2* SL = reinterpret_cast<double2*>(sigma_lesser);
   double2* SG = reinterpret_cast<double2*>(sigma_greater);
+  // terminal currents of each map's RGF, written as Id_iteration.dat does
+  // (src/gw_mod.f90:413-428): sum_E tre and sum_E tr (the caller's tr/tre are the
+  // routine's tre/tr, :376-380) x dE e0^2 spindeg / (2 pi hbar nk), with the
+  // reference's constants (src/static.f90:10,14; src/fft_mod.f90:19)
+  GwCurrents cur;
+  std::vector<double> htr, htre;
+  double dE = 0.0;
+  if (currents) {
+    cur.tre = w.sums + 8;
+    cur.tr = cur.tre + 2048;
+    htr.resize(nE);
+    htre.resize(nE);
+    double e2[2] = {0, 0};
+    cudaMemcpyAsync(e2, E, sizeof(e2), cudaMemcpyDeviceToHost, s);
+    QT_CUDA_TRY(cudaStreamSynchronize(s));
+    dE = e2[1] - e2[0];
+  }
+  const double e0 = 1.6022e-19, hbar = 1.0546e-34, tpi = 3.14159265359 * 2.0;
+  const double ifac = dE * e0 / tpi / hbar * e0 * spindeg;  // nk = 1
   int it = 0;
   for (; it < max_iter; ++it) {
     QT_TRY(gw_map(ctx, pb, reinterpret_cast<const cd*>(V), spindeg, reinterpret_cast<cd*>(SR),
-                  reinterpret_cast<cd*>(SL), w, hn, h1n));
+                  reinterpret_cast<cd*>(SL), w, hn, h1n, cur));
+    if (currents) {
+      cudaMemcpyAsync(htre.data(), cur.tre, nE * sizeof(double), cudaMemcpyDeviceToHost, s);
+      cudaMemcpyAsync(htr.data(), cur.tr, nE * sizeof(double), cudaMemcpyDeviceToHost, s);
+      QT_CUDA_TRY(cudaStreamSynchronize(s));
+      double a = 0.0, b = 0.0;
+      for (int e = 0; e < nE; ++e) { a += htre[e]; b += htr[e]; }
+      currents[2 * it] = a * ifac;
+      currents[2 * it + 1] = b * ifac;
+    }
     cudaMemsetAsync(w.sums, 0, 2 * sizeof(double), s);
     qt::gw_residual(cnt, reinterpret_cast<double2*>(w.NL), SL, reinterpret_cast<double2*>(w.NG),
                     SG, w.sums, s);

@@ -4,7 +4,10 @@
 * ``gw_step``          one evaluation Sigma -> Sigma_new of the SCBA map
                        (src/gw_mod.f90:368-749, 950-959)
 * ``scba``             the plain linear-mixing loop (src/gw_mod.f90:349-749)
-                       run to a residual tolerance
+                       run to a residual tolerance, optionally with the terminal
+                       currents of every iteration (Id_iteration.dat, :413-428)
+* ``currents``         the per-energy contact and bond currents of green_RGF_RS
+                       (:1131-1345) at given self-energies
 
 All arrays are torch CUDA tensors (device pointers); energy-resolved blocks
 are complex128 tensors of shape (nE, nx, nm, nm) stored column-major per
@@ -18,7 +21,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import QtContacts, QtDevice, check
-from .rgf import PREC, _ptr, colmajor
+from .rgf import OUT_KEYS, PREC, _ptr, colmajor
 
 
 def to_dev(A):
@@ -84,17 +87,41 @@ class GwSystem:
                                        _ptr(NR), _ptr(NL), _ptr(NG)))
         return NR, NL, NG
 
-    def scba(self, alpha=0.3, tol=1e-8, max_iter=60, start=None):
-        """Plain linear mixing to tol; returns (SR, SL, SG, residuals)."""
+    def scba(self, alpha=0.3, tol=1e-8, max_iter=60, start=None, with_currents=False):
+        """Plain linear mixing to tol; returns (SR, SL, SG, residuals), and with
+        ``with_currents`` also the (iterations, 2) left/right terminal currents in A, the
+        columns of Id_iteration.dat."""
         SR, SL, SG = start if start is not None else (self.zeros(), self.zeros(), self.zeros())
         res = np.zeros(max_iter)
+        cur = np.zeros((max_iter, 2)) if with_currents else None
         it = C.c_int()
         check(self.ctx._lib.qt_scba_solve(self.ctx.handle, C.byref(self.dev), _ptr(self.E),
                                           self.nE, C.byref(self.con), _ptr(self.V), self.spindeg,
                                           alpha, tol, max_iter, self.prec,
                                           _lib.QT_FLAG_DEVICE_POINTERS, _ptr(SR), _ptr(SL),
-                                          _ptr(SG), res.ctypes.data_as(C.c_void_p), C.byref(it)))
+                                          _ptr(SG), res.ctypes.data_as(C.c_void_p), C.byref(it),
+                                          _ptr(cur)))
+        if with_currents:
+            return SR, SL, SG, res[:it.value], cur[:it.value]
         return SR, SL, SG, res[:it.value]
+
+    def currents(self, SR, SL):
+        """Per-energy currents of the RGF with self-energies (SR, SL): dict of numpy arrays
+        tr, tre (nE,) (green_RGF_RS's right- and left-contact currents) and bond_cur
+        (nE, nx-1), the traces of its cur blocks (src/gw_mod.f90:1254-1276)."""
+        import torch
+        out = {"tr": torch.zeros(self.nE, dtype=torch.float64, device="cuda"),
+               "tre": torch.zeros(self.nE, dtype=torch.float64, device="cuda"),
+               "bond_cur": torch.zeros((self.nE, self.nx - 1), dtype=torch.float64,
+                                       device="cuda"),
+               "status": torch.zeros(self.nE, dtype=torch.int32, device="cuda")}
+        o = _lib.QtOutputs(*[_ptr(out.get(k)) for k in OUT_KEYS])
+        check(self.ctx._lib.qt_rgf_solve(self.ctx.handle, C.byref(self.dev), _ptr(self.E),
+                                         self.nE, C.byref(self.con), _ptr(SR), _ptr(SL),
+                                         self.prec,
+                                         _lib.QT_FLAG_DEVICE_POINTERS | _lib.QT_FLAG_SYNC,
+                                         C.byref(o)), allow_points=True)
+        return {k: v.cpu().numpy() for k, v in out.items()}
 
 
 def residual(NL, NG, SL, SG):

@@ -143,15 +143,22 @@ def _blocks(H, nk, nslab):
     raise ValueError("bad block array rank")
 
 
+# field order of qt_outputs
+OUT_KEYS = ("tr", "tre", "T", "diag_gr", "diag_gl", "diag_gg", "G_r", "G_lesser", "G_greater",
+            "status", "sancho_iters", "bond_cur", "Jdens")
+
+
 def rgf_solve(ctx, Hii, H1i, E, nx, *, nk=1, mul=0.0, mur=0.0, templ=300.0, tempr=300.0,
               eta_lead=1e-5, eta_interior=0.0, sancho_tol=1e-100, sancho_max_iter=50,
               precision="fp64", caroli=False, want_diag=True, want_blocks=False,
-              sigma_r_ph=None, sigma_lesser_ph=None, quirks=0):
+              want_bond=False, sigma_r_ph=None, sigma_lesser_ph=None, quirks=0):
     """Batched RGF over all (E, k) points (points ordered p = ie*nk + ik).
 
     Returns a dict of numpy arrays: tr, tre (nE, nk); T (nE, nk) if caroli;
-    diag_gr/gl/gg (nE, nk, nx, nm) if want_diag; G_r/G_lesser/G_greater
-    (nE, nk, nx, nm, nm) if want_blocks; status (nE, nk); sancho_iters (nE, nk, 2).
+    diag_gr/gl/gg (nE, nk, nx, nm) if want_diag; G_r/G_lesser/G_greater and the
+    bond-current blocks Jdens (nE, nk, nx, nm, nm) if want_blocks; bond_cur
+    (nE, nk, nx-1), the bond currents Re Tr Jdens_l, if want_bond; status (nE, nk);
+    sancho_iters (nE, nk, 2).
 
     ``precision``: "fp64" (FP64 pipes), "mixed" (tensor-core split products,
     complex64 sweep storage) or "mixed-fp64" (the same products with complex128
@@ -177,18 +184,18 @@ def rgf_solve(ctx, Hii, H1i, E, nx, *, nk=1, mul=0.0, mur=0.0, templ=300.0, temp
         for k in ("diag_gr", "diag_gl", "diag_gg"):
             res[k] = np.zeros((npts, nx, nm), dtype=np.complex128)
     if want_blocks:
-        for k in ("G_r", "G_lesser", "G_greater"):
+        for k in ("G_r", "G_lesser", "G_greater") + (() if quirks & 1 else ("Jdens",)):
             res[k] = np.zeros((npts, nx, nm, nm), dtype=np.complex128)
-    out = QtOutputs(*[_ptr(res.get(k)) for k in ("tr", "tre", "T", "diag_gr", "diag_gl",
-                                                 "diag_gg", "G_r", "G_lesser", "G_greater",
-                                                 "status", "sancho_iters")])
+    if want_bond:
+        res["bond_cur"] = np.zeros((npts, nx - 1))
+    out = QtOutputs(*[_ptr(res.get(k)) for k in OUT_KEYS])
     sr = None if sigma_r_ph is None else colmajor(sigma_r_ph)
     sl = None if sigma_lesser_ph is None else colmajor(sigma_lesser_ph)
     flags = _lib.QT_FLAG_SYNC | (_lib.QT_FLAG_CAROLI if caroli else 0)
     check(lib.qt_rgf_solve(ctx.handle, C.byref(dev), _ptr(E), nE, C.byref(con), _ptr(sr),
                            _ptr(sl), PREC[precision], flags, C.byref(out)), allow_points=True)
-    if want_blocks:
-        for k in ("G_r", "G_lesser", "G_greater"):
+    for k in ("G_r", "G_lesser", "G_greater", "Jdens"):
+        if k in res:
             res[k] = from_colmajor(res[k]).reshape(nE, nk, nx, nm, nm)
     for k in ("tr", "tre", "T", "status"):
         if k in res:
@@ -196,13 +203,16 @@ def rgf_solve(ctx, Hii, H1i, E, nx, *, nk=1, mul=0.0, mur=0.0, templ=300.0, temp
     for k in ("diag_gr", "diag_gl", "diag_gg"):
         if k in res:
             res[k] = res[k].reshape(nE, nk, nx, nm)
+    if want_bond:
+        res["bond_cur"] = res["bond_cur"].reshape(nE, nk, nx - 1)
     res["sancho_iters"] = res["sancho_iters"].reshape(nE, nk, 2)
     return res
 
 
 def rgf_variableblock_forward(ctx, Hii, H1i, E, *, nk=1, mul=0.0, mur=0.0, templ=300.0,
                               tempr=300.0, eta_lead=1e-5, eta_interior=0.0, sancho_tol=1e-100,
-                              sancho_max_iter=50, precision="fp64", caroli=False, quirks=0):
+                              sancho_max_iter=50, precision="fp64", caroli=False, quirks=0,
+                              want_bond=False):
     """Batched RGF over slabs of different orbital counts (rgf_variableblock_forward,
     src/rgf_mod.f90:46-269) for all (E, k) points.
 
@@ -210,7 +220,7 @@ def rgf_variableblock_forward(ctx, Hii, H1i, E, *, nk=1, mul=0.0, mur=0.0, templ
     H1i[l] = H_{l,l-1} (n_l, n_{l-1}) for 1 <= l < nx, H1i[0] and H1i[nx] the leads' own
     couplings (square), each optionally per k.  Returns tr, tre (and T) (nE, nk), status,
     sancho_iters and the diagonals diag_gr / diag_gl / diag_gg as lists of nx arrays
-    (nE, nk, n_l).
+    (nE, nk, n_l); with ``want_bond`` the bond currents bond_cur (nE, nk, nx-1).
     """
     lib = ctx._lib
     E = np.ascontiguousarray(np.asarray(E, dtype=np.float64).ravel())
@@ -241,9 +251,9 @@ def rgf_variableblock_forward(ctx, Hii, H1i, E, *, nk=1, mul=0.0, mur=0.0, templ
         res["T"] = np.zeros(npts)
     for k in ("diag_gr", "diag_gl", "diag_gg"):
         res[k] = np.zeros((npts, dsum), dtype=np.complex128)
-    out = QtOutputs(*[_ptr(res.get(k)) for k in ("tr", "tre", "T", "diag_gr", "diag_gl",
-                                                 "diag_gg", "G_r", "G_lesser", "G_greater",
-                                                 "status", "sancho_iters")])
+    if want_bond:
+        res["bond_cur"] = np.zeros((npts, nx - 1))
+    out = QtOutputs(*[_ptr(res.get(k)) for k in OUT_KEYS])
     flags = _lib.QT_FLAG_SYNC | (_lib.QT_FLAG_CAROLI if caroli else 0)
     check(lib.qt_rgf_solve_vb(ctx.handle, C.byref(dev), _ptr(E), nE, C.byref(con),
                               PREC[precision], flags, C.byref(out)), allow_points=True)
@@ -253,6 +263,8 @@ def rgf_variableblock_forward(ctx, Hii, H1i, E, *, nk=1, mul=0.0, mur=0.0, templ
     cut = np.cumsum(sizes)[:-1]
     for k in ("diag_gr", "diag_gl", "diag_gg"):
         res[k] = [d.reshape(nE, nk, -1) for d in np.split(res[k], cut, axis=1)]
+    if want_bond:
+        res["bond_cur"] = res["bond_cur"].reshape(nE, nk, nx - 1)
     res["sancho_iters"] = res["sancho_iters"].reshape(nE, nk, 2)
     return res
 
@@ -263,8 +275,9 @@ def cuda_rgf_constblocksize(ctx, nm, nx, En, mul, mur, TEMPl, TEMPr, Hii, H1i, S
 
     Hii (nx, nm, nm), H1i (nx+1, nm, nm), optional Sii / sigmas (nx, nm, nm).
     mu/T may be scalars or the reference's constant nm x nm matrices.
-    Returns (G_r, G_lesser, G_greater, Jdens, tr, tre); Jdens is all zeros
-    (bond currents are not produced by the batched sweep).
+    Returns (G_r, G_lesser, G_greater, Jdens, tr, tre).  Jdens[l] is the bond-current
+    block H^+ G^<_{l+1,l} - H G^<_{l,l+1} (src/cuda_rgf_mod.f90:293-318); Jdens[nx-1]
+    is zero, as the reference never writes it.
     """
     def scalar(x):
         x = np.asarray(x, dtype=np.float64)
@@ -362,13 +375,15 @@ def cell_spectra(diag, nbnd, nslab, nk_axis=1):
 
 
 def negf_solve(ctx, Hii, H1i, nx, nen, emin, emax, temp, mu, nbnd, nslab, *, nk=1,
-               precision="fp64", **kw):
+               precision="fp64", Lx=None, write_dir=None, **kw):
     """Ballistic NEGF driver (src/negf_mod.f90:41-165).
 
     Energy grid E_ie = emin + ie (emax-emin)/(nen-1) (src/negf_mod.f90:100-101).
     Returns dict with E, tr, tre (nen, nk) and the ldos/ndos/pdos spectra
     (nen, nx*nslab, 2) = (Re*c1, Im*c2) columns with the reference coefficients
-    (1,-2), (1,1), (1,-1) (src/negf_mod.f90:142-149).
+    (1,-2), (1,1), (1,-1) (src/negf_mod.f90:142-149).  With ``write_dir`` (and the cell
+    length ``Lx``) it also writes ldos0000.dat, ndos0000.dat and pdos0000.dat there in the
+    reference's format; their paths are returned under "files".
     """
     E = emin + np.arange(nen) * ((emax - emin) / (nen - 1))
     r = rgf_solve(ctx, Hii, H1i, E, nx, nk=nk, mul=mu[0], mur=mu[1], templ=temp[0],
@@ -378,6 +393,11 @@ def negf_solve(ctx, Hii, H1i, nx, nen, emin, emax, temp, mu, nbnd, nslab, *, nk=
                          ("pdos", "diag_gg", (1.0, -1.0))):
         t = cell_spectra(r[key], nbnd, nslab)
         out[name] = np.stack([t.real * c[0], t.imag * c[1]], axis=-1)
+    if write_dir is not None:
+        from .output import write_negf_spectra
+        if Lx is None:
+            raise ValueError("writing the spectra needs the cell length Lx")
+        out["files"] = write_negf_spectra(r, E, nbnd, nslab, Lx, directory=write_dir)
     return out
 
 
@@ -389,16 +409,14 @@ def rgf_solve_device(ctx, Hii, hk, hl, H1i, h1k, h1l, nm, nx, nk, E, nE, out, *,
 
     Hii/H1i/E: torch CUDA tensors (column-major complex128 blocks, float64
     energies); ``out``: dict of torch CUDA tensors for any of tr, tre, T,
-    diag_gr, diag_gl, diag_gg, status, sancho_iters.  Strides in complex elements.
+    diag_gr, diag_gl, diag_gg, status, sancho_iters, bond_cur.  Strides in complex elements.
     Returns the status code (QT_OK or QT_ERR_POINTS when synchronised).
     """
     lib = ctx._lib
     dev = QtDevice(nm, nx, nk, _ptr(Hii), hk, hl, _ptr(H1i), h1k, h1l, None, 0, 0)
     con = QtContacts(mul, mur, templ, tempr, eta_lead, eta_interior, sancho_tol,
                      int(sancho_max_iter), int(quirks))
-    o = QtOutputs(*[_ptr(out.get(k)) for k in ("tr", "tre", "T", "diag_gr", "diag_gl",
-                                               "diag_gg", "G_r", "G_lesser", "G_greater",
-                                               "status", "sancho_iters")])
+    o = QtOutputs(*[_ptr(out.get(k)) for k in OUT_KEYS])
     flags = _lib.QT_FLAG_DEVICE_POINTERS | (_lib.QT_FLAG_CAROLI if caroli else 0) | \
         (_lib.QT_FLAG_SYNC if sync else 0)
     return check(lib.qt_rgf_solve(ctx.handle, C.byref(dev), _ptr(E), int(nE), C.byref(con),

@@ -67,3 +67,54 @@ def test_scba_converges_like_oracle(ctx):
     assert abs(len(res) - len(ores)) <= 1
     for got, exp in zip((SR, SL, SG), (oR, oL, oG)):
         np.testing.assert_allclose(gw.from_dev(got), exp, rtol=0, atol=1e-7 * np.abs(exp).max())
+
+
+def _random_sigma(nE, nx, nm, seed=0):
+    rng = np.random.default_rng(seed)
+    shape = (nE, nx, nm, nm)
+    SL = 1e-2 * (rng.normal(size=shape) + 1j * rng.normal(size=shape))
+    SL = (SL - np.conj(np.swapaxes(SL, -1, -2))) / 2      # anti-Hermitian Sigma^<
+    SR = 1e-2 * (rng.normal(size=shape) - 1j * np.abs(rng.normal(size=shape)))
+    return (SR + np.swapaxes(SR, -1, -2)) / 2, SL
+
+
+def test_gw_currents_vs_oracle(ctx):
+    """tr, tre and the bond currents (traces of cur, src/gw_mod.f90:1254-1276) of the GW
+    RGF at given self-energies."""
+    from oracle import rgf as orc
+    from quantum_transport_gb300 import gw
+    dev, V, s = _system(ctx)
+    SR0, SL0 = _random_sigma(len(dev.E), dev.nx, 8)
+    c = s.currents(gw.to_dev(SR0), gw.to_dev(SL0))
+    assert (c["status"] == 0).all()
+    Hii, H1i = [dev.H00[0]] * dev.nx, [dev.H10] * (dev.nx + 1)
+    Js = []
+    for ie, e in enumerate(dev.E):
+        o = orc.rgf_constblocksize(e, Hii, H1i, None, list(SL0[ie]), list(SR0[ie]), mul=0.1,
+                                   mur=-0.1, templ=300.0, tempr=300.0, eta_lead=1e-3,
+                                   sancho_nmax=100, sancho_tol=1e-100)
+        J = np.real([np.trace(o["Jdens"][l]) for l in range(dev.nx - 1)])
+        Js.append(J)
+        np.testing.assert_allclose(c["tr"][ie], o["tr"], rtol=1e-8, atol=1e-12)
+        np.testing.assert_allclose(c["tre"][ie], o["tre"], rtol=1e-8, atol=1e-12)
+        np.testing.assert_allclose(c["bond_cur"][ie], J, rtol=0,
+                                   atol=1e-9 * max(np.abs(J).max(), 1e-12))
+    assert np.abs(np.array(Js)).max() > 1e-3
+
+
+def test_scba_iteration_currents(ctx):
+    """The Id_iteration.dat columns of qt_scba_solve are the terminal currents of the RGF at
+    each iteration's self-energies: sum_E tre and sum_E tr x dE e0^2 spindeg / (2 pi hbar)."""
+    from quantum_transport_gb300 import currents
+    dev, V, s = _system(ctx)
+    _, _, _, res, cur = s.scba(alpha=0.3, tol=0.0, max_iter=3, with_currents=True)
+    assert cur.shape == (3, 2)
+    z = s.zeros()
+    c0 = s.currents(z, z)
+    expect0 = [currents.terminal_current(c0["tre"], dev.E), currents.terminal_current(c0["tr"], dev.E)]
+    np.testing.assert_allclose(cur[0], expect0, rtol=1e-10)
+    SR1, SL1, _, _ = s.scba(alpha=0.3, tol=0.0, max_iter=1)  # the iterate the second map sees
+    c1 = s.currents(SR1, SL1)
+    expect1 = [currents.terminal_current(c1["tre"], dev.E), currents.terminal_current(c1["tr"], dev.E)]
+    np.testing.assert_allclose(cur[1], expect1, rtol=1e-10)
+    assert abs(cur[0, 0]) > 0 and not np.allclose(cur[0], cur[1], rtol=1e-6)
