@@ -10,6 +10,8 @@ and writes
   cnt_hr.npz      the model itself: Hr(nb, nb, nxr, nyr, nzr), R ranges, cell vectors
   cnt_golden.npz  the reference outputs as arrays on the exact energy grid
                   E = -6 + ie*5/199 (src/negf_mod.f90:100-101)
+  cnt_text.npz    the text of ldos0000.dat, ndos0000.dat, pdos0000.dat, for
+                  line-by-line checks of the (4E18.4) writer
 
 The run that produced the .dat files used main.f90's defaults nx = 5, ns = 3
 (src/main.f90:75-76), 200 energies on [-6, -1] eV, mu = -3.7 eV, T = 300 K.
@@ -57,6 +59,11 @@ def main(ref):
         assert d.shape == (nen * 15, 4)
         spec[name] = d[:, 2:].reshape(nen, 15, 2)
         spec["x"] = d[:15, 0]
+    text = {}
+    for name in ("ldos", "ndos", "pdos"):
+        with open(os.path.join(tc, f"{name}0000.dat")) as f:
+            text[name] = np.array(f.read())
+    np.savez_compressed(os.path.join(HERE, "cnt_text.npz"), **text)
     np.savez_compressed(os.path.join(HERE, "cnt_golden.npz"), E=E, sancho_g00=by_lead(g00),
                         sancho_gbb=by_lead(gbb), ldos=spec["ldos"], ndos=spec["ndos"],
                         pdos=spec["pdos"], x=spec["x"], nx=5, mu=-3.7, temp=300.0)
