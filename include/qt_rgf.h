@@ -341,6 +341,23 @@ qt_status qt_scba_solve(qt_ctx* ctx, const qt_device* dev, const double* E, int 
                         double* sigma_greater, double* residuals, int* iters,
                         double* currents);
 
+/* e-photon self-energy in the monochromatic approximation
+ * (calc_sigma_ephoton_monochromatic_ext, src/gw_mod.f90:1075-1122), per energy e and
+ * slab x:
+ *   Sigma^<(e) = scale M_x [G^<(e - nop) + G^<(e + nop)] M_x, Sigma^> likewise,
+ *   Sigma^R = i Im(Sigma^> - Sigma^<)/2,
+ * scale = pre_fact * intensity / hw^2 and nop = floor(hw / dE) in the reference.
+ *   M        [nx][nm*nm] interaction blocks (sum_i polarization(i) Pii(:,:,i,x))
+ *   G_*      [nE + 2 nop][nx][nm*nm] with halo != 0 (nop energies from each neighbouring
+ *            energy shard before and after, zero beyond the grid: src/gw_mod.f90:845-863),
+ *            else [nE][nx][nm*nm] with zero beyond the ends
+ *   sigma_*  [nE][nx][nm*nm] outputs
+ * Device pointers (QT_FLAG_DEVICE_POINTERS), column-major complex128 blocks.      */
+qt_status qt_ephoton_sigma(qt_ctx* ctx, int nm, int nx, int nE, int nop, int halo,
+                           const double* M, const double* G_lesser, const double* G_greater,
+                           double scale, qt_precision prec, unsigned flags, double* sigma_r,
+                           double* sigma_lesser, double* sigma_greater);
+
 /* Batched energy correlation (mode 0) / convolution (mode 1) of corr1d2 /
  * conv1d2 (src/fft_mod.f90:58-168) on n-point series stored energy-major,
  * element (e, s) at 2*(e*nseries + s) doubles:

@@ -185,3 +185,33 @@ def coulomb_blocks(nm, spacing_nm=0.25, strength=14.4):
     """V_ij = 14.4 / (|r_i - r_j| + 1) eV on a 1-D grid of 0.25 nm (orbital index x spacing)."""
     r = np.arange(nm) * spacing_nm
     return strength / (np.abs(r[:, None] - r[None, :]) + 1.0)
+
+
+# e-photon prefactor (hbar/m0)^2 / (2 eps0 c0^3), src/gw_mod.f90:92, constants of
+# src/static.f90:10-14
+PHOTON_PRE_FACT = ((1.0546e-34 / 9.109e-31) ** 2) / (2.0 * 8.854e-12 * 2.998e8 ** 3)
+
+
+def ephoton_sigma(M, GL, GG, nop, pre_fact, intensity, hw, halo=False):
+    """calc_sigma_ephoton_monochromatic_ext (src/gw_mod.f90:1075-1122), row-major numpy.
+
+    M (nx, nm, nm); GL, GG (nE + 2 nop, nx, nm, nm) when ``halo`` (energy e at index
+    e + nop) else (nE, nx, nm, nm) with zeros beyond the grid.  Returns (SR, SL, SG),
+    each (nE, nx, nm, nm): Sigma^<> = M [G(e - nop) + G(e + nop)] M * pre_fact *
+    intensity / hw^2 and Sigma^R = i Im(Sigma^> - Sigma^<) / 2."""
+    def ext(G):
+        if halo:
+            return G
+        Z = np.zeros((G.shape[0] + 2 * nop,) + G.shape[1:], dtype=np.complex128)
+        Z[nop:nop + G.shape[0]] = G
+        return Z
+
+    nE = GL.shape[0] - (2 * nop if halo else 0)
+    out = []
+    for G in (GL, GG):
+        Ge = ext(G)
+        A = Ge[0:nE] + Ge[2 * nop:2 * nop + nE]  # ie2 -+ nop with ie2 = ie + nop
+        S = np.einsum("xab,exbc,xcd->exad", M, A, M)
+        out.append(S * pre_fact * intensity / hw ** 2)
+    SL, SG = out
+    return 1j * (SG - SL).imag / 2.0, SL, SG

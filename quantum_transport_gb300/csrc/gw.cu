@@ -172,6 +172,35 @@ __global__ void mix_kernel(long long count, double alpha, double2* S, const doub
   }
 }
 
+// A[e] = scale (G[e - nop] + G[e + nop]) per (energy, slab) block, the photon-shifted sum
+// of calc_sigma_ephoton_monochromatic_ext (src/gw_mod.f90:1095-1110), with the
+// self-energy's prefactor applied here in FP64 (the split products that follow take
+// their alpha in FP32).  With halo != 0, G
+// holds nE + 2 nop energies (nop exchanged from each neighbouring energy shard, zero
+// beyond the global grid) and energy e of the output reads G[e] + G[e + 2 nop]; without,
+// G holds nE energies and terms outside [0, nE) are zero.
+__global__ void photon_shift_sum_kernel(long long per, long long nE, int nop, int halo,
+                                        double scale, const double2* G, double2* A) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nE * per;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long e = t / per, r = t - e * per;
+    const long long lo = halo ? e : e - nop, hi = halo ? e + 2 * nop : e + nop;
+    const long long ne = halo ? nE + 2 * nop : nE;
+    double2 v = make_double2(0.0, 0.0);
+    if (lo >= 0) { const double2 a = G[lo * per + r]; v.x += a.x; v.y += a.y; }
+    if (hi < ne) { const double2 b = G[hi * per + r]; v.x += b.x; v.y += b.y; }
+    A[t] = make_double2(scale * v.x, scale * v.y);
+  }
+}
+
+// Sigma^R = i Im(Sigma^> - Sigma^<) / 2, real part zero (src/gw_mod.f90:1121)
+__global__ void photon_retarded_kernel(long long count, const double2* SL, const double2* SG,
+                                       double2* SR) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < count;
+       t += (long long)gridDim.x * blockDim.x)
+    SR[t] = make_double2(0.0, 0.5 * (SG[t].y - SL[t].y));
+}
+
 inline unsigned g1(long long n) {
   long long g = (n + 255) / 256;
   return (unsigned)(g < 1 ? 1 : (g > 65535LL * 8 ? 65535LL * 8 : g));
@@ -213,6 +242,20 @@ cudaError_t gw_sigma_post(int nm, long long nblocks, double2* SR, double2* SL, d
 cudaError_t gw_residual(long long count, const double2* nl, const double2* ol, const double2* ng,
                         const double2* og, double* sums, cudaStream_t s) {
   residual_kernel<<<g1(count) > 1024 ? 1024 : g1(count), 256, 0, s>>>(count, nl, ol, ng, og, sums);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t photon_shift_sum(long long per, long long nE, int nop, int halo, double scale,
+                             const double2* G, double2* A, cudaStream_t s) {
+  photon_shift_sum_kernel<<<g1(nE * per), 256, 0, s>>>(per, nE, nop, halo, scale, G, A);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t photon_retarded(long long count, const double2* SL, const double2* SG, double2* SR,
+                            cudaStream_t s) {
+  photon_retarded_kernel<<<g1(count), 256, 0, s>>>(count, SL, SG, SR);
   count_launch();
   return cudaGetLastError();
 }

@@ -1925,6 +1925,63 @@ extern "C" qt_status qt_scba_solve(qt_ctx* ctx, const qt_device* dev, const doub
   return QT_OK;
 }
 
+// e-photon self-energy in the monochromatic approximation
+// (calc_sigma_ephoton_monochromatic_ext, src/gw_mod.f90:1075-1122): for every energy
+// and slab, Sigma^{<,>} = scale M [G^{<,>}(E - hw) + G^{<,>}(E + hw)] M with M the slab's
+// interaction block, Sigma^R = i Im(Sigma^> - Sigma^<)/2.  The shifted sum, scaled in FP64,
+// is one elementwise pass (written into sigma_r, which is computed last), then two batched
+// block products per component.
+extern "C" qt_status qt_ephoton_sigma(qt_ctx* ctx, int nm, int nx, int nE, int nop, int halo,
+                                      const double* M, const double* G_lesser,
+                                      const double* G_greater, double scale, qt_precision prec,
+                                      unsigned flags, double* sigma_r, double* sigma_lesser,
+                                      double* sigma_greater) {
+  if (!ctx || !M || !G_lesser || !G_greater || !sigma_r || !sigma_lesser || !sigma_greater ||
+      nm <= 0 || nx <= 0 || nE <= 0 || nop < 0)
+    QT_FAIL(QT_ERR_ARG, "bad e-photon arguments");
+  if (!(flags & QT_FLAG_DEVICE_POINTERS)) QT_FAIL(QT_ERR_UNSUPPORTED, "device pointers required");
+  if (!valid_prec(prec)) QT_FAIL(QT_ERR_ARG, "unknown precision");
+  if (prec != QT_PREC_FP64 && nm > 128) QT_FAIL(QT_ERR_UNSUPPORTED, "mixed path needs nm <= 128");
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = ctx->stream;
+  const long long nm2 = (long long)nm * nm, nblk = (long long)nE * nx, cnt = nblk * nm2;
+  QT_TRY(ensure(ctx->arena, ctx->arena_bytes,
+                (size_t)cnt * sizeof(cd) + (size_t)nblk * 256 * sizeof(int) + 4096));
+  Arena ar{reinterpret_cast<char*>(ctx->arena), ctx->arena_bytes, 0};
+  cd* one = ar.take<cd>(1);
+  cd* T = ar.take<cd>((size_t)cnt);
+  int* scales = ar.take<int>((size_t)nblk * 256);
+  if (!one || !T || !scales) QT_FAIL(QT_ERR_NOMEM, "arena exhausted (e-photon)");
+  const cd h1{1.0, 0.0};
+  cudaMemcpyAsync(one, &h1, sizeof(cd), cudaMemcpyHostToDevice, s);
+  Ops<double2> op{s, nm, prec};
+  op.slices = 7;  // FP64-grade digits on the split path, as for the screened interaction
+  op.one = one;
+  op.scales = scales;
+  op.P = nblk;
+  op.prof = &ctx->prof;
+  const BatchRef Mr = ref(M, nm2, nm, nx);  // block b = e*nx + x uses M[x]
+  auto blk = [&](const void* p) { return ref(p, nm2, nm); };
+  double2* A = reinterpret_cast<double2*>(sigma_r);
+  const double* G[2] = {G_lesser, G_greater};
+  double* out[2] = {sigma_lesser, sigma_greater};
+  for (int c = 0; c < 2; ++c) {
+    cudaError_t e = qt::photon_shift_sum((long long)nx * nm2, nE, nop, halo, scale,
+                                         reinterpret_cast<const double2*>(G[c]), A, s);
+    if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+    QT_TRY(op.gemm(Mr, qt::OP_N, blk(A), qt::OP_N, blk(T), nblk));
+    QT_TRY(op.gemm(blk(T), qt::OP_N, Mr, qt::OP_N, blk(out[c]), nblk));
+  }
+  cudaError_t e = qt::photon_retarded(cnt, reinterpret_cast<const double2*>(sigma_lesser),
+                                      reinterpret_cast<const double2*>(sigma_greater),
+                                      reinterpret_cast<double2*>(sigma_r), s);
+  if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+  if ((flags & QT_FLAG_SYNC) || prec != QT_PREC_FP64) QT_CUDA_TRY(cudaStreamSynchronize(s));
+  if (prec != QT_PREC_FP64 && qt::oz_timeouts_and_reset())
+    QT_FAIL(QT_ERR_CUDA, "tensor-core kernel wait timed out");
+  return QT_OK;
+}
+
 extern "C" qt_status qt_corr_batch(qt_ctx* ctx, int n, int64_t nseries, const double* X,
                                    const double* Y, double* Z, int mode, unsigned flags) {
   if (!ctx || !X || !Y || !Z || n <= 0 || nseries <= 0 || (mode != 0 && mode != 1))

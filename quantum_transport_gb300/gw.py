@@ -8,6 +8,8 @@
                        currents of every iteration (Id_iteration.dat, :413-428)
 * ``currents``         the per-energy contact and bond currents of green_RGF_RS
                        (:1131-1345) at given self-energies
+* ``ephoton_sigma``    the e-photon self-energy in the monochromatic approximation
+                       (:1075-1122); with ``shard.energy_halo`` across energy shards
 
 All arrays are torch CUDA tensors (device pointers); energy-resolved blocks
 are complex128 tensors of shape (nE, nx, nm, nm) stored column-major per
@@ -122,6 +124,35 @@ class GwSystem:
                                          _lib.QT_FLAG_DEVICE_POINTERS | _lib.QT_FLAG_SYNC,
                                          C.byref(o)), allow_points=True)
         return {k: v.cpu().numpy() for k, v in out.items()}
+
+
+# (hbar/m0)^2 / (2 eps0 c0^3) with the reference's constants (src/gw_mod.f90:92,
+# src/static.f90:10-14)
+PHOTON_PRE_FACT = ((1.0546e-34 / 9.109e-31) ** 2) / (2.0 * 8.854e-12 * 2.998e8 ** 3)
+
+
+def photon_steps(hw, dE):
+    """nop = floor(hw / dE): the photon energy in grid steps (src/gw_mod.f90:194)."""
+    return int(np.floor(hw / dE))
+
+
+def ephoton_sigma(ctx, M, GL, GG, nop, intensity, hw, *, halo=False, precision="fp64"):
+    """(SR, SL, SG) e-photon self-energies (nE, nx, nm, nm) on the GPU.
+
+    ``M``: (nx, nm, nm) interaction blocks; ``GL``, ``GG``: (nE, nx, nm, nm) G^<, G^>,
+    or (nE + 2 nop, ...) with ``halo`` (from ``shard.energy_halo``).  All torch CUDA
+    tensors, column-major blocks (``to_dev``)."""
+    import torch
+    nEx, nx, nm = GL.shape[0], GL.shape[1], GL.shape[-1]
+    nE = nEx - 2 * nop if halo else nEx
+    shape = (nE, nx, nm, nm)
+    SR, SL, SG = (torch.empty(shape, dtype=torch.complex128, device=GL.device) for _ in range(3))
+    scale = PHOTON_PRE_FACT * intensity / hw ** 2
+    check(ctx._lib.qt_ephoton_sigma(ctx.handle, nm, nx, nE, int(nop), 1 if halo else 0, _ptr(M),
+                                    _ptr(GL), _ptr(GG), scale, PREC[precision],
+                                    _lib.QT_FLAG_DEVICE_POINTERS | _lib.QT_FLAG_SYNC, _ptr(SR),
+                                    _ptr(SL), _ptr(SG)))
+    return SR, SL, SG
 
 
 def residual(NL, NG, SL, SG):

@@ -1,4 +1,4 @@
-"""Sharding the (E, k) points over ranks: one process per GPU, no data-path collective.
+"""Sharding the (E, k) points over ranks: one process per GPU.
 
 Every (E, k) point of the RGF sweep is independent.  As in the reference, each
 rank takes a contiguous block of the energy grid (src/main.f90:100-101,
@@ -6,7 +6,9 @@ src/negf_mod.f90:100-103).  It solves all k-points of its energies and
 exchanges nothing until the final gather of the per-point results.  The
 reference gives every rank nen / comm_size energies and drops the remaining
 nen mod comm_size; ``energy_range`` spreads them over the first ranks instead,
-and reproduces the reference's split with ``drop_remainder=True``.
+and reproduces the reference's split with ``drop_remainder=True``.  The RGF path
+has no data-path collective.  The one exchange step is ``energy_halo``, for the
+e-photon self-energy, which needs nop energies from each neighbouring shard.
 """
 from __future__ import annotations
 
@@ -61,3 +63,42 @@ def max_over_ranks(x, group=None):
                      device=torch.device("cuda", torch.cuda.current_device()) if cuda else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX, group=group)
     return float(t.item())
+
+
+def energy_halo(local, nop, world, rank, group=None):
+    """This rank's energies with ``nop`` energies of each neighbouring shard around them.
+
+    The e-photon self-energy at energy E needs G(E -+ hw), nop = floor(hw / dE) grid
+    steps away, so each rank receives the last ``nop`` energies of rank - 1 and the first
+    ``nop`` of rank + 1, and zeros beyond the global grid (src/gw_mod.f90:845-863, with the
+    buffer layout of :226-239).  Returns an array of nE_local + 2 nop energies, numpy or
+    torch like ``local``.  Point-to-point sends and receives only; gloo for host tensors,
+    NCCL for device tensors.
+    """
+    import torch
+    import torch.distributed as dist
+    is_np = isinstance(local, np.ndarray)
+    t = torch.from_numpy(np.ascontiguousarray(local)) if is_np else local.contiguous()
+    n = t.shape[0]
+    if nop < 0 or nop > n:
+        raise ValueError("need 0 <= nop <= local energies")
+    ext = torch.zeros((n + 2 * nop,) + tuple(t.shape[1:]), dtype=t.dtype, device=t.device)
+    ext[nop:nop + n] = t
+    if world > 1 and nop > 0:
+        real = (lambda x: torch.view_as_real(x)) if t.is_complex() else (lambda x: x)
+        if dist.get_backend(group) == "nccl" and t.device.type != "cuda":
+            raise ValueError("NCCL halo exchange needs device tensors")
+        reqs, keep = [], []
+        if rank > 0:
+            send = t[:nop].contiguous()
+            keep.append(send)
+            reqs.append(dist.isend(real(send), rank - 1, group=group, tag=0))
+            reqs.append(dist.irecv(real(ext[:nop]), rank - 1, group=group, tag=1))
+        if rank < world - 1:
+            send = t[n - nop:].contiguous()
+            keep.append(send)
+            reqs.append(dist.isend(real(send), rank + 1, group=group, tag=1))
+            reqs.append(dist.irecv(real(ext[nop + n:]), rank + 1, group=group, tag=0))
+        for r in reqs:
+            r.wait()
+    return ext.numpy() if is_np else ext

@@ -4,6 +4,7 @@ import numpy as np
 import pytest
 
 from oracle import gw as ogw
+from quantum_transport_gb300 import _lib as rgf_lib
 from quantum_transport_gb300.devices import make_chain_device
 
 pytestmark = pytest.mark.gpu
@@ -69,13 +70,14 @@ def test_scba_converges_like_oracle(ctx):
         np.testing.assert_allclose(gw.from_dev(got), exp, rtol=0, atol=1e-7 * np.abs(exp).max())
 
 
-def _random_sigma(nE, nx, nm, seed=0):
+def _physical_sigma(nE, nx, nm, seed=0):
+    """Sigma^R = -i Gamma/2, Sigma^< = i f Gamma with Gamma Hermitian positive semidefinite
+    and 0 < f < 1: broadening only, so the leads' decimation stays bounded."""
     rng = np.random.default_rng(seed)
-    shape = (nE, nx, nm, nm)
-    SL = 1e-2 * (rng.normal(size=shape) + 1j * rng.normal(size=shape))
-    SL = (SL - np.conj(np.swapaxes(SL, -1, -2))) / 2      # anti-Hermitian Sigma^<
-    SR = 1e-2 * (rng.normal(size=shape) - 1j * np.abs(rng.normal(size=shape)))
-    return (SR + np.swapaxes(SR, -1, -2)) / 2, SL
+    X = 0.1 * (rng.normal(size=(nE, nx, nm, nm)) + 1j * rng.normal(size=(nE, nx, nm, nm)))
+    gam = X @ np.conj(np.swapaxes(X, -1, -2)) / nm
+    f = rng.random((nE, nx, 1, 1))
+    return -0.5j * gam, 1j * f * gam
 
 
 def test_gw_currents_vs_oracle(ctx):
@@ -84,9 +86,11 @@ def test_gw_currents_vs_oracle(ctx):
     from oracle import rgf as orc
     from quantum_transport_gb300 import gw
     dev, V, s = _system(ctx)
-    SR0, SL0 = _random_sigma(len(dev.E), dev.nx, 8)
+    SR0, SL0 = _physical_sigma(len(dev.E), dev.nx, 8)
     c = s.currents(gw.to_dev(SR0), gw.to_dev(SL0))
-    assert (c["status"] == 0).all()
+    # the decimation runs the reference's fixed 100 steps (TOL = 1e-100), so only the
+    # "not converged" bit may be set
+    assert ((c["status"] & ~rgf_lib.QT_PT_SANCHO_NOT_CONVERGED) == 0).all()
     Hii, H1i = [dev.H00[0]] * dev.nx, [dev.H10] * (dev.nx + 1)
     Js = []
     for ie, e in enumerate(dev.E):
@@ -118,3 +122,29 @@ def test_scba_iteration_currents(ctx):
     expect1 = [currents.terminal_current(c1["tre"], dev.E), currents.terminal_current(c1["tr"], dev.E)]
     np.testing.assert_allclose(cur[1], expect1, rtol=1e-10)
     assert abs(cur[0, 0]) > 0 and not np.allclose(cur[0], cur[1], rtol=1e-6)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 1e-11)])
+def test_ephoton_sigma_vs_oracle(ctx, precision, tol):
+    """qt_ephoton_sigma against calc_sigma_ephoton_monochromatic_ext restated, on one shard
+    (zeros beyond the grid) and on an inner shard with its energy halo."""
+    from quantum_transport_gb300 import gw
+    rng = np.random.default_rng(7)
+    nE, nx, nm, nop = 24, 4, 12, 3
+    shape = (nE, nx, nm, nm)
+    GL = 1e-2 * (rng.normal(size=shape) + 1j * rng.normal(size=shape))
+    GG = 1e-2 * (rng.normal(size=shape) + 1j * rng.normal(size=shape))
+    M = rng.normal(size=(nx, nm, nm)) + 1j * rng.normal(size=(nx, nm, nm))
+    intensity, hw = 1e9, 1.5
+    ref = ogw.ephoton_sigma(M, GL, GG, nop, ogw.PHOTON_PRE_FACT, intensity, hw)
+    got = gw.ephoton_sigma(ctx, gw.to_dev(M), gw.to_dev(GL), gw.to_dev(GG), nop, intensity, hw,
+                           precision=precision)
+    for g, r in zip(got, ref):
+        np.testing.assert_allclose(gw.from_dev(g), r, rtol=0, atol=tol * np.abs(r).max())
+    lo, hi = 8, 16  # an inner shard: its halo is the neighbours' energies
+    got = gw.ephoton_sigma(ctx, gw.to_dev(M), gw.to_dev(GL[lo - nop:hi + nop]),
+                           gw.to_dev(GG[lo - nop:hi + nop]), nop, intensity, hw, halo=True,
+                           precision=precision)
+    for g, r in zip(got, ref):
+        np.testing.assert_allclose(gw.from_dev(g), r[lo:hi], rtol=0, atol=tol * np.abs(r).max())
+    assert not gw.from_dev(got[0]).real.any()  # Sigma^R is purely imaginary

@@ -35,11 +35,14 @@ def test_cnt_spectrum_files(ctx, cnt, tmp_path):
         # layout, cell positions and energies are identical text
         assert [l == "" for l in mr] == [l == "" for l in rr]
         assert all(a[:36] == b[:36] for a, b in zip(mr, rr))
-        # values: the printed digits, except the reference's round-off columns
+        # values: printed digits against printed digits, so a value on a rounding boundary
+        # may differ by one unit in the last digit; the reference's round-off columns skipped
         for col in (2, 3):
             if name != "ldos" and col == 2:
                 continue  # Re Tr G^< / G^> is round-off noise in the reference
-            ok = printed_match(mv[:, col], rv[:, col], full=rv[:, col])
+            ok = printed_match(mv[:, col], rv[:, col], full=rv[:, col], units=1.01)
             assert ok.all(), (name, col, np.argwhere(~ok)[:5])
-        same = np.mean([a == b for a, b in zip(mr, rr) if b])
-        assert same > (0.97 if name == "ldos" else 0.6), (name, same)
+        # records identical as text, over the columns that carry data
+        keep = (lambda l: l) if name == "ldos" else (lambda l: l[:36] + l[54:])
+        same = np.mean([keep(a) == keep(b) for a, b in zip(mr, rr) if b])
+        assert same > 0.97, (name, same)
