@@ -19,6 +19,11 @@ Reported (one JSON line on rank 0):
 
 ``--impl reference`` times the CPU restatement (the reference's Fortran
 cannot be built on this machine or the GPU machine: no Fortran compiler).
+
+``--workload uneven`` measures the uneven-block configuration instead: a
+4000-atom random tight-binding graph sliced into 25 slabs of 134-184 orbitals,
+2048 energies x 8 k-points, every block above one 128-row tile of the split
+product (the tiled products and block inverses), through qt_rgf_solve_vb.
 """
 from __future__ import annotations
 
@@ -59,6 +64,8 @@ def parse():
     ap.add_argument("--scba-size", default="10,16,256",
                     help="slabs,orbitals,energies of the GW-SCBA device family")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="batched", choices=["batched", "uneven"],
+                    help="batched: 100 x 128 slabs (the headline); uneven: the 4000-atom graph")
     return ap.parse_args()
 
 
@@ -274,6 +281,7 @@ def run_ours(a):
     ctx.profile_read()  # drop warm-up entries
     ctx.profile(True)
     n0 = rgf.kernel_launches()
+    ctx.inverse_fallbacks(reset=True)
     barrier()
     torch.cuda.synchronize()
     clocks.start()
@@ -319,7 +327,8 @@ def run_ours(a):
             "scaling": "weak", "vs_baseline": None, "dtype": "bf16-digit split (c64 sweep, "
             "FP64-grade c128 leads)", "data": "synthetic (seeded, no dataset)",
             "config": config_dict(a, {"parallelism": f"points sharded over {world} GPU(s)",
-                                      "points_bad_status": status_bad}),
+                                      "points_bad_status": status_bad,
+                                      "inverses_redone_fp64": ctx.inverse_fallbacks()}),
             "roofline": roofline, "clocks": clk, "gpu_launches": launches}
 
     if rank == 0 and a.fp64_energies > 0:
@@ -408,10 +417,147 @@ def run_ours(a):
         dist.destroy_process_group()
 
 
+def run_uneven(a):
+    """The uneven-block workload on one GPU: one step = ``--batch-energies`` energies x 8 k
+    of the 4000-atom graph device through the variable-block sweep (complex64 split path),
+    plus FP64 and complex128-split samples of the same points for the T(E) error."""
+    import torch
+    from quantum_transport_gb300.build import build
+    build()
+    from quantum_transport_gb300 import rgf
+    from quantum_transport_gb300.devices import config_uneven
+    d = config_uneven()
+    nk, nEg = len(d.kpts), len(d.E)
+    sizes = np.array(d.sizes, dtype=np.int32)
+    hii, hoff, _ = rgf.pack_blocks(d.Hii, nk)
+    h1i, h1off, _ = rgf.pack_blocks(d.H1i, nk)
+    Hd, H1d = torch.from_numpy(hii).cuda(), torch.from_numpy(h1i).cuda()
+    E = torch.from_numpy(d.E).cuda()
+    ctx = rgf.Context(0)
+    B = a.batch_energies
+    P = B * nk
+    dsum = int(sizes.sum())
+
+    def outputs(p):
+        return {"T": torch.zeros(p, dtype=torch.float64, device="cuda"),
+                "tr": torch.zeros(p, dtype=torch.float64, device="cuda"),
+                "tre": torch.zeros(p, dtype=torch.float64, device="cuda"),
+                "diag_gr": torch.zeros(p * dsum, dtype=torch.complex128, device="cuda"),
+                "diag_gl": torch.zeros(p * dsum, dtype=torch.complex128, device="cuda"),
+                "status": torch.zeros(p, dtype=torch.int32, device="cuda")}
+    out = outputs(P)
+    kw = dict(mul=0.1, mur=-0.1, templ=300.0, tempr=300.0, sancho_tol=1e-10,
+              sancho_max_iter=100, caroli=True)
+    nblk = nEg // B
+
+    def step(i, precision="mixed", o=out, nE=B, e0=None):
+        e0 = (i % nblk) * B if e0 is None else e0
+        rgf.rgf_variableblock_device(ctx, sizes, Hd, hoff, H1d, h1off, nk, E[e0:], nE, o,
+                                     precision=precision, **kw)
+
+    for i in range(a.warmup):
+        step(i)
+    ctx.sync()
+    stream = torch.cuda.current_stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = Clocks(0)
+    ctx.profile_read()
+    ctx.profile(True)
+    n0 = rgf.kernel_launches()
+    ctx.inverse_fallbacks(reset=True)
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0.record(stream)
+    for i in range(a.steps):
+        step(a.warmup + i)
+    ev1.record(stream)
+    ev1.synchronize()
+    ctx.sync()
+    clk = clocks.stop()
+    launches = rgf.kernel_launches() - n0
+    ctx.profile(False)
+    prof = ctx.profile_read()
+    ms = ev0.elapsed_time(ev1) / a.steps
+    value = P / (ms / 1e3)
+    flops = sum(120.0 * float(n) ** 3 for n in sizes)  # F_RGF per point, sum over slabs
+    tot_ms = sum(v[1] for v in prof.values()) or 1.0
+    dom = prof.get("zgemm_oz_c64", (0, 0.0, 0.0, 0.0))
+    pk, pk_kind = peaks()
+    peak = pk.get("bf16_tflops_sustained", pk.get("bf16_tflops"))
+    alg_tf = dom[2] / (dom[1] / 1e3) / 1e12 if dom[1] else 0.0
+    line = {"metric": METRIC, "value": value, "unit": "E-points/s", "n_gpus": 1,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16-digit split (c64 sweep, FP64-grade c128 leads)",
+            "data": "synthetic (seeded random graph, no dataset)",
+            "config": {"workload": f"uneven-block RGF, 4000-atom random graph in a 60 x 6 x 6 "
+                                   f"A box sliced into {len(sizes)} slabs of {sizes.min()}-"
+                                   f"{sizes.max()} orbitals, {nk} k x {nEg} E",
+                       "points_per_step": P, "rgf_flop_per_point": flops,
+                       "algorithmic_tflops": value * flops / 1e12,
+                       "l2": "inputs and scratch per step exceed L2 (129 MB)",
+                       "points_bad_status": int((out["status"] != 0).sum().item()),
+                       "inverses_redone_fp64": ctx.inverse_fallbacks()},
+            "roofline": {"kernel": "zgemm_oz_kernel (complex64 split product, 128-row tiles)",
+                         "bound": "tensor", "achieved": alg_tf, "peak": peak, "unit": "TFLOP/s",
+                         "frac": alg_tf / peak if peak else None, "traffic": None,
+                         "peak_source": f"bf16_tflops_sustained of {pk_kind}",
+                         "launches": dom[0],
+                         "time_share": {k: round(v[1] / tot_ms, 4) for k, v in prof.items()}},
+            "clocks": clk, "gpu_launches": launches}
+    # FP64 and complex128-split samples of the first points, and their T(E) errors
+    samples = {}
+    for prec, ne in (("fp64", a.fp64_energies), ("mixed-fp64", a.hi_energies)):
+        if ne <= 0:
+            continue
+        o = outputs(ne * nk)
+        step(0, prec, o, 1, e0=0)  # first-call set-up
+        ctx.sync()
+        t0 = time.perf_counter()
+        step(0, prec, o, ne, e0=0)
+        ctx.sync()
+        samples[prec] = (o, ne * nk / (time.perf_counter() - t0))
+    om = outputs(P)
+    step(0, "mixed", om, B, e0=0)
+    ctx.sync()
+    Tm = om["T"].cpu().numpy()
+    if "fp64" in samples:
+        T64 = samples["fp64"][0]["T"].cpu().numpy()
+        m = T64.size
+        line["fp64_gpu"] = {"value": samples["fp64"][1], "unit": "E-points/s",
+                            "sample_points": m,
+                            "speedup_split_vs_fp64": value / samples["fp64"][1],
+                            "T_rel_err_max_vs_peak": float(np.abs(Tm[:m] - T64).max() /
+                                                           np.abs(T64).max())}
+        if "mixed-fp64" in samples:
+            Th = samples["mixed-fp64"][0]["T"].cpu().numpy()
+            k = min(m, Th.size)
+            line["fp64_gpu"]["mixed_fp64"] = {
+                "value": samples["mixed-fp64"][1], "unit": "E-points/s",
+                "sample_points": Th.size,
+                "T_rel_err_max_vs_peak": float(np.abs(Th[:k] - T64[:k]).max() /
+                                               np.abs(T64[:k]).max())}
+    if not a.no_e2e:
+        r = rgf.rgf_variableblock_forward(ctx, d.Hii, d.H1i, d.E[:B], nk=nk, precision="mixed",
+                                          **kw)  # first call
+        t0 = time.perf_counter()
+        r = rgf.rgf_variableblock_forward(ctx, d.Hii, d.H1i, d.E[B:2 * B], nk=nk,
+                                          precision="mixed", **kw)
+        te = time.perf_counter() - t0
+        line["e2e"] = {"value": P / te, "unit": "E-points/s",
+                       "h2d_bytes_per_step": int(hii.nbytes + h1i.nbytes + B * 8),
+                       "d2h_bytes_per_step": int(P * (3 * 8 + 4 + 8) + 3 * P * dsum * 16),
+                       "steps": 1, "points_bad_status": int((r["status"] != 0).sum())}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "uneven":
+        run_uneven(a)
     else:
         run_ours(a)
 

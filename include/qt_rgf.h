@@ -101,6 +101,13 @@ int64_t qt_kernel_launches(void);
 qt_status qt_ctx_profile(qt_ctx* ctx, int enable);
 qt_status qt_ctx_profile_read(qt_ctx* ctx, int kind, int64_t* launches, double* ms,
                               double* alg_flops, double* tensor_flops);
+
+/* Instrumentation: how many block inverses the split path redid in FP64.  Each
+ * split-path inverse starts from an FP32 elimination and refines it; when the first
+ * residual I - A X is too large for the refinement to reach storage precision (an
+ * ill-conditioned block), the entry is eliminated again in FP64.  reset != 0 zeroes
+ * the counter after reading.                                                  */
+qt_status qt_ctx_inverse_fallbacks(qt_ctx* ctx, int64_t* count, int reset);
 qt_status qt_ctx_stream(qt_ctx* ctx, void** stream);
 
 /* Block-tridiagonal device of nx slabs of constant block size nm at nk

