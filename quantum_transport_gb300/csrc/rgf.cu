@@ -14,7 +14,7 @@
 //   3. forward sweep  g_l, g^<_l (src/cuda_rgf_mod.f90:140-188)
 //   4. right contact  G_NN, G^<_NN, tr (src/cuda_rgf_mod.f90:192-277)
 //   5. backward sweep G_l, G^<_l (src/cuda_rgf_mod.f90:283-381), with the
-//      minimal 8-product form (see the notes at the backward loop), and on
+//      7-product form (see the notes at the backward loop), and on
 //      request the bond currents (:293-318)
 //   6. left-contact current tre (src/cuda_rgf_mod.f90:387-407)
 //   7. optional Caroli T(E) from the left-connected chain G_{N1}.
@@ -154,13 +154,15 @@ __global__ void make_fermi_kernel(const double* E, long long p0, long long P, in
   }
 }
 
-__global__ void sancho_update_kernel(long long P, const double* err, double tol, int it,
-                                     unsigned char* active, int* iters, int* n_active) {
+__global__ void sancho_update_kernel(long long P, const double* err, const double* err2,
+                                     double tol, int it, unsigned char* active, int* iters,
+                                     int* n_active) {
   for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < P;
        b += (long long)gridDim.x * blockDim.x) {
     if (!active[b]) continue;
     iters[b] = it;
-    if (fabs(err[b]) < tol) active[b] = 0;
+    const double e = err2 ? fmax(fabs(err[b]), fabs(err2[b])) : fabs(err[b]);
+    if (e < tol) active[b] = 0;
     else atomicAdd(n_active, 1);
   }
 }
@@ -235,10 +237,12 @@ struct Ops {
   cd* fbw = nullptr;
   int* fallbacks = nullptr;
   double guard_tol() const {
-    // refinement diverges once ||R||_2 >= 1; ||R||_F >= ||R||_2, and 0.25 leaves margin.
-    // QT_GUARD_TOL overrides for accuracy studies.
+    // refinement diverges once ||R||_2 >= 1, and ||R||_F >= ||R||_2: with several steps
+    // to follow, 0.25 leaves margin; a single step (the complex64 sweep) only needs the
+    // divergent entries redone.  QT_GUARD_TOL overrides for accuracy studies.
     const char* v = getenv("QT_GUARD_TOL");
-    return v && *v ? atof(v) : 0.25;
+    if (v && *v) return atof(v);
+    return refine > 1 ? 0.25 : 1.0;
   }
 
   qt_status gemm(BatchRef A, int opA, BatchRef B, int opB, BatchRef C, long long batch,
@@ -476,16 +480,25 @@ size_t wave_bytes(const Problem& pb, long long P) {
 // Batched Sancho-Rubio on the wave (complex128 state).  H00 per point, H_10 the
 // decimation's coupling argument (dag_in: it is H10in^+, the left lead,
 // src/cuda_rgf_mod.f90:101).  G00 = (zS - H_SS)^-1, GBB = (zS - H_BB)^-1.
+//
+// With G00b set, the same run also yields the surface Green's function of the chain
+// that extends the other way (the dual surface): H_S'S' accumulates H_10 A H_01, the
+// term H_BB already receives, and the run stops when both couplings are below tol.  A
+// lead pair that is one chain (equal on-site blocks and couplings, the right lead
+// called with H10 where the left is called with H10^+) costs one decimation, not two.
 qt_status sancho_wave(const Ops<double2>& op0, Arena& ar, long long P, BatchRef H00,
                       BatchRef H10in, bool dag_in, const cd* zlead, double tol, int max_iter,
-                      BatchRef G00, BatchRef GBB, int* status, int* iters_out, int iters_stride) {
+                      BatchRef G00, BatchRef GBB, int* status, int* iters_out, int iters_stride,
+                      BatchRef G00b = nullref()) {
   Ops<double2> op = op0;
   const int n = op.n;
   const long long nm2 = (long long)n * n;
   cudaStream_t s = op.s;
   const size_t mark = ar.off;  // the Sancho state is released on return
-  cd* buf = ar.take<cd>((size_t)7 * P * nm2);
+  const bool dual = G00b.p != nullptr;
+  cd* buf = ar.take<cd>((size_t)(dual ? 8 : 7) * P * nm2);
   double* err = ar.take<double>(P);
+  double* err2 = dual ? ar.take<double>(P) : nullptr;
   unsigned char* active = ar.take<unsigned char>(P);
   int* iters = ar.take<int>(P);
   int* nact = ar.take<int>(1);
@@ -496,14 +509,17 @@ qt_status sancho_wave(const Ops<double2>& op0, Arena& ar, long long P, BatchRef 
     op.P = P;
     if (!op.rt1 || !op.rt2) QT_FAIL(QT_ERR_NOMEM, "wave arena exhausted (sancho refinement)");
   }
-  if (!buf || !err || !active || !iters || !nact) QT_FAIL(QT_ERR_NOMEM, "wave arena exhausted (sancho)");
+  if (!buf || !err || !active || !iters || !nact || (dual && !err2))
+    QT_FAIL(QT_ERR_NOMEM, "wave arena exhausted (sancho)");
   BatchRef HBB = ref(buf + 0 * P * nm2, nm2, n), HSS = ref(buf + 1 * P * nm2, nm2, n);
   BatchRef H10 = ref(buf + 2 * P * nm2, nm2, n), H01 = ref(buf + 3 * P * nm2, nm2, n);
   BatchRef A = ref(buf + 4 * P * nm2, nm2, n), B = ref(buf + 5 * P * nm2, nm2, n);
   BatchRef C = ref(buf + 6 * P * nm2, nm2, n);
+  const BatchRef HSS2 = dual ? ref(buf + 7 * P * nm2, nm2, n) : nullref();
   const BatchRef Zl = ref(zlead, 1, 1);
   qt::zcopy<double2>(n, P, H00, HBB, s);
   qt::zcopy<double2>(n, P, H00, HSS, s);
+  if (dual) qt::zcopy<double2>(n, P, H00, HSS2, s);
   if (dag_in) {
     qt::zdagger<double2>(n, P, H10in, H10, s);
     qt::zcopy<double2>(n, P, H10in, H01, s);
@@ -529,12 +545,14 @@ qt_status sancho_wave(const Ops<double2>& op0, Arena& ar, long long P, BatchRef 
     QT_TRY(op.gemm(H10, qt::OP_N, B, qt::OP_N, A, P, one, nullref(), {0, 0}, nullref(), active));
     std::swap(H10, C);
     qt::zaxpby<double2>(n, P, HBB, 1, 0, A, 1, 0, nullref(), HBB, active, s);
+    if (dual) qt::zaxpby<double2>(n, P, HSS2, 1, 0, A, 1, 0, nullref(), HSS2, active, s);
     // H_01 = H_01 B ; error = sum |H_01|            (:712-726)
     QT_TRY(op.gemm(H01, qt::OP_N, B, qt::OP_N, C, P, one, nullref(), {0, 0}, nullref(), active));
     std::swap(H01, C);
     qt::zabssum<double2>(n, P, H01, err, active, s);
+    if (dual) qt::zabssum<double2>(n, P, H10, err2, active, s);  // the dual run's H_01
     cudaMemsetAsync(nact, 0, sizeof(int), s);
-    sancho_update_kernel<<<g1d(P), 256, 0, s>>>(P, err, tol, it, active, iters, nact);
+    sancho_update_kernel<<<g1d(P), 256, 0, s>>>(P, err, err2, tol, it, active, iters, nact);
     qt::count_launch();
     if ((it % 4) == 0 || it == max_iter) {
       int h = 0;
@@ -549,6 +567,10 @@ qt_status sancho_wave(const Ops<double2>& op0, Arena& ar, long long P, BatchRef 
   // G00 = (z S - H_SS)^-1 ; GBB = (z S - H_BB)^-1    (:740-761)
   qt::zaxpby<double2>(n, P, HSS, -1, 0, nullref(), 0, 0, Zl, C, nullptr, s);
   QT_TRY(op.inv(C, G00, P, status));
+  if (dual) {
+    qt::zaxpby<double2>(n, P, HSS2, -1, 0, nullref(), 0, 0, Zl, C, nullptr, s);
+    QT_TRY(op.inv(C, G00b, P, status));
+  }
   if (GBB.p) {
     qt::zaxpby<double2>(n, P, HBB, -1, 0, nullref(), 0, 0, Zl, C, nullptr, s);
     QT_TRY(op.inv(C, GBB, P, status));
@@ -683,14 +705,33 @@ qt_status solve_wave(qt_ctx* ctx, const Problem& pb, long long p0, long long P, 
   auto OUTB = [&](cd* base, int l) { return ref(base + (p0 * nx + l) * nm2, nx * nm2, n); };
   const BatchRef Zi = ref(zint, 1, 1);
   const cd one_c{1, 0}, mone{-1, 0};
-  const BatchRef SigL = T(13), Pch = T(12);
+  const BatchRef SigL = T(13);
+  BatchRef Pch = T(12), Pnext = T(11);  // Caroli chain P_l, ping-pong
   const bool caroli = (pb.flags & QT_FLAG_CAROLI) && pb.T;
 
   // ---------------- both leads' decimations as one batched wave of 2P entries:
   // [0, P) the left lead, called with H10^+ (src/cuda_rgf_mod.f90:90-134), and
   // [P, 2P) the right lead (:192-277); surface Green's functions into C8(4), C8(5)
   const int N = nx - 1;
-  {
+  // both leads are one chain when every slab shares H_ii and H1i and no scattering
+  // self-energy touches them: one decimation gives both surfaces
+  const bool one_chain = pb.hl == 0 && pb.h1l == 0 && !pb.sigr;
+  if (one_chain) {
+    const size_t mark = ar.off;
+    qt::zcopy<double2>(n, P, HII8(0), C8(0), s);
+    qt::zdagger<double2>(n, P, H1I8(0), C8(2), s);
+    int* it1 = ar.take<int>(P);
+    if (!it1) QT_FAIL(QT_ERR_NOMEM, "wave arena exhausted (leads)");
+    QT_TRY(sancho_wave(cop, ar, P, C8(0), C8(2), false, zlead, pb.c.sancho_tol,
+                       pb.c.sancho_max_iter, C8(4), nullref(), status, it1, 1, C8(5)));
+    if (pb.iters) {
+      cudaMemcpy2DAsync(pb.iters + p0 * 2, 2 * sizeof(int), it1, sizeof(int), sizeof(int), P,
+                        cudaMemcpyDeviceToDevice, s);
+      cudaMemcpy2DAsync(pb.iters + p0 * 2 + 1, 2 * sizeof(int), it1, sizeof(int), sizeof(int),
+                        P, cudaMemcpyDeviceToDevice, s);
+    }
+    ar.off = mark;
+  } else {
     const size_t mark = ar.off;
     cd* z2 = ar.take<cd>(2 * P);
     int* st2 = ar.take<int>(2 * P);
@@ -745,14 +786,28 @@ qt_status solve_wave(qt_ctx* ctx, const Problem& pb, long long p0, long long P, 
       QT_TRY(op.gemm(T(0), qt::OP_N, H10, qt::OP_C, T(1), P, mone, HII(l), mone, Zi));
     }
     QT_TRY(op.inv(T(1), GL(l), P, status));
-    // g^<_l = g (H10 g^<_{l-1} H10^+ + sigma_lesser_ph S) g^+
-    QT_TRY(op.gemm(H10, qt::OP_N, GLN(l - 1), qt::OP_N, T(0), P));
-    QT_TRY(op.gemm(T(0), qt::OP_N, H10, qt::OP_C, T(1), P, one_c, SIGL(l), one_c));
-    QT_TRY(op.gemm(GL(l), qt::OP_N, T(1), qt::OP_N, T(0), P));
-    QT_TRY(op.gemm(T(0), qt::OP_N, GL(l), qt::OP_C, GLN(l), P));
-    if (caroli) {  // P_l = g_l H_{l,l-1} P_{l-1}
-      QT_TRY(op.gemm(H10, qt::OP_N, Pch, qt::OP_N, T(0), P));
-      QT_TRY(op.gemm(GL(l), qt::OP_N, T(0), qt::OP_N, Pch, P));
+    if (!pb.sigl) {
+      // ballistic: g^<_l = M g^<_{l-1} M^+ and P_l = M P_{l-1} with M = g_l H_{l,l-1}
+      // (4 block products where the general form below takes 6)
+      const BatchRef M = T(1);
+      QT_TRY(op.gemm(GL(l), qt::OP_N, H10, qt::OP_N, M, P));
+      QT_TRY(op.gemm(GLN(l - 1), qt::OP_N, M, qt::OP_C, T(0), P));
+      QT_TRY(op.gemm(M, qt::OP_N, T(0), qt::OP_N, GLN(l), P));
+      if (caroli) {
+        QT_TRY(op.gemm(M, qt::OP_N, Pch, qt::OP_N, Pnext, P));
+        std::swap(Pch, Pnext);
+      }
+    } else {
+      // g^<_l = g (H10 g^<_{l-1} H10^+ + sigma_lesser_ph S) g^+
+      QT_TRY(op.gemm(H10, qt::OP_N, GLN(l - 1), qt::OP_N, T(0), P));
+      QT_TRY(op.gemm(T(0), qt::OP_N, H10, qt::OP_C, T(1), P, one_c, SIGL(l), one_c));
+      QT_TRY(op.gemm(GL(l), qt::OP_N, T(1), qt::OP_N, T(0), P));
+      QT_TRY(op.gemm(T(0), qt::OP_N, GL(l), qt::OP_C, GLN(l), P));
+      if (caroli) {  // P_l = g_l H_{l,l-1} P_{l-1}
+        QT_TRY(op.gemm(H10, qt::OP_N, Pch, qt::OP_N, T(0), P));
+        QT_TRY(op.gemm(GL(l), qt::OP_N, T(0), qt::OP_N, Pnext, P));
+        std::swap(Pch, Pnext);
+      }
     }
   }
 
@@ -817,20 +872,20 @@ qt_status solve_wave(qt_ctx* ctx, const Problem& pb, long long p0, long long P, 
                       (size_t)nm2 * sizeof(cd), P, s);
 
   // ---------------- backward sweep (src/cuda_rgf_mod.f90:283-381)
-  //   X = g H^+ ; GN0 = X G_{l+1} ; G_l = g + GN0 (H g)
-  //   G^<_l = g^< + X G^<_{l+1} X^+ + W - W^+ ,  W = (GN0 H) g^<
+  //   X = g H^+ ; GN0 = X G_{l+1} ; Y = GN0 H ; G_l = g + Y g
+  //   G^<_l = g^< + X G^<_{l+1} X^+ + W - W^+ ,  W = Y g^<
   // The reference's fourth term g^< H^+ GN0^+ (:346-348) equals -W^+ because
-  // g^< is anti-Hermitian, which saves two block products per slab.
+  // g^< is anti-Hermitian, and GN0 (H g) = (GN0 H) g shares Y with W: 7 block
+  // products per slab where the reference forms 30.
   for (int l = N - 1; l >= 0; --l) {
     const BatchRef Hc = (q & QT_QUIRK_BACK_H1I_NEXT) ? H1I(l + 1) : H1I(l);
     const BatchRef X = T(0), GN0 = T(1), Y = T(2), T1 = T(5), W = T(10);
     QT_TRY(op.gemm(GL(l), qt::OP_N, Hc, qt::OP_C, X, P));
     QT_TRY(op.gemm(X, qt::OP_N, Gcur, qt::OP_N, GN0, P));
-    QT_TRY(op.gemm(Hc, qt::OP_N, GL(l), qt::OP_N, Y, P));
-    QT_TRY(op.gemm(GN0, qt::OP_N, Y, qt::OP_N, Gnew, P, one_c, GL(l), one_c));
+    QT_TRY(op.gemm(GN0, qt::OP_N, Hc, qt::OP_N, Y, P));
+    QT_TRY(op.gemm(Y, qt::OP_N, GL(l), qt::OP_N, Gnew, P, one_c, GL(l), one_c));
     QT_TRY(op.gemm(X, qt::OP_N, Gncur, qt::OP_N, T1, P));
     QT_TRY(op.gemm(T1, qt::OP_N, X, qt::OP_C, Gnnew, P, one_c, GLN(l), one_c));
-    QT_TRY(op.gemm(GN0, qt::OP_N, Hc, qt::OP_N, Y, P));
     QT_TRY(op.gemm(Y, qt::OP_N, GLN(l), qt::OP_N, W, P));
     qt::zantiherm<TC>(n, P, W, 1, 0, Gnnew, Gnnew, s);
     if (pb.bond || pb.Jd) {
@@ -1016,7 +1071,8 @@ qt_status solve_wave_vb(qt_ctx* ctx, const ProblemVB& pb, long long p0, long lon
     QT_TRY(cop.gemm3(n0, n0, n0, H1I8(0), qt::OP_N, C8(1, n0), qt::OP_N, C8(2, n0), P));
     QT_TRY(cop.gemm3(n0, n0, n0, C8(2, n0), qt::OP_N, H1I8(0), qt::OP_C, C8(3, n0), P));
   }
-  const BatchRef SigL = T(13, n0), Pch = T(12, nm);
+  const BatchRef SigL = T(13, n0);
+  int pc = 12;  // temporary holding the Caroli chain P_l (ping-pongs with 11)
   zconvert_or_copy<TC>(n0, P, C8(3, n0), SigL, s);
   qt::zaxpby<TC>(n0, P, HII(0), -1, 0, SigL, -1, 0, Zi, T(3, n0), nullptr, s);
   QT_TRY(op.inv(T(3, n0), GL(0), P, status, nullptr, n0));
@@ -1035,15 +1091,14 @@ qt_status solve_wave_vb(qt_ctx* ctx, const ProblemVB& pb, long long p0, long lon
     QT_TRY(op.gemm3(nl, nl, np, T(0, nl), qt::OP_N, H10, qt::OP_C, T(1, nl), P, mone, HII(l),
                     mone, Zi));
     QT_TRY(op.inv(T(1, nl), GL(l), P, status, nullptr, nl));
-    QT_TRY(op.gemm3(nl, np, np, H10, qt::OP_N, GLN(l - 1), qt::OP_N, T(0, nl), P));
-    QT_TRY(op.gemm3(nl, nl, np, T(0, nl), qt::OP_N, H10, qt::OP_C, T(1, nl), P));
-    QT_TRY(op.gemm3(nl, nl, nl, GL(l), qt::OP_N, T(1, nl), qt::OP_N, T(0, nl), P));
-    QT_TRY(op.gemm3(nl, nl, nl, T(0, nl), qt::OP_N, GL(l), qt::OP_C, GLN(l), P));
-    if (caroli) {  // P_l = g_l H_{l,l-1} P_{l-1}
-      QT_TRY(op.gemm3(nl, n0, np, H10, qt::OP_N, ref(tmp + (size_t)12 * P * m2, m2, np),
-                      qt::OP_N, T(0, nl), P));
-      QT_TRY(op.gemm3(nl, n0, nl, GL(l), qt::OP_N, T(0, nl), qt::OP_N,
-                      ref(tmp + (size_t)12 * P * m2, m2, nl), P));
+    // g^<_l = M g^<_{l-1} M^+ and P_l = M P_{l-1} with M = g_l H_{l,l-1} (n_l x n_{l-1})
+    QT_TRY(op.gemm3(nl, np, nl, GL(l), qt::OP_N, H10, qt::OP_N, T(1, nl), P));
+    QT_TRY(op.gemm3(np, nl, np, GLN(l - 1), qt::OP_N, T(1, nl), qt::OP_C, T(0, np), P));
+    QT_TRY(op.gemm3(nl, nl, np, T(1, nl), qt::OP_N, T(0, np), qt::OP_N, GLN(l), P));
+    if (caroli) {  // the chain ping-pongs between temporaries 12 and 11
+      QT_TRY(op.gemm3(nl, n0, np, T(1, nl), qt::OP_N, ref(tmp + (size_t)pc * P * m2, m2, np),
+                      qt::OP_N, ref(tmp + (size_t)(23 - pc) * P * m2, m2, nl), P));
+      pc = 23 - pc;
     }
   }
 
@@ -1078,7 +1133,7 @@ qt_status solve_wave_vb(qt_ctx* ctx, const ProblemVB& pb, long long p0, long lon
   if (pb.tr) qt::ztrace_current<TC>(nN, P, SigR, T(8, nN), T(ign, nN), tr_sign, fr, pb.tr + p0, s);
   if (caroli) {
     // G_N1 = G_NN H_{N,N-1} P_{N-1} (n_N x n_0); T = -Re Tr[Gam'_R G_N1 Gam'_L G_N1^+]
-    QT_TRY(op.gemm3(nN, n0, np, Hd, qt::OP_N, ref(tmp + (size_t)12 * P * m2, m2, np), qt::OP_N,
+    QT_TRY(op.gemm3(nN, n0, np, Hd, qt::OP_N, ref(tmp + (size_t)pc * P * m2, m2, np), qt::OP_N,
                     T(0, nN), P));
     QT_TRY(op.gemm3(nN, n0, nN, T(ig, nN), qt::OP_N, T(0, nN), qt::OP_N, T(10, nN), P));
     qt::zantiherm<TC>(n0, P, SigL, -1, 0, nullref(), T(5, n0), s);
@@ -1092,17 +1147,16 @@ qt_status solve_wave_vb(qt_ctx* ctx, const ProblemVB& pb, long long p0, long lon
   for (int l = N - 1; l >= 0; --l) {
     const int nl = n[l], nq = n[l + 1];
     const BatchRef Hc = H1I(l + 1);
-    // X = g H^+ (nl x nq); GN0 = X G_{l+1}; Y = H g (nq x nl); G_l = g + GN0 Y
+    // X = g H^+ (nl x nq); GN0 = X G_{l+1}; Y = GN0 H (nl x nl); G_l = g + Y g
     QT_TRY(op.gemm3(nl, nq, nl, GL(l), qt::OP_N, Hc, qt::OP_C, T(0, nl), P));
     QT_TRY(op.gemm3(nl, nq, nq, T(0, nl), qt::OP_N, T(ig, nq), qt::OP_N, T(1, nl), P));
-    QT_TRY(op.gemm3(nq, nl, nl, Hc, qt::OP_N, GL(l), qt::OP_N, T(2, nq), P));
-    QT_TRY(op.gemm3(nl, nl, nq, T(1, nl), qt::OP_N, T(2, nq), qt::OP_N, T(inew, nl), P, one_c,
+    QT_TRY(op.gemm3(nl, nl, nq, T(1, nl), qt::OP_N, Hc, qt::OP_N, T(2, nl), P));
+    QT_TRY(op.gemm3(nl, nl, nl, T(2, nl), qt::OP_N, GL(l), qt::OP_N, T(inew, nl), P, one_c,
                     GL(l), one_c));
-    // G^<_l = g^< + X G^<_{l+1} X^+ + W - W^+,  W = (GN0 H) g^<
+    // G^<_l = g^< + X G^<_{l+1} X^+ + W - W^+,  W = Y g^<
     QT_TRY(op.gemm3(nl, nq, nq, T(0, nl), qt::OP_N, T(ign, nq), qt::OP_N, T(5, nl), P));
     QT_TRY(op.gemm3(nl, nl, nq, T(5, nl), qt::OP_N, T(0, nl), qt::OP_C, T(innew, nl), P, one_c,
                     GLN(l), one_c));
-    QT_TRY(op.gemm3(nl, nl, nq, T(1, nl), qt::OP_N, Hc, qt::OP_N, T(2, nl), P));
     QT_TRY(op.gemm3(nl, nl, nl, T(2, nl), qt::OP_N, GLN(l), qt::OP_N, T(10, nl), P));
     qt::zantiherm<TC>(nl, P, T(10, nl), 1, 0, T(innew, nl), T(innew, nl), s);
     if (pb.bond) {

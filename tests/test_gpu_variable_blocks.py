@@ -75,7 +75,9 @@ def test_split_paths_match_fp64(ctx, precision, tol):
 
 def test_equal_blocks_match_constblocksize(ctx):
     """With equal blocks and slab-independent couplings the variable-block path is the
-    constant-block sweep with the CPU routine's conventions."""
+    constant-block sweep with the CPU routine's conventions.  The constant-block sweep
+    decimates its two equal leads in one dual-surface run (the variable-block path runs
+    two), which changes the rounding order only."""
     rng = np.random.default_rng(8)
     n, nx = 12, 6
     X = 0.1 * (rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n)))
@@ -89,6 +91,6 @@ def test_equal_blocks_match_constblocksize(ctx):
     b = rgf.rgf_variableblock_forward(ctx, [H00] * nx, [H10] * (nx + 1), E,
                                       quirks=rgf._lib.QT_QUIRK_CPU_FERMI, **kw)
     for key in ("T", "tr", "tre"):
-        np.testing.assert_allclose(b[key], a[key], rtol=1e-12, atol=1e-14)
+        np.testing.assert_allclose(b[key], a[key], rtol=1e-10, atol=1e-13)
     for l in range(nx):
-        np.testing.assert_allclose(b["diag_gr"][l], a["diag_gr"][:, :, l], rtol=1e-12, atol=1e-14)
+        np.testing.assert_allclose(b["diag_gr"][l], a["diag_gr"][:, :, l], rtol=1e-10, atol=1e-13)
