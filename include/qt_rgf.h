@@ -25,7 +25,7 @@ typedef enum {
   QT_ERR_ARG = 1,         /* invalid argument (sizes, null pointers)             */
   QT_ERR_CUDA = 2,        /* CUDA runtime error; see qt_last_error()             */
   QT_ERR_NOMEM = 3,       /* device allocation failed                           */
-  QT_ERR_UNSUPPORTED = 4, /* configuration not supported (e.g. nm > 128 mixed)   */
+  QT_ERR_UNSUPPORTED = 4, /* configuration not supported (e.g. nm > 384 mixed)   */
   QT_ERR_POINTS = 5       /* finished, but at least one point has status != 0   */
 } qt_status;
 
@@ -48,6 +48,10 @@ typedef enum {
                         in the sweep, 7 in the leads, FP32 block LU + three
                         refinements.  FP64-grade results at tensor-core rate  */
 } qt_precision;
+/* Both split precisions take blocks up to 384 orbitals (above 128 the products are
+ * tiled and the inverses use the 2 x 2 block form).  A block whose FP32 elimination
+ * leaves a first residual too large for the refinement to converge is eliminated
+ * again in FP64 (see qt_ctx_inverse_fallbacks).                                 */
 
 #define QT_FLAG_DEVICE_POINTERS 1u /* all arrays are device pointers            */
 #define QT_FLAG_CAROLI 2u          /* also compute Caroli T(E) (qt_outputs.T)    */
@@ -202,7 +206,7 @@ qt_status qt_rgf_solve(qt_ctx* ctx, const qt_device* dev, const double* E, int n
  * right lead is decimated with H1i[nx] as in src/rgf_mod.f90:153.
  * Outputs: tr, tre, T [npts]; diag_gr / diag_gl / diag_gg packed
  * [npts][sum nm[l]] complex128; full blocks are not returned (must be NULL).
- * The split precisions need nm[l] <= 128.                                  */
+ * The split precisions need nm[l] <= 384 (blocks above 128 are tiled).     */
 typedef struct {
   int nx, nk;
   const int* nm;
