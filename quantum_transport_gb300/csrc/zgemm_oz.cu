@@ -13,18 +13,23 @@
 //      A' row i = (Re At[i,k], Im At[i,k])_k
 //      Cr: B' column j = (Re Bt[k,j], -Im Bt[k,j])_k    Ci: (Im Bt[k,j], Re Bt[k,j])_k
 //    so each complex element is loaded once per stage.  One CTA work item is one
-//    real part of one NT-column tile (M = 128 padded rows, K' = 2n);
+//    real part of one NT-column tile (M = 128 padded rows, K' = 2n).  For
+//    complex64 operands one item computes both parts: Ci = A'' B'_r with
+//    A'' row i = (Im At[i,k], -Re At[i,k])_k written from the same digits as A',
+//    so each operand is split once per item;
 //  * digits: every row i of A' is scaled by 2^-e_i (e_i: exponent bound of the
 //    row's largest entry, |entry| < 2^(e_i-1), from the prologue kernel) and
 //    written as S balanced base-256 digits D_s = d_s 2^(-8s), |d_s| <= 128 --
 //    each exactly representable in BF16.  Columns of B' likewise with f_j;
 //  * products: all digit pairs (s, t) with s + t <= L are issued; pair level
 //    l = s + t accumulates into TMEM accumulator min(l, NACC - 1), where the 512
-//    TMEM columns hold NACC = 512 / NT accumulators (4 for NT = 128, 8 for
-//    NT = 64).  A level-l partial sum is an integer multiple of 2^(-8l) below
-//    (l+1) 2^14 K' 2^(-8l), so levels l <= 3 are EXACT in FP32 for K' <= 256;
-//    a higher level on its own accumulator rounds at 2^(-24-8l) <= 2^-56 of
-//    the row/column scale;
+//    TMEM columns hold NACC = 512 / (NT x parts) accumulators (8 for the
+//    complex128 products with NT = 64; 2 per part for complex64 with both
+//    parts, levels 1-3 sharing the second).  A level-l partial sum is an integer
+//    multiple of 2^(-8l) below (l+1) 2^14 K' 2^(-8l), so levels l <= 3 are EXACT
+//    in FP32 for K' <= 256; a higher level on its own accumulator rounds at
+//    2^(-24-8l) <= 2^-56 of the row/column scale, and the shared complex64
+//    accumulator rounds at about 2^-32 per MMA, ~2^-28 of the result;
 //  * epilogue: the accumulators are summed in double-float FP32 arithmetic
 //    (TwoSum), scaled by 2^(e_i + f_j - 16), and written as FP32 (complex64
 //    output) or assembled into FP64 bits with integer operations (complex128
@@ -299,16 +304,25 @@ __global__ void __launch_bounds__(256) oz_scales_kernel(GemmArgs a) {
 template <int S, int L, int NT, typename TIn, typename TOut>
 __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmArgs a, int stages) {
   constexpr int NPROD = Roles<NT>::NPROD, MMA_WARP = Roles<NT>::MMA_WARP;
-  // NT output columns per CTA; the 512 TMEM columns hold 512/NT accumulators.  With
-  // NT = 64 every digit level up to 7 has its own (exact) accumulator.
-  constexpr int NACC_MAX = 512 / NT;
+  // Complex64 operands: one work item computes both real parts of C.  The imaginary
+  // part uses the real part's B' planes against a second A layout A'' = (Im A, -Re A),
+  // written from the same digits (negating a balanced digit is exact), so A and B are
+  // split once per item, not once per part.
+  constexpr bool BOTH = sizeof(TIn) == 8;
+  constexpr int NPARTS = BOTH ? 2 : 1;
+  // NT output columns per CTA; the 512 TMEM columns hold 512/NT accumulators, shared by
+  // the parts of an item.  With NT = 64 and one part every digit level up to 7 has its
+  // own (exact) accumulator; complex64 with both parts keeps level 0 exact and sums
+  // levels 1-3 in one FP32 accumulator (about 2^-28 of the result, below its 2^-24).
+  constexpr int NACC_MAX = 512 / (NT * NPARTS);
   constexpr int NACC = (L + 1 < NACC_MAX) ? L + 1 : NACC_MAX;
   constexpr int BPLANE = NT * KC * 2;  // one B digit plane of an NT-row tile
+  constexpr int APLANES = NPARTS;      // A digit layouts per stage
   constexpr int ITEMS = (512 + 4 * NT) / NPROD;  // (row, 8-K group) items per producer thread
   static_assert((512 + 4 * NT) % NPROD == 0, "item split");
   extern __shared__ __align__(1024) unsigned char smem[];
   // carve: [stages x (A planes | B planes)] [barriers] [tmem slot, abort flag]
-  const int stage_bytes = S * (PLANE_BYTES + BPLANE);
+  const int stage_bytes = S * (APLANES * PLANE_BYTES + BPLANE);
   unsigned char* tiles = smem;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + (size_t)stages * stage_bytes);
   uint64_t* full = bars;                 // [stages] producers -> MMA
@@ -324,8 +338,8 @@ __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmAr
   const int npad = (n + 15) & ~15;
   const int nch = (K + KC / 2 - 1) / (KC / 2);  // stages: KC real K = KC/2 complex k each
   const int ntile = (npad + NT - 1) / NT;  // column tiles per real part
-  // work item: (batch entry, real/imag part of C, column tile)
-  const long long nitems = 2LL * ntile * a.batch;
+  // work item: (batch entry, real/imag part of C unless BOTH, column tile)
+  const long long nitems = (BOTH ? 1LL : 2LL) * ntile * a.batch;
 
   if (tid == 0) {
     for (int s = 0; s < stages; ++s) { mbar_init(&full[s], NPROD); mbar_init(&empty[s], 1); }
@@ -348,8 +362,8 @@ __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmAr
     const int p = tid - 128;  // 0 .. NPROD-1
     uint32_t proc = 0, gchunk = 0;
     for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
-      const long long b = w / (2 * ntile);
-      const int part = (int)((w / ntile) & 1), ct = (int)(w % ntile);
+      const long long b = w / (NPARTS == 2 ? ntile : 2 * ntile);
+      const int part = BOTH ? 0 : (int)((w / ntile) & 1), ct = (int)(w % ntile);
       if (a.active && !a.active[b]) continue;
       // batch strides are in complex elements: address through the element type
       const void* A = batch_ptr<const TIn>(a.A, b);
@@ -366,7 +380,7 @@ __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmAr
         const uint32_t ph = (gchunk / stages) & 1;
         if (!mbar_wait(&empty[st], ph ^ 1, abort_flag)) break;
         unsigned char* stA = tiles + (size_t)st * stage_bytes;
-        unsigned char* stB = stA + S * PLANE_BYTES;
+        unsigned char* stB = stA + APLANES * S * PLANE_BYTES;
         const int kc0 = c * (KC / 2);  // complex k offset of this stage
         TIn xv[ITEMS][4];
 #pragma unroll
@@ -395,6 +409,7 @@ __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmAr
           const int rg = isA ? r : ct * NT + r;  // row of op(A) / column of op(B)
           const int e = isA ? erow[r] : (rg < n ? fcol[rg] : 0);
           uint32_t packed[S][4];
+          uint32_t packed2[BOTH ? S : 1][4];  // A'' = (Im, -Re) of A items (BOTH)
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
             float D0[S], D1[S];
@@ -423,6 +438,10 @@ __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmAr
             }
 #pragma unroll
             for (int s2 = 0; s2 < S; ++s2) packed[s2][u] = pack_bf16x2(D0[s2], D1[s2]);
+            if constexpr (BOTH) {
+#pragma unroll
+              for (int s2 = 0; s2 < S; ++s2) packed2[s2][u] = pack_bf16x2(D1[s2], -D0[s2]);
+            }
           }
           // canonical no-swizzle K-major: (r/8)*SBO + g*LBO + (r%8)*16
           const uint32_t off = (uint32_t)((r >> 3) * SBO + g * LBO + (r & 7) * 16);
@@ -432,6 +451,14 @@ __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmAr
           for (int s2 = 0; s2 < S; ++s2)
             *reinterpret_cast<uint4*>(base + (size_t)s2 * pstride + off) =
                 make_uint4(packed[s2][0], packed[s2][1], packed[s2][2], packed[s2][3]);
+          if constexpr (BOTH) {
+            if (isA) {
+#pragma unroll
+              for (int s2 = 0; s2 < S; ++s2)
+                *reinterpret_cast<uint4*>(base + (size_t)(S + s2) * PLANE_BYTES + off) =
+                    make_uint4(packed2[s2][0], packed2[s2][1], packed2[s2][2], packed2[s2][3]);
+            }
+          }
         }
         fence_proxy_async();
         mbar_arrive(&full[st]);
@@ -444,7 +471,7 @@ __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmAr
       const uint32_t idesc = make_idesc(128, NT);
       uint32_t proc = 0, gchunk = 0;
       for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
-        const long long b = w / (2 * ntile);
+        const long long b = w / (NPARTS == 2 ? ntile : 2 * ntile);
         if (a.active && !a.active[b]) continue;
         if (!mbar_wait(tmem_empty, (proc & 1) ^ 1, abort_flag)) break;
         tc_fence_after();
@@ -455,19 +482,22 @@ __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmAr
           if (!mbar_wait(&full[st], ph, abort_flag)) break;
           tc_fence_after();
           const uint32_t sA = smem_u32(tiles + (size_t)st * stage_bytes);
-          const uint32_t sB = sA + S * PLANE_BYTES;
+          const uint32_t sB = sA + APLANES * S * PLANE_BYTES;
 #pragma unroll
           for (int kk = 0; kk < KC / 16; ++kk) {
 #pragma unroll
-            for (int s = 0; s < S; ++s) {
+            for (int pp = 0; pp < NPARTS; ++pp) {
 #pragma unroll
-              for (int t = 0; t < S; ++t) {
-                if (s + t > L) continue;
-                const int acc = (s + t) < NACC - 1 ? (s + t) : NACC - 1;
-                const uint64_t ad = make_desc(sA + s * PLANE_BYTES + kk * 2 * LBO);
-                const uint64_t bd = make_desc(sB + t * BPLANE + kk * 2 * LBO);
-                umma(tmem + acc * NT, ad, bd, idesc, (touched >> acc) & 1);
-                touched |= 1u << acc;
+              for (int s = 0; s < S; ++s) {
+#pragma unroll
+                for (int t = 0; t < S; ++t) {
+                  if (s + t > L) continue;
+                  const int acc = pp * NACC + ((s + t) < NACC - 1 ? (s + t) : NACC - 1);
+                  const uint64_t ad = make_desc(sA + (pp * S + s) * PLANE_BYTES + kk * 2 * LBO);
+                  const uint64_t bd = make_desc(sB + t * BPLANE + kk * 2 * LBO);
+                  umma(tmem + acc * NT, ad, bd, idesc, (touched >> acc) & 1);
+                  touched |= 1u << acc;
+                }
               }
             }
           }
@@ -489,8 +519,8 @@ __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmAr
     const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
     uint32_t proc = 0;
     for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
-      const long long b = w / (2 * ntile);
-      const int part = (int)((w / ntile) & 1), ct = (int)(w % ntile);
+      const long long b = w / (NPARTS == 2 ? ntile : 2 * ntile);
+      const int part0 = BOTH ? 0 : (int)((w / ntile) & 1), ct = (int)(w % ntile);
       if (a.active && !a.active[b]) continue;
       if (!mbar_wait(tmem_full, proc & 1, abort_flag)) break;
       const int* erow = a.scales + b * 256;
@@ -498,21 +528,24 @@ __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmAr
       tc_fence_after();
       void* C = batch_ptr<TOut>(a.C, b);
       const void* D = a.D.p ? batch_ptr<const TOut>(a.D, b) : nullptr;
+      const int ei = erow[row];
+      const float alpha = (float)a.alpha_re, beta = (float)a.beta_re;
+      // columns per TMEM read (register budget of the wider 128-column CTAs)
+      constexpr int CW = (NACC > 4 || NPROD > 256) ? 8 : 16;
+      for (int pp = 0; pp < NPARTS; ++pp) {
+      const int part = BOTH ? pp : part0;
       double zpart = 0.0;
       if (a.Z.p) {
         const double2 z = *batch_ptr<const double2>(a.Z, b);
         zpart = part ? z.y : z.x;
       }
-      const int ei = erow[row];
-      const float alpha = (float)a.alpha_re, beta = (float)a.beta_re;
-      // columns per TMEM read (register budget of the wider 128-column CTAs)
-      constexpr int CW = (NACC > 4 || NPROD > 256) ? 8 : 16;
       for (int j0 = 0; j0 < NT; j0 += CW) {
         uint32_t r[NACC][16];
 #pragma unroll
         for (int acc = 0; acc < NACC; ++acc) {
-          if constexpr (CW == 16) tmem_ld16(lane_base + acc * NT + j0, r[acc]);
-          else tmem_ld8(lane_base + acc * NT + j0, r[acc]);
+          const uint32_t col = (uint32_t)((pp * NACC + acc) * NT + j0);
+          if constexpr (CW == 16) tmem_ld16(lane_base + col, r[acc]);
+          else tmem_ld8(lane_base + col, r[acc]);
         }
         tmem_wait_ld();
         if (row < m) {
@@ -537,6 +570,7 @@ __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmAr
           }
         }
       }
+      }  // parts
       tc_fence_before();
       mbar_arrive(tmem_empty);
       ++proc;
@@ -557,7 +591,8 @@ cudaError_t launch(const GemmArgs& a, cudaStream_t s) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const int stage_bytes = S * (PLANE_BYTES + NT * KC * 2);
+  constexpr int aplanes = sizeof(TIn) == 8 ? 2 : 1;  // complex64: both parts per item
+  const int stage_bytes = S * (aplanes * PLANE_BYTES + NT * KC * 2);
   const int extra = 2048 + 8 * 64 + 64;  // barriers + exponents + tmem slot
   int stages = (maxsm - extra) / stage_bytes;
   if (stages > 4) stages = 4;
@@ -567,7 +602,7 @@ cudaError_t launch(const GemmArgs& a, cudaStream_t s) {
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const int ntile = (((a.n + 15) & ~15) + NT - 1) / NT;
-  const long long items = 2LL * ntile * a.batch;
+  const long long items = (sizeof(TIn) == 8 ? 1LL : 2LL) * ntile * a.batch;
   const int grid = (int)(items < sms ? items : sms);
   if (!a.scales) return cudaErrorInvalidValue;
   const long long gb = a.batch < 65535 ? a.batch : 65535;
