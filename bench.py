@@ -187,9 +187,10 @@ def scba_comparison(ctx, a):
     from quantum_transport_gb300.devices import disordered_gw_device
     nx, nm, nE = (int(x) for x in a.scba_size.split(","))
 
-    def system(seed):
+    def system(seed, precision="fp64"):
         d = disordered_gw_device(seed, nx=nx, nm=nm, nE=nE)
-        return gw.GwSystem(ctx, d.H00, d.H10, d.E, d.nx, d.V, mu=(0.1, -0.1))
+        return gw.GwSystem(ctx, d.H00, d.H10, d.E, d.nx, d.V, mu=(0.1, -0.1),
+                           precision=precision)
 
     train_sys = [system(100 + i) for i in range(8)]
     test_sys = [system(900 + i) for i in range(2)]
@@ -211,6 +212,26 @@ def scba_comparison(ctx, a):
             out[m]["seconds"].append(r.seconds)
         for x, y in zip(runs["learned"].sigma, runs["plain"].sigma):
             diff = max(diff, float((x - y).abs().max() / y.abs().max()))
+    # plain-mixing SCBA to residual 1e-6 in FP64 and in both split precisions on one held-out
+    # seed: time to converge, and the errors in terminal current and LDOS against FP64
+    runs = {}
+    for p in ("fp64", "mixed-fp64", "mixed"):
+        s = system(900, p)
+        s.scba(alpha=0.3, tol=1e-6, max_iter=2)  # first-call set-up
+        t0 = time.perf_counter()
+        SR, SL, _, res, cur = s.scba(alpha=0.3, tol=1e-6, max_iter=200, with_currents=True)
+        dt = time.perf_counter() - t0
+        ob = s.currents(SR, SL)
+        runs[p] = (dt, len(res), float(res[-1]), cur[-1], -2.0 * ob["diag_gr"].imag)
+    t64, n64, r64, c64, l64 = runs["fp64"]
+    precision = {"fp64": {"seconds": t64, "iterations": n64, "final_residual": r64,
+                          "current_A": [float(x) for x in c64]}}
+    for p in ("mixed-fp64", "mixed"):
+        t, nit, rr, c, ld = runs[p]
+        precision[p] = {"seconds": t, "iterations": nit, "final_residual": rr,
+                        "time_vs_fp64": t / t64,
+                        "current_rel_err": float(np.max(np.abs(c - c64) / np.abs(c64))),
+                        "ldos_rel_err": float(np.abs(ld - l64).max() / np.abs(l64).max())}
     mean = lambda v: float(np.mean(v))
     return {"workload": f"GW-SCBA, {nx} slabs x {nm} orbitals x {nE} energies, on-site disorder "
                         "sigma ~ U[0.05, 0.3] eV, V_ij = 14.4/(|r_i - r_j| + 1) eV, residual <= 1e-8",
@@ -220,7 +241,8 @@ def scba_comparison(ctx, a):
                for m, v in out.items()},
             "learned_vs_plain_time": mean(out["learned"]["seconds"]) / mean(out["plain"]["seconds"]),
             "learned_vs_pulay_time": mean(out["learned"]["seconds"]) / mean(out["pulay"]["seconds"]),
-            "fixed_point_max_rel_diff": diff}
+            "fixed_point_max_rel_diff": diff,
+            "precision_to_1e-6": precision}
 
 
 def run_ours(a):

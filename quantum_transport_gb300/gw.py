@@ -109,10 +109,13 @@ class GwSystem:
 
     def currents(self, SR, SL):
         """Per-energy currents of the RGF with self-energies (SR, SL): dict of numpy arrays
-        tr, tre (nE,) (green_RGF_RS's right- and left-contact currents) and bond_cur
-        (nE, nx-1), the traces of its cur blocks (src/gw_mod.f90:1254-1276)."""
+        tr, tre (nE,) (green_RGF_RS's right- and left-contact currents), bond_cur
+        (nE, nx-1), the traces of its cur blocks (src/gw_mod.f90:1254-1276), and diag_gr
+        (nE, nx*nm), the diagonal of G^R behind the LDOS."""
         import torch
         out = {"tr": torch.zeros(self.nE, dtype=torch.float64, device="cuda"),
+               "diag_gr": torch.zeros((self.nE, self.nx * self.nm), dtype=torch.complex128,
+                                      device="cuda"),
                "tre": torch.zeros(self.nE, dtype=torch.float64, device="cuda"),
                "bond_cur": torch.zeros((self.nE, self.nx - 1), dtype=torch.float64,
                                        device="cuda"),
