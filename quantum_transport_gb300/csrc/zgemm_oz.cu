@@ -140,6 +140,25 @@ __device__ __forceinline__ void digits_f32(float x, float scale, float* D) {
     r -= d;
   }
 }
+// The same digits for a (Re, Im) pair with the packed FP32x2 arithmetic of sm_100+
+// (each lane rounded exactly as the scalar form: bit-identical digits).
+template <int S>
+__device__ __forceinline__ void digits_f32x2(float2 x, float scale, float2* D) {
+  float2 r = __fmul2_rn(x, make_float2(scale, scale));
+  const float2 mone = make_float2(-1.0f, -1.0f);
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    const float M = 12582912.0f * __int_as_float((127 - 8 * s) << 23);  // 1.5 * 2^(23 - 8s)
+    const float2 d = __fadd2_rn(__fadd2_rn(r, make_float2(M, M)), make_float2(-M, -M));
+    D[s] = d;
+    r = __ffma2_rn(d, mone, r);  // r - d, exact
+  }
+}
+// the BF16 halves (upper 16 bits) of lo and hi in one 32-bit word: digits carry <= 8
+// significant bits, so the truncation is exact
+__device__ __forceinline__ uint32_t pack_pair(float2 d) {
+  return __byte_perm(__float_as_uint(d.x), __float_as_uint(d.y), 0x7632);
+}
 // FP64 value via integer arithmetic on its bits: T = round(x 2^(8S - e)), balanced digits
 template <int S>
 __device__ __forceinline__ void digits_f64(double x, int e, float* D) {
@@ -414,9 +433,22 @@ __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmAr
           for (int u = 0; u < 4; ++u) {
             float D0[S], D1[S];
             const TIn x = xv[q][u];
-            if constexpr (sizeof(TIn) == 8) {
+            if constexpr (BOTH) {
               // 2^(8-e) as pre * scale: rows below 2^-119 would overflow a single FP32
               // power of two, so they are first lifted by 2^64 (exact)
+              const bool tiny = e < -118;
+              const float pre = tiny ? 18446744073709551616.0f : 1.0f;
+              const float scale = __int_as_float((127 + 8 - (tiny ? e + 64 : e)) << 23);
+              // B' real layout (Re, -Im) for B items; A as (Re, Im)
+              float2 v = __fmul2_rn(make_float2(x.x, isA ? x.y : -x.y), make_float2(pre, pre));
+              float2 D[S];
+              digits_f32x2<S>(v, scale, D);
+#pragma unroll
+              for (int s2 = 0; s2 < S; ++s2) {
+                packed[s2][u] = pack_pair(D[s2]);
+                packed2[s2][u] = pack_pair(make_float2(D[s2].y, D[s2].x)) ^ 0x80000000u;
+              }
+            } else if constexpr (sizeof(TIn) == 8) {
               const bool tiny = e < -118;
               const float pre = tiny ? 18446744073709551616.0f : 1.0f;
               const float scale = __int_as_float((127 + 8 - (tiny ? e + 64 : e)) << 23);
@@ -436,11 +468,9 @@ __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmAr
               digits_f64<S>(v0, e, D0);
               digits_f64<S>(v1, e, D1);
             }
+            if constexpr (!BOTH) {
 #pragma unroll
-            for (int s2 = 0; s2 < S; ++s2) packed[s2][u] = pack_bf16x2(D0[s2], D1[s2]);
-            if constexpr (BOTH) {
-#pragma unroll
-              for (int s2 = 0; s2 < S; ++s2) packed2[s2][u] = pack_bf16x2(D1[s2], -D0[s2]);
+              for (int s2 = 0; s2 < S; ++s2) packed[s2][u] = pack_bf16x2(D0[s2], D1[s2]);
             }
           }
           // canonical no-swizzle K-major: (r/8)*SBO + g*LBO + (r%8)*16
