@@ -369,6 +369,54 @@ qt_status qt_ephoton_sigma(qt_ctx* ctx, int nm, int nx, int nE, int nop, int hal
                            double scale, qt_precision prec, unsigned flags, double* sigma_r,
                            double* sigma_lesser, double* sigma_greater);
 
+/* ---- The SCBA map in stages, for ranks that share the energy grid.
+ * gw_ephoton_3d_ijs computes G on each rank's energies, moves G to (i, j)-major
+ * order with an all-to-all (energies_to_ijs_2, src/gw_mod.f90:41-73), takes P
+ * by energy correlations over the full grid on each rank's (i, j) elements,
+ * moves P back to energies for W, W to (i, j) for Sigma, and Sigma back
+ * (:452-456, 522-524, 636-638, 700-702).  These entry points are the compute
+ * between those exchanges; qt_gw_step is the same sequence on one rank and
+ * gives the same numbers.
+ *
+ * Series arrays hold nseries energy series of n points (the full energy grid),
+ * energy-major: element (e, s) at 2*(e*nseries + s) doubles.  Block arrays hold
+ * nm x nm column-major complex128 blocks back to back.  Device pointers only
+ * (QT_FLAG_DEVICE_POINTERS); n <= 2048.                                     */
+
+/* P^< = -i scale corr(G^<, G^>t), P^> = -i scale corr(G^>, G^<t),
+ * P^R = -i scale [corr(G^<, conj G^R) + corr(G^R, G^<t)] with Re G zeroed
+ * first (src/gw_mod.f90:444-446, 495-519).  G^<t / G^>t hold the transposed
+ * element (j, i) of the same slab in the place of (i, j).  The reference's
+ * scale is dE / (2 pi) * spindeg / nk.                                       */
+qt_status qt_gw_polarization(qt_ctx* ctx, int n, int64_t nseries, const double* GR,
+                             const double* GL, const double* GG, const double* GLt,
+                             const double* GGt, double scale, double* PR, double* PL,
+                             double* PG, unsigned flags);
+
+/* W^R = (I - V P^R)^-1 V and W^{<,>} = W^R P^{<,>} W^R^+ for nblocks blocks
+ * (the restatement of the absent green_rgf_calc_w, src/gw_mod.f90:597), V one
+ * nm x nm block for all.  W^< and W^> may overwrite P^< and P^>; W^R may not
+ * alias any P.  QT_PREC_MIXED / QT_PREC_MIXED_FP64 take the FP64-grade split
+ * products and refined inverses of the leads (nm <= 384).  Synchronises.    */
+qt_status qt_gw_screened(qt_ctx* ctx, int nm, int64_t nblocks, const double* V,
+                         const double* PR, const double* PL, const double* PG, double* WR,
+                         double* WL, double* WG, qt_precision prec, unsigned flags);
+
+/* Sigma^< = i scale conv(G^<, W^<), Sigma^> = i scale conv(G^>, W^>),
+ * Sigma^R = i scale [conv(G^<, W^R) + conv(G^R, W^<) + conv(G^R, W^R)], Re G
+ * zeroed (src/gw_mod.f90:646-698); the reference's scale is dE / (2 pi) / nk.
+ * Sigma^R is not yet recombined: see qt_gw_sigma_post.                      */
+qt_status qt_gw_selfenergy(qt_ctx* ctx, int n, int64_t nseries, const double* GR,
+                           const double* GL, const double* GG, const double* WR,
+                           const double* WL, const double* WG, double scale, double* SR,
+                           double* SL, double* SG, unsigned flags);
+
+/* In place on [nE][nx] blocks: Sigma^R <- Re Sigma^R + i Im(Sigma^> - Sigma^<)/2
+ * (src/gw_mod.f90:698), S <- (S + S^T)/2 for all three (:731-743), and with
+ * nx >= 5 the edge blocks 1,2 <- 3 and nx-1,nx <- nx-2 (:950-959).          */
+qt_status qt_gw_sigma_post(qt_ctx* ctx, int nm, int nx, int nE, double* SR, double* SL,
+                           double* SG, unsigned flags);
+
 /* Batched energy correlation (mode 0) / convolution (mode 1) of corr1d2 /
  * conv1d2 (src/fft_mod.f90:58-168) on n-point series stored energy-major,
  * element (e, s) at 2*(e*nseries + s) doubles:

@@ -181,6 +181,49 @@ def scba(E, H00, H10, V, nx, *, mu, temp, alpha=0.3, tol=1e-8, max_iter=60, spin
     return SR, SL, SG, res
 
 
+def energies_to_ijs_2(bufs, nm, nx, nk, local_ne):
+    """energies_to_ijs_2 (src/gw_mod.f90:41-73) on every rank at once, MPI_Alltoall done by
+    hand.  ``bufs[r]``: rank r's flat buffer, g(1:nm, 1:nm, 1:nx, 1:local_ne, 1:nk) in
+    Fortran order.  Returns rank r's buffer after the call as a numpy array indexed
+    [e, s, k, x, a] (Fortran p3(1:local_ne, 1:comm_size, 1:nk, 1:nx, 1:local_nij)), i.e.
+    global energy s*local_ne + e of element r*local_nij + a.  Needs nm*nm divisible by the
+    rank count, as the reference's partition does."""
+    size = len(bufs)
+    local_nij = nm * nm // size
+    count = local_nij * nx * local_ne * nk
+    tmp0 = []
+    for b in bufs:
+        p0 = np.reshape(b[:count * size], (local_nij, size, nx, local_ne, nk), order="F")
+        # p1 = reshape(p0, shape(p1), order=[1, 5, 2, 3, 4]): p1(a, x, e, k, r) = p0(a, r, x, e, k)
+        tmp0.append(np.transpose(p0, (0, 2, 3, 4, 1)).reshape(-1, order="F"))
+    # MPI_Alltoall: block s of rank r's receive buffer is block r of rank s's send buffer
+    tmp1 = [np.concatenate([tmp0[s][r * count:(r + 1) * count] for s in range(size)])
+            for r in range(size)]
+    out = []
+    for r in range(size):
+        p2 = np.reshape(tmp1[r], (local_nij, nx, local_ne, nk, size), order="F")
+        # p3 = reshape(p2, shape(p3), order=[5, 4, 1, 3, 2]): p3(e, s, k, x, a) = p2(a, x, e, k, s)
+        out.append(np.transpose(p2, (2, 4, 3, 1, 0)))
+    return out
+
+
+def ijs_to_energies_2(outs, nm, nx, nk, local_ne):
+    """The inverse of ``energies_to_ijs_2`` (ijs_to_energies_2 is called at
+    src/gw_mod.f90:522-524, 700-702 but its source is absent): per-rank arrays [e, s, k, x, a]
+    back to flat Fortran-order g(1:nm, 1:nm, 1:nx, 1:local_ne, 1:nk) buffers."""
+    size = len(outs)
+    local_nij = nm * nm // size
+    count = local_nij * nx * local_ne * nk
+    tmp1 = [np.transpose(o, (4, 3, 0, 2, 1)).reshape(-1, order="F") for o in outs]
+    tmp0 = [np.concatenate([tmp1[s][r * count:(r + 1) * count] for s in range(size)])
+            for r in range(size)]
+    bufs = []
+    for r in range(size):
+        p1 = np.reshape(tmp0[r], (local_nij, nx, local_ne, nk, size), order="F")
+        bufs.append(np.transpose(p1, (0, 4, 1, 2, 3)).reshape(-1, order="F"))
+    return bufs
+
+
 def coulomb_blocks(nm, spacing_nm=0.25, strength=14.4):
     """V_ij = 14.4 / (|r_i - r_j| + 1) eV on a 1-D grid of 0.25 nm (orbital index x spacing)."""
     r = np.arange(nm) * spacing_nm

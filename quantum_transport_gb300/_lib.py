@@ -29,7 +29,8 @@ EXPORTS = [
     "qt_mlp_set_params", "qt_mlp_infer", "qt_mlp_grad", "qt_mlp_train_step",
     "qt_mix_diag", "qt_mix_features", "qt_mix_apply", "qt_mix_gram", "qt_mix_combine",
     "qt_rgf_solve_vb", "qt_ctx_set_stream", "qt_w90_blocks", "qt_coo_blocks",
-    "qt_ephoton_sigma", "qt_ctx_inverse_fallbacks",
+    "qt_ephoton_sigma", "qt_ctx_inverse_fallbacks", "qt_gw_polarization", "qt_gw_screened",
+    "qt_gw_selfenergy", "qt_gw_sigma_post",
 ]
 
 
@@ -105,6 +106,12 @@ def load(path=LIB_PATH):
     lib.qt_scba_solve.argtypes = [vp, C.POINTER(QtDevice), vp, ci, C.POINTER(QtContacts), vp,
                                   dbl, dbl, dbl, ci, ci, C.c_uint, vp, vp, vp, vp, vp, vp]
     lib.qt_corr_batch.argtypes = [vp, ci, i64, vp, vp, vp, ci, C.c_uint]
+    lib.qt_gw_polarization.argtypes = [vp, ci, i64, vp, vp, vp, vp, vp, dbl, vp, vp, vp,
+                                       C.c_uint]
+    lib.qt_gw_screened.argtypes = [vp, ci, i64, vp, vp, vp, vp, vp, vp, vp, ci, C.c_uint]
+    lib.qt_gw_selfenergy.argtypes = [vp, ci, i64, vp, vp, vp, vp, vp, vp, dbl, vp, vp, vp,
+                                     C.c_uint]
+    lib.qt_gw_sigma_post.argtypes = [vp, ci, ci, ci, vp, vp, vp, C.c_uint]
     lib.qt_ephoton_sigma.argtypes = [vp, ci, ci, ci, ci, ci, vp, vp, vp, dbl, ci, C.c_uint, vp, vp,
                                      vp]
     lib.qt_zgemm_batch_noalloc.argtypes = [ci, ci, C.c_char, vp, i64, C.c_char, vp, i64, vp, vp,

@@ -1902,6 +1902,75 @@ struct GwCurrents {
   double *tr = nullptr, *tre = nullptr, *bond = nullptr;
 };
 
+// W^R = (I - V P^R)^-1 V and W^{<,>} = W^R P^{<,>} W^R^+ per (w, slab) block, nblk blocks of
+// nm x nm at stride nm^2.  WL/WG may alias PL/PG; T1, T2 are nblk-block scratch (taken
+// from the context arena when null).
+qt_status gw_screened_blocks(qt_ctx* ctx, int nm, long long nblk, qt_precision prec,
+                             int slices, const cd* V, const cd* PR, const cd* PL, const cd* PG,
+                             cd* WR, cd* WL, cd* WG, cd* T1, cd* T2) {
+  cudaStream_t s = ctx->stream;
+  const long long nm2 = (long long)nm * nm;
+  Ops<double2> op{s, nm, prec};
+  op.slices = slices;
+  op.refine = prec == QT_PREC_FP64 ? 0 : 2;
+  op.prof = &ctx->prof;
+  const size_t scratch = (T1 ? 0 : 2 * (size_t)nblk * nm2 * 16 + 512);
+  const size_t need_extra = (size_t)nblk * 1300 + 2 * (size_t)nblk * nm2 * 16 + 4096 + scratch;
+  QT_TRY(ensure(ctx->arena, ctx->arena_bytes, need_extra));
+  Arena ar{reinterpret_cast<char*>(ctx->arena), ctx->arena_bytes, 0};
+  cd* one = ar.take<cd>(1);
+  const cd h1{1.0, 0.0};
+  cudaMemcpyAsync(one, &h1, sizeof(cd), cudaMemcpyHostToDevice, s);
+  op.one = one;
+  op.scales = ar.take<int>((size_t)nblk * 256);
+  op.rt1 = reinterpret_cast<double2*>(ar.take<cd>((size_t)nblk * nm2));
+  op.rt2 = reinterpret_cast<double2*>(ar.take<cd>((size_t)nblk * nm2));
+  op.P = nblk;
+  op.guard = ar.take<unsigned char>((size_t)nblk);
+  op.fallbacks = ctx->fallbacks;
+  if (!T1) {
+    T1 = ar.take<cd>((size_t)nblk * nm2);
+    T2 = ar.take<cd>((size_t)nblk * nm2);
+  }
+  if (!op.scales || !op.rt2 || !op.guard || !T1 || !T2)
+    QT_FAIL(QT_ERR_NOMEM, "arena exhausted (W)");
+  const BatchRef Vr = ref(V, 0, nm), B = ref(nullptr, nm2, nm);
+  auto blk = [&](const cd* p) { BatchRef r = B; r.p = const_cast<cd*>(p); return r; };
+  // T1 = I - V P^R ; T2 = T1^-1 ; W^R = T2 V
+  QT_TRY(op.gemm(Vr, qt::OP_N, blk(PR), qt::OP_N, blk(T1), nblk, {-1, 0}, nullref(),
+                 {0, 0}, ref(one, 0, 1)));
+  QT_TRY(op.inv(blk(T1), blk(T2), nblk, nullptr));
+  QT_TRY(op.gemm(blk(T2), qt::OP_N, Vr, qt::OP_N, blk(WR), nblk));
+  // W^< = W^R P^< W^R^+, W^> = W^R P^> W^R^+
+  QT_TRY(op.gemm(blk(WR), qt::OP_N, blk(PL), qt::OP_N, blk(T1), nblk));
+  QT_TRY(op.gemm(blk(T1), qt::OP_N, blk(WR), qt::OP_C, blk(WL), nblk));
+  QT_TRY(op.gemm(blk(WR), qt::OP_N, blk(PG), qt::OP_N, blk(T1), nblk));
+  QT_TRY(op.gemm(blk(T1), qt::OP_N, blk(WR), qt::OP_C, blk(WG), nblk));
+  return QT_OK;
+}
+
+// Sigma^R <- Re Sigma^R + i Im(Sigma^> - Sigma^<)/2, (S + S^T)/2 (src/gw_mod.f90:698,
+// 731-743) and the edge blocks 1,2 <- 3 and nx-1,nx <- nx-2 (:950-959) for nE energies of
+// nx slab blocks
+qt_status gw_post(qt_ctx* ctx, int nm, int nx, long long nE, cd* NR, cd* NL, cd* NG) {
+  cudaStream_t s = ctx->stream;
+  const long long nm2 = (long long)nm * nm;
+  cudaError_t e = qt::gw_sigma_post(nm, nE * nx, reinterpret_cast<double2*>(NR),
+                                    reinterpret_cast<double2*>(NL),
+                                    reinterpret_cast<double2*>(NG), s);
+  if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+  if (nx >= 5) {
+    for (cd* S : {NR, NL, NG}) {
+      auto slab = [&](int l) { return ref(S + l * nm2, nx * nm2, nm); };
+      qt::zcopy<double2>(nm, nE, slab(2), slab(0), s);
+      qt::zcopy<double2>(nm, nE, slab(2), slab(1), s);
+      qt::zcopy<double2>(nm, nE, slab(nx - 3), slab(nx - 1), s);
+      qt::zcopy<double2>(nm, nE, slab(nx - 3), slab(nx - 2), s);
+    }
+  }
+  return QT_OK;
+}
+
 qt_status gw_map(qt_ctx* ctx, Problem pb, const cd* V, double spindeg, const cd* SR,
                  const cd* SL, GwBuffers& w, long long hii_n, long long h1i_n,
                  const GwCurrents& cur = GwCurrents{}) {
@@ -1941,40 +2010,10 @@ qt_status gw_map(qt_ctx* ctx, Problem pb, const cd* V, double spindeg, const cd*
   QT_TRY(cc(w.GG, w.GL, w.PG, 1, 1, 0, 1, 1, 0, 0.0, -pf));        // P^> = corr(G^>_ij, G^<_ji)
   QT_TRY(cc(w.GL, w.GR, w.PR, 1, 0, 1, 1, 1, 0, 0.0, -pf));        // corr(G^<_ij, conj G^R_ij)
   QT_TRY(cc(w.GR, w.GL, w.PR, 1, 1, 0, 1, 1, 1, 0.0, -pf));        //   + corr(G^R_ij, G^<_ji)
-  // ---- screened interaction per (w, slab) block
-  Ops<double2> op{s, nm, pb.prec};
-  op.slices = pb.lead_slices;
-  op.refine = pb.prec == QT_PREC_FP64 ? 0 : 2;
-  op.prof = &ctx->prof;
-  {
-    const size_t need_extra = (size_t)nblk * 1300 + 2 * (size_t)nblk * nm2 * 16 + 4096;
-    QT_TRY(ensure(ctx->arena, ctx->arena_bytes, need_extra));
-    Arena ar{reinterpret_cast<char*>(ctx->arena), ctx->arena_bytes, 0};
-    cd* one = ar.take<cd>(1);
-    const cd h1{1.0, 0.0};
-    cudaMemcpyAsync(one, &h1, sizeof(cd), cudaMemcpyHostToDevice, s);
-    op.one = one;
-    op.scales = ar.take<int>((size_t)nblk * 256);
-    op.rt1 = reinterpret_cast<double2*>(ar.take<cd>((size_t)nblk * nm2));
-    op.rt2 = reinterpret_cast<double2*>(ar.take<cd>((size_t)nblk * nm2));
-    op.P = nblk;
-    op.guard = ar.take<unsigned char>((size_t)nblk);
-    op.fallbacks = ctx->fallbacks;
-    if (!op.scales || !op.rt2 || !op.guard) QT_FAIL(QT_ERR_NOMEM, "arena exhausted (W)");
-    const BatchRef Vr = ref(V, 0, nm), B = ref(nullptr, nm2, nm);
-    auto blk = [&](const cd* p) { BatchRef r = B; r.p = const_cast<cd*>(p); return r; };
-    // T1 = I - V P^R ; T2 = T1^-1 ; W^R (-> NR scratch) = T2 V
-    QT_TRY(op.gemm(Vr, qt::OP_N, blk(w.PR), qt::OP_N, blk(w.T1), nblk, {-1, 0}, nullref(),
-                   {0, 0}, ref(one, 0, 1)));
-    QT_TRY(op.inv(blk(w.T1), blk(w.T2), nblk, nullptr));
-    QT_TRY(op.gemm(blk(w.T2), qt::OP_N, Vr, qt::OP_N, blk(w.NR), nblk));
-    // W^< = W^R P^< W^R^+ (-> PL), W^> (-> PG)
-    QT_TRY(op.gemm(blk(w.NR), qt::OP_N, blk(w.PL), qt::OP_N, blk(w.T1), nblk));
-    QT_TRY(op.gemm(blk(w.T1), qt::OP_N, blk(w.NR), qt::OP_C, blk(w.PL), nblk));
-    QT_TRY(op.gemm(blk(w.NR), qt::OP_N, blk(w.PG), qt::OP_N, blk(w.T1), nblk));
-    QT_TRY(op.gemm(blk(w.T1), qt::OP_N, blk(w.NR), qt::OP_C, blk(w.PG), nblk));
-    qt::zcopy<double2>(nm, nblk, blk(w.NR), blk(w.PR), s);  // W^R -> PR
-  }
+  // ---- screened interaction per (w, slab) block: W^R -> NR (scratch) -> PR, W^<> in place
+  QT_TRY(gw_screened_blocks(ctx, nm, nblk, pb.prec, pb.lead_slices, V, w.PR, w.PL, w.PG, w.NR,
+                            w.PL, w.PG, w.T1, w.T2));
+  qt::zcopy<double2>(nm, nblk, ref(w.NR, nm2, nm), ref(w.PR, nm2, nm), s);
   // ---- self-energy: energy convolutions x i dE / (2 pi)
   const double sf = dE / (2.0 * M_PI);
   QT_TRY(cc(w.GL, w.PL, w.NL, 0, 0, 0, 1, 0, 0, 0.0, sf));  // Sigma^< = conv(G^<, W^<)
@@ -1982,20 +2021,8 @@ qt_status gw_map(qt_ctx* ctx, Problem pb, const cd* V, double spindeg, const cd*
   QT_TRY(cc(w.GL, w.PR, w.NR, 0, 0, 0, 1, 0, 0, 0.0, sf));  // Sigma^R = conv(G^<, W^R)
   QT_TRY(cc(w.GR, w.PL, w.NR, 0, 0, 0, 1, 0, 1, 0.0, sf));  //   + conv(G^R, W^<)
   QT_TRY(cc(w.GR, w.PR, w.NR, 0, 0, 0, 1, 0, 1, 0.0, sf));  //   + conv(G^R, W^R)
-  cudaError_t e = qt::gw_sigma_post(nm, nblk, reinterpret_cast<double2*>(w.NR),
-                                    reinterpret_cast<double2*>(w.NL),
-                                    reinterpret_cast<double2*>(w.NG), s);
-  if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
-  // ---- edge blocks 1,2 <- 3 and nx-1,nx <- nx-2 (src/gw_mod.f90:950-959)
-  if (nx >= 5) {
-    for (cd* S : {w.NR, w.NL, w.NG}) {
-      auto slab = [&](int l) { return ref(S + l * nm2, nx * nm2, nm); };
-      qt::zcopy<double2>(nm, nE, slab(2), slab(0), s);
-      qt::zcopy<double2>(nm, nE, slab(2), slab(1), s);
-      qt::zcopy<double2>(nm, nE, slab(nx - 3), slab(nx - 1), s);
-      qt::zcopy<double2>(nm, nE, slab(nx - 3), slab(nx - 2), s);
-    }
-  }
+  // ---- recombination, symmetrisation, edge blocks
+  QT_TRY(gw_post(ctx, nm, nx, nE, w.NR, w.NL, w.NG));
   (void)cnt;
   return QT_OK;
 }
@@ -2222,6 +2249,112 @@ extern "C" qt_status qt_corr_batch(qt_ctx* ctx, int n, int64_t nseries, const do
   a.X = X; a.Y = Y; a.Z = Z; a.corr = mode == 0; a.scale_re = 1.0;
   e = qt::zcorrconv(a, tw, ctx->stream);
   if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+  if (flags & QT_FLAG_SYNC) QT_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return QT_OK;
+}
+
+// ---- GW map stages on one rank's share (the energies <-> (i, j) exchange in between is
+// the caller's: energies_to_ijs_2, src/gw_mod.f90:41-73, and its inverse)
+namespace {
+
+qt_status series_setup(qt_ctx* ctx, int n, int64_t nseries, unsigned flags,
+                       qt::CorrConvArgs& c, double2*& tw) {
+  if (n < 2 || nseries <= 0) QT_FAIL(QT_ERR_ARG, "need n >= 2 energies and nseries > 0");
+  if (!(flags & QT_FLAG_DEVICE_POINTERS)) QT_FAIL(QT_ERR_UNSUPPORTED, "device pointers required");
+  if (2 * n > 4096) QT_FAIL(QT_ERR_UNSUPPORTED, "n <= 2048 (FFT length 4096)");
+  cudaSetDevice(ctx->device);
+  QT_TRY(ensure(ctx->arena, ctx->arena_bytes, 2048 * sizeof(double2) + 256));
+  tw = reinterpret_cast<double2*>(ctx->arena);
+  cudaError_t e = qt::gw_twiddles(tw, ctx->stream);
+  if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+  c = qt::CorrConvArgs{};
+  c.n = n; c.nm = 1; c.nseries = nseries; c.estride = nseries;
+  return QT_OK;
+}
+
+qt_status series_run(qt_ctx* ctx, const qt::CorrConvArgs& c, const double2* tw, const double* X,
+                     const double* Y, double* Z, int corr, int conjY, int imX, int imY,
+                     int acc, double sr, double si) {
+  qt::CorrConvArgs a = c;
+  a.X = X; a.Y = Y; a.Z = Z; a.corr = corr; a.conjY = conjY;
+  a.imagX = imX; a.imagY = imY; a.accumulate = acc; a.scale_re = sr; a.scale_im = si;
+  cudaError_t e = qt::zcorrconv(a, tw, ctx->stream);
+  if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+  return QT_OK;
+}
+
+}  // namespace
+
+extern "C" qt_status qt_gw_polarization(qt_ctx* ctx, int n, int64_t nseries, const double* GR,
+                                        const double* GL, const double* GG, const double* GLt,
+                                        const double* GGt, double scale, double* PR,
+                                        double* PL, double* PG, unsigned flags) {
+  if (!ctx || !GR || !GL || !GG || !GLt || !GGt || !PR || !PL || !PG)
+    QT_FAIL(QT_ERR_ARG, "null polarisation array");
+  qt::CorrConvArgs c;
+  double2* tw;
+  QT_TRY(series_setup(ctx, n, nseries, flags, c, tw));
+  // P = -i scale corr(...) of the Re-zeroed G (src/gw_mod.f90:444-446, 495-519)
+  QT_TRY(series_run(ctx, c, tw, GL, GGt, PL, 1, 0, 1, 1, 0, 0.0, -scale));
+  QT_TRY(series_run(ctx, c, tw, GG, GLt, PG, 1, 0, 1, 1, 0, 0.0, -scale));
+  QT_TRY(series_run(ctx, c, tw, GL, GR, PR, 1, 1, 1, 1, 0, 0.0, -scale));
+  QT_TRY(series_run(ctx, c, tw, GR, GLt, PR, 1, 0, 1, 1, 1, 0.0, -scale));
+  if (flags & QT_FLAG_SYNC) QT_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return QT_OK;
+}
+
+extern "C" qt_status qt_gw_screened(qt_ctx* ctx, int nm, int64_t nblocks, const double* V,
+                                    const double* PR, const double* PL, const double* PG,
+                                    double* WR, double* WL, double* WG, qt_precision prec,
+                                    unsigned flags) {
+  if (!ctx || !V || !PR || !PL || !PG || !WR || !WL || !WG || nm <= 0 || nblocks <= 0)
+    QT_FAIL(QT_ERR_ARG, "bad screened-interaction arguments");
+  if (!(flags & QT_FLAG_DEVICE_POINTERS)) QT_FAIL(QT_ERR_UNSUPPORTED, "device pointers required");
+  if (!valid_prec(prec)) QT_FAIL(QT_ERR_ARG, "unknown precision");
+  if (prec != QT_PREC_FP64 && nm > MAX_SPLIT)
+    QT_FAIL(QT_ERR_UNSUPPORTED, "split-precision path needs nm <= 384");
+  if (WR == PR || WR == PL || WR == PG || WL == PR || WG == PR)
+    QT_FAIL(QT_ERR_ARG, "W^R may not alias P; W^< and W^> may alias only P^< and P^>");
+  cudaSetDevice(ctx->device);
+  // FP64-grade digits on the split path, as inside qt_gw_step
+  QT_TRY(gw_screened_blocks(ctx, nm, nblocks, prec, env_int("QT_LEAD_SLICES", 7),
+                            reinterpret_cast<const cd*>(V), reinterpret_cast<const cd*>(PR),
+                            reinterpret_cast<const cd*>(PL), reinterpret_cast<const cd*>(PG),
+                            reinterpret_cast<cd*>(WR), reinterpret_cast<cd*>(WL),
+                            reinterpret_cast<cd*>(WG), nullptr, nullptr));
+  QT_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  if (prec != QT_PREC_FP64 && qt::oz_timeouts_and_reset())
+    QT_FAIL(QT_ERR_CUDA, "tensor-core kernel wait timed out");
+  return QT_OK;
+}
+
+extern "C" qt_status qt_gw_selfenergy(qt_ctx* ctx, int n, int64_t nseries, const double* GR,
+                                      const double* GL, const double* GG, const double* WR,
+                                      const double* WL, const double* WG, double scale,
+                                      double* SR, double* SL, double* SG, unsigned flags) {
+  if (!ctx || !GR || !GL || !GG || !WR || !WL || !WG || !SR || !SL || !SG)
+    QT_FAIL(QT_ERR_ARG, "null self-energy array");
+  qt::CorrConvArgs c;
+  double2* tw;
+  QT_TRY(series_setup(ctx, n, nseries, flags, c, tw));
+  // Sigma = i scale conv(...) with the Re-zeroed G (src/gw_mod.f90:646-698)
+  QT_TRY(series_run(ctx, c, tw, GL, WL, SL, 0, 0, 1, 0, 0, 0.0, scale));
+  QT_TRY(series_run(ctx, c, tw, GG, WG, SG, 0, 0, 1, 0, 0, 0.0, scale));
+  QT_TRY(series_run(ctx, c, tw, GL, WR, SR, 0, 0, 1, 0, 0, 0.0, scale));
+  QT_TRY(series_run(ctx, c, tw, GR, WL, SR, 0, 0, 1, 0, 1, 0.0, scale));
+  QT_TRY(series_run(ctx, c, tw, GR, WR, SR, 0, 0, 1, 0, 1, 0.0, scale));
+  if (flags & QT_FLAG_SYNC) QT_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return QT_OK;
+}
+
+extern "C" qt_status qt_gw_sigma_post(qt_ctx* ctx, int nm, int nx, int nE, double* SR,
+                                      double* SL, double* SG, unsigned flags) {
+  if (!ctx || !SR || !SL || !SG || nm <= 0 || nx <= 0 || nE <= 0)
+    QT_FAIL(QT_ERR_ARG, "bad self-energy post-processing arguments");
+  if (!(flags & QT_FLAG_DEVICE_POINTERS)) QT_FAIL(QT_ERR_UNSUPPORTED, "device pointers required");
+  cudaSetDevice(ctx->device);
+  QT_TRY(gw_post(ctx, nm, nx, nE, reinterpret_cast<cd*>(SR), reinterpret_cast<cd*>(SL),
+                 reinterpret_cast<cd*>(SG)));
   if (flags & QT_FLAG_SYNC) QT_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return QT_OK;
 }

@@ -7,8 +7,10 @@ exchanges nothing until the final gather of the per-point results.  The
 reference gives every rank nen / comm_size energies and drops the remaining
 nen mod comm_size; ``energy_range`` spreads them over the first ranks instead,
 and reproduces the reference's split with ``drop_remainder=True``.  The RGF path
-has no data-path collective.  The one exchange step is ``energy_halo``, for the
-e-photon self-energy, which needs nop energies from each neighbouring shard.
+has no data-path collective.  The GW self-energy loop has two exchange steps:
+``energy_halo``, for the e-photon self-energy, which needs nop energies from each
+neighbouring shard, and the all-to-all transposes ``energies_to_ijs`` /
+``ijs_to_energies`` around the energy correlations and convolutions.
 """
 from __future__ import annotations
 
@@ -102,3 +104,71 @@ def energy_halo(local, nop, world, rank, group=None):
         for r in reqs:
             r.wait()
     return ext.numpy() if is_np else ext
+
+
+def ij_range(nij, world, rank):
+    """[lo, hi) of the block elements (i, j) that ``rank`` owns in the GW convolutions.
+
+    The reference gives every rank local_Nij = nm*nm / comm_size consecutive elements of the
+    column-major block, rank r from r * local_Nij (src/gw_mod.f90:171-172); a remainder of
+    nm*nm mod comm_size goes to the first ranks here, one each."""
+    return energy_range(nij, world, rank)
+
+
+def _all_to_all(send, out_counts, in_counts, group):
+    import torch
+    import torch.distributed as dist
+    if dist.get_backend(group) == "nccl" and send.device.type != "cuda":
+        raise ValueError("NCCL all-to-all needs device tensors")
+    recv = torch.empty(sum(out_counts), dtype=send.dtype, device=send.device)
+    real = torch.view_as_real if send.is_complex() else (lambda t: t)
+    dist.all_to_all_single(real(recv), real(send.contiguous()), out_counts, in_counts,
+                           group=group)
+    return recv
+
+
+def energies_to_ijs(x, nE, world, rank, group=None):
+    """Energy shards to element shards: energies_to_ijs_2 (src/gw_mod.f90:41-73).
+
+    ``x``: this rank's energies of a block quantity, a torch tensor (nE_local, nx, nij) with
+    nij = nm*nm elements in column-major order and nE_local from ``energy_range``.  Returns
+    (nE, nx, nij_local): every energy of the elements ``ij_range`` gives this rank, the
+    series layout of the energy correlations.  One all-to-all with the reference's
+    partition (each rank sends element range r of its energies to rank r and receives its
+    element range of every rank's energies); gloo for host tensors, NCCL for device
+    tensors.  The reference keeps the energy series contiguous per element
+    ((NE, nk, nx, local_Nij) in Fortran order); here they are interleaved across elements
+    (energy slowest), which the correlation kernel reads coalesced.
+    """
+    import torch
+    ne_loc, nx, nij = x.shape
+    counts = [energy_range(nE, world, r) for r in range(world)]
+    if ne_loc != counts[rank][1] - counts[rank][0]:
+        raise ValueError("local energies do not match energy_range")
+    if world == 1:
+        return x
+    ijr = [ij_range(nij, world, r) for r in range(world)]
+    c = ijr[rank][1] - ijr[rank][0]
+    send = torch.cat([x[:, :, lo:hi].reshape(-1) for lo, hi in ijr])
+    recv = _all_to_all(send, [(hi - lo) * nx * c for lo, hi in counts],
+                       [ne_loc * nx * (hi - lo) for lo, hi in ijr], group)
+    return recv.view(nE, nx, c)
+
+
+def ijs_to_energies(y, nij, world, rank, group=None):
+    """Element shards back to energy shards, the inverse of ``energies_to_ijs`` (the
+    reference calls it ijs_to_energies_2, src/gw_mod.f90:522-524, 700-702; its source is
+    absent).  ``y``: (nE, nx, nij_local) on this rank; returns (nE_local, nx, nij)."""
+    import torch
+    nE, nx, c = y.shape
+    ijr = [ij_range(nij, world, r) for r in range(world)]
+    if c != ijr[rank][1] - ijr[rank][0]:
+        raise ValueError("local elements do not match ij_range")
+    if world == 1:
+        return y
+    counts = [energy_range(nE, world, r) for r in range(world)]
+    ne_loc = counts[rank][1] - counts[rank][0]
+    recv = _all_to_all(y.reshape(-1), [ne_loc * nx * (hi - lo) for lo, hi in ijr],
+                       [(hi - lo) * nx * c for lo, hi in counts], group)
+    parts = recv.split([ne_loc * nx * (hi - lo) for lo, hi in ijr])
+    return torch.cat([p.view(ne_loc, nx, hi - lo) for p, (lo, hi) in zip(parts, ijr)], dim=2)
