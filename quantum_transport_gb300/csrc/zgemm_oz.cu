@@ -380,6 +380,125 @@ __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmAr
     // ======================== producers
     const int p = tid - 128;  // 0 .. NPROD-1
     uint32_t proc = 0, gchunk = 0;
+    if constexpr (BOTH) {
+      // Complex64: thread p stages row r of op(A) and column ct*NT + r of op(B), both in
+      // 8-K group g of every stage.  Pointers, k strides, signs and scales are fixed per
+      // work item.  Where an operand's k run is contiguous (op(A) transposed, op(B) = N)
+      // and 16-byte aligned, its four complex k of a stage come in two 16-byte loads.
+      static_assert(NPROD == 512 && NT == 128 && ITEMS == 2, "complex64 producer layout");
+      const int r = p & 127, g = p >> 7;
+      const uint32_t off = (uint32_t)((r >> 3) * SBO + g * LBO + (r & 7) * 16);
+      for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
+        const long long b = w / ntile;
+        const int ct = (int)(w % ntile);
+        if (a.active && !a.active[b]) continue;
+        const TIn* A = batch_ptr<const TIn>(a.A, b);
+        const TIn* B = batch_ptr<const TIn>(a.B, b);
+        const int* erow = a.scales + b * 256;
+        const int* fcol = erow + 128;
+        const int rb = ct * NT + r;  // column of op(B)
+        const bool okA = r < m, okB = rb < n;
+        const long long ldA = a.A.ld, ldB = a.B.ld;
+        const long long offA = a.opA == OP_N ? r : (long long)r * ldA;
+        const long long ksA = a.opA == OP_N ? ldA : 1;
+        const long long offB = a.opB == OP_N ? (long long)rb * ldB : rb;
+        const long long ksB = a.opB == OP_N ? 1 : ldB;
+        // k0 below is even, so element offset offX + k0 is even when ldX is
+        const bool vecA = ksA == 1 && (ldA & 1) == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0;
+        const bool vecB = ksB == 1 && (ldB & 1) == 0 && (reinterpret_cast<uintptr_t>(B) & 15) == 0;
+        // A' = (Re, Im) of op(A); B' real layout = (Re, -Im) of op(B); OP_C conjugates
+        const float sA = a.opA == OP_C ? -1.f : 1.f, sB = a.opB == OP_C ? 1.f : -1.f;
+        // 2^(8-e) as pre * scale: rows below 2^-119 would overflow a single FP32 power of
+        // two, so they are first lifted by 2^64 (exact).  Rows past m / n are zero.
+        const int eA = okA ? erow[r] : 0, eB = okB ? fcol[rb] : 0;
+        const bool tA = eA < -118, tB = eB < -118;
+        const float preA = tA ? 18446744073709551616.0f : 1.0f;
+        const float preB = tB ? 18446744073709551616.0f : 1.0f;
+        const float2 mA = make_float2(preA, preA * sA), mB = make_float2(preB, preB * sB);
+        const float scA = __int_as_float((127 + 8 - (tA ? eA + 64 : eA)) << 23);
+        const float scB = __int_as_float((127 + 8 - (tB ? eB + 64 : eB)) << 23);
+        for (int c = 0; c < nch; ++c, ++gchunk) {
+          const int st = gchunk % stages;
+          const uint32_t ph = (gchunk / stages) & 1;
+          unsigned char* stA = tiles + (size_t)st * stage_bytes;
+          unsigned char* stB = stA + APLANES * S * PLANE_BYTES;
+          const int k0 = c * (KC / 2) + 4 * g;
+          // the stage's global loads do not need its slot: they are in flight while the
+          // slot is being released
+          TIn xa[4], xb[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            xa[u] = make_float2(0.f, 0.f);
+            xb[u] = make_float2(0.f, 0.f);
+          }
+          if (k0 + 3 < K) {
+            if (okA) {
+              if (vecA) {
+                const float4 v0 = *reinterpret_cast<const float4*>(A + offA + k0);
+                const float4 v1 = *reinterpret_cast<const float4*>(A + offA + k0 + 2);
+                xa[0] = make_float2(v0.x, v0.y); xa[1] = make_float2(v0.z, v0.w);
+                xa[2] = make_float2(v1.x, v1.y); xa[3] = make_float2(v1.z, v1.w);
+              } else {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) xa[u] = A[offA + (k0 + u) * ksA];
+              }
+            }
+            if (okB) {
+              if (vecB) {
+                const float4 v0 = *reinterpret_cast<const float4*>(B + offB + k0);
+                const float4 v1 = *reinterpret_cast<const float4*>(B + offB + k0 + 2);
+                xb[0] = make_float2(v0.x, v0.y); xb[1] = make_float2(v0.z, v0.w);
+                xb[2] = make_float2(v1.x, v1.y); xb[3] = make_float2(v1.z, v1.w);
+              } else {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) xb[u] = B[offB + (k0 + u) * ksB];
+              }
+            }
+          } else {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              if (k0 + u < K) {
+                if (okA) xa[u] = A[offA + (k0 + u) * ksA];
+                if (okB) xb[u] = B[offB + (k0 + u) * ksB];
+              }
+            }
+          }
+          if (!mbar_wait(&empty[st], ph ^ 1, abort_flag)) break;
+          uint32_t pk[S][4], pk2[S][4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            float2 D[S];
+            digits_f32x2<S>(__fmul2_rn(xa[u], mA), scA, D);
+#pragma unroll
+            for (int s2 = 0; s2 < S; ++s2) {
+              pk[s2][u] = pack_pair(D[s2]);
+              pk2[s2][u] = pack_pair(make_float2(D[s2].y, D[s2].x)) ^ 0x80000000u;
+            }
+          }
+#pragma unroll
+          for (int s2 = 0; s2 < S; ++s2) {
+            *reinterpret_cast<uint4*>(stA + (size_t)s2 * PLANE_BYTES + off) =
+                make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
+            *reinterpret_cast<uint4*>(stA + (size_t)(S + s2) * PLANE_BYTES + off) =
+                make_uint4(pk2[s2][0], pk2[s2][1], pk2[s2][2], pk2[s2][3]);
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            float2 D[S];
+            digits_f32x2<S>(__fmul2_rn(xb[u], mB), scB, D);
+#pragma unroll
+            for (int s2 = 0; s2 < S; ++s2) pk[s2][u] = pack_pair(D[s2]);
+          }
+#pragma unroll
+          for (int s2 = 0; s2 < S; ++s2)
+            *reinterpret_cast<uint4*>(stB + (size_t)s2 * BPLANE + off) =
+                make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
+          fence_proxy_async();
+          mbar_arrive(&full[st]);
+        }
+        ++proc;
+      }
+    } else
     for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
       const long long b = w / (NPARTS == 2 ? ntile : 2 * ntile);
       const int part = BOTH ? 0 : (int)((w / ntile) & 1), ct = (int)(w % ntile);
@@ -397,10 +516,10 @@ __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmAr
       for (int c = 0; c < nch; ++c, ++gchunk) {
         const int st = gchunk % stages;
         const uint32_t ph = (gchunk / stages) & 1;
-        if (!mbar_wait(&empty[st], ph ^ 1, abort_flag)) break;
         unsigned char* stA = tiles + (size_t)st * stage_bytes;
         unsigned char* stB = stA + APLANES * S * PLANE_BYTES;
         const int kc0 = c * (KC / 2);  // complex k offset of this stage
+        // loads first: they are in flight while the stage's slot is being released
         TIn xv[ITEMS][4];
 #pragma unroll
         for (int q = 0; q < ITEMS; ++q) {
@@ -419,6 +538,7 @@ __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmAr
             xv[q][u] = x;
           }
         }
+        if (!mbar_wait(&empty[st], ph ^ 1, abort_flag)) break;
 #pragma unroll
         for (int q = 0; q < ITEMS; ++q) {
           const int item = p + q * NPROD;
