@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--scba-size", default="10,16,256",
                     help="slabs,orbitals,energies of the GW-SCBA device family")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="keep the library's default wave size instead of autotuning it")
     ap.add_argument("--workload", default="batched", choices=["batched", "uneven"],
                     help="batched: 100 x 128 slabs (the headline); uneven: the 4000-atom graph")
     return ap.parse_args()
@@ -294,6 +296,11 @@ def run_ours(a):
                              precision=precision, **kw)
 
     torch.cuda.synchronize()
+    # batch schedule: points per wave, measured on this workload before the warm-up
+    wave, wave_ms = 0, {}
+    if not a.no_tune:
+        from quantum_transport_gb300 import autotune
+        wave, wave_ms = autotune.tune_wave(ctx, lambda: step(0), P, nk=NK)
     for i in range(a.warmup):
         step(i)
     ctx.sync()
@@ -350,7 +357,10 @@ def run_ours(a):
             "FP64-grade c128 leads)", "data": "synthetic (seeded, no dataset)",
             "config": config_dict(a, {"parallelism": f"points sharded over {world} GPU(s)",
                                       "points_bad_status": status_bad,
-                                      "inverses_redone_fp64": ctx.inverse_fallbacks()}),
+                                      "inverses_redone_fp64": ctx.inverse_fallbacks(),
+                                      "wave_points": wave or "library default (608)",
+                                      "wave_tuning_ms_per_call": {str(k): round(v, 2) for k, v
+                                                                  in wave_ms.items()}}),
             "roofline": roofline, "clocks": clk, "gpu_launches": launches}
 
     if rank == 0 and a.fp64_energies > 0:
@@ -477,6 +487,10 @@ def run_uneven(a):
         rgf.rgf_variableblock_device(ctx, sizes, Hd, hoff, H1d, h1off, nk, E[e0:], nE, o,
                                      precision=precision, **kw)
 
+    wave, wave_ms = 0, {}
+    if not a.no_tune:
+        from quantum_transport_gb300 import autotune
+        wave, wave_ms = autotune.tune_wave(ctx, lambda: step(0), P, nk=nk)
     for i in range(a.warmup):
         step(i)
     ctx.sync()
@@ -519,7 +533,10 @@ def run_uneven(a):
                        "algorithmic_tflops": value * flops / 1e12,
                        "l2": "inputs and scratch per step exceed L2 (129 MB)",
                        "points_bad_status": int((out["status"] != 0).sum().item()),
-                       "inverses_redone_fp64": ctx.inverse_fallbacks()},
+                       "inverses_redone_fp64": ctx.inverse_fallbacks(),
+                       "wave_points": wave or "library default (608)",
+                       "wave_tuning_ms_per_call": {str(k): round(v, 2)
+                                                   for k, v in wave_ms.items()}},
             "roofline": {"kernel": "zgemm_oz_kernel (complex64 split product, 128-row tiles)",
                          "bound": "tensor", "achieved": alg_tf, "peak": peak, "unit": "TFLOP/s",
                          "frac": alg_tf / peak if peak else None, "traffic": None,

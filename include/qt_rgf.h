@@ -86,6 +86,12 @@ qt_status qt_ctx_sync(qt_ctx* ctx);
 qt_status qt_ctx_set_stream(qt_ctx* ctx, void* stream, int use_own);
 /* Bound (bytes) on the per-wave device scratch; default 48 GiB.            */
 qt_status qt_ctx_set_scratch_limit(qt_ctx* ctx, int64_t bytes);
+/* Batch schedule: (E, k) points solved together in one wave of the sweeps
+ * (qt_rgf_solve, qt_rgf_solve_vb, qt_gw_step, qt_scba_solve), rounded down to
+ * whole energies (multiples of nk) and bounded by the scratch limit; 0 (the
+ * default) = 608, four work items per SM of a 152-SM GPU.  Results do not
+ * depend on it.  quantum_transport_gb300/autotune.py picks it by measurement. */
+qt_status qt_ctx_set_wave_points(qt_ctx* ctx, int64_t points);
 /* Message of the last error on this thread ("" if none).                   */
 const char* qt_last_error(void);
 /* Library version string.                                                   */

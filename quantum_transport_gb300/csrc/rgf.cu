@@ -83,6 +83,7 @@ struct qt_ctx {
   cudaStream_t stream = nullptr;      // where every launch of this context goes
   cudaStream_t own_stream = nullptr;  // created with the context, destroyed with it
   int64_t scratch_limit = 48LL << 30;
+  int64_t wave_points = 0;  // points per wave; 0 = 4 work items per SM (608 on 152 SMs)
   void* arena = nullptr;
   size_t arena_bytes = 0;
   void* io = nullptr;  // staging for host-pointer calls
@@ -1189,7 +1190,8 @@ qt_status solve_wave_vb(qt_ctx* ctx, const ProblemVB& pb, long long p0, long lon
 long long choose_wave(const qt_ctx* ctx, const Problem& pb) {
   const size_t per = wave_bytes(pb, 1);
   long long P = (long long)((size_t)ctx->scratch_limit / (per + 1));
-  const long long target = 152 * 4;  // several work items per SM in every batched launch
+  // several work items per SM in every batched launch unless the context sets the wave
+  const long long target = ctx->wave_points > 0 ? ctx->wave_points : 152 * 4;
   P = std::min<long long>(P, std::max<long long>(target, pb.nk));
   P = std::min<long long>(P, pb.npts);
   P = std::max<long long>(P / pb.nk, 1) * pb.nk;
@@ -1264,6 +1266,12 @@ extern "C" qt_status qt_ctx_sync(qt_ctx* c) {
 extern "C" qt_status qt_ctx_set_scratch_limit(qt_ctx* c, int64_t bytes) {
   if (!c || bytes <= 0) QT_FAIL(QT_ERR_ARG, "bad scratch limit");
   c->scratch_limit = bytes;
+  return QT_OK;
+}
+
+extern "C" qt_status qt_ctx_set_wave_points(qt_ctx* c, int64_t points) {
+  if (!c || points < 0) QT_FAIL(QT_ERR_ARG, "bad wave size");
+  c->wave_points = points;
   return QT_OK;
 }
 
@@ -1409,7 +1417,8 @@ qt_status run_problem_vb(qt_ctx* ctx, ProblemVB& pb, long long hii_n, long long 
   }
   const size_t per = wave_bytes_vb(pb, 1);
   long long P = (long long)((size_t)ctx->scratch_limit / (per + 1));
-  P = std::min<long long>(P, std::max<long long>(152 * 4, pb.nk));
+  P = std::min<long long>(P, std::max<long long>(
+                                 ctx->wave_points > 0 ? ctx->wave_points : 152 * 4, pb.nk));
   P = std::min<long long>(P, pb.npts);
   P = std::max<long long>(P / pb.nk, 1) * pb.nk;
   QT_TRY(ensure(ctx->arena, ctx->arena_bytes, wave_bytes_vb(pb, P)));

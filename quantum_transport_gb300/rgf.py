@@ -65,6 +65,10 @@ class Context:
     def set_scratch_limit(self, nbytes):
         check(self._lib.qt_ctx_set_scratch_limit(self.handle, int(nbytes)))
 
+    def set_wave_points(self, points):
+        """Points per wave of the batched sweeps (0: the library's default of 608)."""
+        check(self._lib.qt_ctx_set_wave_points(self.handle, int(points)))
+
     def profile(self, enable=True):
         """Event-time every block product / inverse launch on this context's stream."""
         check(self._lib.qt_ctx_profile(self.handle, int(bool(enable))))
