@@ -279,7 +279,9 @@ __global__ __launch_bounds__(NT32) void zinv_f32_kernel(InvArgs a) {
 // (no row swaps): step k picks the unused row p with the largest |re|+|im| in column k
 // (warp-local search in the warp owning column k), and at the end the inverse is
 // X[k][j] = M[P[k]][P^-1[j]].  One __syncthreads per step (pivot column and index are
-// double-buffered in shared memory).
+// double-buffered in shared memory).  Lookahead: during step k the warp owning column k+1
+// first forms that column's step-k values (the same FMAs as its update) and takes step
+// k+1's pivot, so the search overlaps the other warps' updates.
 template <typename TC>
 __global__ __launch_bounds__(512, 1) void zinv_f32_rb_kernel(InvArgs a) {
   __shared__ float2 colbuf[2][128];
@@ -304,38 +306,42 @@ __global__ __launch_bounds__(512, 1) void zinv_f32_rb_kernel(InvArgs a) {
       }
     unsigned used = 0;
     if (tid == 0) badflag = 0;
-    for (int k = 0; k < 128; ++k) {
-      const int q = k & 1, wk = k >> 3, ck = k & 7;
-      if (w == wk) {
-        float best = -1.f;
-        int bi = 0x7fffffff;
+    // pivot search over one column (this lane's rows in v) into buffer slot qq: the unused
+    // row with the largest |re|+|im|, the lowest row on ties
+    auto search = [&](const float2 (&v)[4], int qq) {
+      float best = -1.f;
+      int bi = 0x7fffffff;
 #pragma unroll
-        for (int rr = 0; rr < 4; ++rr) {
-          float2 v = M[rr][0];
-#pragma unroll
-          for (int j = 1; j < 8; ++j)
-            if (j == ck) v = M[rr][j];
-          colbuf[q][4 * l + rr] = v;
-          float m = fabsf(v.x) + fabsf(v.y);
-          if (!(m == m)) m = 0.f;  // NaN: still selectable (flagged below), never skipped
-          if (!((used >> rr) & 1u) && (m > best || (m == best && 4 * l + rr < bi))) {
-            best = m;
-            bi = 4 * l + rr;
-          }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          const float ob = __shfl_xor_sync(0xffffffffu, best, o);
-          const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-          if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-        }
-        if (bi > 127) bi = 0;  // unreachable: 128 - k >= 1 unused rows always compete
-        if (l == 0) {
-          pbuf[q] = bi;
-          if (!(best > 0.f) || !isfinite(best)) badflag = 1;
+      for (int rr = 0; rr < 4; ++rr) {
+        colbuf[qq][4 * l + rr] = v[rr];
+        float m = fabsf(v[rr].x) + fabsf(v[rr].y);
+        if (!(m == m)) m = 0.f;  // NaN: still selectable (flagged below), never skipped
+        if (!((used >> rr) & 1u) && (m > best || (m == best && 4 * l + rr < bi))) {
+          best = m;
+          bi = 4 * l + rr;
         }
       }
-      __syncthreads();
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      if (bi > 127) bi = 0;  // unreachable: 128 - k >= 1 unused rows always compete
+      if (l == 0) {
+        pbuf[qq] = bi;
+        if (!(best > 0.f) || !isfinite(best)) badflag = 1;
+      }
+    };
+    if (w == 0) {  // step 0's pivot: column 0 as loaded
+      float2 v[4];
+#pragma unroll
+      for (int rr = 0; rr < 4; ++rr) v[rr] = M[rr][0];
+      search(v, 0);
+    }
+    __syncthreads();
+    for (int k = 0; k < 128; ++k) {
+      const int q = k & 1, wk = k >> 3, ck = k & 7;
       const int p = pbuf[q];
       const int lp = p >> 2, rp = p & 3;
       const float2 piv = colbuf[q][p];
@@ -352,6 +358,33 @@ __global__ __launch_bounds__(512, 1) void zinv_f32_rb_kernel(InvArgs a) {
         v.y = __shfl_sync(0xffffffffu, v.y, lp);
         rowp[j] = make_float2(v.x * inv.x - v.y * inv.y, v.x * inv.y + v.y * inv.x);
         if (w == wk && j == ck) rowp[j] = inv;
+      }
+      if (l == lp) used |= 1u << rp;
+      if (k < 127 && w == ((k + 1) >> 3)) {
+        // lookahead: column k+1 after step k (row p: the normalised pivot row; the others:
+        // the update below), then step k+1's pivot into the other buffer slot
+        const int cn = (k + 1) & 7;
+        float2 rn = rowp[0];
+#pragma unroll
+        for (int j = 1; j < 8; ++j)
+          if (j == cn) rn = rowp[j];
+        float2 v[4];
+#pragma unroll
+        for (int rr = 0; rr < 4; ++rr) {
+          float2 m = M[rr][0];
+#pragma unroll
+          for (int j = 1; j < 8; ++j)
+            if (j == cn) m = M[rr][j];
+          if (4 * l + rr == p) {
+            v[rr] = rn;
+          } else {
+            const float2 f = colbuf[q][4 * l + rr];
+            m.x = fmaf(-f.x, rn.x, m.x); m.x = fmaf(f.y, rn.y, m.x);
+            m.y = fmaf(-f.x, rn.y, m.y); m.y = fmaf(-f.y, rn.x, m.y);
+            v[rr] = m;
+          }
+        }
+        search(v, q ^ 1);
       }
 #pragma unroll
       for (int rr = 0; rr < 4; ++rr) {
@@ -374,8 +407,8 @@ __global__ __launch_bounds__(512, 1) void zinv_f32_rb_kernel(InvArgs a) {
           }
         }
       }
-      if (l == lp) used |= 1u << rp;
       if (tid == 0) perm[k] = p;
+      __syncthreads();
     }
     __syncthreads();
     if (tid < 128) pinv[tid] = -1;
