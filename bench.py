@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the library's default wave size instead of autotuning it")
+    ap.add_argument("--wave", type=int, default=0,
+                    help="points per wave, set without autotuning (0: autotune unless --no-tune)")
     ap.add_argument("--workload", default="batched", choices=["batched", "uneven"],
                     help="batched: 100 x 128 slabs (the headline); uneven: the 4000-atom graph")
     return ap.parse_args()
@@ -297,8 +299,10 @@ def run_ours(a):
 
     torch.cuda.synchronize()
     # batch schedule: points per wave, measured on this workload before the warm-up
-    wave, wave_ms = 0, {}
-    if not a.no_tune:
+    wave, wave_ms = a.wave, {}
+    if a.wave:
+        ctx.set_wave_points(a.wave)
+    elif not a.no_tune:
         from quantum_transport_gb300 import autotune
         wave, wave_ms = autotune.tune_wave(ctx, lambda: step(0), P, nk=NK)
     for i in range(a.warmup):
@@ -487,8 +491,10 @@ def run_uneven(a):
         rgf.rgf_variableblock_device(ctx, sizes, Hd, hoff, H1d, h1off, nk, E[e0:], nE, o,
                                      precision=precision, **kw)
 
-    wave, wave_ms = 0, {}
-    if not a.no_tune:
+    wave, wave_ms = a.wave, {}
+    if a.wave:
+        ctx.set_wave_points(a.wave)
+    elif not a.no_tune:
         from quantum_transport_gb300 import autotune
         wave, wave_ms = autotune.tune_wave(ctx, lambda: step(0), P, nk=nk)
     for i in range(a.warmup):
