@@ -67,10 +67,11 @@ cudaError_t zantiherm(int n, long long batch, BatchRef X, double c_re, double c_
 // Y_b = X_b^+
 template <typename TC>
 cudaError_t zdagger(int n, long long batch, BatchRef X, BatchRef Y, cudaStream_t s);
-// out_b = sum_ij |X_b(i,j)|  (the reference's Sancho error measure)
+// out_b = sum_ij |X_b(i,j)|  (the reference's Sancho error measure), exact to FP64 where it
+// decides the comparison with `near` (the decimation's tolerance), a few 1e-7 elsewhere
 template <typename TC>
 cudaError_t zabssum(int n, long long batch, BatchRef X, double* out, const unsigned char* active,
-                    cudaStream_t s);
+                    double near, cudaStream_t s);
 // out_b = sign * Re(f Tr[K Y1] - (f-1) Tr[K Y2]), K = -(X - X^+), f = fermi[b]
 template <typename TC>
 cudaError_t ztrace_current(int n, long long batch, BatchRef X, BatchRef Y1, BatchRef Y2,

@@ -566,8 +566,8 @@ qt_status sancho_wave(const Ops<double2>& op0, Arena& ar, long long P, BatchRef 
     // H_01 = H_01 B ; error = sum |H_01|            (:712-726)
     QT_TRY(op.gemm(H01, qt::OP_N, B, qt::OP_N, C, P, one, nullref(), {0, 0}, nullref(), active));
     std::swap(H01, C);
-    qt::zabssum<double2>(n, P, H01, err, active, s);
-    if (dual) qt::zabssum<double2>(n, P, H10, err2, active, s);  // the dual run's H_01
+    qt::zabssum<double2>(n, P, H01, err, active, tol, s);
+    if (dual) qt::zabssum<double2>(n, P, H10, err2, active, tol, s);  // the dual run's H_01
     cudaMemsetAsync(nact, 0, sizeof(int), s);
     sancho_update_kernel<<<g1d(P), 256, 0, s>>>(P, err, err2, tol, it, active, iters, nact);
     qt::count_launch();
