@@ -154,24 +154,49 @@ template <typename TC>
 __global__ void zinv_guard_kernel(int n, long long batch, BatchRef R, const unsigned char* active,
                                   double tol, unsigned char* flag, int* count) {
   __shared__ double part[32];
+  __shared__ bool undecided;
   for (long long b = blockIdx.x; b < batch; b += gridDim.x) {
     if (active && !active[b]) {
       if (threadIdx.x == 0) flag[b] = 0;
       continue;
     }
     const TC* r = batch_ptr<const TC>(R, b);
-    double s = 0.0;
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-      const TC v = r[e % n + (long long)(e / n) * R.ld];
-      s += (double)v.x * v.x + (double)v.y * v.y;
-    }
+    // ||R||_F^2 against tol^2.  Complex64 residuals: FP32 squares summed in FP32 per thread
+    // (relative error below 1e-4 for the <= 576 terms a thread adds at n <= 384; the FP64
+    // pipes are the cost of the FP64 sum), the FP64 sum only where that leaves the
+    // comparison undecided.  Complex128 residuals: the FP64 sum.
+    bool exact = sizeof(TC) == 16;
+    double t = 0.0;
+    for (int pass = exact ? 1 : 0; pass < 2; ++pass) {
+      double s = 0.0;
+      if (pass == 0) {
+        float f = 0.f;
+        for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+          const TC v = r[e % n + (long long)(e / n) * R.ld];
+          f = fmaf((float)v.x, (float)v.x, fmaf((float)v.y, (float)v.y, f));
+        }
+        s = f;
+      } else {
+        for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+          const TC v = r[e % n + (long long)(e / n) * R.ld];
+          s += (double)v.x * v.x + (double)v.y * v.y;
+        }
+      }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
-    __syncthreads();
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+      if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
+        // squares of moduli below 1e-19 may be lost in FP32: 2e-38 each at most
+        const double tt = tol * tol, slack = (double)n * n * 2e-38;
+        undecided = pass == 0 && !(t * (1.0 + 1e-4) + slack <= tt || t * (1.0 - 1e-4) - slack > tt);
+      }
+      __syncthreads();
+      if (!undecided) break;
+    }
     if (threadIdx.x == 0) {
-      double t = 0.0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
       const bool bad = !(t <= tol * tol);  // NaN counts as bad
       flag[b] = bad ? 1 : 0;
       if (bad && count) atomicAdd(count, 1);
