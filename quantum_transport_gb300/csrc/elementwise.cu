@@ -130,6 +130,26 @@ __device__ double block_sum(double v) {
   return v;  // valid in thread 0
 }
 
+// Y1_b += X_b and Y2_b += X_b in one pass over X (the decimation's paired updates)
+template <typename TC>
+__global__ void zadd2_kernel(int n, long long batch, BatchRef X, BatchRef Y1, BatchRef Y2,
+                             const unsigned char* active) {
+  for (long long b = blockIdx.x; b < batch; b += gridDim.x) {
+    if (active && !active[b]) continue;
+    const TC* x = batch_ptr<const TC>(X, b);
+    TC* y1 = batch_ptr<TC>(Y1, b);
+    TC* y2 = batch_ptr<TC>(Y2, b);
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      const int i = e % n, j = e / n;
+      const TC v = x[i + (long long)j * X.ld];
+      TC* p1 = y1 + i + (long long)j * Y1.ld;
+      TC* p2 = y2 + i + (long long)j * Y2.ld;
+      *p1 = tadd(*p1, v);
+      *p2 = tadd(*p2, v);
+    }
+  }
+}
+
 // sum_ij |X_ij| per block, compared against `near` by its user.  The moduli come from FP32
 // square roots of the components scaled by 2^40: relative error <= 3 2^-24 where the
 // squares stay normal (moduli above 1e-31), absolute error below 1e-31 under that, inf
@@ -344,6 +364,14 @@ cudaError_t zdagger(int n, long long batch, BatchRef X, BatchRef Y, cudaStream_t
   return cudaGetLastError();
 }
 template <typename TC>
+cudaError_t zadd2(int n, long long batch, BatchRef X, BatchRef Y1, BatchRef Y2,
+                  const unsigned char* active, cudaStream_t s) {
+  if (batch <= 0) return cudaSuccess;
+  zadd2_kernel<TC><<<grid_for(batch), NT, 0, s>>>(n, batch, X, Y1, Y2, active);
+  count_launch();
+  return cudaGetLastError();
+}
+template <typename TC>
 cudaError_t zabssum(int n, long long batch, BatchRef X, double* out, const unsigned char* active,
                     double near, cudaStream_t s) {
   if (batch <= 0) return cudaSuccess;
@@ -429,6 +457,8 @@ cudaError_t zcheck_finite(int n, long long batch, BatchRef X, int* status, cudaS
   template cudaError_t zantiherm<TC>(int, long long, BatchRef, double, double, BatchRef,          \
                                      BatchRef, cudaStream_t);                                     \
   template cudaError_t zdagger<TC>(int, long long, BatchRef, BatchRef, cudaStream_t);             \
+  template cudaError_t zadd2<TC>(int, long long, BatchRef, BatchRef, BatchRef,                   \
+                                 const unsigned char*, cudaStream_t);                             \
   template cudaError_t zabssum<TC>(int, long long, BatchRef, double*, const unsigned char*,       \
                                    double, cudaStream_t);                                         \
   template cudaError_t ztrace_current<TC>(int, long long, BatchRef, BatchRef, BatchRef, double,   \

@@ -67,6 +67,10 @@ cudaError_t zantiherm(int n, long long batch, BatchRef X, double c_re, double c_
 // Y_b = X_b^+
 template <typename TC>
 cudaError_t zdagger(int n, long long batch, BatchRef X, BatchRef Y, cudaStream_t s);
+// Y1_b += X_b; Y2_b += X_b  (Y1, Y2 and X distinct)
+template <typename TC>
+cudaError_t zadd2(int n, long long batch, BatchRef X, BatchRef Y1, BatchRef Y2,
+                  const unsigned char* active, cudaStream_t s);
 // out_b = sum_ij |X_b(i,j)|  (the reference's Sancho error measure), exact to FP64 where it
 // decides the comparison with `near` (the decimation's tolerance), a few 1e-7 elsewhere
 template <typename TC>

@@ -554,15 +554,14 @@ qt_status sancho_wave(const Ops<double2>& op0, Arena& ar, long long P, BatchRef 
     // B = A H_10 ; H_SS += H_01 B ; H_BB += H_01 B      (:698-702)
     QT_TRY(op.gemm(A, qt::OP_N, H10, qt::OP_N, B, P, one, nullref(), {0, 0}, nullref(), active));
     QT_TRY(op.gemm(H01, qt::OP_N, B, qt::OP_N, C, P, one, nullref(), {0, 0}, nullref(), active));
-    qt::zaxpby<double2>(n, P, HSS, 1, 0, C, 1, 0, nullref(), HSS, active, s);
-    qt::zaxpby<double2>(n, P, HBB, 1, 0, C, 1, 0, nullref(), HBB, active, s);
+    qt::zadd2<double2>(n, P, C, HSS, HBB, active, s);  // H_SS += C ; H_BB += C
     // C = H_10 B ; B = A H_01 ; A = H_10 B ; H_10 = C ; H_BB += A    (:704-711)
     QT_TRY(op.gemm(H10, qt::OP_N, B, qt::OP_N, C, P, one, nullref(), {0, 0}, nullref(), active));
     QT_TRY(op.gemm(A, qt::OP_N, H01, qt::OP_N, B, P, one, nullref(), {0, 0}, nullref(), active));
     QT_TRY(op.gemm(H10, qt::OP_N, B, qt::OP_N, A, P, one, nullref(), {0, 0}, nullref(), active));
     std::swap(H10, C);
-    qt::zaxpby<double2>(n, P, HBB, 1, 0, A, 1, 0, nullref(), HBB, active, s);
-    if (dual) qt::zaxpby<double2>(n, P, HSS2, 1, 0, A, 1, 0, nullref(), HSS2, active, s);
+    if (dual) qt::zadd2<double2>(n, P, A, HBB, HSS2, active, s);  // H_BB += A ; H_SS2 += A
+    else qt::zaxpby<double2>(n, P, HBB, 1, 0, A, 1, 0, nullref(), HBB, active, s);
     // H_01 = H_01 B ; error = sum |H_01|            (:712-726)
     QT_TRY(op.gemm(H01, qt::OP_N, B, qt::OP_N, C, P, one, nullref(), {0, 0}, nullref(), active));
     std::swap(H01, C);

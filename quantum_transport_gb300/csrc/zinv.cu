@@ -411,19 +411,41 @@ __global__ __launch_bounds__(512, 1) void zinv_f32_rb_kernel(InvArgs a) {
         }
         search(v, q ^ 1);
       }
+      // the pivot column's special case only exists in warp wk: the other warps run the
+      // update without testing for it (same arithmetic in both)
+      if (w == wk) {
 #pragma unroll
-      for (int rr = 0; rr < 4; ++rr) {
-        const int r = 4 * l + rr;
-        if (r == p) {
+        for (int rr = 0; rr < 4; ++rr) {
+          const int r = 4 * l + rr;
+          if (r == p) {
 #pragma unroll
-          for (int j = 0; j < 8; ++j) M[rr][j] = rowp[j];
-        } else {
-          const float2 f = colbuf[q][r];
+            for (int j = 0; j < 8; ++j) M[rr][j] = rowp[j];
+          } else {
+            const float2 f = colbuf[q][r];
 #pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            if (w == wk && j == ck) {
-              M[rr][j] = make_float2(-(f.x * inv.x - f.y * inv.y), -(f.x * inv.y + f.y * inv.x));
-            } else {
+            for (int j = 0; j < 8; ++j) {
+              if (j == ck) {
+                M[rr][j] = make_float2(-(f.x * inv.x - f.y * inv.y), -(f.x * inv.y + f.y * inv.x));
+              } else {
+                float2 m = M[rr][j];
+                m.x = fmaf(-f.x, rowp[j].x, m.x); m.x = fmaf(f.y, rowp[j].y, m.x);
+                m.y = fmaf(-f.x, rowp[j].y, m.y); m.y = fmaf(-f.y, rowp[j].x, m.y);
+                M[rr][j] = m;
+              }
+            }
+          }
+        }
+      } else {
+#pragma unroll
+        for (int rr = 0; rr < 4; ++rr) {
+          const int r = 4 * l + rr;
+          if (r == p) {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) M[rr][j] = rowp[j];
+          } else {
+            const float2 f = colbuf[q][r];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
               float2 m = M[rr][j];
               m.x = fmaf(-f.x, rowp[j].x, m.x); m.x = fmaf(f.y, rowp[j].y, m.x);
               m.y = fmaf(-f.x, rowp[j].y, m.y); m.y = fmaf(-f.y, rowp[j].x, m.y);
