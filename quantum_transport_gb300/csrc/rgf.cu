@@ -377,11 +377,13 @@ struct Ops {
     const BatchRef R = ref(rt1, (long long)n * n, nn), T = ref(rt2, (long long)n * n, nn);
     const bool guarded = guard && (sizeof(TC) == 16 || fbw);
     if (guarded && batch > P) QT_FAIL(QT_ERR_ARG, "inverse guard scratch too small");
-    // With three or more steps the last one runs only for entries whose previous residual
-    // has ||R||_F > 3e-9: R_{k+1} = R_k^2 up to the products' rounding, so the others are at
-    // FP64 resolution already (||R|| <= 1e-17).  The guard flags hold that mask once the
-    // FP64 redo of step 0 has read them.
-    const bool skip_last = guarded && refine >= 3 && !getenv("QT_REFINE_ALL");
+    // With three or more steps on one-tile blocks, the last step runs only for entries whose
+    // previous residual has ||R||_F > 3e-9: R_{k+1} = R_k^2 up to the products' rounding, so
+    // the others are at FP64 resolution already (||R|| <= 1e-17).  The guard flags hold that
+    // mask once the FP64 redo of step 0 has read them.  Blocks above one tile start from the
+    // 2 x 2 block form, where the last step was measured to still pay (a 4.5x larger T(E)
+    // error without it on an ill-conditioned device), so they keep every step.
+    const bool skip_last = guarded && refine >= 3 && nn <= SPLIT_TILE && !getenv("QT_REFINE_ALL");
     for (int it = 0; it < refine; ++it) {
       const bool masked = skip_last && it == refine - 1;
       const unsigned char* act = masked ? guard : active;
