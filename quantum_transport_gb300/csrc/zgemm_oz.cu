@@ -172,20 +172,24 @@ __device__ __forceinline__ void digits_f64(double x, int e, float* D) {
     else if (sh > -63) T = (m + (1ll << (-sh - 1))) >> (-sh);
     if (bits < 0) T = -T;
   }
-  int d[S];
+  // Balanced digits d_s in [-128, 127], T = sum_s d_s 256^(S-1-s), without the digit-by-digit
+  // carry loop: with V = T + 128 (1 + 256 + ... + 256^(S-2)), byte j of V is d_(S-1-j) + 128
+  // for j < S-1 (each byte's +128 absorbs the borrow of the digit below it), and
+  // V >> 8(S-1) is d_0.
+  unsigned long long K = 0;
 #pragma unroll
-  for (int s = S - 1; s >= 1; --s) {
-    const int lo = (int)((unsigned)T & 255u);
-    const int di = ((lo + 128) & 255) - 128;
-    d[s] = di;
-    T = (T - di) >> 8;
-  }
-  d[0] = (int)T;
+  for (int j = 0; j < S - 1; ++j) K |= 0x80ull << (8 * j);
+  const unsigned long long V = (unsigned long long)T + K;
 #pragma unroll
-  for (int s = 0; s < S; ++s) {
-    const float f = __int_as_float(0x4B400000 + d[s]) - 12582912.0f;  // exact float(d)
-    D[s] = f * __int_as_float((127 - 8 * s) << 23);                     // * 2^-8s (exact)
+  for (int j = 0; j < S - 1; ++j) {
+    const int s = S - 1 - j;
+    const unsigned byte = (unsigned)(V >> (8 * j)) & 255u;
+    const float sc = __int_as_float((127 - 8 * s) << 23);  // 2^-8s
+    // (12582912 + byte) 2^-8s - 12583040 2^-8s = (byte - 128) 2^-8s, exact in one FMA
+    D[s] = fmaf(__uint_as_float(0x4B400000u | byte), sc, -12583040.0f * sc);
   }
+  const int top = (int)((long long)V >> (8 * (S - 1)));
+  D[0] = __int_as_float(0x4B400000 + top) - 12582912.0f;  // exact float(d_0)
 }
 __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
   // the digits carry <= 8 significant bits: truncation to BF16 is exact
