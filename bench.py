@@ -18,7 +18,7 @@ Reported (one JSON line on rank 0):
                and the T(E) error of the split path against it
 
 ``--impl reference`` times the CPU restatement (the reference's Fortran
-cannot be built on this machine or the GPU machine: no Fortran compiler).
+cannot be built here: no Fortran compiler is installed).
 
 ``--workload uneven`` measures the uneven-block configuration instead: a
 4000-atom random tight-binding graph sliced into 25 slabs of 134-184 orbitals,

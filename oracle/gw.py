@@ -1,7 +1,8 @@
 """FP64 oracle of the GW/SCBA self-energy loop -- TEST INFRASTRUCTURE ONLY.
 
-Restates the steps of gw_ephoton_3d_ijs (src/gw_mod.f90:78-1070) that the
-north star names, for one k-point (nk = 1):
+Restates the steps of gw_ephoton_3d_ijs (src/gw_mod.f90:78-1070) that make up
+the GW self-energy loop (RGF, polarisation, screened interaction, self-energy,
+mixing), for one k-point (nk = 1):
 
 * energy correlation / convolution (src/fft_mod.f90:58-168, corr1d2 / conv1d2)
   on a uniform energy grid E_e = E_0 + e dE (e = 0..n-1) and the centred
