@@ -62,6 +62,8 @@ class GpuStages:
         import torch
         s = self.sys
         G = [s.zeros() for _ in range(3)]
+        if s.nE == 0:  # a rank with no energies still takes part in the exchanges
+            return tuple(G)
         out = {"G_r": G[0], "G_lesser": G[1], "G_greater": G[2],
                "status": torch.zeros(s.nE, dtype=torch.int32, device="cuda")}
         o = _lib.QtOutputs(*[_ptr(out.get(k)) for k in OUT_KEYS])
@@ -76,6 +78,8 @@ class GpuStages:
         n = gr.shape[0]
         ns = gr[0].numel()
         P = [self.zeros(gr.shape) for _ in range(3)]
+        if ns == 0:  # no block elements on this rank
+            return tuple(P)
         check(self.lib.qt_gw_polarization(self.ctx.handle, n, ns, _ptr(gr), _ptr(gl), _ptr(gg),
                                           _ptr(glt), _ptr(ggt), scale, _ptr(P[0]), _ptr(P[1]),
                                           _ptr(P[2]), self.flags))
@@ -85,6 +89,8 @@ class GpuStages:
         nm = PR.shape[-1]
         nblk = PR.numel() // (nm * nm)
         W = [self.zeros(PR.shape) for _ in range(3)]
+        if nblk == 0:
+            return tuple(W)
         check(self.lib.qt_gw_screened(self.ctx.handle, nm, nblk, _ptr(self.sys.V), _ptr(PR),
                                       _ptr(PL), _ptr(PG), _ptr(W[0]), _ptr(W[1]), _ptr(W[2]),
                                       self.sys.prec, self.flags))
@@ -94,6 +100,8 @@ class GpuStages:
         n = gr.shape[0]
         ns = gr[0].numel()
         S = [self.zeros(gr.shape) for _ in range(3)]
+        if ns == 0:
+            return tuple(S)
         check(self.lib.qt_gw_selfenergy(self.ctx.handle, n, ns, _ptr(gr), _ptr(gl), _ptr(gg),
                                         _ptr(wr), _ptr(wl), _ptr(wg), scale, _ptr(S[0]),
                                         _ptr(S[1]), _ptr(S[2]), self.flags))
@@ -101,6 +109,8 @@ class GpuStages:
 
     def post(self, SR, SL, SG):
         ne, nx, nm = SR.shape[0], SR.shape[1], SR.shape[-1]
+        if ne == 0:
+            return
         check(self.lib.qt_gw_sigma_post(self.ctx.handle, nm, nx, ne, _ptr(SR), _ptr(SL),
                                         _ptr(SG), self.flags | _lib.QT_FLAG_SYNC))
 

@@ -209,6 +209,15 @@ def test_sharded_scba_matches_one_process(world, nE):
     _check_against_oracle(parts, nE, iters)
 
 
+def test_ranks_without_energies_still_exchange():
+    """Three ranks over two energies: the third owns none and still takes part in every
+    all-to-all; the maps agree with one process."""
+    nE, iters, world = 2, 2, 3
+    parts = _spawn(_scba_rank, world, nE, iters)
+    assert parts[2][0].shape[0] == 0
+    _check_against_oracle(parts, nE, iters)
+
+
 def test_one_rank_scba_needs_no_process_group():
     from quantum_transport_gb300.gw_shard import ShardedGw
     nE, iters = 10, 2
