@@ -199,11 +199,11 @@ def _check_against_oracle(parts, nE, iters):
         np.testing.assert_allclose(p[3], res, rtol=1e-9)
 
 
-@pytest.mark.parametrize("world,nE", [(2, 12), (3, 13)])
+@pytest.mark.parametrize("world,nE", [(2, 12), (3, 13), (4, 13)])
 def test_sharded_scba_matches_one_process(world, nE):
-    """Three maps of the SCBA loop split over ranks (uneven energy and element shares for
-    world 3 with nE = 13, nm*nm = 9 split 3/3/3 and world 2 split 5/4) agree with the
-    oracle's one-process loop, self-energies and residuals."""
+    """Three maps of the SCBA loop split over ranks agree with the oracle's one-process
+    loop, self-energies and residuals. The shares are uneven: nm*nm = 9 elements split 5/4,
+    3/3/3 and 3/2/2/2, and 13 energies split 5/4/4 and 4/3/3/3."""
     iters = 3
     parts = _spawn(_scba_rank, world, nE, iters)
     _check_against_oracle(parts, nE, iters)
