@@ -56,6 +56,10 @@ typedef enum {
 #define QT_FLAG_DEVICE_POINTERS 1u /* all arrays are device pointers            */
 #define QT_FLAG_CAROLI 2u          /* also compute Caroli T(E) (qt_outputs.T)    */
 #define QT_FLAG_SYNC 4u            /* synchronise the stream before returning   */
+#define QT_FLAG_SANCHO_RESET 8u    /* qt_sancho_batch: green_RGF_RS's decimation
+                                      (src/gw_mod.f90:1440-1445): an entry not
+                                      converged after max_iter steps restarts
+                                      from H_SS = H_BB = H00                   */
 
 /* Reference-quirk switches (default 0 = the behaviour that produced the
  * reference's test_cnt/ outputs).                                            */
@@ -68,6 +72,13 @@ typedef enum {
 #define QT_QUIRK_BACK_H1I_NEXT 4u /* backward step couples l,l+1 through
                                     H1i(l+1) instead of the reference's H1i(l)
                                     (identical for slab-independent coupling) */
+#define QT_QUIRK_GW_SANCHO_RESET 8u /* lead decimation of green_RGF_RS
+                                    (src/gw_mod.f90:1440-1445): a point whose
+                                    decimation is not converged after
+                                    sancho_max_iter steps takes H_SS = H_BB =
+                                    H00, i.e. the isolated-slab surface
+                                    function; off by default (the points keep
+                                    their last iterate and are flagged)     */
 
 typedef struct qt_ctx qt_ctx;
 
@@ -310,15 +321,28 @@ qt_status qt_zinv_batch(qt_ctx* ctx, int n, int batch, const double* A, int64_t 
  * array of QT_NOALLOC_MAX_BATCH x 256 ints (512 KiB per GPU, held until the
  * process exits), and it needs no context: work goes on `stream`.
  *   - batch > QT_NOALLOC_MAX_BATCH is rejected with QT_ERR_ARG;
- *   - the first call on a device fetches the array's device address with
- *     cudaGetSymbolAddress; make it before any stream capture;
+ *   - every call looks up the array's device address with
+ *     cudaGetSymbolAddress (the caller's device current).  Under CUDA's
+ *     default lazy module loading the first call on a device loads the
+ *     library's device module, which can allocate module memory and
+ *     synchronise: make one warm-up call outside latency-critical code and
+ *     before any stream capture, or set CUDA_MODULE_LOADING=EAGER;
  *   - all calls share the array, so calls overlapping on the GPU race;
- *   - it calls no cudaMalloc, cudaFree or other allocating routine.         */
+ *   - it calls no cudaMalloc, cudaFree or other allocating routine;
+ *   - QT_OK means the work was enqueued.  A bounded wait inside the
+ *     tensor-core kernel that runs out (4 s) leaves C partly written; it is
+ *     counted in a word of the same static array (never in a context's
+ *     counter) and read back by qt_noalloc_timeouts.                        */
 #define QT_NOALLOC_MAX_BATCH 512
 qt_status qt_zgemm_batch_noalloc(int n, int batch, char opA, const double* A, int64_t a_stride,
                                  char opB, const double* B, int64_t b_stride, const double* alpha,
                                  const double* beta, const double* D, int64_t d_stride, double* C,
                                  int64_t c_stride, int slices, void* stream);
+/* Timeouts of qt_zgemm_batch_noalloc calls on the current device since the last
+ * read: synchronises `stream`, stores the count in *count and clears it.  Call
+ * it after the products' stream has finished; a non-zero count means those
+ * results are incomplete.  No counterpart in the reference (see above).     */
+qt_status qt_noalloc_timeouts(int* count, void* stream);
 
 /* ---- GW / SCBA (one k-point; device pointers: QT_FLAG_DEVICE_POINTERS required).
  * Energy-resolved arrays are [nE][nx][nm*nm] complex128 column-major

@@ -133,9 +133,12 @@ def copy_edges(S):
     return S
 
 
-def green(E, H00, H10, nx, SR, SL, *, mu, temp, eta_lead=1e-3, sancho_nmax=100):
+def green(E, H00, H10, nx, SR, SL, *, mu, temp, eta_lead=1e-3, sancho_nmax=100,
+          sancho_reset=False):
     """G^{R,<,>} diagonal blocks (nE, nx, nm, nm) for self-energies SR, SL (green_RGF_RS).
-    ``H00``: one on-site block (nm, nm) for every slab, or one per slab (nx, nm, nm)."""
+    ``H00``: one on-site block (nm, nm) for every slab, or one per slab (nx, nm, nm).
+    ``sancho_reset``: green_RGF_RS's lead decimation as written, restarting an unconverged
+    run from H_SS = H_BB = H00 (src/gw_mod.f90:1440-1445)."""
     nE = len(E)
     nm = H00.shape[-1]
     Hii = list(H00) if H00.ndim == 3 else [H00] * nx
@@ -146,7 +149,7 @@ def green(E, H00, H10, nx, SR, SL, *, mu, temp, eta_lead=1e-3, sancho_nmax=100):
         o = orc.rgf_constblocksize(e, Hii, [H10] * (nx + 1), None, list(SL[ie]),
                                    list(SR[ie]), mul=mu[0], mur=mu[1], templ=temp[0],
                                    tempr=temp[1], eta_lead=eta_lead, sancho_nmax=sancho_nmax,
-                                   sancho_tol=1e-100)
+                                   sancho_tol=1e-100, sancho_reset=sancho_reset)
         GR[ie] = np.stack(o["G_r"])
         GL[ie] = np.stack(o["G_lesser"])
         GG[ie] = np.stack(o["G_greater"])

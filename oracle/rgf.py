@@ -153,8 +153,11 @@ def _coupling(H1i, l, mode):
 def rgf_constblocksize(E, Hii, H1i, Sii=None, sigma_lesser_ph=None, sigma_r_ph=None,
                        mul=0.0, mur=0.0, templ=300.0, tempr=300.0, *, quirks=None,
                        eta_lead=1e-5, sancho_nmax=50, sancho_tol=1e-100,
-                       interior_eta=0.0, want_blocks=True):
+                       interior_eta=0.0, want_blocks=True, sancho_reset=False):
     """One (E,k) point of the ballistic/phonon RGF, src/cuda_rgf_mod.f90:53-413.
+
+    ``sancho_reset``: the leads use green_RGF_RS's decimation, which restarts an
+    unconverged run from H_SS = H_BB = H00 (src/gw_mod.f90:1440-1445).
 
     Returns a dict with G_r, G_lesser, G_greater, Jdens (lists of nx blocks,
     when ``want_blocks``), their diagonals, tr, tre, the Sancho surface/bulk
@@ -183,7 +186,8 @@ def rgf_constblocksize(E, Hii, H1i, Sii=None, sigma_lesser_ph=None, sigma_r_ph=N
     H00 = Hii[0] + sigma_r_ph[0] @ S00
     H10 = H1i[0]
     G00L, GBBL, itL, errL, inf = sancho(E, S00, H00, dag(H10), eta=eta_lead,
-                                        nmax=sancho_nmax, tol=sancho_tol)
+                                        nmax=sancho_nmax, tol=sancho_tol,
+                                        reset_on_nmax=sancho_reset)
     info = info or inf
     sigmal = H10 @ G00L @ dag(H10)
     fl = fermi(q["left_fermi"][0] + q["left_fermi"][1])
@@ -212,7 +216,8 @@ def rgf_constblocksize(E, Hii, H1i, Sii=None, sigma_lesser_ph=None, sigma_r_ph=N
     # own H1i(nx+1) in the CPU routine (src/rgf_mod.f90:153); device coupling H1i(nx)
     Hlead = H1i[nx - 1] if q.get("right_coupling", "nx") == "nx" else H1i[nx]
     G00R, GBBR, itR, errR, inf = sancho(E, S00, H00, Hlead, eta=eta_lead,
-                                        nmax=sancho_nmax, tol=sancho_tol)
+                                        nmax=sancho_nmax, tol=sancho_tol,
+                                        reset_on_nmax=sancho_reset)
     info = info or inf
     sigmar = dag(Hlead) @ G00R @ Hlead
     H10 = H1i[nx - 1]

@@ -14,8 +14,9 @@ LIB_PATH = os.path.join(HERE, "libqtgpu.so")
 
 QT_OK, QT_ERR_ARG, QT_ERR_CUDA, QT_ERR_NOMEM, QT_ERR_UNSUPPORTED, QT_ERR_POINTS = range(6)
 QT_PREC_FP64, QT_PREC_MIXED, QT_PREC_MIXED_FP64 = 0, 1, 2
-QT_FLAG_DEVICE_POINTERS, QT_FLAG_CAROLI, QT_FLAG_SYNC = 1, 2, 4
+QT_FLAG_DEVICE_POINTERS, QT_FLAG_CAROLI, QT_FLAG_SYNC, QT_FLAG_SANCHO_RESET = 1, 2, 4, 8
 QT_QUIRK_CPU_FERMI, QT_QUIRK_GLP_ZERO, QT_QUIRK_BACK_H1I_NEXT = 1, 2, 4
+QT_QUIRK_GW_SANCHO_RESET = 8
 QT_PT_SINGULAR, QT_PT_SANCHO_NOT_CONVERGED, QT_PT_NONFINITE = 1, 2, 4
 
 # every symbol include/qt_rgf.h declares
@@ -24,7 +25,7 @@ EXPORTS = [
     "qt_last_error", "qt_version", "qt_rgf_solve", "qt_rgf_constblocksize",
     "qt_sancho_batch", "qt_zgemm_batch", "qt_zinv_batch", "qt_kernel_launches",
     "qt_ctx_profile", "qt_ctx_profile_read", "qt_ctx_stream", "qt_gw_step", "qt_scba_solve",
-    "qt_corr_batch", "qt_zgemm_batch_noalloc",
+    "qt_corr_batch", "qt_zgemm_batch_noalloc", "qt_noalloc_timeouts",
     "qt_mlp_create", "qt_mlp_destroy", "qt_mlp_num_params", "qt_mlp_get_params",
     "qt_mlp_set_params", "qt_mlp_infer", "qt_mlp_grad", "qt_mlp_train_step",
     "qt_mix_diag", "qt_mix_features", "qt_mix_apply", "qt_mix_gram", "qt_mix_combine",
@@ -117,6 +118,7 @@ def load(path=LIB_PATH):
                                      vp]
     lib.qt_zgemm_batch_noalloc.argtypes = [ci, ci, C.c_char, vp, i64, C.c_char, vp, i64, vp, vp,
                                            vp, i64, vp, i64, ci, vp]
+    lib.qt_noalloc_timeouts.argtypes = [C.POINTER(ci), vp]
     flt = C.c_float
     lib.qt_mlp_create.argtypes = [vp, ci, ci, ci, ci, ci, vp, C.c_uint64, C.POINTER(vp)]
     lib.qt_mlp_destroy.argtypes = [vp]

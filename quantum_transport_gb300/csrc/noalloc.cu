@@ -11,34 +11,43 @@
 //   * latency-critical loops, where cudaMalloc/cudaFree would implicitly
 //     synchronise the whole device and stall the other streams.
 // For them this entry point keeps the table in a file-scope device array of
-// fixed size, allocated once when the library's module is loaded, and needs no
-// context: it allocates nothing and takes the caller's stream.
+// fixed size and needs no context: it allocates nothing and takes the caller's
+// stream.
 //
 // Limits and sharing rules:
 //   * at most QT_NOALLOC_MAX_BATCH (512) batch entries per call: 512 x 256
 //     ints = 512 KiB of device memory, held by every GPU that loads the library
 //     until the process exits;
-//   * the first call on each device looks up the array's device address
-//     (cudaGetSymbolAddress) with that device current; make that first call
-//     before any stream capture;
+//   * the array belongs to the library's device module.  Under CUDA's default
+//     lazy module loading that module is loaded by the first call on a device,
+//     which can allocate module memory and synchronise: make one warm-up call
+//     outside latency-critical regions and before any stream capture (or set
+//     CUDA_MODULE_LOADING=EAGER);
+//   * every call looks up the array's device address (cudaGetSymbolAddress,
+//     with the caller's device current), so the address stays valid across a
+//     device reset;
 //   * every call shares the one array: calls that overlap on the GPU (other
 //     streams, other host threads) race on it.  Serialise them, e.g. on one
-//     stream.  Nothing needs clearing between calls: the prologue rewrites
-//     every exponent the product then reads.
-#include <mutex>
-
+//     stream.  The exponent table needs no clearing between calls: the prologue
+//     rewrites every exponent the product then reads;
+//   * a wait inside the tensor-core kernel that runs out (4 s) leaves C partly
+//     written.  Such timeouts are counted in a word of the same array, never in
+//     the context library's counter; qt_noalloc_timeouts reads and clears it
+//     after the caller has synchronised its stream.
 #include "../../include/qt_rgf.h"
 #include "qt_common.cuh"
 #include "qt_kernels.h"
 
 namespace {
 
-constexpr int kMaxDevices = 64;
+// [0, MAX * 256): exponent table; [MAX * 256]: timeout count of the tensor-core kernel
+constexpr int kTimeoutWord = QT_NOALLOC_MAX_BATCH * 256;
+static __device__ __align__(256) int g_noalloc_scratch[kTimeoutWord + 64];
 
-static __device__ __align__(256) int g_noalloc_scales[QT_NOALLOC_MAX_BATCH * 256];
-
-int* g_scales_addr[kMaxDevices] = {nullptr};  // device address of the array, per device
-std::mutex g_setup_mutex;
+// device address of the array on the current device (host code only sees a stand-in)
+cudaError_t scratch_address(int** out) {
+  return cudaGetSymbolAddress(reinterpret_cast<void**>(out), g_noalloc_scratch);
+}
 
 int parse_op(char c) {
   if (c == 'N' || c == 'n') return qt::OP_N;
@@ -76,27 +85,11 @@ extern "C" qt_status qt_zgemm_batch_noalloc(int n, int batch, char opA, const do
     qt_set_last_error("qt_zgemm_batch_noalloc: alpha and beta must be real", __FILE__, __LINE__);
     return QT_ERR_UNSUPPORTED;
   }
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
-    qt_set_last_error(e != cudaSuccess ? cudaGetErrorString(e) : "device index out of range",
-                      __FILE__, __LINE__);
-    return QT_ERR_CUDA;
-  }
   int* scales = nullptr;
-  {
-    std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scales_addr[dev]) {
-      // host code sees only a stand-in for the device array: fetch its device address
-      // once per device, with that device current
-      e = cudaGetSymbolAddress(reinterpret_cast<void**>(&g_scales_addr[dev]), g_noalloc_scales);
-      if (e != cudaSuccess) {
-        g_scales_addr[dev] = nullptr;
-        qt_set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
-        return QT_ERR_CUDA;
-      }
-    }
-    scales = g_scales_addr[dev];
+  cudaError_t e = scratch_address(&scales);
+  if (e != cudaSuccess) {
+    qt_set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+    return QT_ERR_CUDA;
   }
   qt::GemmArgs g{};
   g.m = g.n = g.k = n;
@@ -119,10 +112,33 @@ extern "C" qt_status qt_zgemm_batch_noalloc(int n, int batch, char opA, const do
   g.batch = batch;
   g.active = nullptr;
   g.scales = scales;
+  g.timeouts = scales + kTimeoutWord;
   e = qt::zgemm_oz(g, sl, sl - 1, reinterpret_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) {
     qt_set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
     return QT_ERR_CUDA;
   }
+  return QT_OK;
+}
+
+extern "C" qt_status qt_noalloc_timeouts(int* count, void* stream) {
+  if (!count) {
+    qt_set_last_error("qt_noalloc_timeouts: count is null", __FILE__, __LINE__);
+    return QT_ERR_ARG;
+  }
+  int* base = nullptr;
+  cudaError_t e = scratch_address(&base);
+  const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  int h = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, base + kTimeoutWord, sizeof(int),
+                                            cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess && h) e = cudaMemsetAsync(base + kTimeoutWord, 0, sizeof(int), s);
+  if (e == cudaSuccess && h) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    qt_set_last_error(cudaGetErrorString(e), __FILE__, __LINE__);
+    return QT_ERR_CUDA;
+  }
+  *count = h;
   return QT_OK;
 }

@@ -18,6 +18,9 @@ struct GemmArgs {
   long long batch;
   const unsigned char* active;  // optional per-batch mask: skip entry when 0
   int* scales;  // split-precision scratch: batch x 256 ints (row / column exponents)
+  // split-precision waits that time out are counted here; null: the library-wide counter
+  // read by oz_timeouts_and_reset()
+  int* timeouts = nullptr;
 };
 
 cudaError_t zgemm_f64(const GemmArgs& a, cudaStream_t s);

@@ -508,7 +508,7 @@ size_t wave_bytes(const Problem& pb, long long P) {
 qt_status sancho_wave(const Ops<double2>& op0, Arena& ar, long long P, BatchRef H00,
                       BatchRef H10in, bool dag_in, const cd* zlead, double tol, int max_iter,
                       BatchRef G00, BatchRef GBB, int* status, int* iters_out, int iters_stride,
-                      BatchRef G00b = nullref()) {
+                      BatchRef G00b = nullref(), bool reset_on_max = false) {
   Ops<double2> op = op0;
   const int n = op.n;
   const long long nm2 = (long long)n * n;
@@ -579,6 +579,12 @@ qt_status sancho_wave(const Ops<double2>& op0, Arena& ar, long long P, BatchRef 
       if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
       if (h == 0) break;
     }
+  }
+  if (reset_on_max) {
+    // green_RGF_RS's decimation (src/gw_mod.f90:1440-1445): an entry still unconverged after
+    // max_iter steps restarts from H_SS = H_BB = H00, i.e. G00 = GBB = (z S - H00)^-1
+    for (const BatchRef& Hx : {HSS, HBB, HSS2})
+      if (Hx.p) qt::zaxpby<double2>(n, P, H00, 1, 0, nullref(), 0, 0, nullref(), Hx, active, s);
   }
   flag_unconverged_kernel<<<g1d(P), 256, 0, s>>>(P, active, status);
   qt::count_launch();
@@ -733,7 +739,8 @@ qt_status solve_wave(qt_ctx* ctx, const Problem& pb, long long p0, long long P, 
   const int N = nx - 1;
   // both leads are one chain when every slab shares H_ii and H1i and no scattering
   // self-energy touches them: one decimation gives both surfaces
-  const bool one_chain = pb.hl == 0 && pb.h1l == 0 && !pb.sigr;
+  const bool reset = (q & QT_QUIRK_GW_SANCHO_RESET) != 0;
+  const bool one_chain = pb.hl == 0 && pb.h1l == 0 && !pb.sigr && !reset;
   if (one_chain) {
     const size_t mark = ar.off;
     qt::zcopy<double2>(n, P, HII8(0), C8(0), s);
@@ -763,7 +770,7 @@ qt_status solve_wave(qt_ctx* ctx, const Problem& pb, long long p0, long long P, 
     qt::zdagger<double2>(n, P, H1I8(0), C8(2), s);
     qt::zcopy<double2>(n, P, H1I8(N), C8(3), s);
     QT_TRY(sancho_wave(cop, ar, 2 * P, C8(0), C8(2), false, z2, pb.c.sancho_tol,
-                       pb.c.sancho_max_iter, C8(4), nullref(), st2, it2, 1));
+                       pb.c.sancho_max_iter, C8(4), nullref(), st2, it2, 1, nullref(), reset));
     or_halves_kernel<<<g1d(P), 256, 0, s>>>(P, st2, status);
     qt::count_launch();
     if (pb.iters) {
@@ -1085,7 +1092,8 @@ qt_status solve_wave_vb(qt_ctx* ctx, const ProblemVB& pb, long long p0, long lon
     lop.n = n0;
     QT_TRY(sancho_wave(lop, ar, P, HII8(0), H1I8(0), true, zlead, pb.c.sancho_tol,
                        pb.c.sancho_max_iter, C8(1, n0), nullref(), status,
-                       pb.iters ? pb.iters + p0 * 2 : nullptr, 2));
+                       pb.iters ? pb.iters + p0 * 2 : nullptr, 2, nullref(),
+                       (pb.c.quirks & QT_QUIRK_GW_SANCHO_RESET) != 0));
     QT_TRY(cop.gemm3(n0, n0, n0, H1I8(0), qt::OP_N, C8(1, n0), qt::OP_N, C8(2, n0), P));
     QT_TRY(cop.gemm3(n0, n0, n0, C8(2, n0), qt::OP_N, H1I8(0), qt::OP_C, C8(3, n0), P));
   }
@@ -1126,7 +1134,8 @@ qt_status solve_wave_vb(qt_ctx* ctx, const ProblemVB& pb, long long p0, long lon
     lop.n = nN;
     QT_TRY(sancho_wave(lop, ar, P, HII8(N), H1I8(nx), false, zlead, pb.c.sancho_tol,
                        pb.c.sancho_max_iter, C8(1, nN), nullref(), status,
-                       pb.iters ? pb.iters + p0 * 2 + 1 : nullptr, 2));
+                       pb.iters ? pb.iters + p0 * 2 + 1 : nullptr, 2, nullref(),
+                       (pb.c.quirks & QT_QUIRK_GW_SANCHO_RESET) != 0));
     QT_TRY(cop.gemm3(nN, nN, nN, H1I8(nx), qt::OP_C, C8(1, nN), qt::OP_N, C8(2, nN), P));
     QT_TRY(cop.gemm3(nN, nN, nN, C8(2, nN), qt::OP_N, H1I8(nx), qt::OP_N, C8(3, nN), P));
   }
@@ -1754,7 +1763,7 @@ extern "C" qt_status qt_sancho_batch(qt_ctx* ctx, int nm, int npts, const double
   cudaMemsetAsync(st, 0, P * 4, s);
   QT_TRY(sancho_wave(op, ar, P, ref(h00, h00_stride ? nm2 : 0, nm), ref(h10, h10_stride ? nm2 : 0, nm),
                      false, z, tol, max_iter, ref(g00, nm2, nm), gbb ? ref(gbb, nm2, nm) : nullref(),
-                     st, it, 1));
+                     st, it, 1, nullref(), (flags & QT_FLAG_SANCHO_RESET) != 0));
   if (prec != QT_PREC_FP64) {
     QT_CUDA_TRY(cudaStreamSynchronize(s));
     if (qt::oz_timeouts_and_reset()) QT_FAIL(QT_ERR_CUDA, "tensor-core kernel wait timed out");

@@ -79,9 +79,11 @@ using tc::tmem_wait_ld;
 using tc::umma;
 using tc::umma_commit;
 
-// bounded wait (4 s); a timeout raises the CTA's abort flag and counts in g_oz_timeouts
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
-  return tc::mbar_wait(bar, parity, abort_flag, &g_oz_timeouts, TIMEOUT_NS);
+// bounded wait (4 s); a timeout raises the CTA's abort flag and counts in *tcount
+// (GemmArgs::timeouts, else g_oz_timeouts)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                          int* tcount) {
+  return tc::mbar_wait(bar, parity, abort_flag, tcount, TIMEOUT_NS);
 }
 __device__ __forceinline__ void tc_fence_before() { tc::fence_before(); }
 __device__ __forceinline__ void tc_fence_after() { tc::fence_after(); }
@@ -355,6 +357,7 @@ __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmAr
   uint64_t* drain = tmem_full + 2;          // teardown
   uint32_t* tmem_base_sm = reinterpret_cast<uint32_t*>(tmem_full + 4);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_base_sm + 1);
+  int* const tcount = a.timeouts ? a.timeouts : &g_oz_timeouts;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m = a.m, n = a.n, K = a.k;         // C is m x n, op(A) m x K, op(B) K x n
@@ -467,7 +470,7 @@ __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmAr
               }
             }
           }
-          if (!mbar_wait(&empty[st], ph ^ 1, abort_flag)) break;
+          if (!mbar_wait(&empty[st], ph ^ 1, abort_flag, tcount)) break;
           uint32_t pk[S][4], pk2[S][4];
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
@@ -542,7 +545,7 @@ __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmAr
             xv[q][u] = x;
           }
         }
-        if (!mbar_wait(&empty[st], ph ^ 1, abort_flag)) break;
+        if (!mbar_wait(&empty[st], ph ^ 1, abort_flag, tcount)) break;
 #pragma unroll
         for (int q = 0; q < ITEMS; ++q) {
           const int item = p + q * NPROD;
@@ -627,13 +630,13 @@ __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmAr
       for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
         const long long b = w / (NPARTS == 2 ? ntile : 2 * ntile);
         if (a.active && !a.active[b]) continue;
-        if (!mbar_wait(tmem_empty, (proc & 1) ^ 1, abort_flag)) break;
+        if (!mbar_wait(tmem_empty, (proc & 1) ^ 1, abort_flag, tcount)) break;
         tc_fence_after();
         uint32_t touched = 0;
         for (int c = 0; c < nch; ++c, ++gchunk) {
           const int st = gchunk % stages;
           const uint32_t ph = (gchunk / stages) & 1;
-          if (!mbar_wait(&full[st], ph, abort_flag)) break;
+          if (!mbar_wait(&full[st], ph, abort_flag, tcount)) break;
           tc_fence_after();
           const uint32_t sA = smem_u32(tiles + (size_t)st * stage_bytes);
           const uint32_t sB = sA + APLANES * S * PLANE_BYTES;
@@ -664,7 +667,7 @@ __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmAr
       umma_commit(drain);
       int dummy = 0;
       volatile int* never = &dummy;
-      mbar_wait(drain, 0, never);
+      mbar_wait(drain, 0, never, tcount);
     }
     __syncwarp();
   } else {
@@ -676,7 +679,7 @@ __global__ void __launch_bounds__(Roles<NT>::NTHREADS, 1) zgemm_oz_kernel(GemmAr
       const long long b = w / (NPARTS == 2 ? ntile : 2 * ntile);
       const int part0 = BOTH ? 0 : (int)((w / ntile) & 1), ct = (int)(w % ntile);
       if (a.active && !a.active[b]) continue;
-      if (!mbar_wait(tmem_full, proc & 1, abort_flag)) break;
+      if (!mbar_wait(tmem_full, proc & 1, abort_flag, tcount)) break;
       const int* erow = a.scales + b * 256;
       const int* fcol = erow + 128;
       tc_fence_after();

@@ -50,11 +50,14 @@ class GwSystem:
     """Device, energy grid, contacts and Coulomb block of one SCBA problem (nk = 1).
 
     ``H00``: one on-site block shared by all slabs (nm, nm), or one per slab
-    (nx, nm, nm); the leads continue the first and last slab."""
+    (nx, nm, nm); the leads continue the first and last slab.  ``sancho_reset``
+    selects green_RGF_RS's lead decimation as written (src/gw_mod.f90:1440-1445):
+    points not converged after ``sancho_max_iter`` steps take the isolated-slab
+    surface function; by default they keep their last iterate and are flagged."""
 
     def __init__(self, ctx, H00, H10, E, nx, V, *, mu=(0.0, 0.0), temp=(300.0, 300.0),
                  eta_lead=1e-3, sancho_max_iter=100, sancho_tol=1e-100, spindeg=2.0,
-                 precision="fp64"):
+                 precision="fp64", sancho_reset=False):
         import torch
         self.ctx = ctx
         self.nm = H00.shape[-1]
@@ -73,7 +76,8 @@ class GwSystem:
         self.dev = QtDevice(self.nm, nx, 1, _ptr(self.H00), 0, hl, _ptr(self.H10), 0, 0,
                             None, 0, 0)
         self.con = QtContacts(mu[0], mu[1], temp[0], temp[1], eta_lead, 0.0, sancho_tol,
-                              int(sancho_max_iter), 0)
+                              int(sancho_max_iter),
+                              _lib.QT_QUIRK_GW_SANCHO_RESET if sancho_reset else 0)
 
     def zeros(self):
         import torch
@@ -157,10 +161,3 @@ def ephoton_sigma(ctx, M, GL, GG, nop, intensity, hw, *, halo=False, precision="
                                     _ptr(SL), _ptr(SG)))
     return SR, SL, SG
 
-
-def residual(NL, NG, SL, SG):
-    """||S_new - S||_F / ||S_new||_F over Sigma^< and Sigma^> (the SCBA stopping measure)."""
-    import torch
-    num = torch.sqrt(torch.sum(torch.abs(NL - SL) ** 2) + torch.sum(torch.abs(NG - SG) ** 2))
-    den = torch.sqrt(torch.sum(torch.abs(NL) ** 2) + torch.sum(torch.abs(NG) ** 2))
-    return float(num / den.clamp_min(1e-300))

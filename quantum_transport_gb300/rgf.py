@@ -343,9 +343,12 @@ def cuda_rgf_constblocksize(ctx, nm, nx, En, mul, mur, TEMPl, TEMPr, Hii, H1i, S
             tr.value, tre.value)
 
 
-def sancho(ctx, E, H00, H10, *, eta=1e-5, tol=1e-100, max_iter=50, precision="fp64"):
+def sancho(ctx, E, H00, H10, *, eta=1e-5, tol=1e-100, max_iter=50, precision="fp64",
+           reset_on_nmax=False):
     """Batched Sancho-Rubio: E (npts,), H00/H10 (nm,nm) shared or (npts,nm,nm).
 
+    ``reset_on_nmax`` is green_RGF_RS's variant (src/gw_mod.f90:1440-1445): a point not
+    converged after ``max_iter`` steps restarts from H_SS = H_BB = H00.
     Returns (G00, GBB, iters, status) with G00/GBB (npts, nm, nm).
     """
     lib = ctx._lib
@@ -361,7 +364,9 @@ def sancho(ctx, E, H00, H10, *, eta=1e-5, tol=1e-100, max_iter=50, precision="fp
     status = np.zeros(npts, dtype=np.int32)
     check(lib.qt_sancho_batch(ctx.handle, nm, npts, _ptr(E), _ptr(h00), nm * nm if H00.ndim == 3 else 0,
                               _ptr(h10), nm * nm if H10.ndim == 3 else 0, None, 0, eta, tol,
-                              int(max_iter), PREC[precision], 0, _ptr(G00), _ptr(GBB), _ptr(iters),
+                              int(max_iter), PREC[precision],
+                              _lib.QT_FLAG_SANCHO_RESET if reset_on_nmax else 0, _ptr(G00),
+                              _ptr(GBB), _ptr(iters),
                               _ptr(status)))
     return from_colmajor(G00), from_colmajor(GBB), iters, status
 

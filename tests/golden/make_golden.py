@@ -16,7 +16,7 @@ and writes
 The run that produced the .dat files used main.f90's defaults nx = 5, ns = 3
 (src/main.f90:75-76), 200 energies on [-6, -1] eV, mu = -3.7 eV, T = 300 K.
 
-Usage: python tests/golden/make_golden.py [/path/to/reference]
+Usage: python tests/golden/make_golden.py <reference checkout>   (the path is required)
 """
 import os
 import sys
@@ -70,4 +70,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <reference checkout>")
+    main(sys.argv[1])

@@ -1,4 +1,7 @@
-"""A short RGF run on a seeded chain device, sized for kernel profilers.
+"""Profiling case: a short RGF run on a seeded chain device, sized for kernel profilers.
+
+Not a test (pytest does not collect it): the ncu summaries of the split-product
+and inverse kernels are captured on this case.
 
 The batched sweep launches every block product over all points of a wave.
 Each launch therefore carries the full per-launch work of a large run: P
@@ -6,7 +9,7 @@ points x one n x n complex product. The memory held stays a few GB because
 the device has few slabs. Example, 512 points of 128-orbital blocks over 3
 slabs (about 3.5 GB on the device):
 
-    python -m quantum_transport_gb300.profile_case --points 512 --slabs 3
+    python tests/profile_case.py --points 512 --slabs 3
 
 Prints one JSON line with the wall time of each repeat and the number of
 points with a non-zero status.
@@ -15,7 +18,11 @@ from __future__ import annotations
 
 import argparse
 import json
+import os
+import sys
 import time
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 
 
 def main(argv=None):
@@ -32,9 +39,9 @@ def main(argv=None):
 
     import torch
 
-    from . import rgf
-    from .build import build
-    from .devices import make_chain_device
+    from quantum_transport_gb300 import rgf
+    from quantum_transport_gb300.build import build
+    from quantum_transport_gb300.devices import make_chain_device
 
     build()
     nE = a.points // a.nk

@@ -147,3 +147,61 @@ def test_ephoton_sigma_vs_oracle(ctx, precision, tol):
     for g, r in zip(got, ref):
         np.testing.assert_allclose(gw.from_dev(g), r[lo:hi], rtol=0, atol=tol * np.abs(r).max())
     assert not gw.from_dev(got[0]).real.any()  # Sigma^R is purely imaginary
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_sancho_reset_on_nmax_vs_oracle(ctx, precision):
+    """green_RGF_RS's decimation (src/gw_mod.f90:1440-1445): an entry still unconverged after
+    nmax steps restarts from H_SS = H_BB = H00.  With 12 steps at eta = 1e-3 the energies
+    outside the band converge in 7-9 steps and those inside reach nmax, so both branches are
+    checked."""
+    from oracle import rgf as orc
+    from quantum_transport_gb300 import rgf
+    dev = make_chain_device(2, 8, 24, -9.0, 9.0, seed=5)
+    H00, H10, E = dev.H00[0], dev.H10, dev.E
+    nmax, tol = 12, 1e-30
+    S = np.eye(8, dtype=np.complex128)
+    G00, GBB, it, st = rgf.sancho(ctx, E, H00, H10, eta=1e-3, tol=tol, max_iter=nmax,
+                                  precision=precision, reset_on_nmax=True)
+    hit = it >= nmax
+    assert 0 < hit.sum() < len(E)
+    tol_rel = 1e-10 if precision == "fp64" else 1e-9
+    for ie, e in enumerate(E):
+        g00, gbb, oit, _, _ = orc.sancho(e, S, H00, H10, eta=1e-3, nmax=nmax, tol=tol,
+                                         reset_on_nmax=True)
+        assert (oit >= nmax) == hit[ie]
+        for got, exp in ((G00[ie], g00), (GBB[ie], gbb)):
+            np.testing.assert_allclose(got, exp, rtol=0, atol=tol_rel * np.abs(exp).max())
+        if hit[ie]:
+            # the reset leaves the isolated-slab function in both
+            bare = np.linalg.inv(complex(e, 1e-3) * S - H00)
+            np.testing.assert_allclose(G00[ie], bare, rtol=0, atol=tol_rel * np.abs(bare).max())
+    # without the reset the unconverged entries keep their last iterate
+    G00n, _, _, _ = rgf.sancho(ctx, E, H00, H10, eta=1e-3, tol=tol, max_iter=nmax,
+                               precision=precision)
+    assert not np.allclose(G00n[hit], G00[hit])
+    np.testing.assert_array_equal(G00n[~hit], G00[~hit])
+
+
+def test_gw_green_with_sancho_reset_vs_oracle(ctx):
+    """qt_rgf_solve under QT_QUIRK_GW_SANCHO_RESET (green_RGF_RS as written) against the
+    oracle's green() with the same reset, on points that reach the decimation's 100 steps."""
+    from quantum_transport_gb300 import gw
+    dev = make_chain_device(6, 8, 64, -4.0, 4.0, seed=3)
+    V = ogw.coulomb_blocks(8)
+    SR0, SL0 = _physical_sigma(len(dev.E), dev.nx, 8)
+    out = {}
+    for reset in (False, True):
+        s = gw.GwSystem(ctx, dev.H00[0], dev.H10, dev.E, dev.nx, V, mu=(0.1, -0.1),
+                        sancho_reset=reset)
+        c = s.currents(gw.to_dev(SR0), gw.to_dev(SL0))
+        out[reset] = c
+        GR, GL, GG = ogw.green(dev.E, dev.H00[0], dev.H10, dev.nx, SR0, SL0, mu=(0.1, -0.1),
+                               temp=(300.0, 300.0), sancho_reset=reset)
+        ref = np.stack([np.diagonal(GR[ie], axis1=-2, axis2=-1) for ie in range(len(dev.E))])
+        got = c["diag_gr"].reshape(ref.shape)
+        np.testing.assert_allclose(got, ref, rtol=0, atol=1e-8 * np.abs(ref).max())
+    hit = (out[True]["status"] & rgf_lib.QT_PT_SANCHO_NOT_CONVERGED) != 0
+    assert hit.any()
+    assert not np.allclose(out[True]["diag_gr"].reshape(len(dev.E), -1)[hit],
+                           out[False]["diag_gr"].reshape(len(dev.E), -1)[hit])

@@ -25,7 +25,15 @@ def _bound(A, B, opa, opb):
             + a.sum(axis=-1, keepdims=True) * b.max(axis=-2, keepdims=True))
 
 
-def _run_both(ctx, rng, n, batch, opa, opb, slices, alpha, beta):
+def _timeouts(stream):
+    from quantum_transport_gb300 import _lib
+    lib = _lib.load()
+    count = C.c_int(-1)
+    _lib.check(lib.qt_noalloc_timeouts(C.byref(count), C.c_void_p(stream.cuda_stream)))
+    return count.value
+
+
+def _run_both(ctx, rng, n, batch, opa, opb, slices, alpha, beta, stream=None):
     import torch
     from quantum_transport_gb300 import _lib
     from quantum_transport_gb300.rgf import _ptr, colmajor, from_colmajor
@@ -44,11 +52,18 @@ def _run_both(ctx, rng, n, batch, opa, opb, slices, alpha, beta):
     _lib.check(lib.qt_zgemm_batch(ctx.handle, n, batch, opa.encode(), _ptr(Ad), nm2, opb.encode(),
                                   _ptr(Bd), nm2, _ptr(al), _ptr(be), _ptr(Dd), nm2, _ptr(C1), nm2,
                                   _lib.QT_PREC_MIXED, slices, flags))
-    stream = torch.cuda.current_stream()
+    torch.cuda.synchronize()
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    free0 = torch.cuda.mem_get_info()[0]
     _lib.check(lib.qt_zgemm_batch_noalloc(n, batch, opa.encode(), _ptr(Ad), nm2, opb.encode(),
                                           _ptr(Bd), nm2, _ptr(al), _ptr(be), _ptr(Dd), nm2,
                                           _ptr(C2), nm2, slices, C.c_void_p(stream.cuda_stream)))
-    stream.synchronize()
+    stream.synchronize()  # only the caller's stream: the work must have gone there
+    # the call allocated no device memory (the first call of the file warmed the module up)
+    assert torch.cuda.mem_get_info()[0] == free0
+    # no wait of the tensor-core kernel ran out, so C is complete
+    assert _timeouts(stream) == 0
     c1, c2 = from_colmajor(C1.cpu().numpy()), from_colmajor(C2.cpu().numpy())
     tol = TOL[slices] * (abs(alpha) * _bound(A, B, opa, opb) + abs(beta) * np.abs(D))
     assert (np.abs(c2 - c1) <= tol).all()
@@ -57,11 +72,40 @@ def _run_both(ctx, rng, n, batch, opa, opb, slices, alpha, beta):
     assert (np.abs(c2 - ref) <= 4 * tol + 1e-14 * np.abs(ref).max()).all()
 
 
+def _warm_up(ctx):
+    """One small call first: under lazy module loading the first call on a device loads the
+    library's device module (which may allocate), as the header documents."""
+    rng = np.random.default_rng(1)
+    _run_both_unchecked(ctx, rng)
+
+
+def _run_both_unchecked(ctx, rng):
+    import torch
+    from quantum_transport_gb300 import _lib
+    from quantum_transport_gb300.rgf import _ptr
+    lib = _lib.load()
+    X = torch.zeros(16 * 16, dtype=torch.complex128, device="cuda")
+    Y = torch.zeros_like(X)
+    _lib.check(lib.qt_zgemm_batch_noalloc(16, 1, b"N", _ptr(X), 256, b"N", _ptr(X), 256, None,
+                                          None, None, 0, _ptr(Y), 256, 4, None))
+    torch.cuda.synchronize()
+
+
 def test_noalloc_matches_split_product_twice(ctx):
+    _warm_up(ctx)
     rng = np.random.default_rng(77)
     # two calls in a row share the static scratch; sizes differ between them
     _run_both(ctx, rng, 96, 7, "N", "C", 4, 1.0, 0.0)
     _run_both(ctx, rng, 128, 5, "C", "N", 7, -1.0, 1.0)
+
+
+def test_noalloc_on_callers_stream(ctx):
+    import torch
+    _warm_up(ctx)
+    rng = np.random.default_rng(78)
+    side = torch.cuda.Stream()
+    _run_both(ctx, rng, 128, 9, "N", "N", 6, 1.0, -1.0, stream=side)
+    _run_both(ctx, rng, 64, 3, "C", "C", 4, 2.0, 0.5, stream=side)
 
 
 def test_noalloc_rejects_batch_over_limit(ctx):
