@@ -7,7 +7,8 @@
  *   cuda_rgf_constblocksize   src/cuda_rgf_mod.f90:53-413, with G^> = G^< + G - G^+
  *                             in every slab (what produced test_cnt/pdos0000.dat)
  * plus the Caroli transmission Tr[Gam_R G_N1 Gam_L G_N1^+].  Block products are
- * naive column-major loops and inverses Gauss-Jordan with partial pivoting: it
+ * loops over split real / imaginary planes, four columns at a time, and inverses
+ * Gauss-Jordan with partial pivoting: it
  * stands in for the reference's CPU build (no Fortran compiler exists on
  * either machine) as the timed CPU baseline and as a second checker.
  */
@@ -23,29 +24,48 @@ typedef double complex cplx;
 
 static const double BOLTZ = 8.61734e-05;
 
-/* C = op(A) op(B)  (op: 'N' or 'C'), all n x n column-major */
+/* C = op(A) op(B)  (op: 'N' or 'C'), all n x n column-major (n <= 512).  The operands are
+ * first split into real and imaginary planes (op applied), so the inner loop is plain real
+ * multiply-adds that the compiler vectorises; four columns of C are formed together so
+ * that each loaded entry of op(A) feeds four complex multiply-adds from L1.  Every C(i, j)
+ * accumulates over k = 0 .. n-1 in order.  ta, tb hold 2 n^2 doubles each. */
 static void gemm(int n, char opa, const cplx* A, char opb, const cplx* B, cplx* C, cplx* ta,
                  cplx* tb) {
-  const cplx* a = A;
-  const cplx* b = B;
-  if (opa == 'C') {
-    for (int j = 0; j < n; ++j)
-      for (int i = 0; i < n; ++i) ta[i + (size_t)j * n] = conj(A[j + (size_t)i * n]);
-    a = ta;
-  }
-  if (opb == 'C') {
-    for (int j = 0; j < n; ++j)
-      for (int i = 0; i < n; ++i) tb[i + (size_t)j * n] = conj(B[j + (size_t)i * n]);
-    b = tb;
-  }
-  memset(C, 0, sizeof(cplx) * (size_t)n * n);
-  for (int j = 0; j < n; ++j) {
-    cplx* c = C + (size_t)j * n;
-    for (int k = 0; k < n; ++k) {
-      const cplx bk = b[k + (size_t)j * n];
-      const cplx* ak = a + (size_t)k * n;
-      for (int i = 0; i < n; ++i) c[i] += ak[i] * bk;
+  const size_t nn = (size_t)n * n;
+  double* restrict ar = (double*)ta;
+  double* restrict ai = ar + nn;
+  double* restrict br = (double*)tb;
+  double* restrict bi = br + nn;
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) {
+      const cplx x = opa == 'C' ? conj(A[j + (size_t)i * n]) : A[i + (size_t)j * n];
+      const cplx y = opb == 'C' ? conj(B[j + (size_t)i * n]) : B[i + (size_t)j * n];
+      ar[i + (size_t)j * n] = creal(x);
+      ai[i + (size_t)j * n] = cimag(x);
+      br[i + (size_t)j * n] = creal(y);
+      bi[i + (size_t)j * n] = cimag(y);
     }
+  enum { NJ = 4 };
+  double cr[NJ][512], ci[NJ][512];
+  for (int j0 = 0; j0 < n; j0 += NJ) {
+    const int nj = n - j0 < NJ ? n - j0 : NJ;
+    for (int q = 0; q < nj; ++q)
+      for (int i = 0; i < n; ++i) cr[q][i] = ci[q][i] = 0.0;
+    for (int k = 0; k < n; ++k) {
+      const double* restrict xr = ar + (size_t)k * n;
+      const double* restrict xi = ai + (size_t)k * n;
+      for (int q = 0; q < nj; ++q) {
+        const double yr = br[k + (size_t)(j0 + q) * n], yi = bi[k + (size_t)(j0 + q) * n];
+        double* restrict zr = cr[q];
+        double* restrict zi = ci[q];
+        for (int i = 0; i < n; ++i) {
+          zr[i] += xr[i] * yr - xi[i] * yi;
+          zi[i] += xr[i] * yi + xi[i] * yr;
+        }
+      }
+    }
+    for (int q = 0; q < nj; ++q)
+      for (int i = 0; i < n; ++i) C[i + (size_t)(j0 + q) * n] = cr[q][i] + I * ci[q][i];
   }
 }
 
@@ -74,10 +94,12 @@ static int invert(int n, cplx* X, int* perm) {
     for (int j = 0; j < n; ++j) {
       if (j == k) continue;
       const cplx r = X[k + (size_t)j * n];
-      cplx* col = X + (size_t)j * n;
-      const cplx* colk = X + (size_t)k * n;
-      for (int i = 0; i < n; ++i)
-        if (i != k) col[i] -= colk[i] * r;
+      cplx* restrict col = X + (size_t)j * n;
+      const cplx* restrict colk = X + (size_t)k * n;
+      /* all rows, then row k put back: the same operations on rows i != k, in a loop
+         without a branch */
+      for (int i = 0; i < n; ++i) col[i] -= colk[i] * r;
+      col[k] = r;
     }
     for (int i = 0; i < n; ++i)
       if (i != k) X[i + (size_t)k * n] *= -inv;
@@ -272,6 +294,7 @@ int qt_ref_rgf(int nm, int nx, int nk, const double* H00, const double* H10, int
                const double* E, double eta_lead, double eta_int, double tol, int nmax, double mul,
                double mur, double templ, double tempr, int nthreads, double* T, double* tr,
                double* tre, double* dgr, double* dgl, int* status) {
+  if (nm <= 0 || nm > 512) return -1;  /* the block product's column buffers hold 512 rows */
   const long long npts = (long long)nE * nk;
   const size_t b = (size_t)nm * nm;
   int nbad = 0;

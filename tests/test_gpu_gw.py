@@ -185,23 +185,26 @@ def test_sancho_reset_on_nmax_vs_oracle(ctx, precision):
 
 def test_gw_green_with_sancho_reset_vs_oracle(ctx):
     """qt_rgf_solve under QT_QUIRK_GW_SANCHO_RESET (green_RGF_RS as written) against the
-    oracle's green() with the same reset, on points that reach the decimation's 100 steps."""
+    oracle's green() with the same reset.  At TOL = 1e-100 this device's decimations finish
+    within 100 steps, so the step limit is lowered to 12 and the window widened to
+    [-9, 9] eV: the in-band energies then reach the limit and restart from H00, the
+    others converge."""
     from quantum_transport_gb300 import gw
-    dev = make_chain_device(6, 8, 64, -4.0, 4.0, seed=3)
+    dev = make_chain_device(6, 8, 64, -9.0, 9.0, seed=3)
     V = ogw.coulomb_blocks(8)
     SR0, SL0 = _physical_sigma(len(dev.E), dev.nx, 8)
     out = {}
     for reset in (False, True):
         s = gw.GwSystem(ctx, dev.H00[0], dev.H10, dev.E, dev.nx, V, mu=(0.1, -0.1),
-                        sancho_reset=reset)
+                        sancho_max_iter=12, sancho_reset=reset)
         c = s.currents(gw.to_dev(SR0), gw.to_dev(SL0))
         out[reset] = c
         GR, GL, GG = ogw.green(dev.E, dev.H00[0], dev.H10, dev.nx, SR0, SL0, mu=(0.1, -0.1),
-                               temp=(300.0, 300.0), sancho_reset=reset)
+                               temp=(300.0, 300.0), sancho_nmax=12, sancho_reset=reset)
         ref = np.stack([np.diagonal(GR[ie], axis1=-2, axis2=-1) for ie in range(len(dev.E))])
         got = c["diag_gr"].reshape(ref.shape)
         np.testing.assert_allclose(got, ref, rtol=0, atol=1e-8 * np.abs(ref).max())
     hit = (out[True]["status"] & rgf_lib.QT_PT_SANCHO_NOT_CONVERGED) != 0
-    assert hit.any()
+    assert hit.any() and not hit.all()
     assert not np.allclose(out[True]["diag_gr"].reshape(len(dev.E), -1)[hit],
                            out[False]["diag_gr"].reshape(len(dev.E), -1)[hit])
