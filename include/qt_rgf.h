@@ -56,6 +56,9 @@ typedef enum {
 #define QT_FLAG_DEVICE_POINTERS 1u /* all arrays are device pointers            */
 #define QT_FLAG_CAROLI 2u          /* also compute Caroli T(E) (qt_outputs.T)    */
 #define QT_FLAG_SYNC 4u            /* synchronise the stream before returning   */
+#define QT_FLAG_COMPLEX64 16u      /* qt_zgemm_batch: A, B, D, C are complex64
+                                      (interleaved float pairs) device blocks;
+                                      QT_PREC_MIXED, 4 digits, real alpha/beta */
 #define QT_FLAG_SANCHO_RESET 8u    /* qt_sancho_batch: green_RGF_RS's decimation
                                       (src/gw_mod.f90:1440-1445): an entry not
                                       converged after max_iter steps restarts
@@ -296,7 +299,9 @@ qt_status qt_sancho_batch(qt_ctx* ctx, int nm, int npts, const double* E, const 
  * reference's MUL_C / zgemm, src/matrix_c.f90:615-660), square n x n blocks,
  * op 'N' / 'C' / 'T'.  Strides in complex elements (0 = shared block).  D may
  * be NULL.  prec selects the FP64 pipes or the tensor-core split product
- * with `slices` 8-bit digits per operand (ignored for FP64; 0 = default 4). */
+ * with `slices` 8-bit digits per operand (ignored for FP64; 0 = default 4).
+ * With QT_FLAG_COMPLEX64 the blocks are complex64 (the split sweep's storage)
+ * and the pointers are read as float pairs.                                 */
 qt_status qt_zgemm_batch(qt_ctx* ctx, int n, int batch, char opA, const double* A,
                          int64_t a_stride, char opB, const double* B, int64_t b_stride,
                          const double* alpha, const double* beta, const double* D,

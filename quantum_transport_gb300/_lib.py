@@ -15,6 +15,7 @@ LIB_PATH = os.path.join(HERE, "libqtgpu.so")
 QT_OK, QT_ERR_ARG, QT_ERR_CUDA, QT_ERR_NOMEM, QT_ERR_UNSUPPORTED, QT_ERR_POINTS = range(6)
 QT_PREC_FP64, QT_PREC_MIXED, QT_PREC_MIXED_FP64 = 0, 1, 2
 QT_FLAG_DEVICE_POINTERS, QT_FLAG_CAROLI, QT_FLAG_SYNC, QT_FLAG_SANCHO_RESET = 1, 2, 4, 8
+QT_FLAG_COMPLEX64 = 16
 QT_QUIRK_CPU_FERMI, QT_QUIRK_GLP_ZERO, QT_QUIRK_BACK_H1I_NEXT = 1, 2, 4
 QT_QUIRK_GW_SANCHO_RESET = 8
 QT_PT_SINGULAR, QT_PT_SANCHO_NOT_CONVERGED, QT_PT_NONFINITE = 1, 2, 4

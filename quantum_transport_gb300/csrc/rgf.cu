@@ -1809,6 +1809,23 @@ extern "C" qt_status qt_zgemm_batch(qt_ctx* ctx, int n, int batch, char opA, con
   const bool devp = (flags & QT_FLAG_DEVICE_POINTERS) != 0;
   const cd al = alpha ? cd{alpha[0], alpha[1]} : cd{1, 0};
   const cd be = beta ? cd{beta[0], beta[1]} : cd{0, 0};
+  if (flags & QT_FLAG_COMPLEX64) {
+    // complex64 blocks (the complex64 sweep's 4-digit split product), device pointers
+    if (!devp || prec != QT_PREC_MIXED || (slices != 0 && slices != 4) || al.y != 0.0 ||
+        be.y != 0.0)
+      QT_FAIL(QT_ERR_UNSUPPORTED,
+              "complex64 product: device pointers, QT_PREC_MIXED, 4 digits, real alpha/beta");
+    QT_TRY(ensure(ctx->arena, ctx->arena_bytes, (size_t)batch * 1024 + 4096));
+    Ops<float2> op{s, n, prec};
+    op.slices = 4;
+    op.scales = reinterpret_cast<int*>(ctx->arena);
+    op.P = batch;
+    op.prof = &ctx->prof;
+    QT_TRY(op.gemm3(n, n, n, ref(A, a_stride, n), oa, ref(B, b_stride, n), ob,
+                    ref(C, c_stride, n), batch, al, D ? ref(D, d_stride, n) : nullref(), be));
+    if (flags & QT_FLAG_SYNC) QT_CUDA_TRY(cudaStreamSynchronize(s));
+    return QT_OK;
+  }
   const void *a = A, *b = B, *d = D;
   void* c = C;
   if (!devp) {

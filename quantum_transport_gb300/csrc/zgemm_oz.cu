@@ -35,12 +35,20 @@
 //    output) or assembled into FP64 bits with integer operations (complex128
 //    output, no use of the FP64 pipe).
 //
-// Roles (one CTA per SM: the accumulators use all 512 TMEM columns): warps 0-3
+// Two kernel families share the digit arithmetic below: the register-staged kernel
+// (zgemm_oz_kernel, producers slice digits straight from global loads) and the TMA-fed
+// kernels further down (zgemm_c64_tma_kernel, zgemm_c128_tma_kernel: raw tiles copied
+// into shared memory by cp.async.bulk.tensor, digits sliced shared memory to shared
+// memory), which run whenever both operands can be addressed by a tensor map.
+//
+// Roles of the register-staged kernel (one CTA per SM: the accumulators use all 512 TMEM
+// columns): warps 0-3
 // epilogue (TMEM lanes 0-127); 16 producer warps for 128-column tiles, 8 for
 // 64-column tiles (digit slicing straight from global memory into the
 // canonical no-swizzle K-major UMMA layout in shared memory); the last warp
 // allocates TMEM and holds the single MMA-issuing thread.  Stages are handed over with mbarriers; every wait is
 // bounded (a few seconds) and records a timeout instead of hanging.
+#include <cuda.h>
 #include <stdint.h>
 
 #include "qt_common.cuh"
@@ -770,6 +778,822 @@ cudaError_t launch(const GemmArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+
+// ============================================================ TMA-fed complex64 product
+// The complex64 sweep's product C = alpha op(A) op(B) + beta D + z I (S = 4 digits, levels
+// <= 3) with its operands staged by the tensor memory accelerator:
+//  * a loader thread copies each stage's raw complex64 tiles -- op(A) 128 rows x 16 complex
+//    k, op(B) 16 k x 64 columns -- from global memory into a ring of RSTAGES shared-memory
+//    slots with cp.async.bulk.tensor (3-D tensor maps over (floats, vectors, batch entry));
+//  * producer warps split the raw tiles, shared memory to shared memory, into the digit
+//    planes of A' = (Re, Im) op(A) and of the two layouts of op(B), B'_r = (Re, -Im) and
+//    B'_i = (Im, Re), so that Re C = A' B'_r and Im C = A' B'_i (the second layout is
+//    formed on the 64-column operand, not on the 128-row one);
+//  * a work item is one 64-column tile of one batch entry: its four accumulators (level 0
+//    and levels 1-3 of both parts) take 256 TMEM columns, so two items' accumulators fit
+//    and the epilogue of one item runs while the next item's products are issued.
+// A tile that is contiguous along rows (op(A) = N, op(B) = C) is copied as [k][row]; one
+// that is contiguous along k (op(A) = C, op(B) = N) as [row][k] with 128-byte rows and the
+// 128-byte swizzle, so that the producers' 16-byte reads down a column of rows hit eight
+// different bank groups.  The epilogue's arithmetic is the register-staged kernel's: the
+// two kernels give the same bits.
+namespace c64t {
+constexpr int S = 4, L = 3;              // digits, highest level kept
+constexpr int NT = 64;                   // output columns per item
+constexpr int KCC = 16;                  // complex k per stage (32 real K)
+constexpr int DSTAGES = 2, RSTAGES = 4;  // digit stages, raw (TMA) stages
+constexpr int NPROD = 256;               // producer threads
+constexpr int LOAD_WARP = 4 + NPROD / 32, MMA_WARP = LOAD_WARP + 1;
+constexpr int NTHREADS = 32 * (MMA_WARP + 1);
+constexpr int APLANE = 128 * 2 * KCC * 2;  // one digit plane of A': 128 rows x 32 BF16 (8 KB)
+constexpr int BPLANE = NT * 2 * KCC * 2;   // one digit plane of a B layout: 64 rows (4 KB)
+constexpr int DSTAGE = S * APLANE + 2 * S * BPLANE;  // 64 KB
+constexpr int RAW_A = 128 * KCC * 8, RAW_B = NT * KCC * 8;  // 16 KB, 8 KB
+constexpr int RSTAGE = RAW_A + RAW_B;
+constexpr uint32_t SBO_T = (2 * KCC / 8) * 128;  // 8-row groups of a digit plane (512 B)
+constexpr int SMEM = 1024 + RSTAGES * RSTAGE + DSTAGES * DSTAGE + 256;
+static_assert(SMEM <= 232448, "shared memory");
+static_assert(RAW_A % 1024 == 0 && RSTAGE % 1024 == 0, "swizzled boxes need 1 KB alignment");
+
+// operand tile layout in a raw slot
+enum { MN_MAJOR = 0, K_MAJOR = 1 };
+
+struct Args {
+  GemmArgs g;
+  int layoutA, layoutB;  // MN_MAJOR / K_MAJOR
+};
+
+// four consecutive complex k (4g .. 4g+3) of vector v of a raw tile: MN-major tiles hold
+// [kc][v] with `vecs` vectors, K-major tiles [v][kc] in 128-byte swizzled rows (16-byte
+// chunk c of row v at chunk c ^ (v & 7))
+__device__ __forceinline__ void raw_read4(const unsigned char* base, int layout, int v, int g,
+                                          int vecs, float2* x) {
+  if (layout == MN_MAJOR) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      x[u] = *reinterpret_cast<const float2*>(base + ((size_t)(4 * g + u) * vecs + v) * 8);
+  } else {
+    const float4 p0 =
+        *reinterpret_cast<const float4*>(base + v * 128 + (((2 * g) ^ (v & 7)) << 4));
+    const float4 p1 =
+        *reinterpret_cast<const float4*>(base + v * 128 + (((2 * g + 1) ^ (v & 7)) << 4));
+    x[0] = make_float2(p0.x, p0.y);
+    x[1] = make_float2(p0.z, p0.w);
+    x[2] = make_float2(p1.x, p1.y);
+    x[3] = make_float2(p1.z, p1.w);
+  }
+}
+// 2^(8-e) as pre * scale: vectors below 2^-119 would overflow one FP32 power of two, so they
+// are first lifted by 2^64 (exact).  sign = -1 conjugates (op = C).
+__device__ __forceinline__ void digit_scale(int e, float sign, float2& m, float& sc) {
+  const bool tiny = e < -118;
+  const float pre = tiny ? 18446744073709551616.0f : 1.0f;
+  m = make_float2(pre, pre * sign);
+  sc = __int_as_float((127 + 8 - (tiny ? e + 64 : e)) << 23);
+}
+// one real part of an output element from its two accumulators, with the arithmetic of
+// Store<float2>::put: normalised (hi, lo), scaled by 2^e2 and alpha, beta d and z added
+__device__ __forceinline__ float c64_value(uint32_t acc0, uint32_t acc1, int e2, float alpha,
+                                           float beta, const float* d, bool diag, double z) {
+  float hi, lo, s2, e;
+  two_sum(__uint_as_float(acc0), __uint_as_float(acc1), hi, lo);
+  two_sum(hi, lo, s2, e);
+  float v, w;
+  if (e2 > -126 && e2 < 128) {
+    const float sc = __int_as_float((127 + e2) << 23);  // 2^e2
+    v = alpha * (s2 * sc);
+    w = alpha * (e * sc);
+  } else {
+    v = alpha * ldexpf(s2, e2);
+    w = alpha * ldexpf(e, e2);
+  }
+  if (d) v = fmaf(beta, *d, v);
+  if (diag) v += (float)z;
+  return v + w;
+}
+
+__global__ void __launch_bounds__(NTHREADS, 1)
+    zgemm_c64_tma_kernel(const __grid_constant__ Args args, const __grid_constant__ CUtensorMap tmA,
+                         const __grid_constant__ CUtensorMap tmB) {
+  const GemmArgs& a = args.g;
+  extern __shared__ unsigned char smem_raw[];
+  // 1 KB alignment for the swizzled boxes
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  unsigned char* raw = smem;                                 // [RSTAGES][A tile | B tile]
+  unsigned char* dig = smem + (size_t)RSTAGES * RSTAGE;      // [DSTAGES][A' | B'_r | B'_i]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(dig + (size_t)DSTAGES * DSTAGE);
+  uint64_t* dfull = bars;                       // producers -> MMA        [DSTAGES]
+  uint64_t* dempty = dfull + DSTAGES;           // MMA commit -> producers [DSTAGES]
+  uint64_t* rfull = dempty + DSTAGES;           // TMA -> producers        [RSTAGES]
+  uint64_t* rempty = rfull + RSTAGES;           // producers -> loader     [RSTAGES]
+  uint64_t* tfull = rempty + RSTAGES;           // MMA commit -> epilogue  [2]
+  uint64_t* tempty = tfull + 2;                 // epilogue -> MMA         [2]
+  uint64_t* drain = tempty + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  int* const tcount = a.timeouts ? a.timeouts : &g_oz_timeouts;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m = a.m, n = a.n, K = a.k;
+  const int nch = (K + KCC - 1) / KCC;
+  const int ntile = (n + NT - 1) / NT;
+  const long long nitems = (long long)ntile * a.batch;
+
+  if (tid == 0) {
+    for (int s = 0; s < DSTAGES; ++s) { mbar_init(&dfull[s], NPROD); mbar_init(&dempty[s], 1); }
+    for (int s = 0; s < RSTAGES; ++s) { mbar_init(&rfull[s], 1); mbar_init(&rempty[s], NPROD); }
+    for (int s = 0; s < 2; ++s) { mbar_init(&tfull[s], 1); mbar_init(&tempty[s], 128); }
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == MMA_WARP) tc::tmem_alloc(tmem_slot, 512);
+  if (warp == LOAD_WARP && lane == 0) {
+    tc::prefetch_tmap(&tmA);
+    tc::prefetch_tmap(&tmB);
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == LOAD_WARP) {
+    // ======================== loader: one thread issues every stage's two tile copies
+    if (lane == 0) {
+      uint32_t g = 0;                 // stage counter, the same sequence in every role
+      uint32_t pend_parity[RSTAGES];  // phase of each slot's last copy
+      bool pend[RSTAGES];
+#pragma unroll
+      for (int s = 0; s < RSTAGES; ++s) { pend[s] = false; pend_parity[s] = 0; }
+      for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
+        const long long b = w / ntile;
+        const int ct = (int)(w % ntile);
+        if (a.active && !a.active[b]) continue;
+        // batch coordinate of each operand's tensor map (a shared operand has one entry)
+        const int ea = a.A.stride == 0 ? 0 : (int)batch_index(a.A, b);
+        const int eb = a.B.stride == 0 ? 0 : (int)batch_index(a.B, b);
+        bool ok = true;
+        for (int c = 0; c < nch; ++c, ++g) {
+          const int slot = (int)(g % RSTAGES);
+          const uint32_t ph = (g / RSTAGES) & 1;
+          if (!mbar_wait(&rempty[slot], ph ^ 1, abort_flag, tcount)) { ok = false; break; }
+          unsigned char* dA = raw + (size_t)slot * RSTAGE;
+          unsigned char* dB = dA + RAW_A;
+          tc::mbar_arrive_expect_tx(&rfull[slot], RSTAGE);  // full boxes, zero-filled edges
+          const int k0 = c * KCC;
+          if (args.layoutA == MN_MAJOR) tc::tma_load_3d(dA, &tmA, 0, k0, ea, &rfull[slot]);
+          else tc::tma_load_3d(dA, &tmA, 2 * k0, 0, ea, &rfull[slot]);
+          if (args.layoutB == MN_MAJOR) tc::tma_load_3d(dB, &tmB, 2 * ct * NT, k0, eb, &rfull[slot]);
+          else tc::tma_load_3d(dB, &tmB, 2 * k0, ct * NT, eb, &rfull[slot]);
+          pend[slot] = true;
+          pend_parity[slot] = ph;
+        }
+        if (!ok) break;
+      }
+      // every copy lands before the CTA exits (in an aborted run some were never consumed)
+      int zero = 0;
+      volatile int* never = &zero;
+      for (int s = 0; s < RSTAGES; ++s)
+        if (pend[s]) mbar_wait(&rfull[s], pend_parity[s], never, tcount);
+    }
+    __syncwarp();
+  } else if (warp >= 4 && warp < LOAD_WARP) {
+    // ======================== producers: raw tiles -> digit planes (shared -> shared)
+    // thread p: op(A) row r in 4-k groups gA0 and gA0 + 2; op(B) column j in 4-k group gB
+    const int p = tid - 128;
+    const int r = p & 127, gA0 = p >> 7;
+    const int j = p & (NT - 1), gB = p / NT;
+    const uint32_t offA0 = (uint32_t)((r >> 3) * SBO_T + gA0 * 128 + (r & 7) * 16);
+    const uint32_t offA1 = offA0 + 2 * 128;
+    const uint32_t offB = (uint32_t)((j >> 3) * SBO_T + gB * 128 + (j & 7) * 16);
+    const float sgnA = a.opA == OP_C ? -1.f : 1.f, sgnB = a.opB == OP_C ? -1.f : 1.f;
+    uint32_t g = 0;
+    for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
+      const long long b = w / ntile;
+      const int ct = (int)(w % ntile);
+      if (a.active && !a.active[b]) continue;
+      const int* erow = a.scales + b * 256;
+      const int* fcol = erow + 128;
+      const int jc = ct * NT + j;
+      float2 mA, mB;
+      float scA, scB;
+      digit_scale(r < m ? erow[r] : 0, sgnA, mA, scA);
+      digit_scale(jc < n ? fcol[jc] : 0, sgnB, mB, scB);
+      bool ok = true;
+      for (int c = 0; c < nch; ++c, ++g) {
+        const int rs = (int)(g % RSTAGES), ds = (int)(g % DSTAGES);
+        if (!mbar_wait(&rfull[rs], (g / RSTAGES) & 1, abort_flag, tcount)) { ok = false; break; }
+        const unsigned char* rA = raw + (size_t)rs * RSTAGE;
+        float2 xa[8], xb[4];
+        raw_read4(rA, args.layoutA, r, gA0, 128, xa);
+        raw_read4(rA, args.layoutA, r, gA0 + 2, 128, xa + 4);
+        raw_read4(rA + RAW_A, args.layoutB, j, gB, NT, xb);
+        mbar_arrive(&rempty[rs]);  // the values are in registers: the slot may refill
+        if (!mbar_wait(&dempty[ds], ((g / DSTAGES) & 1) ^ 1, abort_flag, tcount)) {
+          ok = false;
+          break;
+        }
+        unsigned char* dA = dig + (size_t)ds * DSTAGE;
+        unsigned char* dBr = dA + S * APLANE;
+        unsigned char* dBi = dBr + S * BPLANE;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          uint32_t pk[S][4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            float2 D[S];
+            digits_f32x2<S>(__fmul2_rn(xa[4 * h + u], mA), scA, D);
+#pragma unroll
+            for (int s2 = 0; s2 < S; ++s2) pk[s2][u] = pack_pair(D[s2]);  // (Re, Im)
+          }
+#pragma unroll
+          for (int s2 = 0; s2 < S; ++s2)
+            *reinterpret_cast<uint4*>(dA + (size_t)s2 * APLANE + (h ? offA1 : offA0)) =
+                make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
+        }
+        {
+          uint32_t pr[S][4], pi[S][4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            float2 D[S];
+            digits_f32x2<S>(__fmul2_rn(xb[u], mB), scB, D);
+#pragma unroll
+            for (int s2 = 0; s2 < S; ++s2) {
+              pr[s2][u] = pack_pair(D[s2]) ^ 0x80000000u;  // (Re, -Im): negating a digit is exact
+              pi[s2][u] = __byte_perm(__float_as_uint(D[s2].x), __float_as_uint(D[s2].y),
+                                      0x3276);             // (Im, Re)
+            }
+          }
+#pragma unroll
+          for (int s2 = 0; s2 < S; ++s2) {
+            *reinterpret_cast<uint4*>(dBr + (size_t)s2 * BPLANE + offB) =
+                make_uint4(pr[s2][0], pr[s2][1], pr[s2][2], pr[s2][3]);
+            *reinterpret_cast<uint4*>(dBi + (size_t)s2 * BPLANE + offB) =
+                make_uint4(pi[s2][0], pi[s2][1], pi[s2][2], pi[s2][3]);
+          }
+        }
+        fence_proxy_async();
+        mbar_arrive(&dfull[ds]);
+      }
+      if (!ok) break;
+    }
+  } else if (warp == MMA_WARP) {
+    // ======================== MMA issuer (one thread); item i uses TMEM columns
+    // [256 (i & 1), 256 (i & 1) + 256): Re level 0, Re levels 1-3, Im level 0, Im levels 1-3
+    if (lane == 0) {
+      const uint32_t idesc = make_idesc(128, NT);
+      uint32_t g = 0, li = 0;
+      for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
+        const long long b = w / ntile;
+        if (a.active && !a.active[b]) continue;
+        const int buf = (int)(li & 1);
+        if (!mbar_wait(&tempty[buf], ((li >> 1) & 1) ^ 1, abort_flag, tcount)) break;
+        tc_fence_after();
+        uint32_t touched = 0;
+        bool ok = true;
+        for (int c = 0; c < nch; ++c, ++g) {
+          const int ds = (int)(g % DSTAGES);
+          if (!mbar_wait(&dfull[ds], (g / DSTAGES) & 1, abort_flag, tcount)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t sA = smem_u32(dig + (size_t)ds * DSTAGE);
+          const uint32_t sB = sA + S * APLANE;
+#pragma unroll
+          for (int kk = 0; kk < 2; ++kk) {
+#pragma unroll
+            for (int part = 0; part < 2; ++part) {
+#pragma unroll
+              for (int s2 = 0; s2 < S; ++s2) {
+#pragma unroll
+                for (int t = 0; t < S; ++t) {
+                  if (s2 + t > L) continue;
+                  const int acc = 2 * part + (s2 + t > 0 ? 1 : 0);
+                  const uint64_t ad = tc::make_desc(sA + s2 * APLANE + kk * 256, 128, SBO_T);
+                  const uint64_t bd =
+                      tc::make_desc(sB + (part * S + t) * BPLANE + kk * 256, 128, SBO_T);
+                  umma(tmem + (uint32_t)(buf * 256 + acc * NT), ad, bd, idesc,
+                       (touched >> acc) & 1);
+                  touched |= 1u << acc;
+                }
+              }
+            }
+          }
+          umma_commit(&dempty[ds]);
+        }
+        if (!ok) break;
+        umma_commit(&tfull[buf]);
+        ++li;
+      }
+      // drain: every MMA issued by this thread has completed before TMEM is freed
+      umma_commit(drain);
+      int zero = 0;
+      volatile int* never = &zero;
+      mbar_wait(drain, 0, never, tcount);
+    }
+    __syncwarp();
+  } else {
+    // ======================== epilogue (warps 0-3 own TMEM lanes 0-127 = rows of C)
+    const int row = warp * 32 + lane;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    const float alpha = (float)a.alpha_re, beta = (float)a.beta_re;
+    uint32_t li = 0;
+    for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
+      const long long b = w / ntile;
+      const int ct = (int)(w % ntile);
+      if (a.active && !a.active[b]) continue;
+      const int buf = (int)(li & 1);
+      if (!mbar_wait(&tfull[buf], (li >> 1) & 1, abort_flag, tcount)) break;
+      tc_fence_after();
+      const int* erow = a.scales + b * 256;
+      const int* fcol = erow + 128;
+      float2* C = batch_ptr<float2>(a.C, b);
+      const float2* D = a.D.p ? batch_ptr<const float2>(a.D, b) : nullptr;
+      double2 z = make_double2(0.0, 0.0);
+      if (a.Z.p) z = *batch_ptr<const double2>(a.Z, b);
+      const int ei = erow[row];
+#pragma unroll 1
+      for (int j0 = 0; j0 < NT; j0 += 16) {
+        uint32_t v[4][16];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          tmem_ld16(lane_base + (uint32_t)(buf * 256 + q * NT + j0), v[q]);
+        tmem_wait_ld();
+        if (row < m) {
+#pragma unroll
+          for (int jj = 0; jj < 16; ++jj) {
+            const int jcol = ct * NT + j0 + jj;
+            if (jcol < n) {
+              const int e2 = ei + fcol[jcol] - 16;
+              const bool diag = a.Z.p && row == jcol;
+              const float* d = D ? reinterpret_cast<const float*>(D + row + (long long)jcol * a.D.ld)
+                                 : nullptr;
+              const float cr = c64_value(v[0][jj], v[1][jj], e2, alpha, beta, d, diag, z.x);
+              const float ci = c64_value(v[2][jj], v[3][jj], e2, alpha, beta, d ? d + 1 : nullptr,
+                                         diag, z.y);
+              C[row + (long long)jcol * a.C.ld] = make_float2(cr, ci);
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&tempty[buf]);
+      ++li;
+    }
+  }
+  // ---- teardown: every MMA has completed (drained above); free TMEM
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == MMA_WARP) tc::tmem_dealloc(tmem, 512);
+}
+
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                 const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                 const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                 CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// the driver's tensor-map encoder, looked up once through the runtime (no -lcuda)
+EncodeTiled encode_tiled() {
+  static EncodeTiled fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return static_cast<EncodeTiled>(nullptr);
+    return reinterpret_cast<EncodeTiled>(p);
+  }();
+  return fn;
+}
+
+// 3-D tensor map (floats, vectors or k, batch entry) of one complex64 operand.  A
+// batch reference qualifies when a tensor map can address it: no index array, a 16-byte
+// aligned base, and even leading dimension and batch stride (16-byte strides).
+bool make_map(CUtensorMap* map, const BatchRef& R, int layout, int vecs, int K, int boxv,
+              long long batch) {
+  const EncodeTiled fn = encode_tiled();
+  if (!fn || !R.p || R.idx || (reinterpret_cast<uintptr_t>(R.p) & 15) || (R.ld & 1) ||
+      (R.stride & 1) || R.ld < (layout == MN_MAJOR ? vecs : K))
+    return false;
+  const cuuint64_t ldb = (cuuint64_t)R.ld * 8;
+  cuuint64_t dims[3], strides[2];
+  cuuint32_t box[3], es[3] = {1, 1, 1};
+  if (layout == MN_MAJOR) {
+    dims[0] = 2 * (cuuint64_t)vecs; dims[1] = K;
+    box[0] = 2 * boxv; box[1] = KCC;
+  } else {
+    dims[0] = 2 * (cuuint64_t)K; dims[1] = vecs;
+    box[0] = 2 * KCC; box[1] = boxv;
+  }
+  box[2] = 1;
+  const long long entries = R.stride == 0 ? 1 : (R.mod > 0 ? R.mod : batch);
+  dims[2] = (cuuint64_t)entries;
+  strides[0] = ldb;
+  strides[1] = R.stride == 0 ? ((ldb * dims[1] + 15) & ~(cuuint64_t)15)
+                             : (cuuint64_t)R.stride * 8;
+  if (strides[1] < ldb * dims[1]) return false;  // entries must not overlap
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, R.p, dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE,
+            layout == K_MAJOR ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Launches the TMA-fed product when both operands qualify; *used = false otherwise (the
+// caller then runs the register-staged kernel).
+cudaError_t launch(const GemmArgs& g, cudaStream_t s, bool* used) {
+  *used = false;
+  Args args;
+  args.g = g;
+  args.layoutA = g.opA == OP_N ? MN_MAJOR : K_MAJOR;  // op(A) rows contiguous for N
+  args.layoutB = g.opB == OP_N ? K_MAJOR : MN_MAJOR;  // op(B) columns contiguous in k for N
+  alignas(64) CUtensorMap ma, mb;
+  if (!make_map(&ma, g.A, args.layoutA, g.m, g.k, 128, g.batch) ||
+      !make_map(&mb, g.B, args.layoutB, g.n, g.k, NT, g.batch))
+    return cudaSuccess;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaError_t e = cudaFuncSetAttribute(zgemm_c64_tma_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
+  if (e != cudaSuccess) return e;
+  const long long gb = g.batch < 65535 ? g.batch : 65535;
+  oz_scales_kernel<float2><<<dim3((unsigned)gb, 2), 256, 0, s>>>(g);
+  count_launch();
+  const long long items = (long long)((g.n + NT - 1) / NT) * g.batch;
+  const int grid = (int)(items < sms ? items : sms);
+  zgemm_c64_tma_kernel<<<grid, NTHREADS, SMEM, s>>>(args, ma, mb);
+  count_launch();
+  *used = true;
+  return cudaGetLastError();
+}
+}  // namespace c64t
+
+// ============================================================ TMA-fed complex128 product
+// The FP64-grade split product (complex128 blocks; S = 7 digits for the leads, 6 for the
+// complex128 sweep, 4 for refinement updates) with the operands staged by the tensor
+// memory accelerator, as the complex64 product above: raw complex128 tiles (op(A) 128 rows
+// x 8 complex k, op(B) 8 k x 64 columns) arrive in a ring of shared-memory slots by
+// cp.async.bulk.tensor, producer warps split them shared memory to shared memory into the
+// digit planes (integer digit extraction of the FP64 values), one MMA warp issues every
+// digit pair, and the epilogue assembles FP64 results from the per-level accumulators.
+// A work item is one real part of one 64-column tile; every level keeps its own (exact)
+// accumulator, NACC = S accumulators x 64 columns of TMEM (two items' worth when they fit,
+// S = 4, so that the epilogue overlaps the next item).  complex128 strides are always
+// multiples of 16 bytes, so every operand qualifies for a tensor map.
+namespace c128t {
+constexpr int NT = 64;                   // output columns per item
+constexpr int KCC = 8;                   // complex k per stage (16 real K: one MMA K step)
+constexpr int DSTAGES = 3, RSTAGES = 4;  // digit stages, raw (TMA) stages
+constexpr int NPROD = 384;               // producer threads: one (row/column, 4-k group) each
+constexpr int LOAD_WARP = 4 + NPROD / 32, MMA_WARP = LOAD_WARP + 1;
+constexpr int NTHREADS = 32 * (MMA_WARP + 1);
+constexpr int APLANE = 128 * 2 * KCC * 2;  // one digit plane of A': 128 rows x 16 BF16 (4 KB)
+constexpr int BPLANE = NT * 2 * KCC * 2;   // one digit plane of B': 64 rows (2 KB)
+constexpr int RAW_A = 128 * KCC * 16, RAW_B = NT * KCC * 16;  // 16 KB, 8 KB
+constexpr int RSTAGE = RAW_A + RAW_B;
+constexpr uint32_t SBO_T = (2 * KCC / 8) * 128;  // 8-row groups of a digit plane (256 B)
+template <int S> struct Cfg {
+  static constexpr int NACC = S;  // levels 0 .. S-1, one exact accumulator each
+  static constexpr int NBUF = 2 * NACC * NT <= 512 ? 2 : 1;
+  static constexpr int DSTAGE = S * (APLANE + BPLANE);
+  static constexpr int SMEM = 1024 + RSTAGES * RSTAGE + DSTAGES * DSTAGE + 256;
+  static_assert(SMEM <= 232448, "shared memory");
+};
+static_assert(RAW_A % 1024 == 0 && RSTAGE % 1024 == 0, "swizzled boxes need 1 KB alignment");
+
+enum { MN_MAJOR = 0, K_MAJOR = 1 };
+
+struct Args {
+  GemmArgs g;
+  int layoutA, layoutB;
+};
+
+// complex element (v, kc) of a raw tile: MN-major tiles hold [kc][v] (vecs vectors),
+// K-major tiles [v][kc] in 128-byte swizzled rows (one complex per 16-byte chunk)
+__device__ __forceinline__ double2 raw_elem(const unsigned char* base, int layout, int v, int kc,
+                                            int vecs) {
+  if (layout == MN_MAJOR)
+    return *reinterpret_cast<const double2*>(base + ((size_t)kc * vecs + v) * 16);
+  return *reinterpret_cast<const double2*>(base + v * 128 + ((kc ^ (v & 7)) << 4));
+}
+__device__ __forceinline__ double dneg(double x) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (1ll << 63));
+}
+
+template <int S>
+__global__ void __launch_bounds__(NTHREADS, 1)
+    zgemm_c128_tma_kernel(const __grid_constant__ Args args,
+                          const __grid_constant__ CUtensorMap tmA,
+                          const __grid_constant__ CUtensorMap tmB) {
+  constexpr int L = S - 1, NACC = Cfg<S>::NACC, NBUF = Cfg<S>::NBUF;
+  constexpr int DSTAGE = Cfg<S>::DSTAGE;
+  const GemmArgs& a = args.g;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  unsigned char* raw = smem;                               // [RSTAGES][A tile | B tile]
+  unsigned char* dig = smem + (size_t)RSTAGES * RSTAGE;    // [DSTAGES][A' planes | B' planes]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(dig + (size_t)DSTAGES * DSTAGE);
+  uint64_t* dfull = bars;
+  uint64_t* dempty = dfull + DSTAGES;
+  uint64_t* rfull = dempty + DSTAGES;
+  uint64_t* rempty = rfull + RSTAGES;
+  uint64_t* tfull = rempty + RSTAGES;  // [NBUF]
+  uint64_t* tempty = tfull + 2;        // [NBUF]
+  uint64_t* drain = tempty + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  int* const tcount = a.timeouts ? a.timeouts : &g_oz_timeouts;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m = a.m, n = a.n, K = a.k;
+  const int nch = (K + KCC - 1) / KCC;
+  const int ntile = (n + NT - 1) / NT;
+  // item w: batch entry w / (2 ntile), real part (w / ntile) % 2, column tile w % ntile
+  const long long nitems = 2LL * ntile * a.batch;
+
+  if (tid == 0) {
+    for (int s = 0; s < DSTAGES; ++s) { mbar_init(&dfull[s], NPROD); mbar_init(&dempty[s], 1); }
+    for (int s = 0; s < RSTAGES; ++s) { mbar_init(&rfull[s], 1); mbar_init(&rempty[s], NPROD); }
+    for (int s = 0; s < NBUF; ++s) { mbar_init(&tfull[s], 1); mbar_init(&tempty[s], 128); }
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == MMA_WARP) tc::tmem_alloc(tmem_slot, 512);
+  if (warp == LOAD_WARP && lane == 0) {
+    tc::prefetch_tmap(&tmA);
+    tc::prefetch_tmap(&tmB);
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == LOAD_WARP) {
+    // ======================== loader
+    if (lane == 0) {
+      uint32_t g = 0;
+      uint32_t pend_parity[RSTAGES];
+      bool pend[RSTAGES];
+#pragma unroll
+      for (int s = 0; s < RSTAGES; ++s) { pend[s] = false; pend_parity[s] = 0; }
+      for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
+        const long long b = w / (2 * ntile);
+        const int ct = (int)(w % ntile);
+        if (a.active && !a.active[b]) continue;
+        const int ea = a.A.stride == 0 ? 0 : (int)batch_index(a.A, b);
+        const int eb = a.B.stride == 0 ? 0 : (int)batch_index(a.B, b);
+        bool ok = true;
+        for (int c = 0; c < nch; ++c, ++g) {
+          const int slot = (int)(g % RSTAGES);
+          const uint32_t ph = (g / RSTAGES) & 1;
+          if (!mbar_wait(&rempty[slot], ph ^ 1, abort_flag, tcount)) { ok = false; break; }
+          unsigned char* dA = raw + (size_t)slot * RSTAGE;
+          unsigned char* dB = dA + RAW_A;
+          tc::mbar_arrive_expect_tx(&rfull[slot], RSTAGE);
+          const int k0 = c * KCC;
+          if (args.layoutA == MN_MAJOR) tc::tma_load_3d(dA, &tmA, 0, k0, ea, &rfull[slot]);
+          else tc::tma_load_3d(dA, &tmA, 2 * k0, 0, ea, &rfull[slot]);
+          if (args.layoutB == MN_MAJOR) tc::tma_load_3d(dB, &tmB, 2 * ct * NT, k0, eb, &rfull[slot]);
+          else tc::tma_load_3d(dB, &tmB, 2 * k0, ct * NT, eb, &rfull[slot]);
+          pend[slot] = true;
+          pend_parity[slot] = ph;
+        }
+        if (!ok) break;
+      }
+      int zero = 0;
+      volatile int* never = &zero;
+      for (int s = 0; s < RSTAGES; ++s)
+        if (pend[s]) mbar_wait(&rfull[s], pend_parity[s], never, tcount);
+    }
+    __syncwarp();
+  } else if (warp >= 4 && warp < LOAD_WARP) {
+    // ======================== producers: one (row or column, 4-k group) per thread:
+    // p < 256: row p & 127 of op(A), group p >> 7; else column q & 63 of op(B), group q >> 6
+    const int p = tid - 128;
+    const bool isA = p < 256;
+    const int q = isA ? p : p - 256;
+    const int v = isA ? (q & 127) : (q & (NT - 1)), gq = isA ? (q >> 7) : (q / NT);
+    const uint32_t off = (uint32_t)((v >> 3) * SBO_T + gq * 128 + (v & 7) * 16);
+    const int layout = isA ? args.layoutA : args.layoutB;
+    const int conj = isA ? (a.opA == OP_C) : (a.opB == OP_C);
+    uint32_t g = 0;
+    for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
+      const long long b = w / (2 * ntile);
+      const int part = (int)((w / ntile) & 1), ct = (int)(w % ntile);
+      if (a.active && !a.active[b]) continue;
+      const int* erow = a.scales + b * 256;
+      const int vg = isA ? v : ct * NT + v;  // row of op(A) / column of op(B)
+      const int e = isA ? (vg < m ? erow[vg] : 0) : (vg < n ? erow[128 + vg] : 0);
+      bool ok = true;
+      for (int c = 0; c < nch; ++c, ++g) {
+        const int rs = (int)(g % RSTAGES), ds = (int)(g % DSTAGES);
+        if (!mbar_wait(&rfull[rs], (g / RSTAGES) & 1, abort_flag, tcount)) { ok = false; break; }
+        const unsigned char* rt = raw + (size_t)rs * RSTAGE + (isA ? 0 : RAW_A);
+        double2 x[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) x[u] = raw_elem(rt, layout, v, 4 * gq + u, isA ? 128 : NT);
+        mbar_arrive(&rempty[rs]);
+        if (!mbar_wait(&dempty[ds], ((g / DSTAGES) & 1) ^ 1, abort_flag, tcount)) {
+          ok = false;
+          break;
+        }
+        uint32_t pk[S][4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          // A' = (Re, Im) of op(A); B' = (Re, -Im) (real part of C) or (Im, Re) (imaginary)
+          // of op(B); op = C conjugates; negating an FP64 value is exact
+          double v0 = x[u].x, v1 = conj ? dneg(x[u].y) : x[u].y;
+          if (!isA) {
+            if (part == 0) v1 = dneg(v1);
+            else { const double t = v0; v0 = v1; v1 = t; }
+          }
+          float D0[S], D1[S];
+          digits_f64<S>(v0, e, D0);
+          digits_f64<S>(v1, e, D1);
+#pragma unroll
+          for (int s2 = 0; s2 < S; ++s2) pk[s2][u] = pack_bf16x2(D0[s2], D1[s2]);
+        }
+        unsigned char* dbase = dig + (size_t)ds * DSTAGE + (isA ? 0 : S * APLANE);
+        const int pstride = isA ? APLANE : BPLANE;
+#pragma unroll
+        for (int s2 = 0; s2 < S; ++s2)
+          *reinterpret_cast<uint4*>(dbase + (size_t)s2 * pstride + off) =
+              make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
+        fence_proxy_async();
+        mbar_arrive(&dfull[ds]);
+      }
+      if (!ok) break;
+    }
+  } else if (warp == MMA_WARP) {
+    // ======================== MMA issuer; item i uses TMEM columns from
+    // (i % NBUF) NACC NT, one 64-column accumulator per digit level
+    if (lane == 0) {
+      const uint32_t idesc = make_idesc(128, NT);
+      uint32_t g = 0, li = 0;
+      for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
+        const long long b = w / (2 * ntile);
+        if (a.active && !a.active[b]) continue;
+        const int buf = (int)(li % NBUF);
+        if (!mbar_wait(&tempty[buf], ((li / NBUF) & 1) ^ 1, abort_flag, tcount)) break;
+        tc_fence_after();
+        uint32_t touched = 0;
+        bool ok = true;
+        for (int c = 0; c < nch; ++c, ++g) {
+          const int ds = (int)(g % DSTAGES);
+          if (!mbar_wait(&dfull[ds], (g / DSTAGES) & 1, abort_flag, tcount)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t sA = smem_u32(dig + (size_t)ds * DSTAGE);
+          const uint32_t sB = sA + S * APLANE;
+#pragma unroll
+          for (int s2 = 0; s2 < S; ++s2) {
+#pragma unroll
+            for (int t = 0; t < S; ++t) {
+              if (s2 + t > L) continue;
+              const int acc = s2 + t;
+              const uint64_t ad = tc::make_desc(sA + s2 * APLANE, 128, SBO_T);
+              const uint64_t bd = tc::make_desc(sB + t * BPLANE, 128, SBO_T);
+              umma(tmem + (uint32_t)((buf * NACC + acc) * NT), ad, bd, idesc,
+                   (touched >> acc) & 1);
+              touched |= 1u << acc;
+            }
+          }
+          umma_commit(&dempty[ds]);
+        }
+        if (!ok) break;
+        umma_commit(&tfull[buf]);
+        ++li;
+      }
+      umma_commit(drain);
+      int zero = 0;
+      volatile int* never = &zero;
+      mbar_wait(drain, 0, never, tcount);
+    }
+    __syncwarp();
+  } else {
+    // ======================== epilogue (warps 0-3 own TMEM lanes 0-127 = rows of C)
+    const int row = warp * 32 + lane;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    const float alpha = (float)a.alpha_re, beta = (float)a.beta_re;
+    uint32_t li = 0;
+    for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
+      const long long b = w / (2 * ntile);
+      const int part = (int)((w / ntile) & 1), ct = (int)(w % ntile);
+      if (a.active && !a.active[b]) continue;
+      const int buf = (int)(li % NBUF);
+      if (!mbar_wait(&tfull[buf], (li / NBUF) & 1, abort_flag, tcount)) break;
+      tc_fence_after();
+      const int* erow = a.scales + b * 256;
+      const int* fcol = erow + 128;
+      void* C = batch_ptr<double2>(a.C, b);
+      const void* D = a.D.p ? batch_ptr<const double2>(a.D, b) : nullptr;
+      double zpart = 0.0;
+      if (a.Z.p) {
+        const double2 z = *batch_ptr<const double2>(a.Z, b);
+        zpart = part ? z.y : z.x;
+      }
+      const int ei = erow[row];
+      constexpr int CW = 8;  // columns per TMEM read
+#pragma unroll 1
+      for (int j0 = 0; j0 < NT; j0 += CW) {
+        uint32_t r[NACC][CW];
+#pragma unroll
+        for (int acc = 0; acc < NACC; ++acc)
+          tmem_ld8(lane_base + (uint32_t)((buf * NACC + acc) * NT + j0), r[acc]);
+        tmem_wait_ld();
+        if (row < m) {
+#pragma unroll
+          for (int jj = 0; jj < CW; ++jj) {
+            const int j = ct * NT + j0 + jj;
+            if (j < n) {
+              float hi = __uint_as_float(r[0][jj]), lo = 0.f, e;
+#pragma unroll
+              for (int acc = 1; acc < NACC; ++acc) {
+                float s;
+                two_sum(hi, __uint_as_float(r[acc][jj]), s, e);
+                hi = s;
+                lo += e;
+              }
+              float s2;
+              two_sum(hi, lo, s2, e);  // normalise: |lo| <= ulp(hi)/2
+              const int e2 = ei + fcol[j] - 16;
+              Store<double2>::put(C, row + (long long)j * a.C.ld, part, s2, e, e2, alpha, beta,
+                                  D, row + (long long)j * a.D.ld, row == j && a.Z.p, zpart);
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&tempty[buf]);
+      ++li;
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == MMA_WARP) tc::tmem_dealloc(tmem, 512);
+}
+
+// 3-D tensor map (doubles, vectors or k, batch entry) of one complex128 operand
+bool make_map(CUtensorMap* map, const BatchRef& R, int layout, int vecs, int K, int boxv,
+              long long batch) {
+  const c64t::EncodeTiled fn = c64t::encode_tiled();
+  if (!fn || !R.p || R.idx || (reinterpret_cast<uintptr_t>(R.p) & 15) ||
+      R.ld < (layout == MN_MAJOR ? vecs : K))
+    return false;
+  const cuuint64_t ldb = (cuuint64_t)R.ld * 16;
+  cuuint64_t dims[3], strides[2];
+  cuuint32_t box[3], es[3] = {1, 1, 1};
+  if (layout == MN_MAJOR) {
+    dims[0] = 2 * (cuuint64_t)vecs; dims[1] = K;
+    box[0] = 2 * boxv; box[1] = KCC;
+  } else {
+    dims[0] = 2 * (cuuint64_t)K; dims[1] = vecs;
+    box[0] = 2 * KCC; box[1] = boxv;
+  }
+  box[2] = 1;
+  const long long entries = R.stride == 0 ? 1 : (R.mod > 0 ? R.mod : batch);
+  dims[2] = (cuuint64_t)entries;
+  strides[0] = ldb;
+  strides[1] = R.stride == 0 ? ldb * dims[1] : (cuuint64_t)R.stride * 16;
+  if (strides[1] < ldb * dims[1]) return false;  // entries must not overlap
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, R.p, dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE,
+            layout == K_MAJOR ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int S>
+cudaError_t launch(const GemmArgs& g, cudaStream_t s, bool* used) {
+  *used = false;
+  Args args;
+  args.g = g;
+  args.layoutA = g.opA == OP_N ? MN_MAJOR : K_MAJOR;
+  args.layoutB = g.opB == OP_N ? K_MAJOR : MN_MAJOR;
+  alignas(64) CUtensorMap ma, mb;
+  if (!make_map(&ma, g.A, args.layoutA, g.m, g.k, 128, g.batch) ||
+      !make_map(&mb, g.B, args.layoutB, g.n, g.k, NT, g.batch))
+    return cudaSuccess;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  constexpr int smem = Cfg<S>::SMEM;
+  cudaError_t e = cudaFuncSetAttribute(zgemm_c128_tma_kernel<S>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  const long long gb = g.batch < 65535 ? g.batch : 65535;
+  oz_scales_kernel<double2><<<dim3((unsigned)gb, 2), 256, 0, s>>>(g);
+  count_launch();
+  const long long items = 2LL * ((g.n + NT - 1) / NT) * g.batch;
+  const int grid = (int)(items < sms ? items : sms);
+  zgemm_c128_tma_kernel<S><<<grid, NTHREADS, smem, s>>>(args, ma, mb);
+  count_launch();
+  *used = true;
+  return cudaGetLastError();
+}
+}  // namespace c128t
+
 }  // namespace
 
 cudaError_t zgemm_oz(const GemmArgs& a, int slices, int levels, cudaStream_t s) {
@@ -779,6 +1603,13 @@ cudaError_t zgemm_oz(const GemmArgs& a, int slices, int levels, cudaStream_t s) 
   if (a.opA == OP_T || a.opB == OP_T || a.alpha_im != 0.0 || a.beta_im != 0.0)
     return cudaErrorInvalidValue;
   (void)levels;
+  if (slices == 4 || slices == 6 || slices == 7) {
+    bool used = false;
+    const cudaError_t e = slices == 4   ? c128t::launch<4>(a, s, &used)
+                          : slices == 6 ? c128t::launch<6>(a, s, &used)
+                                        : c128t::launch<7>(a, s, &used);
+    if (e != cudaSuccess || used) return e;
+  }
   switch (slices) {
     case 4: return launch<4, 3, 128, double2, double2>(a, s);
     case 6: return launch<6, 5, 64, double2, double2>(a, s);   // one exact accumulator per level
@@ -793,6 +1624,11 @@ cudaError_t zgemm_oz_c64(const GemmArgs& a, int slices, cudaStream_t s) {
     return cudaErrorInvalidValue;
   if (a.opA == OP_T || a.opB == OP_T || a.alpha_im != 0.0 || a.beta_im != 0.0)
     return cudaErrorInvalidValue;
+  if (slices == 4) {
+    bool used = false;
+    const cudaError_t e = c64t::launch(a, s, &used);
+    if (e != cudaSuccess || used) return e;
+  }
   switch (slices) {
     case 3: return launch<3, 2, 128, float2, float2>(a, s);
     case 4: return launch<4, 3, 128, float2, float2>(a, s);
