@@ -69,8 +69,15 @@ def parse():
                     help="keep the library's default wave size instead of autotuning it")
     ap.add_argument("--wave", type=int, default=0,
                     help="points per wave, set without autotuning (0: autotune unless --no-tune)")
-    ap.add_argument("--workload", default="batched", choices=["batched", "uneven"],
-                    help="batched: 100 x 128 slabs (the headline); uneven: the 4000-atom graph")
+    ap.add_argument("--workload", default="batched", choices=["batched", "uneven", "gw"],
+                    help="batched: 100 x 128 slabs (the headline); uneven: the 4000-atom graph; "
+                         "gw: GW-SCBA on the 80-slab x 96-orbital device with 2048 energies")
+    ap.add_argument("--gw-size", default="80,96,2048",
+                    help="slabs,orbitals,energies of the --workload gw device")
+    ap.add_argument("--gw-precisions", default="mixed,mixed-fp64,fp64",
+                    help="--workload gw: precisions to converge (the last is the reference)")
+    ap.add_argument("--gw-max-iter", type=int, default=60)
+    ap.add_argument("--gw-tol", type=float, default=1e-8)
     return ap.parse_args()
 
 
@@ -632,12 +639,78 @@ def run_uneven(a):
     ctx.close()
 
 
+def run_gw(a):
+    """GW-SCBA at size: plain linear mixing (alpha = 0.3, the reference's scheme) to residual
+    --gw-tol on a seeded 80-slab x 96-orbital chain (H_ii shared by all slabs: on-site
+    U[-1, 1] eV, off-diagonal N(0, 0.1) eV; H_i,i+1 = -2.7 I + N(0, 0.05)), 2048 energies
+    on [-4, 4] eV, V_ij = 14.4 / (|r_i - r_j| + 1) eV on a 0.25 nm grid, FFT length 4096.
+    Each precision runs to convergence in turn (the device holds one SCBA at a time); the
+    terminal currents and the LDOS of the converged self-energies are compared with the
+    last precision's (FP64)."""
+    import torch
+    from quantum_transport_gb300.build import build
+    build()
+    from quantum_transport_gb300 import gw, rgf
+    from quantum_transport_gb300.devices import coulomb_block, make_chain_device
+    nx, nm, nE = (int(x) for x in a.gw_size.split(","))
+    d = make_chain_device(nx, nm, nE, -4.0, 4.0, seed=SEED)
+    V = coulomb_block(nm)
+    ctx = rgf.Context(0)
+    precs = a.gw_precisions.split(",")
+    runs = {}
+    clocks = Clocks(0)
+    clocks.start()
+    for p in precs:
+        s = gw.GwSystem(ctx, d.H00[0], d.H10, d.E, nx, V, mu=(0.1, -0.1), precision=p)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        SR, SL, SG, res, cur = s.scba(alpha=0.3, tol=a.gw_tol, max_iter=a.gw_max_iter,
+                                      with_currents=True)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        ob = s.currents(SR, SL)
+        runs[p] = {"seconds": dt, "iterations": int(len(res)),
+                   "seconds_per_iteration": dt / max(1, len(res)),
+                   "final_residual": float(res[-1]), "converged": bool(res[-1] <= a.gw_tol),
+                   "residuals": [float(x) for x in res],
+                   "current_A": [float(x) for x in cur[-1]],
+                   "_ldos": -2.0 * ob["diag_gr"].imag}
+        del SR, SL, SG, s
+        torch.cuda.empty_cache()
+    clk = clocks.stop()
+    ref = precs[-1]
+    r0 = runs[ref]
+    out = {}
+    for p, r in runs.items():
+        e = {k: v for k, v in r.items() if not k.startswith("_")}
+        if p != ref:
+            e["time_vs_" + ref] = r["seconds"] / r0["seconds"]
+            c, c0 = np.array(r["current_A"]), np.array(r0["current_A"])
+            e["current_rel_err"] = float(np.max(np.abs(c - c0) / np.abs(c0)))
+            e["ldos_rel_err"] = float(np.abs(r["_ldos"] - r0["_ldos"]).max() /
+                                      np.abs(r0["_ldos"]).max())
+        out[p] = e
+    L = 1 << int(np.ceil(np.log2(2 * nE)))
+    line = {"metric": METRIC, "workload": "gw", "unit": "s to residual", "tol": a.gw_tol,
+            "higher_is_better": False, "n_gpus": 1, "data": "synthetic (seeded, no dataset)",
+            "config": {"workload": f"GW-SCBA, {nx} slabs x {nm} orbitals x {nE} energies on "
+                                   f"[-4, 4] eV, plain linear mixing alpha = 0.3 to residual "
+                                   f"{a.gw_tol:g} (max {a.gw_max_iter} iterations), FFT length {L}",
+                       "memory": "six [nE][nx][nm^2] complex128 arrays in the map (G, then P "
+                                 "-> W in place, Sigma_new over G) + the three Sigma arrays"},
+            "runs": out, "clocks": clk}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     a = parse()
     if a.impl == "reference":
         run_reference(a)
     elif a.workload == "uneven":
         run_uneven(a)
+    elif a.workload == "gw":
+        run_gw(a)
     else:
         run_ours(a)
 

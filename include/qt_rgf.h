@@ -430,9 +430,11 @@ qt_status qt_gw_polarization(qt_ctx* ctx, int n, int64_t nseries, const double* 
 
 /* W^R = (I - V P^R)^-1 V and W^{<,>} = W^R P^{<,>} W^R^+ for nblocks blocks
  * (the restatement of the absent green_rgf_calc_w, src/gw_mod.f90:597), V one
- * nm x nm block for all.  W^< and W^> may overwrite P^< and P^>; W^R may not
- * alias any P.  QT_PREC_MIXED / QT_PREC_MIXED_FP64 take the FP64-grade split
- * products and refined inverses of the leads (nm <= 384).  Synchronises.    */
+ * nm x nm block for all.  Each W may overwrite its own P (W^R over P^R, W^<
+ * over P^<, W^> over P^>), not another one; the blocks are processed in chunks
+ * of about 8 GB of context scratch.  QT_PREC_MIXED / QT_PREC_MIXED_FP64 take
+ * the FP64-grade split products and refined inverses of the leads
+ * (nm <= 384).  Synchronises.                                               */
 qt_status qt_gw_screened(qt_ctx* ctx, int nm, int64_t nblocks, const double* V,
                          const double* PR, const double* PL, const double* PG, double* WR,
                          double* WL, double* WG, qt_precision prec, unsigned flags);

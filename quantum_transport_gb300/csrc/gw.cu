@@ -59,52 +59,79 @@ __device__ void fft_smem(double2* a, int L, int logL, const double2* tw, bool in
   }
 }
 
+// load one series pair into bit-reversed shared-memory buffers x, y (zero-padded to L)
+__device__ __forceinline__ void load_pair(const CorrConvArgs& a, const double2* X,
+                                          const double2* Y, const double2* Yb, long long sx,
+                                          long long sy, int conjY, double2* x, double2* y) {
+  const int n = a.n, L = a.L, logL = a.logL;
+  for (int t = threadIdx.x; t < L; t += blockDim.x) {
+    double2 vx = make_double2(0.0, 0.0), vy = vx;
+    if (t < n) {
+      vx = X[(long long)t * a.estride + sx];
+      if (a.imagX) vx.x = 0.0;
+      const int ty = a.corr ? (n - 1 - t) : t;  // correlation: reversed Y
+      vy = Y[(long long)ty * a.estride + sy];
+      if (Yb) {
+        const double2 b = Yb[(long long)ty * a.estride + sy];
+        vy.x += b.x;
+        vy.y += b.y;
+      }
+      if (a.imagY) vy.x = 0.0;
+      if (conjY) vy.y = -vy.y;
+    }
+    const int r = (int)(__brev((unsigned)t) >> (32 - logL));
+    x[r] = vx;
+    y[r] = vy;
+  }
+}
+
 __global__ void __launch_bounds__(FFT_NT) zcorrconv_kernel(CorrConvArgs a, const double2* tw) {
   extern __shared__ double2 sm[];
   const int n = a.n, L = a.L, logL = a.logL;
+  const bool two = a.X2 != nullptr;
   double2* x = sm;
   double2* y = sm + L;
+  double2* z = two ? sm + 2 * L : y;  // third buffer for the second term
   const long long nm2 = (long long)a.nm * a.nm;
   const double2* X = reinterpret_cast<const double2*>(a.X);
   const double2* Y = reinterpret_cast<const double2*>(a.Y);
+  const double2* X2 = reinterpret_cast<const double2*>(a.X2);
+  const double2* Y2 = reinterpret_cast<const double2*>(a.Y2);
+  const double2* Y2b = reinterpret_cast<const double2*>(a.Y2b);
   double2* Z = reinterpret_cast<double2*>(a.Z);
   for (long long s = blockIdx.x; s < a.nseries; s += gridDim.x) {
     const long long ix = s / nm2, ij = s % nm2;
     const int i = (int)(ij % a.nm), j = (int)(ij / a.nm);
     const long long sx = ix * nm2 + ij;
-    const long long sy = a.transY ? ix * nm2 + i * (long long)a.nm + j : sx;
-    for (int t = threadIdx.x; t < L; t += blockDim.x) {
-      double2 vx = make_double2(0.0, 0.0), vy = vx;
-      if (t < n) {
-        vx = X[(long long)t * a.estride + sx];
-        if (a.imagX) vx.x = 0.0;
-        const int ty = a.corr ? (n - 1 - t) : t;  // correlation: reversed Y
-        vy = Y[(long long)ty * a.estride + sy];
-        if (a.imagY) vy.x = 0.0;
-        if (a.conjY) vy.y = -vy.y;
-      }
-      const int r = (int)(__brev((unsigned)t) >> (32 - logL));
-      x[r] = vx;
-      y[r] = vy;
-    }
+    const long long st = ix * nm2 + i * (long long)a.nm + j;  // the transposed element
+    load_pair(a, X, Y, nullptr, sx, a.transY ? st : sx, a.conjY, x, y);
     __syncthreads();
     fft_smem(x, L, logL, tw, false);
     fft_smem(y, L, logL, tw, false);
-    // pointwise product, bit-reversed into y for the inverse transform
-    for (int t = threadIdx.x; t < L; t += blockDim.x) {
-      const double2 p = dmul(x[t], y[t]);
-      x[t] = p;
+    for (int t = threadIdx.x; t < L; t += blockDim.x) x[t] = dmul(x[t], y[t]);
+    __syncthreads();
+    if (two) {
+      // second term: x += FFT(X2) FFT(Y2 + Y2b) (linearity: one inverse transform)
+      load_pair(a, X2, Y2, Y2b, sx, a.transY2 ? st : sx, a.conjY2, y, z);
+      __syncthreads();
+      fft_smem(y, L, logL, tw, false);
+      fft_smem(z, L, logL, tw, false);
+      for (int t = threadIdx.x; t < L; t += blockDim.x) {
+        const double2 p = dmul(y[t], z[t]);
+        x[t] = make_double2(x[t].x + p.x, x[t].y + p.y);
+      }
+      __syncthreads();
     }
-    __syncthreads();
+    // bit-reversed into z for the inverse transform
     for (int t = threadIdx.x; t < L; t += blockDim.x)
-      y[(int)(__brev((unsigned)t) >> (32 - logL))] = x[t];
+      z[(int)(__brev((unsigned)t) >> (32 - logL))] = x[t];
     __syncthreads();
-    fft_smem(y, L, logL, tw, true);
+    fft_smem(z, L, logL, tw, true);
     const double inv = 1.0 / L;
     const double2 sc = make_double2(a.scale_re * inv, a.scale_im * inv);
     for (int m = threadIdx.x; m < n; m += blockDim.x) {
       const int t = a.corr ? (m - n / 2 + n - 1) : (m + n / 2);
-      const double2 v = dmul(y[t], sc);
+      const double2 v = dmul(z[t], sc);
       double2* zp = &Z[(long long)m * a.estride + sx];
       if (a.accumulate) {
         const double2 o = *zp;
@@ -221,7 +248,7 @@ cudaError_t zcorrconv(CorrConvArgs a, const double2* tw, cudaStream_t s) {
   if (L > LMAX) return cudaErrorInvalidValue;
   a.L = L;
   a.logL = logL;
-  const size_t smem = (size_t)2 * L * sizeof(double2);
+  const size_t smem = (size_t)(a.X2 ? 3 : 2) * L * sizeof(double2);
   cudaError_t e = cudaFuncSetAttribute(zcorrconv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return e;

@@ -129,6 +129,14 @@ struct CorrConvArgs {
   int conjY, imagX, imagY;  // conj(Y); Re(X) := 0; Re(Y) := 0 (applied before conj)
   int accumulate;     // Z += result
   double scale_re, scale_im;
+  // optional second term, summed before the inverse transform:
+  //   Z = scale (op(X, Y) + op(X2, Y2 + Y2b))   (X2 null: one term; Y2b may be null)
+  // with its own transposition / conjugation of Y2 (imagX / imagY apply to both terms).
+  // Z may alias X or X2: a series is read completely before it is written.
+  const void* X2 = nullptr;
+  const void* Y2 = nullptr;
+  const void* Y2b = nullptr;
+  int transY2 = 0, conjY2 = 0;
   int L, logL;        // set by the launcher
 };
 cudaError_t gw_twiddles(double2* tw, cudaStream_t s);  // 2048 entries exp(-2 pi i k / 4096)

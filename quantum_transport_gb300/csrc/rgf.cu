@@ -1942,8 +1942,11 @@ extern "C" qt_status qt_zinv_batch(qt_ctx* ctx, int n, int batch, const double* 
 // the edge-block copy (:950-959).
 namespace {
 
+// The map holds six [nE][nx][nm^2] arrays: G^{R,<,>}, then P^{R,<,>}, which become
+// W^{R,<,>} in place; the new self-energies are written over G (a series is read
+// completely before it is written), so NR/NL/NG alias GR/GL/GG.
 struct GwBuffers {
-  cd *GR, *GL, *GG, *PR, *PL, *PG, *T1, *T2, *NR, *NL, *NG;
+  cd *GR, *GL, *GG, *PR, *PL, *PG, *NR, *NL, *NG;
   double2* tw;
   double* sums;
 };
@@ -1955,49 +1958,54 @@ struct GwCurrents {
 };
 
 // W^R = (I - V P^R)^-1 V and W^{<,>} = W^R P^{<,>} W^R^+ per (w, slab) block, nblk blocks of
-// nm x nm at stride nm^2.  WL/WG may alias PL/PG; T1, T2 are nblk-block scratch (taken
-// from the context arena when null).
+// nm x nm at stride nm^2, in chunks of blocks whose scratch (two chunk-sized blocks, the
+// refinement blocks, exponent table and guard flags) comes from the context arena.  Each
+// output may alias its own P (W^R -> P^R, W^< -> P^<, W^> -> P^>): a chunk of P is read
+// before that chunk of W is written.
 qt_status gw_screened_blocks(qt_ctx* ctx, int nm, long long nblk, qt_precision prec,
                              int slices, const cd* V, const cd* PR, const cd* PL, const cd* PG,
-                             cd* WR, cd* WL, cd* WG, cd* T1, cd* T2) {
+                             cd* WR, cd* WL, cd* WG) {
   cudaStream_t s = ctx->stream;
   const long long nm2 = (long long)nm * nm;
   Ops<double2> op{s, nm, prec};
   op.slices = slices;
   op.refine = prec == QT_PREC_FP64 ? 0 : 2;
   op.prof = &ctx->prof;
-  const size_t scratch = (T1 ? 0 : 2 * (size_t)nblk * nm2 * 16 + 512);
-  const size_t need_extra = (size_t)nblk * 1300 + 2 * (size_t)nblk * nm2 * 16 + 4096 + scratch;
-  QT_TRY(ensure(ctx->arena, ctx->arena_bytes, need_extra));
+  // about 8 GB of scratch per chunk
+  const size_t per_block = 4 * (size_t)nm2 * 16 + 1300;
+  const long long chunk = std::max(1LL, std::min(nblk, (long long)((8ull << 30) / per_block)));
+  QT_TRY(ensure(ctx->arena, ctx->arena_bytes, (size_t)chunk * per_block + 8192));
   Arena ar{reinterpret_cast<char*>(ctx->arena), ctx->arena_bytes, 0};
   cd* one = ar.take<cd>(1);
   const cd h1{1.0, 0.0};
   cudaMemcpyAsync(one, &h1, sizeof(cd), cudaMemcpyHostToDevice, s);
   op.one = one;
-  op.scales = ar.take<int>((size_t)nblk * 256);
-  op.rt1 = reinterpret_cast<double2*>(ar.take<cd>((size_t)nblk * nm2));
-  op.rt2 = reinterpret_cast<double2*>(ar.take<cd>((size_t)nblk * nm2));
-  op.P = nblk;
-  op.guard = ar.take<unsigned char>((size_t)nblk);
+  op.scales = ar.take<int>((size_t)chunk * 256);
+  op.rt1 = reinterpret_cast<double2*>(ar.take<cd>((size_t)chunk * nm2));
+  op.rt2 = reinterpret_cast<double2*>(ar.take<cd>((size_t)chunk * nm2));
+  op.P = chunk;
+  op.guard = ar.take<unsigned char>((size_t)chunk);
   op.fallbacks = ctx->fallbacks;
-  if (!T1) {
-    T1 = ar.take<cd>((size_t)nblk * nm2);
-    T2 = ar.take<cd>((size_t)nblk * nm2);
-  }
+  cd* T1 = ar.take<cd>((size_t)chunk * nm2);
+  cd* T2 = ar.take<cd>((size_t)chunk * nm2);
   if (!op.scales || !op.rt2 || !op.guard || !T1 || !T2)
     QT_FAIL(QT_ERR_NOMEM, "arena exhausted (W)");
   const BatchRef Vr = ref(V, 0, nm), B = ref(nullptr, nm2, nm);
   auto blk = [&](const cd* p) { BatchRef r = B; r.p = const_cast<cd*>(p); return r; };
-  // T1 = I - V P^R ; T2 = T1^-1 ; W^R = T2 V
-  QT_TRY(op.gemm(Vr, qt::OP_N, blk(PR), qt::OP_N, blk(T1), nblk, {-1, 0}, nullref(),
-                 {0, 0}, ref(one, 0, 1)));
-  QT_TRY(op.inv(blk(T1), blk(T2), nblk, nullptr));
-  QT_TRY(op.gemm(blk(T2), qt::OP_N, Vr, qt::OP_N, blk(WR), nblk));
-  // W^< = W^R P^< W^R^+, W^> = W^R P^> W^R^+
-  QT_TRY(op.gemm(blk(WR), qt::OP_N, blk(PL), qt::OP_N, blk(T1), nblk));
-  QT_TRY(op.gemm(blk(T1), qt::OP_N, blk(WR), qt::OP_C, blk(WL), nblk));
-  QT_TRY(op.gemm(blk(WR), qt::OP_N, blk(PG), qt::OP_N, blk(T1), nblk));
-  QT_TRY(op.gemm(blk(T1), qt::OP_N, blk(WR), qt::OP_C, blk(WG), nblk));
+  for (long long c0 = 0; c0 < nblk; c0 += chunk) {
+    const long long cb = std::min(chunk, nblk - c0), o = c0 * nm2;
+    // T1 = I - V P^R ; T2 = T1^-1 ; T1 = T2 V = W^R
+    QT_TRY(op.gemm(Vr, qt::OP_N, blk(PR + o), qt::OP_N, blk(T1), cb, {-1, 0}, nullref(),
+                   {0, 0}, ref(one, 0, 1)));
+    QT_TRY(op.inv(blk(T1), blk(T2), cb, nullptr));
+    QT_TRY(op.gemm(blk(T2), qt::OP_N, Vr, qt::OP_N, blk(T1), cb));
+    // W^< = W^R P^< W^R^+, W^> = W^R P^> W^R^+
+    QT_TRY(op.gemm(blk(T1), qt::OP_N, blk(PL + o), qt::OP_N, blk(T2), cb));
+    QT_TRY(op.gemm(blk(T2), qt::OP_N, blk(T1), qt::OP_C, blk(WL + o), cb));
+    QT_TRY(op.gemm(blk(T1), qt::OP_N, blk(PG + o), qt::OP_N, blk(T2), cb));
+    QT_TRY(op.gemm(blk(T2), qt::OP_N, blk(T1), qt::OP_C, blk(WG + o), cb));
+    qt::zcopy<double2>(nm, cb, blk(T1), blk(WR + o), s);
+  }
   return QT_OK;
 }
 
@@ -2060,19 +2068,31 @@ qt_status gw_map(qt_ctx* ctx, Problem pb, const cd* V, double spindeg, const cd*
   };
   QT_TRY(cc(w.GL, w.GG, w.PL, 1, 1, 0, 1, 1, 0, 0.0, -pf));        // P^< = corr(G^<_ij, G^>_ji)
   QT_TRY(cc(w.GG, w.GL, w.PG, 1, 1, 0, 1, 1, 0, 0.0, -pf));        // P^> = corr(G^>_ij, G^<_ji)
-  QT_TRY(cc(w.GL, w.GR, w.PR, 1, 0, 1, 1, 1, 0, 0.0, -pf));        // corr(G^<_ij, conj G^R_ij)
-  QT_TRY(cc(w.GR, w.GL, w.PR, 1, 1, 0, 1, 1, 1, 0.0, -pf));        //   + corr(G^R_ij, G^<_ji)
-  // ---- screened interaction per (w, slab) block: W^R -> NR (scratch) -> PR, W^<> in place
-  QT_TRY(gw_screened_blocks(ctx, nm, nblk, pb.prec, pb.lead_slices, V, w.PR, w.PL, w.PG, w.NR,
-                            w.PL, w.PG, w.T1, w.T2));
-  qt::zcopy<double2>(nm, nblk, ref(w.NR, nm2, nm), ref(w.PR, nm2, nm), s);
-  // ---- self-energy: energy convolutions x i dE / (2 pi)
+  {
+    // P^R = corr(G^<_ij, conj G^R_ij) + corr(G^R_ij, G^<_ji), one inverse transform
+    qt::CorrConvArgs a = c;
+    a.X = w.GL; a.Y = w.GR; a.conjY = 1; a.X2 = w.GR; a.Y2 = w.GL; a.transY2 = 1;
+    a.Z = w.PR; a.corr = 1; a.imagX = 1; a.imagY = 1; a.scale_re = 0.0; a.scale_im = -pf;
+    cudaError_t e = qt::zcorrconv(a, w.tw, s);
+    if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+  }
+  // ---- screened interaction per (w, slab) block, in place: P -> W
+  QT_TRY(gw_screened_blocks(ctx, nm, nblk, pb.prec, pb.lead_slices, V, w.PR, w.PL, w.PG, w.PR,
+                            w.PL, w.PG));
+  // ---- self-energy: energy convolutions x i dE / (2 pi), written over G: Sigma^R first
+  // (it reads G^< and G^R), then Sigma^< over G^<, Sigma^> over G^>
   const double sf = dE / (2.0 * M_PI);
+  {
+    // Sigma^R = conv(G^<, W^R) + conv(G^R, W^<) + conv(G^R, W^R)
+    //         = conv(G^<, W^R) + conv(G^R, W^< + W^R)
+    qt::CorrConvArgs a = c;
+    a.X = w.GL; a.Y = w.PR; a.X2 = w.GR; a.Y2 = w.PL; a.Y2b = w.PR;
+    a.Z = w.NR; a.corr = 0; a.imagX = 1; a.scale_re = 0.0; a.scale_im = sf;
+    cudaError_t e = qt::zcorrconv(a, w.tw, s);
+    if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+  }
   QT_TRY(cc(w.GL, w.PL, w.NL, 0, 0, 0, 1, 0, 0, 0.0, sf));  // Sigma^< = conv(G^<, W^<)
   QT_TRY(cc(w.GG, w.PG, w.NG, 0, 0, 0, 1, 0, 0, 0.0, sf));  // Sigma^> = conv(G^>, W^>)
-  QT_TRY(cc(w.GL, w.PR, w.NR, 0, 0, 0, 1, 0, 0, 0.0, sf));  // Sigma^R = conv(G^<, W^R)
-  QT_TRY(cc(w.GR, w.PL, w.NR, 0, 0, 0, 1, 0, 1, 0.0, sf));  //   + conv(G^R, W^<)
-  QT_TRY(cc(w.GR, w.PR, w.NR, 0, 0, 0, 1, 0, 1, 0.0, sf));  //   + conv(G^R, W^R)
   // ---- recombination, symmetrisation, edge blocks
   QT_TRY(gw_post(ctx, nm, nx, nE, w.NR, w.NL, w.NG));
   (void)cnt;
@@ -2110,17 +2130,20 @@ struct GwAlloc {
 
 qt_status gw_alloc(qt_ctx* ctx, long long cnt, GwBuffers& w, GwAlloc& hold) {
   const size_t blk = (size_t)cnt * sizeof(cd);
-  // 11 block arrays, FFT twiddles, then 64 B of sums and 2 x 2048 doubles of currents
-  const size_t need = 11 * blk + 2048 * sizeof(double2) + 64 + 2 * 2048 * sizeof(double);
+  // 6 block arrays, FFT twiddles, then 64 B of sums and 2 x 2048 doubles of currents
+  const size_t need = 6 * blk + 2048 * sizeof(double2) + 64 + 2 * 2048 * sizeof(double);
   if (cudaMalloc(&hold.p, need) != cudaSuccess) {
     cudaGetLastError();
     QT_FAIL(QT_ERR_NOMEM, "GW buffers");
   }
   char* b = reinterpret_cast<char*>(hold.p);
-  cd** slots[] = {&w.GR, &w.GL, &w.GG, &w.PR, &w.PL, &w.PG, &w.T1, &w.T2, &w.NR, &w.NL, &w.NG};
-  for (int i = 0; i < 11; ++i) *slots[i] = reinterpret_cast<cd*>(b + i * blk);
-  w.tw = reinterpret_cast<double2*>(b + 11 * blk);
-  w.sums = reinterpret_cast<double*>(b + 11 * blk + 2048 * sizeof(double2));
+  cd** slots[] = {&w.GR, &w.GL, &w.GG, &w.PR, &w.PL, &w.PG};
+  for (int i = 0; i < 6; ++i) *slots[i] = reinterpret_cast<cd*>(b + i * blk);
+  w.NR = w.GR;
+  w.NL = w.GL;
+  w.NG = w.GG;
+  w.tw = reinterpret_cast<double2*>(b + 6 * blk);
+  w.sums = reinterpret_cast<double*>(b + 6 * blk + 2048 * sizeof(double2));
   cudaError_t e = qt::gw_twiddles(w.tw, ctx->stream);
   if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
   return QT_OK;
@@ -2349,8 +2372,10 @@ extern "C" qt_status qt_gw_polarization(qt_ctx* ctx, int n, int64_t nseries, con
   // P = -i scale corr(...) of the Re-zeroed G (src/gw_mod.f90:444-446, 495-519)
   QT_TRY(series_run(ctx, c, tw, GL, GGt, PL, 1, 0, 1, 1, 0, 0.0, -scale));
   QT_TRY(series_run(ctx, c, tw, GG, GLt, PG, 1, 0, 1, 1, 0, 0.0, -scale));
-  QT_TRY(series_run(ctx, c, tw, GL, GR, PR, 1, 1, 1, 1, 0, 0.0, -scale));
-  QT_TRY(series_run(ctx, c, tw, GR, GLt, PR, 1, 0, 1, 1, 1, 0.0, -scale));
+  // P^R = corr(G^<, conj G^R) + corr(G^R, G^<t), one inverse transform (as qt_gw_step)
+  qt::CorrConvArgs a = c;
+  a.X2 = GR; a.Y2 = GLt;
+  QT_TRY(series_run(ctx, a, tw, GL, GR, PR, 1, 1, 1, 1, 0, 0.0, -scale));
   if (flags & QT_FLAG_SYNC) QT_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return QT_OK;
 }
@@ -2365,15 +2390,15 @@ extern "C" qt_status qt_gw_screened(qt_ctx* ctx, int nm, int64_t nblocks, const 
   if (!valid_prec(prec)) QT_FAIL(QT_ERR_ARG, "unknown precision");
   if (prec != QT_PREC_FP64 && nm > MAX_SPLIT)
     QT_FAIL(QT_ERR_UNSUPPORTED, "split-precision path needs nm <= 384");
-  if (WR == PR || WR == PL || WR == PG || WL == PR || WG == PR)
-    QT_FAIL(QT_ERR_ARG, "W^R may not alias P; W^< and W^> may alias only P^< and P^>");
+  if (WR == PL || WR == PG || WL == PR || WL == PG || WG == PR || WG == PL)
+    QT_FAIL(QT_ERR_ARG, "each W may alias only its own P (W^R -> P^R, W^< -> P^<, W^> -> P^>)");
   cudaSetDevice(ctx->device);
   // FP64-grade digits on the split path, as inside qt_gw_step
   QT_TRY(gw_screened_blocks(ctx, nm, nblocks, prec, env_int("QT_LEAD_SLICES", 7),
                             reinterpret_cast<const cd*>(V), reinterpret_cast<const cd*>(PR),
                             reinterpret_cast<const cd*>(PL), reinterpret_cast<const cd*>(PG),
                             reinterpret_cast<cd*>(WR), reinterpret_cast<cd*>(WL),
-                            reinterpret_cast<cd*>(WG), nullptr, nullptr));
+                            reinterpret_cast<cd*>(WG)));
   QT_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   if (prec != QT_PREC_FP64 && qt::oz_timeouts_and_reset())
     QT_FAIL(QT_ERR_CUDA, "tensor-core kernel wait timed out");
@@ -2392,9 +2417,10 @@ extern "C" qt_status qt_gw_selfenergy(qt_ctx* ctx, int n, int64_t nseries, const
   // Sigma = i scale conv(...) with the Re-zeroed G (src/gw_mod.f90:646-698)
   QT_TRY(series_run(ctx, c, tw, GL, WL, SL, 0, 0, 1, 0, 0, 0.0, scale));
   QT_TRY(series_run(ctx, c, tw, GG, WG, SG, 0, 0, 1, 0, 0, 0.0, scale));
-  QT_TRY(series_run(ctx, c, tw, GL, WR, SR, 0, 0, 1, 0, 0, 0.0, scale));
-  QT_TRY(series_run(ctx, c, tw, GR, WL, SR, 0, 0, 1, 0, 1, 0.0, scale));
-  QT_TRY(series_run(ctx, c, tw, GR, WR, SR, 0, 0, 1, 0, 1, 0.0, scale));
+  // Sigma^R = conv(G^<, W^R) + conv(G^R, W^< + W^R), one inverse transform (as qt_gw_step)
+  qt::CorrConvArgs a = c;
+  a.X2 = GR; a.Y2 = WL; a.Y2b = WR;
+  QT_TRY(series_run(ctx, a, tw, GL, WR, SR, 0, 0, 1, 0, 0, 0.0, scale));
   if (flags & QT_FLAG_SYNC) QT_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return QT_OK;
 }
