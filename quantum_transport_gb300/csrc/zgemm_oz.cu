@@ -1237,8 +1237,7 @@ cudaError_t launch(const GemmArgs& g, cudaStream_t s, bool* used) {
 // digit planes (integer digit extraction of the FP64 values), one MMA warp issues every
 // digit pair, and the epilogue assembles FP64 results from the per-level accumulators.
 // A work item is one real part of one 64-column tile; every level keeps its own (exact)
-// accumulator, NACC = S accumulators x 64 columns of TMEM (two items' worth when they fit,
-// S = 4, so that the epilogue overlaps the next item).  complex128 strides are always
+// accumulator, NACC = S accumulators x 64 columns of TMEM.  complex128 strides are always
 // multiples of 16 bytes, so every operand qualifies for a tensor map.
 namespace c128t {
 constexpr int NT = 64;                   // output columns per item
@@ -1254,7 +1253,10 @@ constexpr int RSTAGE = RAW_A + RAW_B;
 constexpr uint32_t SBO_T = (2 * KCC / 8) * 128;  // 8-row groups of a digit plane (256 B)
 template <int S> struct Cfg {
   static constexpr int NACC = S;  // levels 0 .. S-1, one exact accumulator each
-  static constexpr int NBUF = 2 * NACC * NT <= 512 ? 2 : 1;
+  // One accumulator set per CTA.  A second set (the 4-digit product fits two) let the
+  // epilogue overlap the next item, but gave results that differed from run to run when
+  // the product had a beta D term; with one set the results are bit-reproducible.
+  static constexpr int NBUF = 1;
   static constexpr int DSTAGE = S * (APLANE + BPLANE);
   static constexpr int SMEM = 1024 + RSTAGES * RSTAGE + DSTAGES * DSTAGE + 256;
   static_assert(SMEM <= 232448, "shared memory");

@@ -116,3 +116,31 @@ def test_c128_product_shared_and_tiled(ctx, slices, n, shared):
         tol = TOL128[slices] * _bound(A, B, opa, opb) * tiles + 4e-16 * tiles * np.abs(exact)
         err = np.abs(got - exact)
         assert (err <= tol).all(), float((err / tol).max())
+
+
+@pytest.mark.parametrize("kind,slices", [("c64", 4), ("c128", 4), ("c128", 6), ("c128", 7)])
+def test_products_repeat_bitwise_with_beta_d(ctx, kind, slices):
+    """2048 products per launch (many work items per CTA) with a beta D term give the same
+    bits on every call.  A two-accumulator-set variant of the complex128 kernel did not: its
+    results differed from run to run only in this configuration."""
+    import torch
+    from quantum_transport_gb300 import _lib
+    from quantum_transport_gb300.rgf import _ptr
+    lib = ctx._lib
+    n, batch = 128, 2048
+    g = torch.Generator(device="cuda").manual_seed(5)
+    dt = torch.complex64 if kind == "c64" else torch.complex128
+    A = torch.randn(batch, n, n, dtype=dt, device="cuda", generator=g)
+    B = 1e-3 * torch.randn(batch, n, n, dtype=dt, device="cuda", generator=g)
+    D = torch.randn(batch, n, n, dtype=dt, device="cuda", generator=g)
+    one = np.array([1.0, 0.0])
+    flags = _lib.QT_FLAG_DEVICE_POINTERS | _lib.QT_FLAG_SYNC | (
+        _lib.QT_FLAG_COMPLEX64 if kind == "c64" else 0)
+    outs = []
+    for _ in range(4):
+        C = torch.zeros_like(A)
+        _lib.check(lib.qt_zgemm_batch(ctx.handle, n, batch, b"N", _ptr(A), n * n, b"N", _ptr(B),
+                                      n * n, _ptr(one), _ptr(one), _ptr(D), n * n, _ptr(C), n * n,
+                                      _lib.QT_PREC_MIXED, slices, flags))
+        outs.append(C)
+    assert all(torch.equal(outs[0], o) for o in outs[1:])
