@@ -851,25 +851,38 @@ __device__ __forceinline__ void digit_scale(int e, float sign, float2& m, float&
   m = make_float2(pre, pre * sign);
   sc = __int_as_float((127 + 8 - (tiny ? e + 64 : e)) << 23);
 }
-// one real part of an output element from its two accumulators, with the arithmetic of
-// Store<float2>::put: normalised (hi, lo), scaled by 2^e2 and alpha, beta d and z added
-__device__ __forceinline__ float c64_value(uint32_t acc0, uint32_t acc1, int e2, float alpha,
-                                           float beta, const float* d, bool diag, double z) {
-  float hi, lo, s2, e;
-  two_sum(__uint_as_float(acc0), __uint_as_float(acc1), hi, lo);
-  two_sum(hi, lo, s2, e);
-  float v, w;
+// both real parts of an output element from their accumulators (level 0, levels 1-3),
+// with the arithmetic of Store<float2>::put lane by lane in packed FP32x2 operations (each
+// lane rounds exactly as the scalar form: the same bits in half the instructions):
+// normalised (hi, lo) by two TwoSums, scaled by 2^e2 and alpha, beta d and z added
+__device__ __forceinline__ float2 fsub2(float2 x, float2 y) {  // x - y, exact as a subtraction
+  return __ffma2_rn(y, make_float2(-1.0f, -1.0f), x);
+}
+__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2& s, float2& e) {
+  s = __fadd2_rn(a, b);
+  const float2 bb = fsub2(s, a);
+  e = __fadd2_rn(fsub2(a, fsub2(s, bb)), fsub2(b, bb));
+}
+__device__ __forceinline__ float2 c64_pair(uint32_t r0, uint32_t r1, uint32_t i0, uint32_t i1,
+                                           int e2, float alpha, float beta, const float2* d,
+                                           bool diag, double2 z) {
+  float2 hi, lo, s2, e;
+  two_sum2(make_float2(__uint_as_float(r0), __uint_as_float(i0)),
+           make_float2(__uint_as_float(r1), __uint_as_float(i1)), hi, lo);
+  two_sum2(hi, lo, s2, e);
+  float2 v, w;
+  const float2 al = make_float2(alpha, alpha);
   if (e2 > -126 && e2 < 128) {
     const float sc = __int_as_float((127 + e2) << 23);  // 2^e2
-    v = alpha * (s2 * sc);
-    w = alpha * (e * sc);
+    v = __fmul2_rn(al, __fmul2_rn(s2, make_float2(sc, sc)));
+    w = __fmul2_rn(al, __fmul2_rn(e, make_float2(sc, sc)));
   } else {
-    v = alpha * ldexpf(s2, e2);
-    w = alpha * ldexpf(e, e2);
+    v = make_float2(alpha * ldexpf(s2.x, e2), alpha * ldexpf(s2.y, e2));
+    w = make_float2(alpha * ldexpf(e.x, e2), alpha * ldexpf(e.y, e2));
   }
-  if (d) v = fmaf(beta, *d, v);
-  if (diag) v += (float)z;
-  return v + w;
+  if (d) v = __ffma2_rn(make_float2(beta, beta), *d, v);
+  if (diag) v = __fadd2_rn(v, make_float2((float)z.x, (float)z.y));
+  return __fadd2_rn(v, w);
 }
 
 __global__ void __launch_bounds__(NTHREADS, 1)
@@ -1123,14 +1136,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           for (int jj = 0; jj < 16; ++jj) {
             const int jcol = ct * NT + j0 + jj;
             if (jcol < n) {
-              const int e2 = ei + fcol[jcol] - 16;
-              const bool diag = a.Z.p && row == jcol;
-              const float* d = D ? reinterpret_cast<const float*>(D + row + (long long)jcol * a.D.ld)
-                                 : nullptr;
-              const float cr = c64_value(v[0][jj], v[1][jj], e2, alpha, beta, d, diag, z.x);
-              const float ci = c64_value(v[2][jj], v[3][jj], e2, alpha, beta, d ? d + 1 : nullptr,
-                                         diag, z.y);
-              C[row + (long long)jcol * a.C.ld] = make_float2(cr, ci);
+              const float2* d = D ? D + row + (long long)jcol * a.D.ld : nullptr;
+              C[row + (long long)jcol * a.C.ld] =
+                  c64_pair(v[0][jj], v[1][jj], v[2][jj], v[3][jj], ei + fcol[jcol] - 16, alpha,
+                           beta, d, a.Z.p && row == jcol, z);
             }
           }
         }
