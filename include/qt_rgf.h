@@ -349,12 +349,27 @@ qt_status qt_zgemm_batch_noalloc(int n, int batch, char opA, const double* A, in
  * results are incomplete.  No counterpart in the reference (see above).     */
 qt_status qt_noalloc_timeouts(int* count, void* stream);
 
-/* ---- GW / SCBA (one k-point; device pointers: QT_FLAG_DEVICE_POINTERS required).
- * Energy-resolved arrays are [nE][nx][nm*nm] complex128 column-major
- * slab-diagonal blocks; the energy grid E must be uniform (dE = E[1]-E[0]) and
- * nE <= 2048 (zero-padded FFT length 4096).  V: the nm x nm slab-diagonal
- * Coulomb block (the reference passes Vii/V1i, src/gw_mod.f90:84,597-600;
- * only the diagonal block enters the per-slab W restatement).                */
+/* ---- GW / SCBA (device pointers: QT_FLAG_DEVICE_POINTERS required).
+ * Energy-resolved arrays are [nk][nE][nx][nm*nm] complex128 column-major
+ * slab-diagonal blocks, k slowest as the reference's (nm, nm, nx, nE, nk)
+ * arrays; the energy grid E must be uniform (dE = E[1]-E[0]) and nE <= 2048
+ * (zero-padded FFT length 4096).  V: nk nm x nm slab-diagonal Coulomb blocks,
+ * one per momentum transfer q (the reference passes Vii/V1i per q,
+ * src/gw_mod.f90:84,597-600; only the diagonal block enters the per-slab W
+ * restatement).  dev->nk k-points need H blocks per k (hii_kstride or
+ * h1i_kstride non-zero).
+ *
+ * k-point grid and band (src/gw_mod.f90:466-555, 640-730): P at momentum
+ * transfer q sums corr(G_k, G_kd) over k, Sigma at k sums conv(G_kd, W_q) over
+ * q, with kd per direction = k - q + n_dir/2 (1-based, integer division)
+ * wrapped once into range, k = kz + ky * nkz; the scales carry 1/nk.  ndiag >= 0
+ * keeps only the elements |i - j| <= ndiag of P and Sigma (the reference's
+ * ndiag), ndiag < 0 the full blocks.  qt_ctx_set_gw_grid sets nky x nkz and
+ * ndiag for the context (default 1 x 1, full blocks); qt_gw_step and
+ * qt_scba_solve use it when nky * nkz = dev->nk and take a one-direction grid
+ * 1 x dev->nk when the context's grid is 1 x 1.  No counterpart: the
+ * reference reads nky, nkz and ndiag as arguments of gw_ephoton_3d_ijs.    */
+qt_status qt_ctx_set_gw_grid(qt_ctx* ctx, int nky, int nkz, int ndiag);
 
 /* One evaluation of the SCBA map Sigma -> Sigma_new of gw_ephoton_3d_ijs
  * (src/gw_mod.f90:368-749 and :950-959): G by the batched RGF with
@@ -405,6 +420,10 @@ qt_status qt_ephoton_sigma(qt_ctx* ctx, int nm, int nx, int nE, int nop, int hal
                            double* sigma_lesser, double* sigma_greater);
 
 /* ---- The SCBA map in stages, for ranks that share the energy grid.
+ * With the context's grid of nk = nky * nkz k-points every array holds nk
+ * k-blocks one after another (k slowest), each laid out as below, and the
+ * polarisation / self-energy sum over k-pairs as qt_gw_step does; the band
+ * is applied to blocks: P's in qt_gw_screened, Sigma's in qt_gw_sigma_post.
  * gw_ephoton_3d_ijs computes G on each rank's energies, moves G to (i, j)-major
  * order with an all-to-all (energies_to_ijs_2, src/gw_mod.f90:41-73), takes P
  * by energy correlations over the full grid on each rank's (i, j) elements,
@@ -429,10 +448,12 @@ qt_status qt_gw_polarization(qt_ctx* ctx, int n, int64_t nseries, const double* 
                              double* PG, unsigned flags);
 
 /* W^R = (I - V P^R)^-1 V and W^{<,>} = W^R P^{<,>} W^R^+ for nblocks blocks
- * (the restatement of the absent green_rgf_calc_w, src/gw_mod.f90:597), V one
- * nm x nm block for all.  Each W may overwrite its own P (W^R over P^R, W^<
- * over P^<, W^> over P^>), not another one; the blocks are processed in chunks
- * of about 8 GB of context scratch.  QT_PREC_MIXED / QT_PREC_MIXED_FP64 take
+ * (the restatement of the absent green_rgf_calc_w, src/gw_mod.f90:597): nk
+ * equal groups of blocks, group q with V block q (one group and one V block
+ * for one k-point), P banded first when the context's ndiag >= 0.  Each W
+ * may overwrite its own P (W^R over P^R, W^< over P^<, W^> over P^>), not
+ * another one; the blocks are processed in chunks of about 8 GB of context
+ * scratch.  QT_PREC_MIXED / QT_PREC_MIXED_FP64 take
  * the FP64-grade split products and refined inverses of the leads
  * (nm <= 384).  Synchronises.                                               */
 qt_status qt_gw_screened(qt_ctx* ctx, int nm, int64_t nblocks, const double* V,
@@ -448,7 +469,8 @@ qt_status qt_gw_selfenergy(qt_ctx* ctx, int n, int64_t nseries, const double* GR
                            const double* WL, const double* WG, double scale, double* SR,
                            double* SL, double* SG, unsigned flags);
 
-/* In place on [nE][nx] blocks: Sigma^R <- Re Sigma^R + i Im(Sigma^> - Sigma^<)/2
+/* In place on [nk][nE][nx] blocks: the band (context's ndiag >= 0), then
+ * Sigma^R <- Re Sigma^R + i Im(Sigma^> - Sigma^<)/2
  * (src/gw_mod.f90:698), S <- (S + S^T)/2 for all three (:731-743), and with
  * nx >= 5 the edge blocks 1,2 <- 3 and nx-1,nx <- nx-2 (:950-959).          */
 qt_status qt_gw_sigma_post(qt_ctx* ctx, int nm, int nx, int nE, double* SR, double* SL,

@@ -2,7 +2,9 @@
 
 Restates the steps of gw_ephoton_3d_ijs (src/gw_mod.f90:78-1070) that make up
 the GW self-energy loop (RGF, polarisation, screened interaction, self-energy,
-mixing), for one k-point (nk = 1):
+mixing); the functions below are for one k-point, and ``*_k`` further down sum
+over the k-pairs of nk = nky * nkz k-points and restrict P and Sigma to the
+``ndiag`` band:
 
 * energy correlation / convolution (src/fft_mod.f90:58-168, corr1d2 / conv1d2)
   on a uniform energy grid E_e = E_0 + e dE (e = 0..n-1) and the centred
@@ -177,6 +179,140 @@ def scba(E, H00, H10, V, nx, *, mu, temp, alpha=0.3, tol=1e-8, max_iter=60, spin
         res.append(r)
         if history is not None:
             history.append((SL.copy(), SG.copy(), nL.copy(), nG.copy()))
+        SR = SR + alpha * (nR - SR)
+        SL = SL + alpha * (nL - SL)
+        SG = SG + alpha * (nG - SG)
+        if r <= tol:
+            break
+    return SR, SL, SG, res
+
+
+# ---------------------------------------------------------------- several k-points, band
+#
+# With nk = nky * nkz transverse k-points (ik = ikz + iky nkz, 0-based; the reference's
+# ik = ikz + (iky-1) nkz, 1-based) the polarisation of momentum transfer q sums over the
+# k-pairs (k, kd(k, q)) and the self-energy at k over (kd(k, q), q)
+# (src/gw_mod.f90:476-512, 653-690):
+#     P_q   = sum_k  corr(G_k, G_kd)          (each of the P^{<,>,R} terms)
+#     S_k   = sum_q  conv(G_kd, W_q)          (each of the Sigma terms)
+# with the scales -i dE/(2 pi) spindeg/nk and i dE/(2 pi)/nk, W_q from the Coulomb block
+# V_q (Vii(:,:,:,iq), :597-600), and G, P, W, Sigma stored k-slowest as the reference's
+# (nm, nm, nx, nE, nk) arrays: numpy (nk, nE, nx, nm, nm).  ndiag keeps only the
+# elements |i - j| <= ndiag of P and Sigma (:473-475, 527-555, 650-654, 705-730);
+# None keeps the full blocks.
+
+
+def kd_index(ik, iq, nky, nkz):
+    """0-based k-pair partner ikd of ik and iq: per direction ikzd = ikz - iqz + nkz/2
+    (1-based, integer division) wrapped once into [1, nkz], and 1 when nkz = 1
+    (src/gw_mod.f90:478-487, 658-667)."""
+    iky, ikz = divmod(ik, nkz)
+    iqy, iqz = divmod(iq, nkz)
+    kzd = (ikz - iqz + nkz // 2 - 1) % nkz
+    kyd = (iky - iqy + nky // 2 - 1) % nky
+    return kzd + kyd * nkz
+
+
+def band_mask(nm, ndiag):
+    """True where |i - j| <= ndiag (all True for ndiag None), the elements the reference's
+    P and Sigma loops compute (src/gw_mod.f90:471-475) and its zeroing keeps (:527-555)."""
+    i = np.arange(nm)
+    if ndiag is None or ndiag < 0:
+        return np.ones((nm, nm), dtype=bool)
+    return np.abs(i[:, None] - i[None, :]) <= ndiag
+
+
+def _pol_terms(grk, glk, ggk, grd, gld, ggd):
+    """Unscaled (P^R, P^<, P^>) of one k-pair: G at k (grk, ...) and at kd (grd, ...),
+    each (nE, nx, nm, nm)."""
+    s = lambda A: np.moveaxis(A, 0, -1)
+    t = lambda A: np.swapaxes(s(A), 1, 2)
+    PL = corr(s(glk), t(ggd))
+    PG = corr(s(ggk), t(gld))
+    PR = corr(s(glk), np.conj(s(grd))) + corr(s(grk), t(gld))
+    back = lambda A: np.moveaxis(A, -1, 0)
+    return back(PR), back(PL), back(PG)
+
+
+def _sigma_terms(grd, gld, ggd, wr, wl, wg):
+    """Unscaled (S^R, S^<, S^>) of one pair: G at kd, W at q, each (nE, nx, nm, nm)."""
+    s = lambda A: np.moveaxis(A, 0, -1)
+    SL = conv(s(gld), s(wl))
+    SG = conv(s(ggd), s(wg))
+    SR = conv(s(gld), s(wr)) + conv(s(grd), s(wl)) + conv(s(grd), s(wr))
+    back = lambda A: np.moveaxis(A, -1, 0)
+    return back(SR), back(SL), back(SG)
+
+
+def polarization_k(GR, GL, GG, dE, nky, nkz, spindeg=2.0, ndiag=None):
+    """P^{R,<,>} (nk, nE, nx, nm, nm) of the k-pair sums from Re-zeroed G of the same
+    shape, banded by ndiag."""
+    nk = nky * nkz
+    P = [np.zeros_like(GR) for _ in range(3)]
+    for iq in range(nk):
+        for ik in range(nk):
+            kd = kd_index(ik, iq, nky, nkz)
+            for acc, v in zip(P, _pol_terms(GR[ik], GL[ik], GG[ik], GR[kd], GL[kd], GG[kd])):
+                acc[iq] += v
+    m = band_mask(GR.shape[-1], ndiag)
+    fac = -1j * dE / (2 * np.pi) * spindeg / nk
+    return tuple(A * fac * m for A in P)
+
+
+def screened_k(V, PR, PL, PG):
+    """W per momentum transfer q with its own Coulomb block V[q] (nk, nm, nm)."""
+    out = [screened(V[q], PR[q], PL[q], PG[q]) for q in range(PR.shape[0])]
+    return tuple(np.stack([o[c] for o in out]) for c in range(3))
+
+
+def self_energy_k(GR, GL, GG, WR, WL, WG, dE, nky, nkz, ndiag=None):
+    """Sigma^{R,<,>} (nk, nE, nx, nm, nm) of the k-pair sums, recombined
+    (Re S^R + i Im(S^> - S^<)/2), banded by ndiag and symmetrised."""
+    nk = nky * nkz
+    S = [np.zeros_like(GR) for _ in range(3)]
+    for ik in range(nk):
+        for iq in range(nk):
+            kd = kd_index(ik, iq, nky, nkz)
+            for acc, v in zip(S, _sigma_terms(GR[kd], GL[kd], GG[kd], WR[iq], WL[iq], WG[iq])):
+                acc[ik] += v
+    m = band_mask(GR.shape[-1], ndiag)
+    fac = 1j * dE / (2 * np.pi) / nk
+    SR, SL, SG = (A * fac * m for A in S)
+    SR = SR.real + 1j * (SG - SL).imag / 2
+    sym = lambda A: (A + np.swapaxes(A, -1, -2)) / 2
+    return sym(SR), sym(SL), sym(SG)
+
+
+def gw_map_k(E, H00k, H10k, V, nx, SR, SL, *, nky, nkz, mu, temp, spindeg=2.0,
+             eta_lead=1e-3, ndiag=None, sancho_reset=False):
+    """One evaluation of the SCBA map at nk = nky * nkz k-points.  H00k (nk, [nx,] nm, nm),
+    H10k (nk, nm, nm), V (nk, nm, nm); SR, SL (nk, nE, nx, nm, nm).  Returns the new
+    (SR, SL, SG) with the edge blocks copied."""
+    nk = nky * nkz
+    dE = E[1] - E[0]
+    G = [zero_real(*green(E, H00k[k], H10k[k], nx, SR[k], SL[k], mu=mu, temp=temp,
+                          eta_lead=eta_lead, sancho_reset=sancho_reset)) for k in range(nk)]
+    GR, GL, GG = (np.stack([g[c] for g in G]) for c in range(3))
+    P = polarization_k(GR, GL, GG, dE, nky, nkz, spindeg, ndiag)
+    W = screened_k(V, *P)
+    N = self_energy_k(GR, GL, GG, *W, dE, nky, nkz, ndiag)
+    # copy_edges works on axis 1 = slabs: apply per k
+    return tuple(np.stack([copy_edges(A[k]) for k in range(nk)]) for A in N)
+
+
+def scba_k(E, H00k, H10k, V, nx, *, nky, nkz, mu, temp, alpha=0.3, tol=1e-8, max_iter=60,
+           spindeg=2.0, eta_lead=1e-3, ndiag=None):
+    """Plain linear-mixing SCBA over k-points; returns (SR, SL, SG, residuals)."""
+    nk, nm = nky * nkz, H00k.shape[-1]
+    z = np.zeros((nk, len(E), nx, nm, nm), dtype=np.complex128)
+    SR, SL, SG = z.copy(), z.copy(), z.copy()
+    res = []
+    for _ in range(max_iter):
+        nR, nL, nG = gw_map_k(E, H00k, H10k, V, nx, SR, SL, nky=nky, nkz=nkz, mu=mu,
+                              temp=temp, spindeg=spindeg, eta_lead=eta_lead, ndiag=ndiag)
+        r = np.sqrt(np.sum(np.abs(nL - SL) ** 2) + np.sum(np.abs(nG - SG) ** 2)) / \
+            max(np.sqrt(np.sum(np.abs(nL) ** 2) + np.sum(np.abs(nG) ** 2)), 1e-300)
+        res.append(r)
         SR = SR + alpha * (nR - SR)
         SL = SL + alpha * (nL - SL)
         SG = SG + alpha * (nG - SG)

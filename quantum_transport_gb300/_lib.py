@@ -32,7 +32,7 @@ EXPORTS = [
     "qt_mix_diag", "qt_mix_features", "qt_mix_apply", "qt_mix_gram", "qt_mix_combine",
     "qt_rgf_solve_vb", "qt_ctx_set_stream", "qt_w90_blocks", "qt_coo_blocks",
     "qt_ephoton_sigma", "qt_ctx_inverse_fallbacks", "qt_gw_polarization", "qt_gw_screened",
-    "qt_gw_selfenergy", "qt_gw_sigma_post", "qt_ctx_set_wave_points",
+    "qt_gw_selfenergy", "qt_gw_sigma_post", "qt_ctx_set_wave_points", "qt_ctx_set_gw_grid",
 ]
 
 
@@ -84,6 +84,7 @@ def load(path=LIB_PATH):
     lib.qt_ctx_sync.argtypes = [vp]
     lib.qt_ctx_set_scratch_limit.argtypes = [vp, i64]
     lib.qt_ctx_set_wave_points.argtypes = [vp, i64]
+    lib.qt_ctx_set_gw_grid.argtypes = [vp, ci, ci, ci]
     lib.qt_ctx_set_stream.argtypes = [vp, vp, ci]
     lib.qt_ctx_inverse_fallbacks.argtypes = [vp, C.POINTER(i64), ci]
     lib.qt_w90_blocks.argtypes = [vp, ci, ci, vp, vp, vp, ci, vp, vp, vp, C.c_uint]

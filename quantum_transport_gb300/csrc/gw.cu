@@ -1,11 +1,14 @@
 // GW/SCBA self-energy loop on the GPU (rows of gw_ephoton_3d_ijs,
-// src/gw_mod.f90:444-749, restated for one k-point).
+// src/gw_mod.f90:444-749).
 //
 // Data layout: every energy-resolved quantity (G^{R,<,>}, P, W, Sigma) is an
-// array [nE][nx][nm*nm] of complex128 column-major slab-diagonal blocks -- the
-// block layout qt_rgf_solve reads (sigmas) and writes (full G blocks).  An
-// energy SERIES is one matrix element (i, j) of one slab followed through the
-// energy grid: element stride nx*nm*nm.
+// array [nk][nE][nx][nm*nm] of complex128 column-major slab-diagonal blocks, k
+// slowest as in the reference's (nm, nm, nx, nE, nk) arrays; per k-point it is the
+// block layout qt_rgf_solve reads (sigmas) and writes (full G blocks).  An energy
+// SERIES is one matrix element (i, j) of one slab at one k followed through the
+// energy grid: element stride nx*nm*nm.  With several k-points the polarisation
+// and self-energy sum over k-pairs (src/gw_mod.f90:476-512, 653-690), and the
+// ndiag band skips the elements |i - j| > ndiag (:471-475).
 //
 //  * zcorrconv: batched energy correlation / convolution through zero-padded
 //    radix-2 FFTs in shared memory (one CTA per series, L = 2^ceil(log2 2n)),
@@ -85,62 +88,102 @@ __device__ __forceinline__ void load_pair(const CorrConvArgs& a, const double2* 
   }
 }
 
+// 0-based k-pair partner of ik and iq: per direction kd = k - q + nk_dir/2 (1-based
+// indices, integer division) wrapped once into range (src/gw_mod.f90:478-487, 658-667)
+__device__ __forceinline__ int kpair(int ik, int iq, int nky, int nkz) {
+  const int iky = ik / nkz, ikz = ik - iky * nkz, iqy = iq / nkz, iqz = iq - iqy * nkz;
+  int kzd = (ikz - iqz + nkz / 2 - 1) % nkz;
+  int kyd = (iky - iqy + nky / 2 - 1) % nky;
+  if (kzd < 0) kzd += nkz;
+  if (kyd < 0) kyd += nky;
+  return kzd + kyd * nkz;
+}
+
+// One output series per CTA iteration: for each k-pair (one with kmode 0) and term, the
+// two series are loaded bit-reversed into b1, b2, transformed, and their product summed
+// into acc (b1 itself when there is one product only); then one inverse transform.
 __global__ void __launch_bounds__(FFT_NT) zcorrconv_kernel(CorrConvArgs a, const double2* tw) {
   extern __shared__ double2 sm[];
-  const int n = a.n, L = a.L, logL = a.logL;
+  const int n = a.n, L = a.L, logL = a.logL, nk = a.nk;
   const bool two = a.X2 != nullptr;
-  double2* x = sm;
-  double2* y = sm + L;
-  double2* z = two ? sm + 2 * L : y;  // third buffer for the second term
-  const long long nm2 = (long long)a.nm * a.nm;
+  const int tn = a.kmode ? nk : 1;
+  double2* b1 = sm;
+  double2* b2 = sm + L;
+  double2* acc = (two || tn > 1) ? sm + 2 * L : b1;
+  double2* inv_buf = acc == b1 ? b2 : b1;
+  const long long nm2 = (long long)a.nm * a.nm, nel = a.nel ? a.nel : nm2;
   const double2* X = reinterpret_cast<const double2*>(a.X);
   const double2* Y = reinterpret_cast<const double2*>(a.Y);
   const double2* X2 = reinterpret_cast<const double2*>(a.X2);
   const double2* Y2 = reinterpret_cast<const double2*>(a.Y2);
   const double2* Y2b = reinterpret_cast<const double2*>(a.Y2b);
   double2* Z = reinterpret_cast<double2*>(a.Z);
-  for (long long s = blockIdx.x; s < a.nseries; s += gridDim.x) {
-    const long long ix = s / nm2, ij = s % nm2;
+  const long long total = (long long)nk * a.nseries;
+  for (long long s = blockIdx.x; s < total; s += gridDim.x) {
+    const int o = (int)(s / a.nseries);
+    const long long r = s - (long long)o * a.nseries;
+    const long long ix = r / nel, el = r - ix * nel, ij = a.ij0 + el;
     const int i = (int)(ij % a.nm), j = (int)(ij / a.nm);
-    const long long sx = ix * nm2 + ij;
-    const long long st = ix * nm2 + i * (long long)a.nm + j;  // the transposed element
-    load_pair(a, X, Y, nullptr, sx, a.transY ? st : sx, a.conjY, x, y);
-    __syncthreads();
-    fft_smem(x, L, logL, tw, false);
-    fft_smem(y, L, logL, tw, false);
-    for (int t = threadIdx.x; t < L; t += blockDim.x) x[t] = dmul(x[t], y[t]);
-    __syncthreads();
-    if (two) {
-      // second term: x += FFT(X2) FFT(Y2 + Y2b) (linearity: one inverse transform)
-      load_pair(a, X2, Y2, Y2b, sx, a.transY2 ? st : sx, a.conjY2, y, z);
-      __syncthreads();
-      fft_smem(y, L, logL, tw, false);
-      fft_smem(z, L, logL, tw, false);
-      for (int t = threadIdx.x; t < L; t += blockDim.x) {
-        const double2 p = dmul(y[t], z[t]);
-        x[t] = make_double2(x[t].x + p.x, x[t].y + p.y);
-      }
-      __syncthreads();
+    const long long rt = ix * nel + i * (long long)a.nm + j;  // the transposed element
+    double2* Zo = Z + o * a.kstride;
+    if (a.ndiag >= 0 && abs(i - j) > a.ndiag) {  // outside the band: the series is zero
+      if (!a.accumulate)
+        for (int m = threadIdx.x; m < n; m += blockDim.x)
+          Zo[(long long)m * a.estride + r] = make_double2(0.0, 0.0);
+      continue;  // uniform over the CTA
     }
-    // bit-reversed into z for the inverse transform
-    for (int t = threadIdx.x; t < L; t += blockDim.x)
-      z[(int)(__brev((unsigned)t) >> (32 - logL))] = x[t];
+    for (int t = 0; t < tn; ++t) {
+      int xs = o, ys = o;
+      if (a.kmode == 1) { xs = t; ys = kpair(t, o, a.nky, a.nkz); }
+      else if (a.kmode == 2) { xs = kpair(o, t, a.nky, a.nkz); ys = t; }
+      for (int term = 0; term < (two ? 2 : 1); ++term) {
+        const long long xo = xs * a.kstride, yo = ys * a.kstride;
+        if (term == 0)
+          load_pair(a, X + xo, Y + yo, nullptr, r, a.transY ? rt : r, a.conjY, b1, b2);
+        else
+          load_pair(a, X2 + xo, Y2 + yo, Y2b ? Y2b + yo : nullptr, r, a.transY2 ? rt : r,
+                    a.conjY2, b1, b2);
+        __syncthreads();
+        fft_smem(b1, L, logL, tw, false);
+        fft_smem(b2, L, logL, tw, false);
+        const bool first = t == 0 && term == 0;
+        for (int q = threadIdx.x; q < L; q += blockDim.x) {
+          const double2 p = dmul(b1[q], b2[q]);
+          acc[q] = first ? p : make_double2(acc[q].x + p.x, acc[q].y + p.y);
+        }
+        __syncthreads();
+      }
+    }
+    // bit-reversed into the free buffer for the inverse transform
+    for (int q = threadIdx.x; q < L; q += blockDim.x)
+      inv_buf[(int)(__brev((unsigned)q) >> (32 - logL))] = acc[q];
     __syncthreads();
-    fft_smem(z, L, logL, tw, true);
+    fft_smem(inv_buf, L, logL, tw, true);
     const double inv = 1.0 / L;
     const double2 sc = make_double2(a.scale_re * inv, a.scale_im * inv);
     for (int m = threadIdx.x; m < n; m += blockDim.x) {
-      const int t = a.corr ? (m - n / 2 + n - 1) : (m + n / 2);
-      const double2 v = dmul(z[t], sc);
-      double2* zp = &Z[(long long)m * a.estride + sx];
+      const int q = a.corr ? (m - n / 2 + n - 1) : (m + n / 2);
+      const double2 v = dmul(inv_buf[q], sc);
+      double2* zp = &Zo[(long long)m * a.estride + r];
       if (a.accumulate) {
-        const double2 o = *zp;
-        *zp = make_double2(o.x + v.x, o.y + v.y);
+        const double2 w = *zp;
+        *zp = make_double2(w.x + v.x, w.y + v.y);
       } else {
         *zp = v;
       }
     }
     __syncthreads();
+  }
+}
+
+// zero |i - j| > ndiag of column-major nm x nm blocks (src/gw_mod.f90:527-555, 705-730)
+__global__ void band_zero_kernel(int nm, long long count, int ndiag, double2* A) {
+  const long long nm2 = (long long)nm * nm;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < count;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long e = t % nm2;
+    const int i = (int)(e % nm), j = (int)(e / nm);
+    if (abs(i - j) > ndiag) A[t] = make_double2(0.0, 0.0);
   }
 }
 
@@ -248,11 +291,17 @@ cudaError_t zcorrconv(CorrConvArgs a, const double2* tw, cudaStream_t s) {
   if (L > LMAX) return cudaErrorInvalidValue;
   a.L = L;
   a.logL = logL;
-  const size_t smem = (size_t)(a.X2 ? 3 : 2) * L * sizeof(double2);
+  if (a.nk < 1 || a.nky * a.nkz != a.nk) return cudaErrorInvalidValue;
+  if (a.nk > 1 && a.kmode != 0 &&
+      (a.Z == a.X || a.Z == a.Y || (a.X2 && (a.Z == a.X2 || a.Z == a.Y2 || a.Z == a.Y2b))))
+    return cudaErrorInvalidValue;  // a k-sum reads every k of its inputs
+  const bool three = a.X2 != nullptr || (a.kmode != 0 && a.nk > 1);
+  const size_t smem = (size_t)(three ? 3 : 2) * L * sizeof(double2);
   cudaError_t e = cudaFuncSetAttribute(zcorrconv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return e;
-  const long long g = a.nseries < 65535LL * 16 ? a.nseries : 65535LL * 16;
+  const long long total = (long long)a.nk * a.nseries;
+  const long long g = total < 65535LL * 16 ? total : 65535LL * 16;
   zcorrconv_kernel<<<(unsigned)g, FFT_NT, smem, s>>>(a, tw);
   count_launch();
   return cudaGetLastError();
@@ -262,6 +311,14 @@ cudaError_t gw_sigma_post(int nm, long long nblocks, double2* SR, double2* SL, d
                           cudaStream_t s) {
   const long long g = nblocks < 65535LL * 8 ? nblocks : 65535LL * 8;
   sigma_post_kernel<<<(unsigned)g, 256, 0, s>>>(nm, nblocks, SR, SL, SG);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t gw_band_zero(int nm, long long nblocks, int ndiag, double2* A, cudaStream_t s) {
+  if (ndiag < 0 || nblocks <= 0) return cudaSuccess;
+  const long long count = nblocks * nm * (long long)nm;
+  band_zero_kernel<<<g1(count), 256, 0, s>>>(nm, count, ndiag, A);
   count_launch();
   return cudaGetLastError();
 }

@@ -119,7 +119,7 @@ cudaError_t zcheck_finite(int n, long long batch, BatchRef X, int* status, cudaS
 struct CorrConvArgs {
   int n;              // energies per series
   int nm;             // block size
-  long long nseries;  // nx * nm * nm
+  long long nseries;  // series per k-point (nx * nm * nm)
   long long estride;  // element stride between consecutive energies (nx * nm * nm)
   const void* X;
   const void* Y;
@@ -132,11 +132,25 @@ struct CorrConvArgs {
   // optional second term, summed before the inverse transform:
   //   Z = scale (op(X, Y) + op(X2, Y2 + Y2b))   (X2 null: one term; Y2b may be null)
   // with its own transposition / conjugation of Y2 (imagX / imagY apply to both terms).
-  // Z may alias X or X2: a series is read completely before it is written.
+  // With one k-point (or kmode 0), Z may alias X or X2: a series is read completely
+  // before it is written.
   const void* X2 = nullptr;
   const void* Y2 = nullptr;
   const void* Y2b = nullptr;
   int transY2 = 0, conjY2 = 0;
+  // k-points (src/gw_mod.f90:476-512, 653-690): the arrays hold nk = nky * nkz blocks of
+  // nseries series, kstride elements apart, and the output covers all nk * nseries.
+  //   kmode 0: output k from X, Y at k;
+  //   kmode 1: output q = sum over k of op(X_k, Y_kd(k,q))   (polarisation);
+  //   kmode 2: output k = sum over q of op(X_kd(k,q), Y_q)   (self-energy).
+  // With nk > 1 and kmode != 0, Z must not alias any input.
+  int nk = 1, nky = 1, nkz = 1, kmode = 0;
+  long long kstride = 0;
+  // band (:471-475): series whose element (i, j) has |i - j| > ndiag are written as zero
+  // (ndiag < 0: none).  A series' element is ij0 + (series mod nel) in column-major order
+  // (nel = 0: nm * nm, the full blocks of qt_gw_step).
+  int ndiag = -1;
+  long long nel = 0, ij0 = 0;
   int L, logL;        // set by the launcher
 };
 cudaError_t gw_twiddles(double2* tw, cudaStream_t s);  // 2048 entries exp(-2 pi i k / 4096)
@@ -146,6 +160,8 @@ cudaError_t gw_sigma_post(int nm, long long nblocks, double2* SR, double2* SL, d
 cudaError_t gw_residual(long long count, const double2* nl, const double2* ol, const double2* ng,
                         const double2* og, double* sums, cudaStream_t s);
 cudaError_t gw_mix(long long count, double alpha, double2* S, const double2* N, cudaStream_t s);
+// zero the elements |i - j| > ndiag of nblocks column-major nm x nm blocks (ndiag >= 0)
+cudaError_t gw_band_zero(int nm, long long nblocks, int ndiag, double2* A, cudaStream_t s);
 // e-photon self-energy pieces (src/gw_mod.f90:1075-1122): A[e] = scale (G[e-nop] + G[e+nop])
 // per block of per = nx*nm*nm elements (halo != 0: G carries nop extra energies on each
 // side), and Sigma^R = i Im(Sigma^> - Sigma^<)/2

@@ -91,6 +91,9 @@ struct qt_ctx {
   void* conv = nullptr;  // complex64 copies of H / sigma for the split-precision sweep
   size_t conv_bytes = 0;
   int* fallbacks = nullptr;  // device counter: inverses redone in FP64 by the guard
+  // GW k-point grid of the stage entry points (nky x nkz, 1 x 1 = one k-point) and the
+  // band half-width of P and Sigma (< 0: full blocks), set by qt_ctx_set_gw_grid
+  int gw_nky = 1, gw_nkz = 1, gw_ndiag = -1;
 };
 
 int qt::ctx_device(const qt_ctx* c) { return c->device; }
@@ -1301,6 +1304,14 @@ extern "C" qt_status qt_ctx_set_wave_points(qt_ctx* c, int64_t points) {
   return QT_OK;
 }
 
+extern "C" qt_status qt_ctx_set_gw_grid(qt_ctx* c, int nky, int nkz, int ndiag) {
+  if (!c || nky < 1 || nkz < 1) QT_FAIL(QT_ERR_ARG, "need nky >= 1 and nkz >= 1");
+  c->gw_nky = nky;
+  c->gw_nkz = nkz;
+  c->gw_ndiag = ndiag < 0 ? -1 : ndiag;
+  return QT_OK;
+}
+
 extern "C" qt_status qt_ctx_profile(qt_ctx* c, int enable) {
   if (!c) QT_FAIL(QT_ERR_ARG, "null ctx");
   c->prof.on = enable != 0;
@@ -1932,19 +1943,27 @@ extern "C" qt_status qt_zinv_batch(qt_ctx* ctx, int n, int batch, const double* 
 }
 
 // ================================================================ GW / SCBA
-// One evaluation of the SCBA map Sigma -> Sigma_new for one k-point
-// (gw_ephoton_3d_ijs, src/gw_mod.f90:368-749): G by the batched RGF with the
-// scattering self-energies (green_RGF_RS, :1131-1345), P by energy
-// correlations of the Re-zeroed G (:444-519), W per slab-diagonal block
+// One evaluation of the SCBA map Sigma -> Sigma_new (gw_ephoton_3d_ijs,
+// src/gw_mod.f90:368-749): G by the batched RGF with the scattering self-energies at
+// every k-point (green_RGF_RS, :1131-1345), P by energy correlations of the Re-zeroed G
+// summed over k-pairs (:444-519), W per momentum transfer and slab-diagonal block
 // (green_rgf_calc_w is absent from the reference; restated as
-// W^R = (I - V P^R)^-1 V, W^{<,>} = W^R P^{<,>} W^R^+), Sigma by energy
-// convolutions (:646-698), recombination + symmetrisation (:698, 731-743) and
+// W^R = (I - V_q P^R)^-1 V_q, W^{<,>} = W^R P^{<,>} W^R^+), Sigma by energy
+// convolutions summed over k-pairs (:646-698), the ndiag band of P and Sigma
+// (:471-475, 527-555, 705-730), recombination + symmetrisation (:698, 731-743) and
 // the edge-block copy (:950-959).
 namespace {
 
-// The map holds six [nE][nx][nm^2] arrays: G^{R,<,>}, then P^{R,<,>}, which become
-// W^{R,<,>} in place; the new self-energies are written over G (a series is read
-// completely before it is written), so NR/NL/NG alias GR/GL/GG.
+// k-point grid and band of one GW problem
+struct GwGrid {
+  int nk = 1, nky = 1, nkz = 1, ndiag = -1;
+  long long hk = 0, h1k = 0;  // H / H1i strides between k-points (complex elements)
+};
+
+// The map holds six [nk][nE][nx][nm^2] arrays: G^{R,<,>}, then P^{R,<,>}, which become
+// W^{R,<,>} in place.  With one k-point the new self-energies are written over G (a
+// series is read completely before it is written), so NR/NL/NG alias GR/GL/GG; the
+// k-pair sums read every k of G, so with several k-points they have arrays of their own.
 struct GwBuffers {
   cd *GR, *GL, *GG, *PR, *PL, *PG, *NR, *NL, *NG;
   double2* tw;
@@ -1964,7 +1983,7 @@ struct GwCurrents {
 // before that chunk of W is written.
 qt_status gw_screened_blocks(qt_ctx* ctx, int nm, long long nblk, qt_precision prec,
                              int slices, const cd* V, const cd* PR, const cd* PL, const cd* PG,
-                             cd* WR, cd* WL, cd* WG) {
+                             cd* WR, cd* WL, cd* WG, int ndiag = -1) {
   cudaStream_t s = ctx->stream;
   const long long nm2 = (long long)nm * nm;
   Ops<double2> op{s, nm, prec};
@@ -1992,29 +2011,49 @@ qt_status gw_screened_blocks(qt_ctx* ctx, int nm, long long nblk, qt_precision p
     QT_FAIL(QT_ERR_NOMEM, "arena exhausted (W)");
   const BatchRef Vr = ref(V, 0, nm), B = ref(nullptr, nm2, nm);
   auto blk = [&](const cd* p) { BatchRef r = B; r.p = const_cast<cd*>(p); return r; };
+  // the ndiag band of P (src/gw_mod.f90:527-555): a banded copy of each P chunk (in T2
+  // for P^R, in the W chunk for P^< and P^>, which the products below then overwrite)
+  auto banded = [&](const cd* P, cd* dst, long long cb) -> const cd* {
+    if (ndiag < 0) return P;
+    qt::zcopy<double2>(nm, cb, blk(P), blk(dst), s);
+    cudaError_t e = qt::gw_band_zero(nm, cb, ndiag, reinterpret_cast<double2*>(dst), s);
+    return e == cudaSuccess ? dst : nullptr;
+  };
   for (long long c0 = 0; c0 < nblk; c0 += chunk) {
     const long long cb = std::min(chunk, nblk - c0), o = c0 * nm2;
     // T1 = I - V P^R ; T2 = T1^-1 ; T1 = T2 V = W^R
-    QT_TRY(op.gemm(Vr, qt::OP_N, blk(PR + o), qt::OP_N, blk(T1), cb, {-1, 0}, nullref(),
+    const cd* pr = banded(PR + o, T2, cb);
+    if (!pr) QT_FAIL(QT_ERR_CUDA, "band launch failed");
+    QT_TRY(op.gemm(Vr, qt::OP_N, blk(pr), qt::OP_N, blk(T1), cb, {-1, 0}, nullref(),
                    {0, 0}, ref(one, 0, 1)));
     QT_TRY(op.inv(blk(T1), blk(T2), cb, nullptr));
     QT_TRY(op.gemm(blk(T2), qt::OP_N, Vr, qt::OP_N, blk(T1), cb));
     // W^< = W^R P^< W^R^+, W^> = W^R P^> W^R^+
-    QT_TRY(op.gemm(blk(T1), qt::OP_N, blk(PL + o), qt::OP_N, blk(T2), cb));
+    const cd* pl = banded(PL + o, WL + o, cb);
+    if (!pl) QT_FAIL(QT_ERR_CUDA, "band launch failed");
+    QT_TRY(op.gemm(blk(T1), qt::OP_N, blk(pl), qt::OP_N, blk(T2), cb));
     QT_TRY(op.gemm(blk(T2), qt::OP_N, blk(T1), qt::OP_C, blk(WL + o), cb));
-    QT_TRY(op.gemm(blk(T1), qt::OP_N, blk(PG + o), qt::OP_N, blk(T2), cb));
+    const cd* pg = banded(PG + o, WG + o, cb);
+    if (!pg) QT_FAIL(QT_ERR_CUDA, "band launch failed");
+    QT_TRY(op.gemm(blk(T1), qt::OP_N, blk(pg), qt::OP_N, blk(T2), cb));
     QT_TRY(op.gemm(blk(T2), qt::OP_N, blk(T1), qt::OP_C, blk(WG + o), cb));
     qt::zcopy<double2>(nm, cb, blk(T1), blk(WR + o), s);
   }
   return QT_OK;
 }
 
-// Sigma^R <- Re Sigma^R + i Im(Sigma^> - Sigma^<)/2, (S + S^T)/2 (src/gw_mod.f90:698,
-// 731-743) and the edge blocks 1,2 <- 3 and nx-1,nx <- nx-2 (:950-959) for nE energies of
-// nx slab blocks
-qt_status gw_post(qt_ctx* ctx, int nm, int nx, long long nE, cd* NR, cd* NL, cd* NG) {
+// The ndiag band (src/gw_mod.f90:705-730), Sigma^R <- Re Sigma^R + i Im(Sigma^> -
+// Sigma^<)/2, (S + S^T)/2 (:698, 731-743) and the edge blocks 1,2 <- 3 and nx-1,nx <- nx-2
+// (:950-959) for nE energies (all k-points) of nx slab blocks
+qt_status gw_post(qt_ctx* ctx, int nm, int nx, long long nE, cd* NR, cd* NL, cd* NG,
+                  int ndiag = -1) {
   cudaStream_t s = ctx->stream;
   const long long nm2 = (long long)nm * nm;
+  if (ndiag >= 0)
+    for (cd* S : {NR, NL, NG}) {
+      cudaError_t e = qt::gw_band_zero(nm, nE * nx, ndiag, reinterpret_cast<double2*>(S), s);
+      if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+    }
   cudaError_t e = qt::gw_sigma_post(nm, nE * nx, reinterpret_cast<double2*>(NR),
                                     reinterpret_cast<double2*>(NL),
                                     reinterpret_cast<double2*>(NG), s);
@@ -2031,22 +2070,32 @@ qt_status gw_post(qt_ctx* ctx, int nm, int nx, long long nE, cd* NR, cd* NL, cd*
   return QT_OK;
 }
 
-qt_status gw_map(qt_ctx* ctx, Problem pb, const cd* V, double spindeg, const cd* SR,
-                 const cd* SL, GwBuffers& w, long long hii_n, long long h1i_n,
+qt_status gw_map(qt_ctx* ctx, Problem pb, const GwGrid& g, const cd* V, double spindeg,
+                 const cd* SR, const cd* SL, GwBuffers& w, long long hii_n, long long h1i_n,
                  const GwCurrents& cur = GwCurrents{}) {
   cudaStream_t s = ctx->stream;
-  const int nm = pb.nm, nx = pb.nx;
-  const long long nE = pb.npts;  // nk == 1
-  const long long nm2 = (long long)nm * nm, nblk = nE * nx, cnt = nblk * nm2;
-  // ---- G with the current self-energies
-  pb.sigr = SR;
-  pb.sigl = SL;
-  pb.T = pb.dgr = pb.dgl = pb.dgg = nullptr;
-  pb.tr = cur.tr; pb.tre = cur.tre; pb.bond = cur.bond; pb.Jd = nullptr;
-  pb.Gr = w.GR; pb.Gl = w.GL; pb.Gg = w.GG;
-  pb.flags &= ~QT_FLAG_CAROLI;
-  QT_TRY(run_problem(ctx, pb, hii_n, h1i_n));
-  // ---- polarisation: energy correlations of Re-zeroed G, x -i dE/(2 pi) spindeg
+  const int nm = pb.nm, nx = pb.nx, nk = g.nk;
+  const long long nE = pb.npts;  // energies per k-point
+  const long long nm2 = (long long)nm * nm, nblk = nE * nx, kst = nblk * nm2;
+  // ---- G with the current self-energies, one k-point at a time (its H blocks)
+  const cd* Hii = pb.Hii;
+  const cd* H1i = pb.H1i;
+  for (int k = 0; k < nk; ++k) {
+    Problem pk = pb;
+    pk.Hii = Hii + k * g.hk;
+    pk.H1i = H1i + k * g.h1k;
+    pk.sigr = SR + k * kst;
+    pk.sigl = SL + k * kst;
+    pk.T = pk.dgr = pk.dgl = pk.dgg = nullptr;
+    pk.tr = cur.tr ? cur.tr + k * nE : nullptr;
+    pk.tre = cur.tre ? cur.tre + k * nE : nullptr;
+    pk.bond = cur.bond ? cur.bond + k * nE * (nx - 1) : nullptr;
+    pk.Jd = nullptr;
+    pk.Gr = w.GR + k * kst; pk.Gl = w.GL + k * kst; pk.Gg = w.GG + k * kst;
+    pk.flags &= ~QT_FLAG_CAROLI;
+    QT_TRY(run_problem(ctx, pk, hii_n, h1i_n));
+  }
+  // ---- polarisation: energy correlations of Re-zeroed G, x -i dE/(2 pi) spindeg / nk
   double dE = 0.0;
   {
     double e2[2] = {0, 0};
@@ -2054,57 +2103,79 @@ qt_status gw_map(qt_ctx* ctx, Problem pb, const cd* V, double spindeg, const cd*
     QT_CUDA_TRY(cudaStreamSynchronize(s));
     dE = e2[1] - e2[0];
   }
-  const double pf = dE / (2.0 * M_PI) * spindeg;  // P scale = -i * pf
+  const double pf = dE / (2.0 * M_PI) * spindeg / nk;  // P scale = -i * pf
   qt::CorrConvArgs c{};
   c.n = (int)nE; c.nm = nm; c.nseries = nx * nm2; c.estride = nx * nm2;
-  auto cc = [&](const cd* X, const cd* Y, cd* Z, int corr, int transY, int conjY, int imX,
-                int imY, int acc, double sr, double si) -> qt_status {
-    qt::CorrConvArgs a = c;
-    a.X = X; a.Y = Y; a.Z = Z; a.corr = corr; a.transY = transY; a.conjY = conjY;
-    a.imagX = imX; a.imagY = imY; a.accumulate = acc; a.scale_re = sr; a.scale_im = si;
+  c.nk = nk; c.nky = g.nky; c.nkz = g.nkz; c.kstride = kst; c.ndiag = g.ndiag;
+  auto run = [&](const qt::CorrConvArgs& a) -> qt_status {
     cudaError_t e = qt::zcorrconv(a, w.tw, s);
     if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
     return QT_OK;
   };
-  QT_TRY(cc(w.GL, w.GG, w.PL, 1, 1, 0, 1, 1, 0, 0.0, -pf));        // P^< = corr(G^<_ij, G^>_ji)
-  QT_TRY(cc(w.GG, w.GL, w.PG, 1, 1, 0, 1, 1, 0, 0.0, -pf));        // P^> = corr(G^>_ij, G^<_ji)
+  auto cc = [&](const cd* X, const cd* Y, cd* Z, int corr, int transY, int conjY, int imX,
+                int imY, double sr, double si, int kmode) -> qt_status {
+    qt::CorrConvArgs a = c;
+    a.X = X; a.Y = Y; a.Z = Z; a.corr = corr; a.transY = transY; a.conjY = conjY;
+    a.imagX = imX; a.imagY = imY; a.scale_re = sr; a.scale_im = si; a.kmode = kmode;
+    return run(a);
+  };
+  QT_TRY(cc(w.GL, w.GG, w.PL, 1, 1, 0, 1, 1, 0.0, -pf, 1));  // P^< = corr(G^<_ij, G^>_ji)
+  QT_TRY(cc(w.GG, w.GL, w.PG, 1, 1, 0, 1, 1, 0.0, -pf, 1));  // P^> = corr(G^>_ij, G^<_ji)
   {
     // P^R = corr(G^<_ij, conj G^R_ij) + corr(G^R_ij, G^<_ji), one inverse transform
     qt::CorrConvArgs a = c;
     a.X = w.GL; a.Y = w.GR; a.conjY = 1; a.X2 = w.GR; a.Y2 = w.GL; a.transY2 = 1;
     a.Z = w.PR; a.corr = 1; a.imagX = 1; a.imagY = 1; a.scale_re = 0.0; a.scale_im = -pf;
-    cudaError_t e = qt::zcorrconv(a, w.tw, s);
-    if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+    a.kmode = 1;
+    QT_TRY(run(a));
   }
-  // ---- screened interaction per (w, slab) block, in place: P -> W
-  QT_TRY(gw_screened_blocks(ctx, nm, nblk, pb.prec, pb.lead_slices, V, w.PR, w.PL, w.PG, w.PR,
-                            w.PL, w.PG));
-  // ---- self-energy: energy convolutions x i dE / (2 pi), written over G: Sigma^R first
-  // (it reads G^< and G^R), then Sigma^< over G^<, Sigma^> over G^>
-  const double sf = dE / (2.0 * M_PI);
+  // ---- screened interaction per momentum transfer q and (w, slab) block, in place: P -> W
+  for (int q = 0; q < nk; ++q) {
+    const long long o = q * kst;
+    QT_TRY(gw_screened_blocks(ctx, nm, nblk, pb.prec, pb.lead_slices, V + q * nm2, w.PR + o,
+                              w.PL + o, w.PG + o, w.PR + o, w.PL + o, w.PG + o, g.ndiag));
+  }
+  // ---- self-energy: energy convolutions x i dE / (2 pi) / nk; with one k-point written
+  // over G: Sigma^R first (it reads G^< and G^R), then Sigma^< over G^<, Sigma^> over G^>
+  const double sf = dE / (2.0 * M_PI) / nk;
   {
     // Sigma^R = conv(G^<, W^R) + conv(G^R, W^<) + conv(G^R, W^R)
     //         = conv(G^<, W^R) + conv(G^R, W^< + W^R)
     qt::CorrConvArgs a = c;
     a.X = w.GL; a.Y = w.PR; a.X2 = w.GR; a.Y2 = w.PL; a.Y2b = w.PR;
-    a.Z = w.NR; a.corr = 0; a.imagX = 1; a.scale_re = 0.0; a.scale_im = sf;
-    cudaError_t e = qt::zcorrconv(a, w.tw, s);
-    if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+    a.Z = w.NR; a.corr = 0; a.imagX = 1; a.scale_re = 0.0; a.scale_im = sf; a.kmode = 2;
+    QT_TRY(run(a));
   }
-  QT_TRY(cc(w.GL, w.PL, w.NL, 0, 0, 0, 1, 0, 0, 0.0, sf));  // Sigma^< = conv(G^<, W^<)
-  QT_TRY(cc(w.GG, w.PG, w.NG, 0, 0, 0, 1, 0, 0, 0.0, sf));  // Sigma^> = conv(G^>, W^>)
-  // ---- recombination, symmetrisation, edge blocks
-  QT_TRY(gw_post(ctx, nm, nx, nE, w.NR, w.NL, w.NG));
-  (void)cnt;
+  QT_TRY(cc(w.GL, w.PL, w.NL, 0, 0, 0, 1, 0, 0.0, sf, 2));  // Sigma^< = conv(G^<, W^<)
+  QT_TRY(cc(w.GG, w.PG, w.NG, 0, 0, 0, 1, 0, 0.0, sf, 2));  // Sigma^> = conv(G^>, W^>)
+  // ---- band, recombination, symmetrisation, edge blocks
+  QT_TRY(gw_post(ctx, nm, nx, nk * nE, w.NR, w.NL, w.NG, g.ndiag));
   return QT_OK;
 }
 
 qt_status gw_setup(qt_ctx* ctx, const qt_device* dev, const double* E, int nE,
                    const qt_contacts* c, qt_precision prec, unsigned flags, Problem& pb,
-                   long long& hii_n, long long& h1i_n) {
+                   GwGrid& g, long long& hii_n, long long& h1i_n) {
   if (!ctx || !dev || !E || !c) QT_FAIL(QT_ERR_ARG, "null argument");
   if (!(flags & QT_FLAG_DEVICE_POINTERS)) QT_FAIL(QT_ERR_UNSUPPORTED, "GW entry points take device pointers");
-  if (dev->nk != 1) QT_FAIL(QT_ERR_UNSUPPORTED, "GW path: one k-point");
+  if (dev->nk < 1) QT_FAIL(QT_ERR_ARG, "need nk >= 1");
+  // the k-point grid: the context's when it covers dev->nk points, else one direction
+  g = GwGrid{};
+  g.nk = dev->nk;
+  if (ctx->gw_nky * ctx->gw_nkz == dev->nk) {
+    g.nky = ctx->gw_nky;
+    g.nkz = ctx->gw_nkz;
+  } else if (ctx->gw_nky * ctx->gw_nkz == 1) {
+    g.nky = 1;
+    g.nkz = dev->nk;
+  } else {
+    QT_FAIL(QT_ERR_ARG, "dev->nk differs from the k-point grid of qt_ctx_set_gw_grid");
+  }
+  g.ndiag = ctx->gw_ndiag;
+  g.hk = dev->hii_kstride;
+  g.h1k = dev->h1i_kstride;
+  if (dev->nk > 1 && (g.hk == 0 && g.h1k == 0))
+    QT_FAIL(QT_ERR_ARG, "several k-points need H blocks per k (hii_kstride / h1i_kstride)");
   if (dev->nm <= 0 || dev->nx < 2 || nE < 2) QT_FAIL(QT_ERR_ARG, "need nm > 0, nx >= 2, nE >= 2");
   if (2 * nE > 4096) QT_FAIL(QT_ERR_UNSUPPORTED, "GW path: nE <= 2048 (FFT length 4096)");
   if (dev->Sii) QT_FAIL(QT_ERR_UNSUPPORTED, "Sii must be NULL (identity overlap)");
@@ -2112,7 +2183,7 @@ qt_status gw_setup(qt_ctx* ctx, const qt_device* dev, const double* E, int nE,
   if (prec != QT_PREC_FP64 && dev->nm > MAX_SPLIT)
     QT_FAIL(QT_ERR_UNSUPPORTED, "split-precision path needs nm <= 384");
   cudaSetDevice(ctx->device);
-  pb = Problem{};
+  pb = Problem{};  // one k-point per RGF call: gw_map offsets H by g.hk / g.h1k
   pb.nm = dev->nm; pb.nx = dev->nx; pb.nk = 1; pb.npts = nE;
   pb.Hii = reinterpret_cast<const cd*>(dev->Hii); pb.hk = 0; pb.hl = dev->hii_lstride;
   pb.H1i = reinterpret_cast<const cd*>(dev->H1i); pb.h1k = 0; pb.h1l = dev->h1i_lstride;
@@ -2128,22 +2199,27 @@ struct GwAlloc {
   ~GwAlloc() { if (p) cudaFree(p); }
 };
 
-qt_status gw_alloc(qt_ctx* ctx, long long cnt, GwBuffers& w, GwAlloc& hold) {
+// cnt: elements of one [nk][nE][nx][nm^2] array; npts = nk * nE (per-point currents)
+qt_status gw_alloc(qt_ctx* ctx, long long cnt, long long npts, int nk, GwBuffers& w,
+                   GwAlloc& hold) {
   const size_t blk = (size_t)cnt * sizeof(cd);
-  // 6 block arrays, FFT twiddles, then 64 B of sums and 2 x 2048 doubles of currents
-  const size_t need = 6 * blk + 2048 * sizeof(double2) + 64 + 2 * 2048 * sizeof(double);
+  const int narr = nk > 1 ? 9 : 6;  // separate new self-energies for the k-pair sums
+  // block arrays, FFT twiddles, then 64 B of sums and 2 x npts doubles of currents
+  const size_t need = narr * blk + 2048 * sizeof(double2) + 64 + 2 * (size_t)npts * sizeof(double);
   if (cudaMalloc(&hold.p, need) != cudaSuccess) {
     cudaGetLastError();
     QT_FAIL(QT_ERR_NOMEM, "GW buffers");
   }
   char* b = reinterpret_cast<char*>(hold.p);
-  cd** slots[] = {&w.GR, &w.GL, &w.GG, &w.PR, &w.PL, &w.PG};
-  for (int i = 0; i < 6; ++i) *slots[i] = reinterpret_cast<cd*>(b + i * blk);
-  w.NR = w.GR;
-  w.NL = w.GL;
-  w.NG = w.GG;
-  w.tw = reinterpret_cast<double2*>(b + 6 * blk);
-  w.sums = reinterpret_cast<double*>(b + 6 * blk + 2048 * sizeof(double2));
+  cd** slots[] = {&w.GR, &w.GL, &w.GG, &w.PR, &w.PL, &w.PG, &w.NR, &w.NL, &w.NG};
+  for (int i = 0; i < narr; ++i) *slots[i] = reinterpret_cast<cd*>(b + i * blk);
+  if (narr == 6) {
+    w.NR = w.GR;
+    w.NL = w.GL;
+    w.NG = w.GG;
+  }
+  w.tw = reinterpret_cast<double2*>(b + narr * blk);
+  w.sums = reinterpret_cast<double*>(b + narr * blk + 2048 * sizeof(double2));
   cudaError_t e = qt::gw_twiddles(w.tw, ctx->stream);
   if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
   return QT_OK;
@@ -2157,15 +2233,16 @@ extern "C" qt_status qt_gw_step(qt_ctx* ctx, const qt_device* dev, const double*
                                 const double* sigma_lesser, double* new_r, double* new_lesser,
                                 double* new_greater) {
   Problem pb;
+  GwGrid g;
   long long hn, h1n;
-  QT_TRY(gw_setup(ctx, dev, E, nE, c, prec, flags, pb, hn, h1n));
+  QT_TRY(gw_setup(ctx, dev, E, nE, c, prec, flags, pb, g, hn, h1n));
   if (!V || !sigma_r || !sigma_lesser || !new_r || !new_lesser || !new_greater)
     QT_FAIL(QT_ERR_ARG, "null GW array");
-  const long long cnt = (long long)nE * dev->nx * dev->nm * dev->nm;
+  const long long cnt = (long long)g.nk * nE * dev->nx * dev->nm * dev->nm;
   GwBuffers w{};
   GwAlloc hold;
-  QT_TRY(gw_alloc(ctx, cnt, w, hold));
-  QT_TRY(gw_map(ctx, pb, reinterpret_cast<const cd*>(V), spindeg,
+  QT_TRY(gw_alloc(ctx, cnt, (long long)g.nk * nE, g.nk, w, hold));
+  QT_TRY(gw_map(ctx, pb, g, reinterpret_cast<const cd*>(V), spindeg,
                 reinterpret_cast<const cd*>(sigma_r), reinterpret_cast<const cd*>(sigma_lesser),
                 w, hn, h1n));
   cudaStream_t s = ctx->stream;
@@ -2185,14 +2262,16 @@ extern "C" qt_status qt_scba_solve(qt_ctx* ctx, const qt_device* dev, const doub
                                    double* sigma_greater, double* residuals, int* iters,
                                    double* currents) {
   Problem pb;
+  GwGrid g;
   long long hn, h1n;
-  QT_TRY(gw_setup(ctx, dev, E, nE, c, prec, flags, pb, hn, h1n));
+  QT_TRY(gw_setup(ctx, dev, E, nE, c, prec, flags, pb, g, hn, h1n));
   if (!V || !sigma_r || !sigma_lesser || !sigma_greater || max_iter <= 0)
     QT_FAIL(QT_ERR_ARG, "bad SCBA arguments");
-  const long long cnt = (long long)nE * dev->nx * dev->nm * dev->nm;
+  const long long npts = (long long)g.nk * nE;
+  const long long cnt = npts * dev->nx * dev->nm * dev->nm;
   GwBuffers w{};
   GwAlloc hold;
-  QT_TRY(gw_alloc(ctx, cnt, w, hold));
+  QT_TRY(gw_alloc(ctx, cnt, npts, g.nk, w, hold));
   cudaStream_t s = ctx->stream;
   double2* SR = reinterpret_cast<double2*>(sigma_r);
   double2* SL = reinterpret_cast<double2*>(sigma_lesser);
@@ -2206,26 +2285,26 @@ extern "C" qt_status qt_scba_solve(qt_ctx* ctx, const qt_device* dev, const doub
   double dE = 0.0;
   if (currents) {
     cur.tre = w.sums + 8;
-    cur.tr = cur.tre + 2048;
-    htr.resize(nE);
-    htre.resize(nE);
+    cur.tr = cur.tre + npts;
+    htr.resize(npts);
+    htre.resize(npts);
     double e2[2] = {0, 0};
     cudaMemcpyAsync(e2, E, sizeof(e2), cudaMemcpyDeviceToHost, s);
     QT_CUDA_TRY(cudaStreamSynchronize(s));
     dE = e2[1] - e2[0];
   }
   const double e0 = 1.6022e-19, hbar = 1.0546e-34, tpi = 3.14159265359 * 2.0;
-  const double ifac = dE * e0 / tpi / hbar * e0 * spindeg;  // nk = 1
+  const double ifac = dE * e0 / tpi / hbar * e0 * spindeg / g.nk;
   int it = 0;
   for (; it < max_iter; ++it) {
-    QT_TRY(gw_map(ctx, pb, reinterpret_cast<const cd*>(V), spindeg, reinterpret_cast<cd*>(SR),
+    QT_TRY(gw_map(ctx, pb, g, reinterpret_cast<const cd*>(V), spindeg, reinterpret_cast<cd*>(SR),
                   reinterpret_cast<cd*>(SL), w, hn, h1n, cur));
     if (currents) {
-      cudaMemcpyAsync(htre.data(), cur.tre, nE * sizeof(double), cudaMemcpyDeviceToHost, s);
-      cudaMemcpyAsync(htr.data(), cur.tr, nE * sizeof(double), cudaMemcpyDeviceToHost, s);
+      cudaMemcpyAsync(htre.data(), cur.tre, npts * sizeof(double), cudaMemcpyDeviceToHost, s);
+      cudaMemcpyAsync(htr.data(), cur.tr, npts * sizeof(double), cudaMemcpyDeviceToHost, s);
       QT_CUDA_TRY(cudaStreamSynchronize(s));
       double a = 0.0, b = 0.0;
-      for (int e = 0; e < nE; ++e) { a += htre[e]; b += htr[e]; }
+      for (long long e = 0; e < npts; ++e) { a += htre[e]; b += htr[e]; }
       currents[2 * it] = a * ifac;
       currents[2 * it + 1] = b * ifac;
     }
@@ -2344,6 +2423,10 @@ qt_status series_setup(qt_ctx* ctx, int n, int64_t nseries, unsigned flags,
   if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
   c = qt::CorrConvArgs{};
   c.n = n; c.nm = 1; c.nseries = nseries; c.estride = nseries;
+  // the context's k-point grid: arrays [nk][n][nseries], the k-pair sums of the caller's
+  // kmode; the band is applied on the blocks (qt_gw_screened, qt_gw_sigma_post)
+  c.nky = ctx->gw_nky; c.nkz = ctx->gw_nkz; c.nk = c.nky * c.nkz;
+  c.kstride = (long long)n * nseries;
   return QT_OK;
 }
 
@@ -2351,6 +2434,7 @@ qt_status series_run(qt_ctx* ctx, const qt::CorrConvArgs& c, const double2* tw, 
                      const double* Y, double* Z, int corr, int conjY, int imX, int imY,
                      int acc, double sr, double si) {
   qt::CorrConvArgs a = c;
+  a.kmode = corr ? 1 : 2;  // P sums over k at fixed q, Sigma over q at fixed k
   a.X = X; a.Y = Y; a.Z = Z; a.corr = corr; a.conjY = conjY;
   a.imagX = imX; a.imagY = imY; a.accumulate = acc; a.scale_re = sr; a.scale_im = si;
   cudaError_t e = qt::zcorrconv(a, tw, ctx->stream);
@@ -2392,13 +2476,18 @@ extern "C" qt_status qt_gw_screened(qt_ctx* ctx, int nm, int64_t nblocks, const 
     QT_FAIL(QT_ERR_UNSUPPORTED, "split-precision path needs nm <= 384");
   if (WR == PL || WR == PG || WL == PR || WL == PG || WG == PR || WG == PL)
     QT_FAIL(QT_ERR_ARG, "each W may alias only its own P (W^R -> P^R, W^< -> P^<, W^> -> P^>)");
+  const int nk = ctx->gw_nky * ctx->gw_nkz;
+  if (nblocks % nk) QT_FAIL(QT_ERR_ARG, "nblocks must cover the nk k-points equally");
   cudaSetDevice(ctx->device);
-  // FP64-grade digits on the split path, as inside qt_gw_step
-  QT_TRY(gw_screened_blocks(ctx, nm, nblocks, prec, env_int("QT_LEAD_SLICES", 7),
-                            reinterpret_cast<const cd*>(V), reinterpret_cast<const cd*>(PR),
-                            reinterpret_cast<const cd*>(PL), reinterpret_cast<const cd*>(PG),
-                            reinterpret_cast<cd*>(WR), reinterpret_cast<cd*>(WL),
-                            reinterpret_cast<cd*>(WG)));
+  // FP64-grade digits on the split path, as inside qt_gw_step; group q of the blocks takes
+  // V block q
+  const long long nb = nblocks / nk, nm2 = (long long)nm * nm;
+  auto P = [&](const double* a, int q) { return reinterpret_cast<const cd*>(a) + q * nb * nm2; };
+  auto W = [&](double* a, int q) { return reinterpret_cast<cd*>(a) + q * nb * nm2; };
+  for (int q = 0; q < nk; ++q)
+    QT_TRY(gw_screened_blocks(ctx, nm, nb, prec, env_int("QT_LEAD_SLICES", 7),
+                              reinterpret_cast<const cd*>(V) + q * nm2, P(PR, q), P(PL, q),
+                              P(PG, q), W(WR, q), W(WL, q), W(WG, q), ctx->gw_ndiag));
   QT_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   if (prec != QT_PREC_FP64 && qt::oz_timeouts_and_reset())
     QT_FAIL(QT_ERR_CUDA, "tensor-core kernel wait timed out");
@@ -2431,8 +2520,9 @@ extern "C" qt_status qt_gw_sigma_post(qt_ctx* ctx, int nm, int nx, int nE, doubl
     QT_FAIL(QT_ERR_ARG, "bad self-energy post-processing arguments");
   if (!(flags & QT_FLAG_DEVICE_POINTERS)) QT_FAIL(QT_ERR_UNSUPPORTED, "device pointers required");
   cudaSetDevice(ctx->device);
-  QT_TRY(gw_post(ctx, nm, nx, nE, reinterpret_cast<cd*>(SR), reinterpret_cast<cd*>(SL),
-                 reinterpret_cast<cd*>(SG)));
+  const long long nk = (long long)ctx->gw_nky * ctx->gw_nkz;
+  QT_TRY(gw_post(ctx, nm, nx, nk * nE, reinterpret_cast<cd*>(SR), reinterpret_cast<cd*>(SL),
+                 reinterpret_cast<cd*>(SG), ctx->gw_ndiag));
   if (flags & QT_FLAG_SYNC) QT_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return QT_OK;
 }

@@ -75,6 +75,7 @@ class GpuStages:
         return tuple(G)
 
     def polarization(self, gr, gl, gg, glt, ggt, scale):
+        self.sys._grid()
         n = gr.shape[0]
         ns = gr[0].numel()
         P = [self.zeros(gr.shape) for _ in range(3)]
@@ -86,6 +87,7 @@ class GpuStages:
         return tuple(P)
 
     def screened(self, PR, PL, PG):
+        self.sys._grid()
         nm = PR.shape[-1]
         nblk = PR.numel() // (nm * nm)
         W = [self.zeros(PR.shape) for _ in range(3)]
@@ -97,6 +99,7 @@ class GpuStages:
         return tuple(W)
 
     def self_energy(self, gr, gl, gg, wr, wl, wg, scale):
+        self.sys._grid()
         n = gr.shape[0]
         ns = gr[0].numel()
         S = [self.zeros(gr.shape) for _ in range(3)]
@@ -108,6 +111,7 @@ class GpuStages:
         return tuple(S)
 
     def post(self, SR, SL, SG):
+        self.sys._grid()
         ne, nx, nm = SR.shape[0], SR.shape[1], SR.shape[-1]
         if ne == 0:
             return
