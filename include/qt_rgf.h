@@ -63,6 +63,10 @@ typedef enum {
                                       (src/gw_mod.f90:1440-1445): an entry not
                                       converged after max_iter steps restarts
                                       from H_SS = H_BB = H00                   */
+#define QT_FLAG_V_PER_SLAB 32u     /* qt_gw_step, qt_scba_solve: V holds one
+                                      Coulomb block per q and slab,
+                                      [nk][nx][nm*nm], as the reference's
+                                      Vii(nm, nm, nx, nk) (src/gw_mod.f90:84) */
 
 /* Reference-quirk switches (default 0 = the behaviour that produced the
  * reference's test_cnt/ outputs).                                            */
@@ -354,7 +358,8 @@ qt_status qt_noalloc_timeouts(int* count, void* stream);
  * slab-diagonal blocks, k slowest as the reference's (nm, nm, nx, nE, nk)
  * arrays; the energy grid E must be uniform (dE = E[1]-E[0]) and nE <= 2048
  * (zero-padded FFT length 4096).  V: nk nm x nm slab-diagonal Coulomb blocks,
- * one per momentum transfer q (the reference passes Vii/V1i per q,
+ * one per momentum transfer q, or with QT_FLAG_V_PER_SLAB nk x nx blocks, one
+ * per q and slab (the reference passes Vii/V1i per slab and q,
  * src/gw_mod.f90:84,597-600; only the diagonal block enters the per-slab W
  * restatement).  dev->nk k-points need H blocks per k (hii_kstride or
  * h1i_kstride non-zero).

@@ -18,6 +18,7 @@ QT_FLAG_DEVICE_POINTERS, QT_FLAG_CAROLI, QT_FLAG_SYNC, QT_FLAG_SANCHO_RESET = 1,
 QT_FLAG_COMPLEX64 = 16
 QT_QUIRK_CPU_FERMI, QT_QUIRK_GLP_ZERO, QT_QUIRK_BACK_H1I_NEXT = 1, 2, 4
 QT_QUIRK_GW_SANCHO_RESET = 8
+QT_FLAG_V_PER_SLAB = 32
 QT_PT_SINGULAR, QT_PT_SANCHO_NOT_CONVERGED, QT_PT_NONFINITE = 1, 2, 4
 
 # every symbol include/qt_rgf.h declares

@@ -176,14 +176,16 @@ __global__ void __launch_bounds__(FFT_NT) zcorrconv_kernel(CorrConvArgs a, const
   }
 }
 
-// zero |i - j| > ndiag of column-major nm x nm blocks (src/gw_mod.f90:527-555, 705-730)
-__global__ void band_zero_kernel(int nm, long long count, int ndiag, double2* A) {
+// zero |i - j| > ndiag of column-major nm x nm blocks bstride elements apart
+// (src/gw_mod.f90:527-555, 705-730)
+__global__ void band_zero_kernel(int nm, long long count, long long bstride, int ndiag,
+                                 double2* A) {
   const long long nm2 = (long long)nm * nm;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < count;
        t += (long long)gridDim.x * blockDim.x) {
-    const long long e = t % nm2;
+    const long long b = t / nm2, e = t - b * nm2;
     const int i = (int)(e % nm), j = (int)(e / nm);
-    if (abs(i - j) > ndiag) A[t] = make_double2(0.0, 0.0);
+    if (abs(i - j) > ndiag) A[b * bstride + e] = make_double2(0.0, 0.0);
   }
 }
 
@@ -315,10 +317,11 @@ cudaError_t gw_sigma_post(int nm, long long nblocks, double2* SR, double2* SL, d
   return cudaGetLastError();
 }
 
-cudaError_t gw_band_zero(int nm, long long nblocks, int ndiag, double2* A, cudaStream_t s) {
+cudaError_t gw_band_zero(int nm, long long nblocks, int ndiag, double2* A, cudaStream_t s,
+                         long long bstride) {
   if (ndiag < 0 || nblocks <= 0) return cudaSuccess;
-  const long long count = nblocks * nm * (long long)nm;
-  band_zero_kernel<<<g1(count), 256, 0, s>>>(nm, count, ndiag, A);
+  const long long nm2 = nm * (long long)nm, count = nblocks * nm2;
+  band_zero_kernel<<<g1(count), 256, 0, s>>>(nm, count, bstride ? bstride : nm2, ndiag, A);
   count_launch();
   return cudaGetLastError();
 }

@@ -160,8 +160,10 @@ cudaError_t gw_sigma_post(int nm, long long nblocks, double2* SR, double2* SL, d
 cudaError_t gw_residual(long long count, const double2* nl, const double2* ol, const double2* ng,
                         const double2* og, double* sums, cudaStream_t s);
 cudaError_t gw_mix(long long count, double alpha, double2* S, const double2* N, cudaStream_t s);
-// zero the elements |i - j| > ndiag of nblocks column-major nm x nm blocks (ndiag >= 0)
-cudaError_t gw_band_zero(int nm, long long nblocks, int ndiag, double2* A, cudaStream_t s);
+// zero the elements |i - j| > ndiag of nblocks column-major nm x nm blocks, bstride
+// elements apart (0: nm * nm), when ndiag >= 0
+cudaError_t gw_band_zero(int nm, long long nblocks, int ndiag, double2* A, cudaStream_t s,
+                         long long bstride = 0);
 // e-photon self-energy pieces (src/gw_mod.f90:1075-1122): A[e] = scale (G[e-nop] + G[e+nop])
 // per block of per = nx*nm*nm elements (halo != 0: G carries nop extra energies on each
 // side), and Sigma^R = i Im(Sigma^> - Sigma^<)/2

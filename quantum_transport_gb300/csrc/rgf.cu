@@ -1957,6 +1957,7 @@ namespace {
 // k-point grid and band of one GW problem
 struct GwGrid {
   int nk = 1, nky = 1, nkz = 1, ndiag = -1;
+  bool v_per_slab = false;  // V holds [nk][nx] blocks (QT_FLAG_V_PER_SLAB)
   long long hk = 0, h1k = 0;  // H / H1i strides between k-points (complex elements)
 };
 
@@ -1977,13 +1978,13 @@ struct GwCurrents {
 };
 
 // W^R = (I - V P^R)^-1 V and W^{<,>} = W^R P^{<,>} W^R^+ per (w, slab) block, nblk blocks of
-// nm x nm at stride nm^2, in chunks of blocks whose scratch (two chunk-sized blocks, the
-// refinement blocks, exponent table and guard flags) comes from the context arena.  Each
-// output may alias its own P (W^R -> P^R, W^< -> P^<, W^> -> P^>): a chunk of P is read
-// before that chunk of W is written.
+// nm x nm at stride bstride (0: nm^2), in chunks of blocks whose scratch (two chunk-sized
+// blocks, the refinement blocks, exponent table and guard flags) comes from the context
+// arena.  Each output may alias its own P (W^R -> P^R, W^< -> P^<, W^> -> P^>): a chunk of
+// P is read before that chunk of W is written.
 qt_status gw_screened_blocks(qt_ctx* ctx, int nm, long long nblk, qt_precision prec,
                              int slices, const cd* V, const cd* PR, const cd* PL, const cd* PG,
-                             cd* WR, cd* WL, cd* WG, int ndiag = -1) {
+                             cd* WR, cd* WL, cd* WG, int ndiag = -1, long long bstride = 0) {
   cudaStream_t s = ctx->stream;
   const long long nm2 = (long long)nm * nm;
   Ops<double2> op{s, nm, prec};
@@ -2009,35 +2010,43 @@ qt_status gw_screened_blocks(qt_ctx* ctx, int nm, long long nblk, qt_precision p
   cd* T2 = ar.take<cd>((size_t)chunk * nm2);
   if (!op.scales || !op.rt2 || !op.guard || !T1 || !T2)
     QT_FAIL(QT_ERR_NOMEM, "arena exhausted (W)");
-  const BatchRef Vr = ref(V, 0, nm), B = ref(nullptr, nm2, nm);
-  auto blk = [&](const cd* p) { BatchRef r = B; r.p = const_cast<cd*>(p); return r; };
+  if (!bstride) bstride = nm2;
+  const BatchRef Vr = ref(V, 0, nm), B = ref(nullptr, nm2, nm), Bs = ref(nullptr, bstride, nm);
+  auto blk = [&](const cd* p) { BatchRef r = B; r.p = const_cast<cd*>(p); return r; };  // scratch
+  auto arr = [&](const cd* p) { BatchRef r = Bs; r.p = const_cast<cd*>(p); return r; };  // P, W
   // the ndiag band of P (src/gw_mod.f90:527-555): a banded copy of each P chunk (in T2
   // for P^R, in the W chunk for P^< and P^>, which the products below then overwrite)
-  auto banded = [&](const cd* P, cd* dst, long long cb) -> const cd* {
-    if (ndiag < 0) return P;
-    qt::zcopy<double2>(nm, cb, blk(P), blk(dst), s);
-    cudaError_t e = qt::gw_band_zero(nm, cb, ndiag, reinterpret_cast<double2*>(dst), s);
-    return e == cudaSuccess ? dst : nullptr;
+  auto banded = [&](BatchRef P, BatchRef dst, long long cb) -> bool {
+    qt::zcopy<double2>(nm, cb, P, dst, s);
+    return qt::gw_band_zero(nm, cb, ndiag, reinterpret_cast<double2*>(dst.p), s,
+                            dst.stride) == cudaSuccess;
   };
   for (long long c0 = 0; c0 < nblk; c0 += chunk) {
-    const long long cb = std::min(chunk, nblk - c0), o = c0 * nm2;
+    const long long cb = std::min(chunk, nblk - c0), o = c0 * bstride;
     // T1 = I - V P^R ; T2 = T1^-1 ; T1 = T2 V = W^R
-    const cd* pr = banded(PR + o, T2, cb);
-    if (!pr) QT_FAIL(QT_ERR_CUDA, "band launch failed");
-    QT_TRY(op.gemm(Vr, qt::OP_N, blk(pr), qt::OP_N, blk(T1), cb, {-1, 0}, nullref(),
-                   {0, 0}, ref(one, 0, 1)));
+    BatchRef pr = arr(PR + o), pl = arr(PL + o), pg = arr(PG + o);
+    if (ndiag >= 0) {
+      if (!banded(pr, blk(T2), cb)) QT_FAIL(QT_ERR_CUDA, "band launch failed");
+      pr = blk(T2);
+    }
+    QT_TRY(op.gemm(Vr, qt::OP_N, pr, qt::OP_N, blk(T1), cb, {-1, 0}, nullref(), {0, 0},
+                   ref(one, 0, 1)));
     QT_TRY(op.inv(blk(T1), blk(T2), cb, nullptr));
     QT_TRY(op.gemm(blk(T2), qt::OP_N, Vr, qt::OP_N, blk(T1), cb));
-    // W^< = W^R P^< W^R^+, W^> = W^R P^> W^R^+
-    const cd* pl = banded(PL + o, WL + o, cb);
-    if (!pl) QT_FAIL(QT_ERR_CUDA, "band launch failed");
-    QT_TRY(op.gemm(blk(T1), qt::OP_N, blk(pl), qt::OP_N, blk(T2), cb));
-    QT_TRY(op.gemm(blk(T2), qt::OP_N, blk(T1), qt::OP_C, blk(WL + o), cb));
-    const cd* pg = banded(PG + o, WG + o, cb);
-    if (!pg) QT_FAIL(QT_ERR_CUDA, "band launch failed");
-    QT_TRY(op.gemm(blk(T1), qt::OP_N, blk(pg), qt::OP_N, blk(T2), cb));
-    QT_TRY(op.gemm(blk(T2), qt::OP_N, blk(T1), qt::OP_C, blk(WG + o), cb));
-    qt::zcopy<double2>(nm, cb, blk(T1), blk(WR + o), s);
+    // W^< = W^R P^< W^R^+, W^> = W^R P^> W^R^+ (a banded P^< / P^> goes to its W chunk first)
+    if (ndiag >= 0) {
+      if (!banded(pl, arr(WL + o), cb)) QT_FAIL(QT_ERR_CUDA, "band launch failed");
+      pl = arr(WL + o);
+    }
+    QT_TRY(op.gemm(blk(T1), qt::OP_N, pl, qt::OP_N, blk(T2), cb));
+    QT_TRY(op.gemm(blk(T2), qt::OP_N, blk(T1), qt::OP_C, arr(WL + o), cb));
+    if (ndiag >= 0) {
+      if (!banded(pg, arr(WG + o), cb)) QT_FAIL(QT_ERR_CUDA, "band launch failed");
+      pg = arr(WG + o);
+    }
+    QT_TRY(op.gemm(blk(T1), qt::OP_N, pg, qt::OP_N, blk(T2), cb));
+    QT_TRY(op.gemm(blk(T2), qt::OP_N, blk(T1), qt::OP_C, arr(WG + o), cb));
+    qt::zcopy<double2>(nm, cb, blk(T1), arr(WR + o), s);
   }
   return QT_OK;
 }
@@ -2129,11 +2138,21 @@ qt_status gw_map(qt_ctx* ctx, Problem pb, const GwGrid& g, const cd* V, double s
     a.kmode = 1;
     QT_TRY(run(a));
   }
-  // ---- screened interaction per momentum transfer q and (w, slab) block, in place: P -> W
+  // ---- screened interaction per momentum transfer q and (w, slab) block, in place: P -> W;
+  // with a Coulomb block per slab, the blocks of slab x (every energy) take V_{q,x}
   for (int q = 0; q < nk; ++q) {
     const long long o = q * kst;
-    QT_TRY(gw_screened_blocks(ctx, nm, nblk, pb.prec, pb.lead_slices, V + q * nm2, w.PR + o,
-                              w.PL + o, w.PG + o, w.PR + o, w.PL + o, w.PG + o, g.ndiag));
+    if (!g.v_per_slab) {
+      QT_TRY(gw_screened_blocks(ctx, nm, nblk, pb.prec, pb.lead_slices, V + q * nm2, w.PR + o,
+                                w.PL + o, w.PG + o, w.PR + o, w.PL + o, w.PG + o, g.ndiag));
+      continue;
+    }
+    for (int x = 0; x < nx; ++x) {
+      const long long ox = o + x * nm2;
+      QT_TRY(gw_screened_blocks(ctx, nm, nE, pb.prec, pb.lead_slices, V + (q * nx + x) * nm2,
+                                w.PR + ox, w.PL + ox, w.PG + ox, w.PR + ox, w.PL + ox, w.PG + ox,
+                                g.ndiag, nx * nm2));
+    }
   }
   // ---- self-energy: energy convolutions x i dE / (2 pi) / nk; with one k-point written
   // over G: Sigma^R first (it reads G^< and G^R), then Sigma^< over G^<, Sigma^> over G^>
@@ -2172,6 +2191,7 @@ qt_status gw_setup(qt_ctx* ctx, const qt_device* dev, const double* E, int nE,
     QT_FAIL(QT_ERR_ARG, "dev->nk differs from the k-point grid of qt_ctx_set_gw_grid");
   }
   g.ndiag = ctx->gw_ndiag;
+  g.v_per_slab = (flags & QT_FLAG_V_PER_SLAB) != 0;
   g.hk = dev->hii_kstride;
   g.h1k = dev->h1i_kstride;
   if (dev->nk > 1 && (g.hk == 0 && g.h1k == 0))
@@ -2476,6 +2496,8 @@ extern "C" qt_status qt_gw_screened(qt_ctx* ctx, int nm, int64_t nblocks, const 
     QT_FAIL(QT_ERR_UNSUPPORTED, "split-precision path needs nm <= 384");
   if (WR == PL || WR == PG || WL == PR || WL == PG || WG == PR || WG == PL)
     QT_FAIL(QT_ERR_ARG, "each W may alias only its own P (W^R -> P^R, W^< -> P^<, W^> -> P^>)");
+  if (flags & QT_FLAG_V_PER_SLAB)
+    QT_FAIL(QT_ERR_UNSUPPORTED, "per-slab Coulomb blocks: qt_gw_step / qt_scba_solve");
   const int nk = ctx->gw_nky * ctx->gw_nkz;
   if (nblocks % nk) QT_FAIL(QT_ERR_ARG, "nblocks must cover the nk k-points equally");
   cudaSetDevice(ctx->device);

@@ -52,12 +52,14 @@ class GwSystem:
     """Device, energy grid, contacts and Coulomb blocks of one SCBA problem.
 
     One k-point (``kgrid=(1, 1)``): ``H00`` one on-site block shared by all slabs
-    (nm, nm), or one per slab (nx, nm, nm); ``H10`` (nm, nm); ``V`` (nm, nm).  A grid of
-    nk = nky * nkz k-points (``kgrid=(nky, nkz)``, k = kz + ky nkz): ``H00`` (nk, nm, nm)
-    or (nk, nx, nm, nm), ``H10`` (nm, nm) or (nk, nm, nm), ``V`` (nk, nm, nm), one block
-    per momentum transfer q (or (nm, nm) for all q); self-energies are then
-    (nk, nE, nx, nm, nm).  The leads continue the first and last slab.  ``ndiag``: keep
-    only |i - j| <= ndiag of P and Sigma (src/gw_mod.f90:471-475), None for full blocks.
+    (nm, nm), or one per slab (nx, nm, nm); ``H10`` (nm, nm); ``V`` (nm, nm), or one
+    Coulomb block per slab (nx, nm, nm).  A grid of nk = nky * nkz k-points
+    (``kgrid=(nky, nkz)``, k = kz + ky nkz): ``H00`` (nk, nm, nm) or (nk, nx, nm, nm),
+    ``H10`` (nm, nm) or (nk, nm, nm), ``V`` (nk, nm, nm) one block per momentum transfer q,
+    (nk, nx, nm, nm) one per q and slab (the reference's Vii), or (nm, nm) for all; the
+    self-energies are then (nk, nE, nx, nm, nm).  The leads continue the first and last
+    slab.  ``ndiag``: keep only |i - j| <= ndiag of P and Sigma (src/gw_mod.f90:471-475),
+    None for full blocks.
     ``sancho_reset`` selects green_RGF_RS's lead decimation as written
     (src/gw_mod.f90:1440-1445): points not converged after ``sancho_max_iter`` steps take
     the isolated-slab surface function; by default they keep their last iterate and are
@@ -78,13 +80,18 @@ class GwSystem:
                 raise ValueError("with several k-points H00 is (nk, [nx,] nm, nm)")
             if V.ndim == 2:
                 V = np.repeat(V[None], nk, axis=0)
-            if V.shape[0] != nk:
-                raise ValueError("V must be (nk, nm, nm) or (nm, nm)")
+            if V.shape[0] != nk or V.ndim not in (3, 4):
+                raise ValueError("V must be (nk, [nx,] nm, nm) or (nm, nm)")
             per_slab = H00.ndim == 4
             h10_k = H10.ndim == 3
+            v_slab = V.ndim == 4
         else:
             per_slab = H00.ndim == 3
             h10_k = False
+            v_slab = V.ndim == 3
+        if v_slab and V.shape[-3] != nx:
+            raise ValueError("per-slab V must have nx blocks")
+        self.vflag = _lib.QT_FLAG_V_PER_SLAB if v_slab else 0
         self.nm = H00.shape[-1]
         self.nx = nx
         self.nE = len(E)
@@ -128,8 +135,8 @@ class GwSystem:
         self._grid()
         check(self.ctx._lib.qt_gw_step(self.ctx.handle, C.byref(self.dev), _ptr(self.E), self.nE,
                                        C.byref(self.con), _ptr(self.V), self.spindeg, self.prec,
-                                       _lib.QT_FLAG_DEVICE_POINTERS, _ptr(SR), _ptr(SL),
-                                       _ptr(NR), _ptr(NL), _ptr(NG)))
+                                       _lib.QT_FLAG_DEVICE_POINTERS | self.vflag, _ptr(SR),
+                                       _ptr(SL), _ptr(NR), _ptr(NL), _ptr(NG)))
         return NR, NL, NG
 
     def scba(self, alpha=0.3, tol=1e-8, max_iter=60, start=None, with_currents=False):
@@ -144,8 +151,9 @@ class GwSystem:
         check(self.ctx._lib.qt_scba_solve(self.ctx.handle, C.byref(self.dev), _ptr(self.E),
                                           self.nE, C.byref(self.con), _ptr(self.V), self.spindeg,
                                           alpha, tol, max_iter, self.prec,
-                                          _lib.QT_FLAG_DEVICE_POINTERS, _ptr(SR), _ptr(SL),
-                                          _ptr(SG), res.ctypes.data_as(C.c_void_p), C.byref(it),
+                                          _lib.QT_FLAG_DEVICE_POINTERS | self.vflag, _ptr(SR),
+                                          _ptr(SL), _ptr(SG), res.ctypes.data_as(C.c_void_p),
+                                          C.byref(it),
                                           _ptr(cur)))
         if with_currents:
             return SR, SL, SG, res[:it.value], cur[:it.value]

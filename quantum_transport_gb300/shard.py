@@ -116,15 +116,21 @@ def ij_range(nij, world, rank):
 
 
 def _all_to_all(send, out_counts, in_counts, group):
+    """One all_to_all_single; over gloo, device tensors go through host memory (ranks on
+    GPUs of one host without NCCL, or several ranks on one GPU)."""
     import torch
     import torch.distributed as dist
-    if dist.get_backend(group) == "nccl" and send.device.type != "cuda":
+    backend = dist.get_backend(group)
+    if backend == "nccl" and send.device.type != "cuda":
         raise ValueError("NCCL all-to-all needs device tensors")
+    dev = send.device
+    if backend == "gloo" and dev.type == "cuda":
+        send = send.cpu()
     recv = torch.empty(sum(out_counts), dtype=send.dtype, device=send.device)
     real = torch.view_as_real if send.is_complex() else (lambda t: t)
     dist.all_to_all_single(real(recv), real(send.contiguous()), out_counts, in_counts,
                            group=group)
-    return recv
+    return recv.to(dev)
 
 
 def energies_to_ijs(x, nE, world, rank, group=None):

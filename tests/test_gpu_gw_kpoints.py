@@ -124,3 +124,23 @@ def test_stage_entries_sum_over_k_pairs(ctx):
     for got, exp in zip(S, refS):
         exp = 0.21j * exp
         np.testing.assert_allclose(got.cpu().numpy(), exp, rtol=0, atol=1e-12 * np.abs(exp).max())
+
+
+@pytest.mark.parametrize("nky,nkz", [(1, 1), (1, 2)])
+def test_gw_step_per_slab_coulomb_blocks(ctx, nky, nkz):
+    """V per momentum transfer and slab (the reference's Vii(nm, nm, nx, nk)):
+    QT_FLAG_V_PER_SLAB, W of slab x from V_{q,x}."""
+    from quantum_transport_gb300 import gw
+    nk = nky * nkz
+    dev, V, SR0, SL0 = _kproblem(nky, nkz, nE=32)
+    Vs = np.stack([[V[q] * (1.0 + 0.05 * x) for x in range(dev.nx)] for q in range(nk)])
+    H00 = dev.H00 if nk > 1 else dev.H00[0]
+    s = gw.GwSystem(ctx, H00, dev.H10, dev.E, dev.nx, Vs if nk > 1 else Vs[0], mu=MU,
+                    kgrid=(nky, nkz), ndiag=2)
+    sr, sl = (SR0, SL0) if nk > 1 else (SR0[0], SL0[0])
+    N = s.step(gw.to_dev(sr), gw.to_dev(sl))
+    H10k = np.repeat(dev.H10[None], nk, axis=0)
+    ref = ogw.gw_map_k(dev.E, dev.H00, H10k, Vs, dev.nx, SR0, SL0, nky=nky, nkz=nkz, mu=MU,
+                       temp=TEMP, ndiag=2)
+    for got, exp in zip(N, ref):
+        np.testing.assert_allclose(_host(got, nk), exp, rtol=0, atol=1e-8 * np.abs(exp).max())

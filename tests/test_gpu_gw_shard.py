@@ -106,3 +106,72 @@ def test_stage_entries_reject_bad_arguments(ctx):
         _lib.QT_ERR_ARG
     assert lib.qt_gw_sigma_post(h, 0, 1, 1, p, p, p, f) == _lib.QT_ERR_ARG
     assert math.isfinite(float(t.abs().sum()))
+
+
+def _two_rank_child(rank, world, port, q, precision):
+    """One rank of a gloo group whose ranks share cuda:0: the sharded map and three SCBA
+    iterations of the _system problem, computed by GpuStages through the C-ABI."""
+    import os
+    import torch
+    import torch.distributed as dist
+    from quantum_transport_gb300 import gw
+    from quantum_transport_gb300.gw_shard import ShardedGw
+    from quantum_transport_gb300.rgf import Context
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    torch.cuda.set_device(0)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    ctx = Context(0)
+    try:
+        dev = make_chain_device(6, 8, 64, -4.0, 4.0, seed=3)
+        V = ogw.coulomb_blocks(8)
+        g = ShardedGw.on_gpu(ctx, dev.H00[0], dev.H10, dev.E, dev.nx, V, world=world,
+                             rank=rank, mu=(0.1, -0.1), precision=precision)
+        SR0, SL0 = _physical_sigma(len(dev.E), dev.nx, 8)
+        SR, SL = gw.to_dev(SR0[g.lo:g.hi]), gw.to_dev(SL0[g.lo:g.hi])
+        N = [gw.from_dev(x) for x in g.step(SR, SL)]
+        R, L, G, res = g.scba(alpha=0.3, tol=0.0, max_iter=3)
+        out = (g.lo, g.hi, N, [gw.from_dev(x) for x in (R, L, G)], np.asarray(res))
+    finally:
+        ctx.close()
+        dist.destroy_process_group()
+    q.put((rank, out))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed-fp64"])
+def test_two_gloo_ranks_on_one_gpu_match_fused(ctx, precision):
+    """Two ranks of a gloo group on cuda:0, each with its own library context: the
+    fourteen all-to-alls of the map move the ranks' G, P, W and Sigma (through host memory
+    for gloo), and the product's stage kernels compute on each share.  The map equals
+    qt_gw_step bit for bit; three SCBA iterations equal qt_scba_solve's to round-off of the
+    mixing."""
+    import multiprocessing as mp
+    import socket
+    from quantum_transport_gb300 import gw
+    dev, V, s = _system(ctx, precision)
+    SR0, SL0 = _physical_sigma(len(dev.E), dev.nx, 8)
+    fused = [gw.from_dev(x) for x in s.step(gw.to_dev(SR0), gw.to_dev(SL0))]
+    R, L, G, res = s.scba(alpha=0.3, tol=0.0, max_iter=3)
+    mixed = [gw.from_dev(x) for x in (R, L, G)]
+    with socket.socket() as so:
+        so.bind(("127.0.0.1", 0))
+        port = so.getsockname()[1]
+    spawn = mp.get_context("spawn")
+    q = spawn.Queue()
+    world = 2
+    procs = [spawn.Process(target=_two_rank_child, args=(r, world, port, q, precision))
+             for r in range(world)]
+    for p in procs:
+        p.start()
+    out = dict(q.get(timeout=600) for _ in range(world))
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    assert [out[r][:2] for r in range(world)] == [(0, 32), (32, 64)]
+    for c in range(3):
+        got = np.concatenate([out[r][2][c] for r in range(world)])
+        assert np.abs(fused[c]).max() > 0
+        np.testing.assert_array_equal(got, fused[c])
+        got = np.concatenate([out[r][3][c] for r in range(world)])
+        np.testing.assert_allclose(got, mixed[c], rtol=0, atol=1e-12 * np.abs(mixed[c]).max())
+    for r in range(world):
+        np.testing.assert_allclose(out[r][4], res, rtol=1e-9)
