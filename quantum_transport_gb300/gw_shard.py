@@ -20,7 +20,9 @@ results.
 
 Blocks are torch complex128 tensors of shape (nE_local, nx, nm, nm), stored column-major
 per block: the last two axes are (column, row), as ``gw.to_dev`` makes them. Element
-series are (nE, nx, nij_local) tensors. The stage object does the compute: ``GpuStages``
+series are (nE, nx, nij_local) tensors.  With a grid of nk > 1 k-points every array has a
+leading k axis (k slowest, the reference's (nm, nm, nx, nE, nk) order); one all-to-all
+moves all k-points, and the stages sum over the k-pairs. The stage object does the compute: ``GpuStages``
 calls the library on this rank's GPU; any object with the same five methods can stand in
 for it.
 """
@@ -44,11 +46,15 @@ class GpuStages:
     energies."""
 
     def __init__(self, ctx, H00, H10, E_local, nx, V, *, mu=(0.0, 0.0), temp=(300.0, 300.0),
-                 eta_lead=1e-3, sancho_max_iter=100, sancho_tol=1e-100, precision="fp64"):
+                 eta_lead=1e-3, sancho_max_iter=100, sancho_tol=1e-100, precision="fp64",
+                 kgrid=(1, 1), ndiag=None):
         from .gw import GwSystem
         self.sys = GwSystem(ctx, H00, H10, E_local, nx, V, mu=mu, temp=temp,
                             eta_lead=eta_lead, sancho_max_iter=sancho_max_iter,
-                            sancho_tol=sancho_tol, precision=precision)
+                            sancho_tol=sancho_tol, precision=precision, kgrid=kgrid,
+                            ndiag=ndiag)
+        if self.sys.vflag:
+            raise ValueError("the stages take one Coulomb block per momentum transfer")
         self.ctx = ctx
         self.lib = ctx._lib
         self.flags = _lib.QT_FLAG_DEVICE_POINTERS
@@ -58,26 +64,36 @@ class GpuStages:
         return torch.zeros(shape, dtype=torch.complex128, device="cuda")
 
     def green(self, SR, SL):
-        """G^R, G^<, G^> diagonal blocks with scattering self-energies SR, SL."""
+        """G^R, G^<, G^> diagonal blocks with scattering self-energies SR, SL, one k-point
+        at a time."""
         import torch
         s = self.sys
         G = [s.zeros() for _ in range(3)]
         if s.nE == 0:  # a rank with no energies still takes part in the exchanges
             return tuple(G)
-        out = {"G_r": G[0], "G_lesser": G[1], "G_greater": G[2],
-               "status": torch.zeros(s.nE, dtype=torch.int32, device="cuda")}
-        o = _lib.QtOutputs(*[_ptr(out.get(k)) for k in OUT_KEYS])
-        SR, SL = SR.contiguous(), SL.contiguous()  # held until the call has been made
-        check(self.lib.qt_rgf_solve(self.ctx.handle, C.byref(s.dev), _ptr(s.E), s.nE,
-                                    C.byref(s.con), _ptr(SR), _ptr(SL), s.prec, self.flags,
-                                    C.byref(o)),
-              allow_points=True)
+        one = s.nk == 1
+        for k in range(s.nk):
+            out = {"G_r": G[0] if one else G[0][k], "G_lesser": G[1] if one else G[1][k],
+                   "G_greater": G[2] if one else G[2][k],
+                   "status": torch.zeros(s.nE, dtype=torch.int32, device="cuda")}
+            o = _lib.QtOutputs(*[_ptr(out.get(n)) for n in OUT_KEYS])
+            sr = (SR if one else SR[k]).contiguous()  # held until the call has been made
+            sl = (SL if one else SL[k]).contiguous()
+            check(self.lib.qt_rgf_solve(self.ctx.handle, C.byref(s.devk[k]), _ptr(s.E), s.nE,
+                                        C.byref(s.con), _ptr(sr), _ptr(sl), s.prec, self.flags,
+                                        C.byref(o)),
+                  allow_points=True)
         return tuple(G)
+
+    def _series_shape(self, g):
+        """(energies, series per k-point) of an element-series array"""
+        if self.sys.nk == 1:
+            return g.shape[0], g[0].numel()
+        return g.shape[1], g[0, 0].numel()
 
     def polarization(self, gr, gl, gg, glt, ggt, scale):
         self.sys._grid()
-        n = gr.shape[0]
-        ns = gr[0].numel()
+        n, ns = self._series_shape(gr)
         P = [self.zeros(gr.shape) for _ in range(3)]
         if ns == 0:  # no block elements on this rank
             return tuple(P)
@@ -100,8 +116,7 @@ class GpuStages:
 
     def self_energy(self, gr, gl, gg, wr, wl, wg, scale):
         self.sys._grid()
-        n = gr.shape[0]
-        ns = gr[0].numel()
+        n, ns = self._series_shape(gr)
         S = [self.zeros(gr.shape) for _ in range(3)]
         if ns == 0:
             return tuple(S)
@@ -112,7 +127,7 @@ class GpuStages:
 
     def post(self, SR, SL, SG):
         self.sys._grid()
-        ne, nx, nm = SR.shape[0], SR.shape[1], SR.shape[-1]
+        ne, nx, nm = SR.shape[-4], SR.shape[-3], SR.shape[-1]
         if ne == 0:
             return
         check(self.lib.qt_gw_sigma_post(self.ctx.handle, nm, nx, ne, _ptr(SR), _ptr(SL),
@@ -139,30 +154,44 @@ class ShardedGw:
     @classmethod
     def on_gpu(cls, ctx, H00, H10, E, nx, V, *, world=1, rank=0, group=None, mu=(0.0, 0.0),
                temp=(300.0, 300.0), eta_lead=1e-3, sancho_max_iter=100, sancho_tol=1e-100,
-               spindeg=2.0, precision="fp64"):
+               spindeg=2.0, precision="fp64", kgrid=(1, 1), ndiag=None):
         """The rank's share of a ``gw.GwSystem`` problem on its GPU."""
         E = np.ascontiguousarray(E, dtype=np.float64)
         lo, hi = energy_range(len(E), world, rank)
         st = GpuStages(ctx, H00, H10, E[lo:hi], nx, V, mu=mu, temp=temp, eta_lead=eta_lead,
                        sancho_max_iter=sancho_max_iter, sancho_tol=sancho_tol,
-                       precision=precision)
+                       precision=precision, kgrid=kgrid, ndiag=ndiag)
         return cls(st, len(E), nx, np.asarray(H00).shape[-1], E[1] - E[0], world=world,
-                   rank=rank, group=group, spindeg=spindeg)
+                   rank=rank, group=group, spindeg=spindeg, nk=kgrid[0] * kgrid[1])
 
     @property
     def local_energies(self):
         return self.hi - self.lo
 
     def zeros(self):
-        return self.stages.zeros((self.local_energies, self.nx, self.nm, self.nm))
+        shape = (self.local_energies, self.nx, self.nm, self.nm)
+        return self.stages.zeros(shape if self.nk == 1 else (self.nk,) + shape)
 
     def _to_ijs(self, A):
-        return energies_to_ijs(A.reshape(self.local_energies, self.nx, self.nm * self.nm),
-                               self.nE, self.world, self.rank, self.group)
+        """(nk,) nE_local, nx, nm, nm blocks -> (nk,) nE, nx, nij_local series; the k-points
+        travel in the same all-to-all, as the slabs do"""
+        ne, nk, nx = self.local_energies, self.nk, self.nx
+        if nk > 1:
+            A = A.permute(1, 0, 2, 3, 4)
+        y = energies_to_ijs(A.reshape(ne, nk * nx, self.nm * self.nm), self.nE, self.world,
+                            self.rank, self.group)
+        if nk == 1:
+            return y
+        return y.view(self.nE, nk, nx, -1).permute(1, 0, 2, 3).contiguous()
 
     def _to_energies(self, A):
-        x = ijs_to_energies(A, self.nm * self.nm, self.world, self.rank, self.group)
-        return x.reshape(self.local_energies, self.nx, self.nm, self.nm).contiguous()
+        ne, nk, nx, nm = self.local_energies, self.nk, self.nx, self.nm
+        if nk > 1:
+            A = A.permute(1, 0, 2, 3).reshape(self.nE, nk * nx, -1)
+        x = ijs_to_energies(A, nm * nm, self.world, self.rank, self.group)
+        if nk == 1:
+            return x.reshape(ne, nx, nm, nm).contiguous()
+        return x.view(ne, nk, nx, nm, nm).permute(1, 0, 2, 3, 4).contiguous()
 
     def step(self, SR, SL):
         """Sigma_new (R, <, >) on this rank's energies from Sigma (R, <) there: one evaluation
