@@ -64,18 +64,24 @@ def parse():
     ap.add_argument("--no-scba", action="store_true", help="skip the GW-SCBA mixing comparison")
     ap.add_argument("--scba-size", default="10,16,256",
                     help="slabs,orbitals,energies of the GW-SCBA device family")
+    ap.add_argument("--scba-train", type=int, default=8,
+                    help="training seeds of the learned mixer (disorder realisations)")
+    ap.add_argument("--scba-test", type=int, default=2, help="held-out seeds")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the library's default wave size instead of autotuning it")
     ap.add_argument("--wave", type=int, default=0,
                     help="points per wave, set without autotuning (0: autotune unless --no-tune)")
-    ap.add_argument("--workload", default="batched", choices=["batched", "uneven", "gw"],
+    ap.add_argument("--workload", default="batched",
+                    choices=["batched", "uneven", "gw", "scba"],
                     help="batched: 100 x 128 slabs (the headline); uneven: the 4000-atom graph; "
-                         "gw: GW-SCBA on the 80-slab x 96-orbital device with 2048 energies")
+                         "gw: GW-SCBA on the 80-slab x 96-orbital device with 2048 energies; "
+                         "scba: the plain / Pulay / learned mixing comparison alone "
+                         "(--scba-size, --scba-train, --scba-test)")
     ap.add_argument("--gw-size", default="80,96,2048",
                     help="slabs,orbitals,energies of the --workload gw device")
-    ap.add_argument("--gw-precisions", default="mixed,mixed-fp64,fp64",
-                    help="--workload gw: precisions to converge (the last is the reference)")
+    ap.add_argument("--gw-precisions", default="mixed-fp64,mixed",
+                    help="--workload gw: split precisions to converge (each checked in FP64)")
     ap.add_argument("--gw-max-iter", type=int, default=60)
     ap.add_argument("--gw-tol", type=float, default=1e-8)
     return ap.parse_args()
@@ -204,8 +210,8 @@ def scba_comparison(ctx, a):
         return gw.GwSystem(ctx, d.H00, d.H10, d.E, d.nx, d.V, mu=(0.1, -0.1),
                            precision=precision)
 
-    train_sys = [system(100 + i) for i in range(8)]
-    test_sys = [system(900 + i) for i in range(2)]
+    train_sys = [system(100 + i) for i in range(a.scba_train)]
+    test_sys = [system(900 + i) for i in range(a.scba_test)]
     t0 = time.perf_counter()
     mixer = mixing.LearnedMixer(ctx, nE, seed=5, max_batch=max(2048, nx * nm))
     X, T, fps, _ = mixing.collect(train_sys)
@@ -214,7 +220,8 @@ def scba_comparison(ctx, a):
     mixing.train(mixer, np.concatenate([X, X2]), np.concatenate([T, T2]), steps=800,
                  batch=2048, lr=5e-4, seed=1)
     t_train = time.perf_counter() - t0
-    out = {m: {"evaluations": [], "seconds": []} for m in ("plain", "pulay", "learned")}
+    out = {m: {"evaluations": [], "seconds": [], "converged": []}
+           for m in ("plain", "pulay", "learned")}
     diff = 0.0
     for s in test_sys:
         runs = {m: mixing.run_scba(s, method=m, mixer=mixer if m == "learned" else None,
@@ -222,6 +229,7 @@ def scba_comparison(ctx, a):
         for m, r in runs.items():
             out[m]["evaluations"].append(r.evaluations)
             out[m]["seconds"].append(r.seconds)
+            out[m]["converged"].append(r.residuals[-1] <= 1e-8)
         for x, y in zip(runs["learned"].sigma, runs["plain"].sigma):
             diff = max(diff, float((x - y).abs().max() / y.abs().max()))
     # plain-mixing SCBA to residual 1e-6 in FP64 and in both split precisions on one held-out
@@ -249,8 +257,12 @@ def scba_comparison(ctx, a):
                         "sigma ~ U[0.05, 0.3] eV, V_ij = 14.4/(|r_i - r_j| + 1) eV, residual <= 1e-8",
             "train_seeds": len(train_sys), "test_seeds": len(test_sys),
             "training_seconds": t_train,
-            **{m: {"evaluations": mean(v["evaluations"]), "seconds": mean(v["seconds"])}
+            **{m: {"evaluations": mean(v["evaluations"]),
+                   "evaluations_median": float(np.median(v["evaluations"])),
+                   "seconds": mean(v["seconds"]), "converged": int(sum(v["converged"]))}
                for m, v in out.items()},
+            "learned_faster_than_pulay_seeds": int(sum(
+                x < y for x, y in zip(out["learned"]["seconds"], out["pulay"]["seconds"]))),
             "learned_vs_plain_time": mean(out["learned"]["seconds"]) / mean(out["plain"]["seconds"]),
             "learned_vs_pulay_time": mean(out["learned"]["seconds"]) / mean(out["pulay"]["seconds"]),
             "fixed_point_max_rel_diff": diff,
@@ -644,9 +656,15 @@ def run_gw(a):
     --gw-tol on a seeded 80-slab x 96-orbital chain (H_ii shared by all slabs: on-site
     U[-1, 1] eV, off-diagonal N(0, 0.1) eV; H_i,i+1 = -2.7 I + N(0, 0.05)), 2048 energies
     on [-4, 4] eV, V_ij = 14.4 / (|r_i - r_j| + 1) eV on a 0.25 nm grid, FFT length 4096.
-    Each precision runs to convergence in turn (the device holds one SCBA at a time); the
-    terminal currents and the LDOS of the converged self-energies are compared with the
-    last precision's (FP64)."""
+
+    Each split precision runs to convergence in turn (the device holds one SCBA at a time:
+    the three self-energies and the map's six arrays, 24 GB each).  Its fixed point S* is
+    then checked in FP64, which would take about 45 minutes to converge itself:
+      - one FP64 evaluation of the map at S*: its residual ||F64(S*) - S*|| / ||F64(S*)||
+        and its time (the FP64 seconds per iteration);
+      - the FP64 RGF at S*: terminal currents and LDOS against the split RGF's at S*.
+    The FP64 time to converge is projected as the split run's iteration count times the
+    FP64 seconds per iteration, and labelled so."""
     import torch
     from quantum_transport_gb300.build import build
     build()
@@ -656,10 +674,11 @@ def run_gw(a):
     d = make_chain_device(nx, nm, nE, -4.0, 4.0, seed=SEED)
     V = coulomb_block(nm)
     ctx = rgf.Context(0)
-    precs = a.gw_precisions.split(",")
-    runs = {}
+    precs = [p for p in a.gw_precisions.split(",") if p != "fp64"]
+    out = {}
     clocks = Clocks(0)
     clocks.start()
+    s64 = gw.GwSystem(ctx, d.H00[0], d.H10, d.E, nx, V, mu=(0.1, -0.1), precision="fp64")
     for p in precs:
         s = gw.GwSystem(ctx, d.H00[0], d.H10, d.E, nx, V, mu=(0.1, -0.1), precision=p)
         torch.cuda.synchronize()
@@ -668,36 +687,61 @@ def run_gw(a):
                                       with_currents=True)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
+        it6 = next((i + 1 for i, r in enumerate(res) if r <= 1e-6), None)
+        e = {"seconds": dt, "iterations": int(len(res)),
+             "seconds_per_iteration": dt / max(1, len(res)),
+             "iterations_to_1e-6": it6,
+             "seconds_to_1e-6": None if it6 is None else it6 * dt / len(res),
+             "final_residual": float(res[-1]), "converged": bool(res[-1] <= a.gw_tol),
+             "residuals": [float(x) for x in res],
+             "current_A": [float(x) for x in cur[-1]]}
+        # the split RGF and the FP64 RGF at the same S* (each timed: the RGF's share of an
+        # iteration)
+        t0 = time.perf_counter()
         ob = s.currents(SR, SL)
-        runs[p] = {"seconds": dt, "iterations": int(len(res)),
-                   "seconds_per_iteration": dt / max(1, len(res)),
-                   "final_residual": float(res[-1]), "converged": bool(res[-1] <= a.gw_tol),
-                   "residuals": [float(x) for x in res],
-                   "current_A": [float(x) for x in cur[-1]],
-                   "_ldos": -2.0 * ob["diag_gr"].imag}
-        del SR, SL, SG, s
+        t_rgf = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        o64 = s64.currents(SR, SL)
+        t_rgf64 = time.perf_counter() - t0
+        ld, ld64 = -2.0 * ob["diag_gr"].imag, -2.0 * o64["diag_gr"].imag
+        e["rgf_at_fixed_point"] = {
+            "seconds": t_rgf, "fp64_seconds": t_rgf64,
+            "tr_rel_err": float(np.abs(ob["tr"] - o64["tr"]).max() / np.abs(o64["tr"]).max()),
+            "tre_rel_err": float(np.abs(ob["tre"] - o64["tre"]).max() /
+                                 np.abs(o64["tre"]).max()),
+            "ldos_rel_err": float(np.abs(ld - ld64).max() / np.abs(ld64).max())}
+        del s
+        torch.cuda.empty_cache()
+        # one FP64 map at S* (in place: S becomes the FP64 iterate mixed with S*)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, _, _, r64, c64 = s64.scba(alpha=0.3, tol=0.0, max_iter=1, start=(SR, SL, SG),
+                                     with_currents=True)
+        torch.cuda.synchronize()
+        t64 = time.perf_counter() - t0
+        e["fp64_map_at_fixed_point"] = {
+            "residual": float(r64[0]), "seconds": t64,
+            "current_A": [float(x) for x in c64[0]],
+            "current_rel_err": float(np.max(np.abs(np.array(e["current_A"]) - c64[0]) /
+                                            np.abs(c64[0])))}
+        if it6 is not None:
+            e["fp64_seconds_to_1e-6_projected"] = it6 * t64
+            e["speedup_vs_fp64_to_1e-6"] = it6 * t64 / e["seconds_to_1e-6"]
+        out[p] = e
+        del SR, SL, SG
         torch.cuda.empty_cache()
     clk = clocks.stop()
-    ref = precs[-1]
-    r0 = runs[ref]
-    out = {}
-    for p, r in runs.items():
-        e = {k: v for k, v in r.items() if not k.startswith("_")}
-        if p != ref:
-            e["time_vs_" + ref] = r["seconds"] / r0["seconds"]
-            c, c0 = np.array(r["current_A"]), np.array(r0["current_A"])
-            e["current_rel_err"] = float(np.max(np.abs(c - c0) / np.abs(c0)))
-            e["ldos_rel_err"] = float(np.abs(r["_ldos"] - r0["_ldos"]).max() /
-                                      np.abs(r0["_ldos"]).max())
-        out[p] = e
     L = 1 << int(np.ceil(np.log2(2 * nE)))
     line = {"metric": METRIC, "workload": "gw", "unit": "s to residual", "tol": a.gw_tol,
             "higher_is_better": False, "n_gpus": 1, "data": "synthetic (seeded, no dataset)",
             "config": {"workload": f"GW-SCBA, {nx} slabs x {nm} orbitals x {nE} energies on "
                                    f"[-4, 4] eV, plain linear mixing alpha = 0.3 to residual "
                                    f"{a.gw_tol:g} (max {a.gw_max_iter} iterations), FFT length {L}",
-                       "memory": "six [nE][nx][nm^2] complex128 arrays in the map (G, then P "
-                                 "-> W in place, Sigma_new over G) + the three Sigma arrays"},
+                       "memory": "the three Sigma arrays + six [nE][nx][nm^2] complex128 "
+                                 "arrays in the map (G, then P -> W in place, Sigma_new over "
+                                 f"G): {9 * nE * nx * nm * nm * 16 / 1e9:.0f} GB",
+                       "fp64_reference": "one FP64 map and the FP64 RGF at each split fixed "
+                                         "point; FP64 time to converge projected"},
             "runs": out, "clocks": clk}
     print(json.dumps(line), flush=True)
     ctx.close()
@@ -711,6 +755,14 @@ def main():
         run_uneven(a)
     elif a.workload == "gw":
         run_gw(a)
+    elif a.workload == "scba":
+        from quantum_transport_gb300.build import build
+        build()
+        from quantum_transport_gb300 import rgf
+        ctx = rgf.Context(0)
+        print(json.dumps({"metric": METRIC, "workload": "scba",
+                          "scba": scba_comparison(ctx, a)}), flush=True)
+        ctx.close()
     else:
         run_ours(a)
 

@@ -2086,6 +2086,9 @@ qt_status gw_map(qt_ctx* ctx, Problem pb, const GwGrid& g, const cd* V, double s
   const int nm = pb.nm, nx = pb.nx, nk = g.nk;
   const long long nE = pb.npts;  // energies per k-point
   const long long nm2 = (long long)nm * nm, nblk = nE * nx, kst = nblk * nm2;
+  // digits of the screened interaction's products: the leads' FP64 grade, as run_problem
+  // sets them for the RGF
+  pb.lead_slices = env_int("QT_LEAD_SLICES", 7);
   // ---- G with the current self-energies, one k-point at a time (its H blocks)
   const cd* Hii = pb.Hii;
   const cd* H1i = pb.H1i;
