@@ -1002,7 +1002,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         raw_read4(rA, args.layoutA, r, gA0, 128, xa);
         raw_read4(rA, args.layoutA, r, gA0 + 2, 128, xa + 4);
         raw_read4(rA + RAW_A, args.layoutB, j, gB, NT, xb);
-        mbar_arrive(&rempty[rs]);  // the values are in registers: the slot may refill
+        // the slot goes back to the tensor memory accelerator: order these generic-proxy
+        // reads before its next (async-proxy) write into the slot
+        fence_proxy_async();
+        mbar_arrive(&rempty[rs]);
         if (!mbar_wait(&dempty[ds], ((g / DSTAGES) & 1) ^ 1, abort_flag, tcount)) {
           ok = false;
           break;
@@ -1405,6 +1408,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         double2 x[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) x[u] = raw_elem(rt, layout, v, 4 * gq + u, isA ? 128 : NT);
+        // release the slot to the next cp.async.bulk.tensor only after a proxy fence: the
+        // mbarrier orders these generic-proxy reads for the loader thread, not for the
+        // async-proxy write that follows, which could otherwise land before them
+        fence_proxy_async();
         mbar_arrive(&rempty[rs]);
         if (!mbar_wait(&dempty[ds], ((g / DSTAGES) & 1) ^ 1, abort_flag, tcount)) {
           ok = false;

@@ -144,3 +144,40 @@ def test_products_repeat_bitwise_with_beta_d(ctx, kind, slices):
                                       _lib.QT_PREC_MIXED, slices, flags))
         outs.append(C)
     assert all(torch.equal(outs[0], o) for o in outs[1:])
+
+
+@pytest.mark.parametrize("kind,slices", [("c64", 4), ("c128", 4), ("c128", 6), ("c128", 7)])
+def test_raw_slot_reuse_repeats_bitwise(ctx, kind, slices):
+    """88 x 88 x 88 products (11 k-chunks per item, so the ring of TMA slots wraps inside
+    items) repeated 24 times: every repeat equals the first bit for bit, and the first is
+    within the digit bound of numpy.  Without a proxy fence between the producers' reads of
+    a slot and its release to the next tensor copy, about one 6-digit launch in five here
+    read a refilled slot."""
+    import torch
+    from quantum_transport_gb300 import _lib
+    from quantum_transport_gb300.rgf import _ptr
+    lib = ctx._lib
+    n, batch = 88, 256
+    g = torch.Generator(device="cuda").manual_seed(11)
+    dt = torch.complex64 if kind == "c64" else torch.complex128
+    A = torch.randn(batch, n, n, dtype=dt, device="cuda", generator=g)
+    B = torch.randn(batch, n, n, dtype=dt, device="cuda", generator=g)
+    one, zero = np.array([1.0, 0.0]), np.array([0.0, 0.0])
+    flags = _lib.QT_FLAG_DEVICE_POINTERS | _lib.QT_FLAG_SYNC | (
+        _lib.QT_FLAG_COMPLEX64 if kind == "c64" else 0)
+    outs = []
+    for _ in range(24):
+        C = torch.zeros_like(A)
+        _lib.check(lib.qt_zgemm_batch(ctx.handle, n, batch, b"N", _ptr(A), n * n, b"N", _ptr(B),
+                                      n * n, _ptr(one), _ptr(zero), None, 0, _ptr(C), n * n,
+                                      _lib.QT_PREC_MIXED, slices, flags))
+        outs.append(C)
+    assert all(torch.equal(outs[0], o) for o in outs[1:])
+    # device blocks are column-major: the stored transpose of each operand
+    Ah = _host(A.to(torch.complex64) if kind == "c64" else A)
+    Bh = _host(B.to(torch.complex64) if kind == "c64" else B)
+    got = _host(outs[0])
+    exact = Ah @ Bh
+    tol = (TOL128.get(slices, 2.0 ** -28) * _bound(Ah, Bh, "N", "N")
+           + (2.0 ** -23 if kind == "c64" else 4e-16) * np.abs(exact))
+    assert (np.abs(got - exact) <= tol).all()
