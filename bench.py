@@ -68,6 +68,8 @@ def parse():
                     help="training seeds of the learned mixer (disorder realisations)")
     ap.add_argument("--scba-test", type=int, default=2, help="held-out seeds")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-uneven", action="store_true",
+                    help="skip the uneven-block sample of the default line")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the library's default wave size instead of autotuning it")
     ap.add_argument("--wave", type=int, default=0,
@@ -277,6 +279,64 @@ def _point_errors(x, ref, per_point):
     return float(r.max()), float(np.median(r))
 
 
+def uneven_sample(ctx, n_energies=64, n_fp64=16):
+    """The uneven-block configuration beside the headline: the 4000-atom graph device
+    (25 slabs of 134-184 orbitals, 8 k) through the variable-block sweep.  Both split modes
+    solve n_energies energies spread over the [-2, 2] eV window x 8 k in one wave (timed
+    with CUDA events after a one-energy warm-up call); the FP64 path solves every
+    (n_energies / n_fp64)-th of them, which gives its throughput and the T(E) errors."""
+    import torch
+    from quantum_transport_gb300 import rgf
+    from quantum_transport_gb300.devices import config_uneven
+    d = config_uneven()
+    nk = len(d.kpts)
+    sizes = np.array(d.sizes, dtype=np.int32)
+    hii, hoff, _ = rgf.pack_blocks(d.Hii, nk)
+    h1i, h1off, _ = rgf.pack_blocks(d.H1i, nk)
+    Hd, H1d = torch.from_numpy(hii).cuda(), torch.from_numpy(h1i).cuda()
+    Eall = torch.from_numpy(d.E).cuda()
+    Es = Eall[::len(d.E) // n_energies][:n_energies].contiguous()
+    sub = n_energies // n_fp64
+    E64 = Es[::sub].contiguous()
+    kw = dict(mul=0.1, mur=-0.1, templ=300.0, tempr=300.0, sancho_tol=1e-10,
+              sancho_max_iter=100, caroli=True)
+    stream = torch.cuda.current_stream()
+
+    def solve(prec, E, ne):
+        o = {"T": torch.zeros(ne * nk, dtype=torch.float64, device="cuda"),
+             "status": torch.zeros(ne * nk, dtype=torch.int32, device="cuda")}
+        rgf.rgf_variableblock_device(ctx, sizes, Hd, hoff, H1d, h1off, nk, E, 1, o,
+                                     precision=prec, **kw)  # first-call set-up
+        ctx.sync()
+        ctx.inverse_fallbacks(reset=True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        rgf.rgf_variableblock_device(ctx, sizes, Hd, hoff, H1d, h1off, nk, E, ne, o,
+                                     precision=prec, **kw)
+        e1.record(stream)
+        e1.synchronize()
+        ctx.sync()
+        return (ne * nk / (e0.elapsed_time(e1) / 1e3), o["T"].cpu().numpy(),
+                int((o["status"] != 0).sum().item()), ctx.inverse_fallbacks())
+
+    v64, T64, bad64, _ = solve("fp64", E64, E64.numel())
+    out = {"workload": f"uneven-block RGF, 4000-atom random graph sliced into {len(sizes)} slabs "
+                       f"of {sizes.min()}-{sizes.max()} orbitals, {nk} k; {n_energies} energies "
+                       f"across [-2, 2] eV per split-mode wave, every {sub}th in FP64",
+           "fp64": {"value": v64, "unit": "E-points/s", "points": int(T64.size),
+                    "points_bad_status": bad64}}
+    for prec in ("mixed-fp64", "mixed"):
+        v, T, bad, fb = solve(prec, Es, n_energies)
+        Tm = T.reshape(n_energies, nk)[::sub].reshape(-1)
+        err = np.abs(Tm - T64)
+        out[prec] = {"value": v, "unit": "E-points/s", "points": int(T.size),
+                     "speedup_vs_fp64": v / v64,
+                     "T_rel_err_max": float(err.max() / np.abs(T64).max()),
+                     "T_rel_err_median": float(np.median(err) / np.abs(T64).max()),
+                     "points_bad_status": bad, "inverses_redone_fp64": fb}
+    return out
+
+
 def accuracy_sample(ctx, H00, H10, E, nm2, kw, n_energies, split_value):
     """FP64-pipe path against both split precisions on a strided sample of the workload:
     every (NE / n_energies)-th energy across the whole [-2, 2] eV window x 16 k.  Reports
@@ -471,6 +531,8 @@ def run_ours(a):
                                                 value / world)
     if rank == 0 and not a.no_scba:
         line["scba"] = scba_comparison(ctx, a)
+    if rank == 0 and not a.no_uneven:
+        line["uneven"] = uneven_sample(ctx)
     if rank == 0:
         if world == 1 and not a.no_cpu:
             threads = os.cpu_count() or 1

@@ -782,35 +782,36 @@ cudaError_t launch(const GemmArgs& a, cudaStream_t s) {
 // ============================================================ TMA-fed complex64 product
 // The complex64 sweep's product C = alpha op(A) op(B) + beta D + z I (S = 4 digits, levels
 // <= 3) with its operands staged by the tensor memory accelerator:
-//  * a loader thread copies each stage's raw complex64 tiles -- op(A) 128 rows x 16 complex
-//    k, op(B) 16 k x 64 columns -- from global memory into a ring of RSTAGES shared-memory
+//  * a loader thread copies each stage's raw complex64 tiles -- op(A) 128 rows x 8 complex
+//    k and op(B) 8 k x 128 columns -- from global memory into a ring of RSTAGES shared-memory
 //    slots with cp.async.bulk.tensor (3-D tensor maps over (floats, vectors, batch entry));
 //  * producer warps split the raw tiles, shared memory to shared memory, into the digit
 //    planes of A' = (Re, Im) op(A) and of the two layouts of op(B), B'_r = (Re, -Im) and
-//    B'_i = (Im, Re), so that Re C = A' B'_r and Im C = A' B'_i (the second layout is
-//    formed on the 64-column operand, not on the 128-row one);
-//  * a work item is one 64-column tile of one batch entry: its four accumulators (level 0
-//    and levels 1-3 of both parts) take 256 TMEM columns, so two items' accumulators fit
-//    and the epilogue of one item runs while the next item's products are issued.
+//    B'_i = (Im, Re), so that Re C = A' B'_r and Im C = A' B'_i, and fence each slot's reads
+//    against the async proxy before handing the slot back to the loader;
+//  * a work item is a whole product (n <= 128): both real parts of all columns, so every
+//    MMA is 128 x 128 x 16 and op(A) is split once per product.  The four accumulators (two
+//    parts x level 0 / levels 1-3) take all 512 TMEM columns; eight epilogue warps (two per
+//    TMEM lane quarter, one column half each) keep the unoverlapped epilogue short.
 // A tile that is contiguous along rows (op(A) = N, op(B) = C) is copied as [k][row]; one
-// that is contiguous along k (op(A) = C, op(B) = N) as [row][k] with 128-byte rows and the
-// 128-byte swizzle, so that the producers' 16-byte reads down a column of rows hit eight
-// different bank groups.  The epilogue's arithmetic is the register-staged kernel's: the
-// two kernels give the same bits.
+// that is contiguous along k (op(A) = C, op(B) = N) as [row][k] in 64-byte rows under the
+// 64-byte swizzle, so that the producers' 16-byte reads down a column of rows spread over
+// the banks.  The epilogue's arithmetic is the register-staged kernel's: the two kernels
+// give the same bits.
 namespace c64t {
 constexpr int S = 4, L = 3;              // digits, highest level kept
-constexpr int NT = 64;                   // output columns per item
-constexpr int KCC = 16;                  // complex k per stage (32 real K)
-constexpr int DSTAGES = 2, RSTAGES = 4;  // digit stages, raw (TMA) stages
-constexpr int NPROD = 256;               // producer threads
-constexpr int LOAD_WARP = 4 + NPROD / 32, MMA_WARP = LOAD_WARP + 1;
+constexpr int NT = 128;                  // output columns per item (all of them)
+constexpr int KCC = 8;                   // complex k per stage (16 real K: one MMA K step)
+constexpr int DSTAGES = 3, RSTAGES = 5;  // digit stages, raw (TMA) stages
+constexpr int NEPI = 256;                // epilogue threads (8 warps)
+constexpr int NPROD = 256;               // producer threads (8 warps)
+constexpr int PROD_WARP0 = NEPI / 32, LOAD_WARP = PROD_WARP0 + NPROD / 32, MMA_WARP = LOAD_WARP + 1;
 constexpr int NTHREADS = 32 * (MMA_WARP + 1);
-constexpr int APLANE = 128 * 2 * KCC * 2;  // one digit plane of A': 128 rows x 32 BF16 (8 KB)
-constexpr int BPLANE = NT * 2 * KCC * 2;   // one digit plane of a B layout: 64 rows (4 KB)
-constexpr int DSTAGE = S * APLANE + 2 * S * BPLANE;  // 64 KB
-constexpr int RAW_A = 128 * KCC * 8, RAW_B = NT * KCC * 8;  // 16 KB, 8 KB
+constexpr int PLANE = 128 * 2 * KCC * 2;  // one digit plane: 128 rows x 16 BF16 (4 KB)
+constexpr int DSTAGE = 3 * S * PLANE;     // A', B'_r, B'_i: 48 KB
+constexpr int RAW_A = 128 * KCC * 8, RAW_B = NT * KCC * 8;  // 8 KB, 8 KB
 constexpr int RSTAGE = RAW_A + RAW_B;
-constexpr uint32_t SBO_T = (2 * KCC / 8) * 128;  // 8-row groups of a digit plane (512 B)
+constexpr uint32_t SBO_T = (2 * KCC / 8) * 128;  // 8-row groups of a digit plane (256 B)
 constexpr int SMEM = 1024 + RSTAGES * RSTAGE + DSTAGES * DSTAGE + 256;
 static_assert(SMEM <= 232448, "shared memory");
 static_assert(RAW_A % 1024 == 0 && RSTAGE % 1024 == 0, "swizzled boxes need 1 KB alignment");
@@ -823,26 +824,26 @@ struct Args {
   int layoutA, layoutB;  // MN_MAJOR / K_MAJOR
 };
 
-// four consecutive complex k (4g .. 4g+3) of vector v of a raw tile: MN-major tiles hold
-// [kc][v] with `vecs` vectors, K-major tiles [v][kc] in 128-byte swizzled rows (16-byte
-// chunk c of row v at chunk c ^ (v & 7))
+// complex elements 4g .. 4g+3 (g = 0, 1) of vector v of a raw tile of 8 complex k:
+// MN-major [kc][v] (128 vectors), K-major [v][kc] in 64-byte rows under the 64-byte swizzle
+// (16-byte chunk c of row v at chunk c ^ ((v >> 1) & 3))
 __device__ __forceinline__ void raw_read4(const unsigned char* base, int layout, int v, int g,
-                                          int vecs, float2* x) {
+                                          float2* x) {
   if (layout == MN_MAJOR) {
 #pragma unroll
     for (int u = 0; u < 4; ++u)
-      x[u] = *reinterpret_cast<const float2*>(base + ((size_t)(4 * g + u) * vecs + v) * 8);
+      x[u] = *reinterpret_cast<const float2*>(base + ((size_t)(4 * g + u) * 128 + v) * 8);
   } else {
-    const float4 p0 =
-        *reinterpret_cast<const float4*>(base + v * 128 + (((2 * g) ^ (v & 7)) << 4));
-    const float4 p1 =
-        *reinterpret_cast<const float4*>(base + v * 128 + (((2 * g + 1) ^ (v & 7)) << 4));
+    const int sw = (v >> 1) & 3;
+    const float4 p0 = *reinterpret_cast<const float4*>(base + v * 64 + (((2 * g) ^ sw) << 4));
+    const float4 p1 = *reinterpret_cast<const float4*>(base + v * 64 + (((2 * g + 1) ^ sw) << 4));
     x[0] = make_float2(p0.x, p0.y);
     x[1] = make_float2(p0.z, p0.w);
     x[2] = make_float2(p1.x, p1.y);
     x[3] = make_float2(p1.z, p1.w);
   }
 }
+
 // 2^(8-e) as pre * scale: vectors below 2^-119 would overflow one FP32 power of two, so they
 // are first lifted by 2^64 (exact).  sign = -1 conjugates (op = C).
 __device__ __forceinline__ void digit_scale(int e, float sign, float2& m, float& sc) {
@@ -887,22 +888,21 @@ __device__ __forceinline__ float2 c64_pair(uint32_t r0, uint32_t r1, uint32_t i0
 
 __global__ void __launch_bounds__(NTHREADS, 1)
     zgemm_c64_tma_kernel(const __grid_constant__ Args args, const __grid_constant__ CUtensorMap tmA,
-                         const __grid_constant__ CUtensorMap tmB) {
+                          const __grid_constant__ CUtensorMap tmB) {
   const GemmArgs& a = args.g;
   extern __shared__ unsigned char smem_raw[];
-  // 1 KB alignment for the swizzled boxes
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-  unsigned char* raw = smem;                                 // [RSTAGES][A tile | B tile]
-  unsigned char* dig = smem + (size_t)RSTAGES * RSTAGE;      // [DSTAGES][A' | B'_r | B'_i]
+  unsigned char* raw = smem;
+  unsigned char* dig = smem + (size_t)RSTAGES * RSTAGE;
   uint64_t* bars = reinterpret_cast<uint64_t*>(dig + (size_t)DSTAGES * DSTAGE);
-  uint64_t* dfull = bars;                       // producers -> MMA        [DSTAGES]
-  uint64_t* dempty = dfull + DSTAGES;           // MMA commit -> producers [DSTAGES]
-  uint64_t* rfull = dempty + DSTAGES;           // TMA -> producers        [RSTAGES]
-  uint64_t* rempty = rfull + RSTAGES;           // producers -> loader     [RSTAGES]
-  uint64_t* tfull = rempty + RSTAGES;           // MMA commit -> epilogue  [2]
-  uint64_t* tempty = tfull + 2;                 // epilogue -> MMA         [2]
-  uint64_t* drain = tempty + 2;
+  uint64_t* dfull = bars;
+  uint64_t* dempty = dfull + DSTAGES;
+  uint64_t* rfull = dempty + DSTAGES;
+  uint64_t* rempty = rfull + RSTAGES;
+  uint64_t* tfull = rempty + RSTAGES;
+  uint64_t* tempty = tfull + 1;
+  uint64_t* drain = tempty + 1;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
   int* const tcount = a.timeouts ? a.timeouts : &g_oz_timeouts;
@@ -910,13 +910,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m = a.m, n = a.n, K = a.k;
   const int nch = (K + KCC - 1) / KCC;
-  const int ntile = (n + NT - 1) / NT;
-  const long long nitems = (long long)ntile * a.batch;
+  const long long nitems = a.batch;
 
   if (tid == 0) {
     for (int s = 0; s < DSTAGES; ++s) { mbar_init(&dfull[s], NPROD); mbar_init(&dempty[s], 1); }
     for (int s = 0; s < RSTAGES; ++s) { mbar_init(&rfull[s], 1); mbar_init(&rempty[s], NPROD); }
-    for (int s = 0; s < 2; ++s) { mbar_init(&tfull[s], 1); mbar_init(&tempty[s], 128); }
+    mbar_init(tfull, 1);
+    mbar_init(tempty, NEPI);
     mbar_init(drain, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -932,18 +932,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const uint32_t tmem = *tmem_slot;
 
   if (warp == LOAD_WARP) {
-    // ======================== loader: one thread issues every stage's two tile copies
     if (lane == 0) {
-      uint32_t g = 0;                 // stage counter, the same sequence in every role
-      uint32_t pend_parity[RSTAGES];  // phase of each slot's last copy
+      uint32_t g = 0;
+      uint32_t pend_parity[RSTAGES];
       bool pend[RSTAGES];
 #pragma unroll
       for (int s = 0; s < RSTAGES; ++s) { pend[s] = false; pend_parity[s] = 0; }
-      for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
-        const long long b = w / ntile;
-        const int ct = (int)(w % ntile);
+      for (long long b = blockIdx.x; b < nitems && !*abort_flag; b += gridDim.x) {
         if (a.active && !a.active[b]) continue;
-        // batch coordinate of each operand's tensor map (a shared operand has one entry)
         const int ea = a.A.stride == 0 ? 0 : (int)batch_index(a.A, b);
         const int eb = a.B.stride == 0 ? 0 : (int)batch_index(a.B, b);
         bool ok = true;
@@ -953,57 +949,45 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           if (!mbar_wait(&rempty[slot], ph ^ 1, abort_flag, tcount)) { ok = false; break; }
           unsigned char* dA = raw + (size_t)slot * RSTAGE;
           unsigned char* dB = dA + RAW_A;
-          tc::mbar_arrive_expect_tx(&rfull[slot], RSTAGE);  // full boxes, zero-filled edges
+          tc::mbar_arrive_expect_tx(&rfull[slot], RSTAGE);
           const int k0 = c * KCC;
           if (args.layoutA == MN_MAJOR) tc::tma_load_3d(dA, &tmA, 0, k0, ea, &rfull[slot]);
           else tc::tma_load_3d(dA, &tmA, 2 * k0, 0, ea, &rfull[slot]);
-          if (args.layoutB == MN_MAJOR) tc::tma_load_3d(dB, &tmB, 2 * ct * NT, k0, eb, &rfull[slot]);
-          else tc::tma_load_3d(dB, &tmB, 2 * k0, ct * NT, eb, &rfull[slot]);
+          if (args.layoutB == MN_MAJOR) tc::tma_load_3d(dB, &tmB, 0, k0, eb, &rfull[slot]);
+          else tc::tma_load_3d(dB, &tmB, 2 * k0, 0, eb, &rfull[slot]);
           pend[slot] = true;
           pend_parity[slot] = ph;
         }
         if (!ok) break;
       }
-      // every copy lands before the CTA exits (in an aborted run some were never consumed)
       int zero = 0;
       volatile int* never = &zero;
       for (int s = 0; s < RSTAGES; ++s)
         if (pend[s]) mbar_wait(&rfull[s], pend_parity[s], never, tcount);
     }
     __syncwarp();
-  } else if (warp >= 4 && warp < LOAD_WARP) {
-    // ======================== producers: raw tiles -> digit planes (shared -> shared)
-    // thread p: op(A) row r in 4-k groups gA0 and gA0 + 2; op(B) column j in 4-k group gB
-    const int p = tid - 128;
-    const int r = p & 127, gA0 = p >> 7;
-    const int j = p & (NT - 1), gB = p / NT;
-    const uint32_t offA0 = (uint32_t)((r >> 3) * SBO_T + gA0 * 128 + (r & 7) * 16);
-    const uint32_t offA1 = offA0 + 2 * 128;
-    const uint32_t offB = (uint32_t)((j >> 3) * SBO_T + gB * 128 + (j & 7) * 16);
+  } else if (warp >= PROD_WARP0 && warp < LOAD_WARP) {
+    // thread p: row r of op(A) and column r of op(B), 4-k group g
+    const int p = tid - NEPI;
+    const int r = p & 127, g4 = p >> 7;
+    const uint32_t off = (uint32_t)((r >> 3) * SBO_T + g4 * 128 + (r & 7) * 16);
     const float sgnA = a.opA == OP_C ? -1.f : 1.f, sgnB = a.opB == OP_C ? -1.f : 1.f;
     uint32_t g = 0;
-    for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
-      const long long b = w / ntile;
-      const int ct = (int)(w % ntile);
+    for (long long b = blockIdx.x; b < nitems && !*abort_flag; b += gridDim.x) {
       if (a.active && !a.active[b]) continue;
       const int* erow = a.scales + b * 256;
-      const int* fcol = erow + 128;
-      const int jc = ct * NT + j;
       float2 mA, mB;
       float scA, scB;
       digit_scale(r < m ? erow[r] : 0, sgnA, mA, scA);
-      digit_scale(jc < n ? fcol[jc] : 0, sgnB, mB, scB);
+      digit_scale(r < n ? erow[128 + r] : 0, sgnB, mB, scB);
       bool ok = true;
       for (int c = 0; c < nch; ++c, ++g) {
         const int rs = (int)(g % RSTAGES), ds = (int)(g % DSTAGES);
         if (!mbar_wait(&rfull[rs], (g / RSTAGES) & 1, abort_flag, tcount)) { ok = false; break; }
         const unsigned char* rA = raw + (size_t)rs * RSTAGE;
-        float2 xa[8], xb[4];
-        raw_read4(rA, args.layoutA, r, gA0, 128, xa);
-        raw_read4(rA, args.layoutA, r, gA0 + 2, 128, xa + 4);
-        raw_read4(rA + RAW_A, args.layoutB, j, gB, NT, xb);
-        // the slot goes back to the tensor memory accelerator: order these generic-proxy
-        // reads before its next (async-proxy) write into the slot
+        float2 xa[4], xb[4];
+        raw_read4(rA, args.layoutA, r, g4, xa);
+        raw_read4(rA + RAW_A, args.layoutB, r, g4, xb);
         fence_proxy_async();
         mbar_arrive(&rempty[rs]);
         if (!mbar_wait(&dempty[ds], ((g / DSTAGES) & 1) ^ 1, abort_flag, tcount)) {
@@ -1011,43 +995,30 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           break;
         }
         unsigned char* dA = dig + (size_t)ds * DSTAGE;
-        unsigned char* dBr = dA + S * APLANE;
-        unsigned char* dBi = dBr + S * BPLANE;
+        unsigned char* dBr = dA + S * PLANE;
+        unsigned char* dBi = dBr + S * PLANE;
+        uint32_t pa[S][4], pr[S][4], pi[S][4];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          uint32_t pk[S][4];
+        for (int u = 0; u < 4; ++u) {
+          float2 D[S];
+          digits_f32x2<S>(__fmul2_rn(xa[u], mA), scA, D);
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            float2 D[S];
-            digits_f32x2<S>(__fmul2_rn(xa[4 * h + u], mA), scA, D);
-#pragma unroll
-            for (int s2 = 0; s2 < S; ++s2) pk[s2][u] = pack_pair(D[s2]);  // (Re, Im)
-          }
-#pragma unroll
-          for (int s2 = 0; s2 < S; ++s2)
-            *reinterpret_cast<uint4*>(dA + (size_t)s2 * APLANE + (h ? offA1 : offA0)) =
-                make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
-        }
-        {
-          uint32_t pr[S][4], pi[S][4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            float2 D[S];
-            digits_f32x2<S>(__fmul2_rn(xb[u], mB), scB, D);
-#pragma unroll
-            for (int s2 = 0; s2 < S; ++s2) {
-              pr[s2][u] = pack_pair(D[s2]) ^ 0x80000000u;  // (Re, -Im): negating a digit is exact
-              pi[s2][u] = __byte_perm(__float_as_uint(D[s2].x), __float_as_uint(D[s2].y),
-                                      0x3276);             // (Im, Re)
-            }
-          }
+          for (int s2 = 0; s2 < S; ++s2) pa[s2][u] = pack_pair(D[s2]);
+          digits_f32x2<S>(__fmul2_rn(xb[u], mB), scB, D);
 #pragma unroll
           for (int s2 = 0; s2 < S; ++s2) {
-            *reinterpret_cast<uint4*>(dBr + (size_t)s2 * BPLANE + offB) =
-                make_uint4(pr[s2][0], pr[s2][1], pr[s2][2], pr[s2][3]);
-            *reinterpret_cast<uint4*>(dBi + (size_t)s2 * BPLANE + offB) =
-                make_uint4(pi[s2][0], pi[s2][1], pi[s2][2], pi[s2][3]);
+            pr[s2][u] = pack_pair(D[s2]) ^ 0x80000000u;
+            pi[s2][u] = __byte_perm(__float_as_uint(D[s2].x), __float_as_uint(D[s2].y), 0x3276);
           }
+        }
+#pragma unroll
+        for (int s2 = 0; s2 < S; ++s2) {
+          *reinterpret_cast<uint4*>(dA + (size_t)s2 * PLANE + off) =
+              make_uint4(pa[s2][0], pa[s2][1], pa[s2][2], pa[s2][3]);
+          *reinterpret_cast<uint4*>(dBr + (size_t)s2 * PLANE + off) =
+              make_uint4(pr[s2][0], pr[s2][1], pr[s2][2], pr[s2][3]);
+          *reinterpret_cast<uint4*>(dBi + (size_t)s2 * PLANE + off) =
+              make_uint4(pi[s2][0], pi[s2][1], pi[s2][2], pi[s2][3]);
         }
         fence_proxy_async();
         mbar_arrive(&dfull[ds]);
@@ -1055,16 +1026,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       if (!ok) break;
     }
   } else if (warp == MMA_WARP) {
-    // ======================== MMA issuer (one thread); item i uses TMEM columns
-    // [256 (i & 1), 256 (i & 1) + 256): Re level 0, Re levels 1-3, Im level 0, Im levels 1-3
+    // TMEM columns: [128 (2 part + level class)]: Re level 0, Re 1-3, Im level 0, Im 1-3
     if (lane == 0) {
       const uint32_t idesc = make_idesc(128, NT);
       uint32_t g = 0, li = 0;
-      for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
-        const long long b = w / ntile;
+      for (long long b = blockIdx.x; b < nitems && !*abort_flag; b += gridDim.x) {
         if (a.active && !a.active[b]) continue;
-        const int buf = (int)(li & 1);
-        if (!mbar_wait(&tempty[buf], ((li >> 1) & 1) ^ 1, abort_flag, tcount)) break;
+        if (!mbar_wait(tempty, (li & 1) ^ 1, abort_flag, tcount)) break;
         tc_fence_after();
         uint32_t touched = 0;
         bool ok = true;
@@ -1073,34 +1041,28 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           if (!mbar_wait(&dfull[ds], (g / DSTAGES) & 1, abort_flag, tcount)) { ok = false; break; }
           tc_fence_after();
           const uint32_t sA = smem_u32(dig + (size_t)ds * DSTAGE);
-          const uint32_t sB = sA + S * APLANE;
+          const uint32_t sB = sA + S * PLANE;
 #pragma unroll
-          for (int kk = 0; kk < 2; ++kk) {
+          for (int part = 0; part < 2; ++part) {
 #pragma unroll
-            for (int part = 0; part < 2; ++part) {
+            for (int s2 = 0; s2 < S; ++s2) {
 #pragma unroll
-              for (int s2 = 0; s2 < S; ++s2) {
-#pragma unroll
-                for (int t = 0; t < S; ++t) {
-                  if (s2 + t > L) continue;
-                  const int acc = 2 * part + (s2 + t > 0 ? 1 : 0);
-                  const uint64_t ad = tc::make_desc(sA + s2 * APLANE + kk * 256, 128, SBO_T);
-                  const uint64_t bd =
-                      tc::make_desc(sB + (part * S + t) * BPLANE + kk * 256, 128, SBO_T);
-                  umma(tmem + (uint32_t)(buf * 256 + acc * NT), ad, bd, idesc,
-                       (touched >> acc) & 1);
-                  touched |= 1u << acc;
-                }
+              for (int t = 0; t < S; ++t) {
+                if (s2 + t > L) continue;
+                const int acc = 2 * part + (s2 + t > 0 ? 1 : 0);
+                const uint64_t ad = tc::make_desc(sA + s2 * PLANE, 128, SBO_T);
+                const uint64_t bd = tc::make_desc(sB + (part * S + t) * PLANE, 128, SBO_T);
+                umma(tmem + (uint32_t)(acc * NT), ad, bd, idesc, (touched >> acc) & 1);
+                touched |= 1u << acc;
               }
             }
           }
           umma_commit(&dempty[ds]);
         }
         if (!ok) break;
-        umma_commit(&tfull[buf]);
+        umma_commit(tfull);
         ++li;
       }
-      // drain: every MMA issued by this thread has completed before TMEM is freed
       umma_commit(drain);
       int zero = 0;
       volatile int* never = &zero;
@@ -1108,17 +1070,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
     __syncwarp();
   } else {
-    // ======================== epilogue (warps 0-3 own TMEM lanes 0-127 = rows of C)
-    const int row = warp * 32 + lane;
-    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. (rows) for columns 64 (w / 4) ..
+    const int row = (warp & 3) * 32 + lane, half = warp >> 2;
+    const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
     const float alpha = (float)a.alpha_re, beta = (float)a.beta_re;
     uint32_t li = 0;
-    for (long long w = blockIdx.x; w < nitems && !*abort_flag; w += gridDim.x) {
-      const long long b = w / ntile;
-      const int ct = (int)(w % ntile);
+    for (long long b = blockIdx.x; b < nitems && !*abort_flag; b += gridDim.x) {
       if (a.active && !a.active[b]) continue;
-      const int buf = (int)(li & 1);
-      if (!mbar_wait(&tfull[buf], (li >> 1) & 1, abort_flag, tcount)) break;
+      if (!mbar_wait(tfull, li & 1, abort_flag, tcount)) break;
       tc_fence_after();
       const int* erow = a.scales + b * 256;
       const int* fcol = erow + 128;
@@ -1128,31 +1087,29 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       if (a.Z.p) z = *batch_ptr<const double2>(a.Z, b);
       const int ei = erow[row];
 #pragma unroll 1
-      for (int j0 = 0; j0 < NT; j0 += 16) {
+      for (int j0 = half * 64; j0 < half * 64 + 64; j0 += 16) {
         uint32_t v[4][16];
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
-          tmem_ld16(lane_base + (uint32_t)(buf * 256 + q * NT + j0), v[q]);
+        for (int q = 0; q < 4; ++q) tmem_ld16(lane_base + (uint32_t)(q * NT + j0), v[q]);
         tmem_wait_ld();
         if (row < m) {
 #pragma unroll
           for (int jj = 0; jj < 16; ++jj) {
-            const int jcol = ct * NT + j0 + jj;
+            const int jcol = j0 + jj;
             if (jcol < n) {
               const float2* d = D ? D + row + (long long)jcol * a.D.ld : nullptr;
               C[row + (long long)jcol * a.C.ld] =
-                  c64_pair(v[0][jj], v[1][jj], v[2][jj], v[3][jj], ei + fcol[jcol] - 16, alpha,
-                           beta, d, a.Z.p && row == jcol, z);
+                  c64_pair(v[0][jj], v[1][jj], v[2][jj], v[3][jj], ei + fcol[jcol] - 16,
+                                 alpha, beta, d, a.Z.p && row == jcol, z);
             }
           }
         }
       }
       tc_fence_before();
-      mbar_arrive(&tempty[buf]);
+      mbar_arrive(tempty);
       ++li;
     }
   }
-  // ---- teardown: every MMA has completed (drained above); free TMEM
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -1178,11 +1135,11 @@ EncodeTiled encode_tiled() {
   return fn;
 }
 
-// 3-D tensor map (floats, vectors or k, batch entry) of one complex64 operand.  A
-// batch reference qualifies when a tensor map can address it: no index array, a 16-byte
-// aligned base, and even leading dimension and batch stride (16-byte strides).
-bool make_map(CUtensorMap* map, const BatchRef& R, int layout, int vecs, int K, int boxv,
-              long long batch) {
+// 3-D tensor map (floats, vectors or k, batch entry) of one complex64 operand: boxes of 8
+// complex k x 128 vectors; K-major boxes (64-byte rows) take the 64-byte swizzle.  A batch
+// reference qualifies when a tensor map can address it: no index array, a 16-byte aligned
+// base, and even leading dimension and batch stride (16-byte strides).
+bool make_map(CUtensorMap* map, const BatchRef& R, int layout, int vecs, int K, long long batch) {
   const EncodeTiled fn = encode_tiled();
   if (!fn || !R.p || R.idx || (reinterpret_cast<uintptr_t>(R.p) & 15) || (R.ld & 1) ||
       (R.stride & 1) || R.ld < (layout == MN_MAJOR ? vecs : K))
@@ -1192,10 +1149,10 @@ bool make_map(CUtensorMap* map, const BatchRef& R, int layout, int vecs, int K, 
   cuuint32_t box[3], es[3] = {1, 1, 1};
   if (layout == MN_MAJOR) {
     dims[0] = 2 * (cuuint64_t)vecs; dims[1] = K;
-    box[0] = 2 * boxv; box[1] = KCC;
+    box[0] = 2 * 128; box[1] = KCC;
   } else {
     dims[0] = 2 * (cuuint64_t)K; dims[1] = vecs;
-    box[0] = 2 * KCC; box[1] = boxv;
+    box[0] = 2 * KCC; box[1] = 128;
   }
   box[2] = 1;
   const long long entries = R.stride == 0 ? 1 : (R.mod > 0 ? R.mod : batch);
@@ -1203,10 +1160,10 @@ bool make_map(CUtensorMap* map, const BatchRef& R, int layout, int vecs, int K, 
   strides[0] = ldb;
   strides[1] = R.stride == 0 ? ((ldb * dims[1] + 15) & ~(cuuint64_t)15)
                              : (cuuint64_t)R.stride * 8;
-  if (strides[1] < ldb * dims[1]) return false;  // entries must not overlap
+  if (strides[1] < ldb * dims[1]) return false;
   return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, R.p, dims, strides, box, es,
             CU_TENSOR_MAP_INTERLEAVE_NONE,
-            layout == K_MAJOR ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+            layout == K_MAJOR ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_NONE,
             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
@@ -1216,11 +1173,11 @@ cudaError_t launch(const GemmArgs& g, cudaStream_t s, bool* used) {
   *used = false;
   Args args;
   args.g = g;
-  args.layoutA = g.opA == OP_N ? MN_MAJOR : K_MAJOR;  // op(A) rows contiguous for N
-  args.layoutB = g.opB == OP_N ? K_MAJOR : MN_MAJOR;  // op(B) columns contiguous in k for N
+  args.layoutA = g.opA == OP_N ? MN_MAJOR : K_MAJOR;
+  args.layoutB = g.opB == OP_N ? K_MAJOR : MN_MAJOR;
   alignas(64) CUtensorMap ma, mb;
-  if (!make_map(&ma, g.A, args.layoutA, g.m, g.k, 128, g.batch) ||
-      !make_map(&mb, g.B, args.layoutB, g.n, g.k, NT, g.batch))
+  if (!make_map(&ma, g.A, args.layoutA, g.m, g.k, g.batch) ||
+      !make_map(&mb, g.B, args.layoutB, g.n, g.k, g.batch))
     return cudaSuccess;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -1231,8 +1188,7 @@ cudaError_t launch(const GemmArgs& g, cudaStream_t s, bool* used) {
   const long long gb = g.batch < 65535 ? g.batch : 65535;
   oz_scales_kernel<float2><<<dim3((unsigned)gb, 2), 256, 0, s>>>(g);
   count_launch();
-  const long long items = (long long)((g.n + NT - 1) / NT) * g.batch;
-  const int grid = (int)(items < sms ? items : sms);
+  const int grid = (int)(g.batch < sms ? g.batch : sms);
   zgemm_c64_tma_kernel<<<grid, NTHREADS, SMEM, s>>>(args, ma, mb);
   count_launch();
   *used = true;
@@ -1265,10 +1221,9 @@ constexpr int RSTAGE = RAW_A + RAW_B;
 constexpr uint32_t SBO_T = (2 * KCC / 8) * 128;  // 8-row groups of a digit plane (256 B)
 template <int S> struct Cfg {
   static constexpr int NACC = S;  // levels 0 .. S-1, one exact accumulator each
-  // One accumulator set per CTA.  A second set (the 4-digit product fits two) let the
-  // epilogue overlap the next item, but gave results that differed from run to run when
-  // the product had a beta D term; with one set the results are bit-reproducible.
-  static constexpr int NBUF = 1;
+  // Two accumulator sets where they fit the 512 TMEM columns (the 4-digit product): the
+  // epilogue of one item then runs while the next item's products are issued.
+  static constexpr int NBUF = 2 * NACC * NT <= 512 ? 2 : 1;
   static constexpr int DSTAGE = S * (APLANE + BPLANE);
   static constexpr int SMEM = 1024 + RSTAGES * RSTAGE + DSTAGES * DSTAGE + 256;
   static_assert(SMEM <= 232448, "shared memory");
