@@ -500,10 +500,10 @@ def run_ours(a):
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp) and dom[0]:
         with open(tp) as f:
-            bpp = json.load(f).get("zgemm_oz_c64_dram_bytes_per_product")
+            bpp = json.load(f).get("zgemm_c64_tma_dram_bytes_per_product")
         if bpp:
             traffic = bpp * (dom[2] / (8.0 * NM ** 3)) / dom[0]
-    roofline = {"kernel": "zgemm_oz_kernel<4,3,float2,float2> (complex64 split product)",
+    roofline = {"kernel": "zgemm_c64_tma_kernel (complex64 4-digit split product, TMA-fed)",
                 "bound": "tensor", "achieved": alg_tf, "peak": peak, "unit": "TFLOP/s",
                 "frac": alg_tf / peak if peak else None, "traffic": traffic,
                 "peak_source": f"bf16_tflops_sustained of {pk_kind}",
