@@ -21,10 +21,6 @@ struct GemmArgs {
   // split-precision waits that time out are counted here; null: the library-wide counter
   // read by oz_timeouts_and_reset()
   int* timeouts = nullptr;
-  // optional scratch for the complex64 product's op(B) digit planes when one B is shared by
-  // many batch entries (null: op(B) is split inside the product)
-  void* bsplit = nullptr;
-  long long bsplit_bytes = 0;
 };
 
 cudaError_t zgemm_f64(const GemmArgs& a, cudaStream_t s);

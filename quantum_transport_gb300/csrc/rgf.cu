@@ -220,9 +220,6 @@ __global__ void flat_d2f_kernel(const double2* x, float2* y, long long count) {
 // <= 128, inverses by the 2 x 2 block form over such tiles.
 constexpr int SPLIT_TILE = 128;
 constexpr int MAX_SPLIT = 3 * SPLIT_TILE;
-// scratch for the digit planes of a shared op(B) in the complex64 sweep's products: 32 KB per
-// 8-k chunk, 16 chunks per 128-orbital block, room for 64 distinct blocks (k-points)
-constexpr size_t BSPLIT_BYTES = (size_t)64 * 16 * 32768;
 
 template <typename TC>
 struct Ops {
@@ -234,8 +231,6 @@ struct Ops {
   const cd* one = nullptr;  // device scalar (1, 0)
   Prof* prof = nullptr;     // optional launch timing
   int* scales = nullptr;    // P * 256 ints: exponent scratch of the split product
-  void* bsplit = nullptr;   // complex64 products: digit planes of a shared op(B) (may be null)
-  long long bsplit_bytes = 0;
   TC* rt1 = nullptr;        // P * n*n refinement scratch
   TC* rt2 = nullptr;
   long long P = 0;
@@ -320,8 +315,6 @@ struct Ops {
     g.batch = batch;
     g.active = active;
     g.scales = scales;
-    g.bsplit = bsplit;
-    g.bsplit_bytes = bsplit_bytes;
     if (prec != QT_PREC_FP64 && (!scales || batch > P)) QT_FAIL(QT_ERR_ARG, "split product scratch too small");
     cudaError_t e;
     const bool timed = prof && prof->on;
@@ -503,8 +496,7 @@ size_t wave_bytes(const Problem& pb, long long P) {
   const size_t sweep = (2 * (size_t)pb.nx + 14 + 2) * tc;  // g_l, g^<_l, temporaries, refinement
   const size_t lead = (2 * (7 + 2) + 6) * 16;  // Sancho state + refinement of both leads + contact
   const size_t guard = tc == 8 ? 16 : 0;        // complex128 workspace of the inverse guard
-  return (sweep + lead + guard) * nm2 * P + (size_t)P * 4096 + (512 << 10) +
-         (tc == 8 ? BSPLIT_BYTES : 0);
+  return (sweep + lead + guard) * nm2 * P + (size_t)P * 4096 + (512 << 10);
 }
 
 // Batched Sancho-Rubio on the wave (complex128 state).  H00 per point, H_10 the
@@ -671,17 +663,14 @@ qt_status solve_wave(qt_ctx* ctx, const Problem& pb, long long p0, long long P, 
   int* scales = ar.take<int>((size_t)P * 256);       // split-product exponent scratch
   unsigned char* guard = ar.take<unsigned char>((size_t)2 * P);  // both leads' 2P entries
   cd* fbw = sizeof(TC) == 8 ? ar.take<cd>((size_t)P * nm2) : nullptr;
-  const size_t bsb = sizeof(TC) == 8 ? BSPLIT_BYTES : 0;
-  void* bsplit = bsb ? ar.take<unsigned char>(bsb) : nullptr;
   if (!zint || !zlead || !fl || !fr || !fe || !one || !status || !gl_all || !gln_all || !tmp ||
-      !rt1 || !rt2 || !cbuf || !scales || !guard || (sizeof(TC) == 8 && (!fbw || !bsplit)))
+      !rt1 || !rt2 || !cbuf || !scales || !guard || (sizeof(TC) == 8 && !fbw))
     QT_FAIL(QT_ERR_NOMEM, "wave arena exhausted");
   // sweep operations on TC, contact operations on complex128
   Ops<TC> op{s, n, pb.prec};
   op.slices = pb.sweep_slices;
   op.refine = split ? pb.sweep_refine : 0;
   op.one = one; op.rt1 = rt1; op.rt2 = rt2; op.P = P; op.scales = scales;
-  op.bsplit = bsplit; op.bsplit_bytes = (long long)bsb;
   op.prof = &ctx->prof;
   op.guard = guard; op.fbw = fbw; op.fallbacks = ctx->fallbacks;
   Ops<double2> cop{s, n, pb.prec};
@@ -1837,15 +1826,10 @@ extern "C" qt_status qt_zgemm_batch(qt_ctx* ctx, int n, int batch, char opA, con
         be.y != 0.0)
       QT_FAIL(QT_ERR_UNSUPPORTED,
               "complex64 product: device pointers, QT_PREC_MIXED, 4 digits, real alpha/beta");
-    // exponent scratch, then room for the digit planes of a shared op(B) (one 128-orbital
-    // block: 16 chunks of 32 KB)
-    const size_t sc_bytes = ((size_t)batch * 1024 + 4095) & ~(size_t)4095, bs_bytes = 16 * 32768;
-    QT_TRY(ensure(ctx->arena, ctx->arena_bytes, sc_bytes + bs_bytes));
+    QT_TRY(ensure(ctx->arena, ctx->arena_bytes, (size_t)batch * 1024 + 4096));
     Ops<float2> op{s, n, prec};
     op.slices = 4;
     op.scales = reinterpret_cast<int*>(ctx->arena);
-    op.bsplit = static_cast<char*>(ctx->arena) + sc_bytes;
-    op.bsplit_bytes = (long long)bs_bytes;
     op.P = batch;
     op.prof = &ctx->prof;
     QT_TRY(op.gemm3(n, n, n, ref(A, a_stride, n), oa, ref(B, b_stride, n), ob,

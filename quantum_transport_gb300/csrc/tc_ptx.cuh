@@ -144,15 +144,5 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const void* tmap, int c0,
       : "memory");
 }
 
-// untiled bulk copy of `bytes` (a multiple of 16; both addresses 16-byte aligned) from
-// global memory into dst; complete_tx on bar
-__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes,
-                                          uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-
 }  // namespace tc
 }  // namespace qt

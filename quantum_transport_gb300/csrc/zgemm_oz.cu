@@ -815,18 +815,6 @@ constexpr uint32_t SBO_T = (2 * KCC / 8) * 128;  // 8-row groups of a digit plan
 constexpr int SMEM = 1024 + RSTAGES * RSTAGE + DSTAGES * DSTAGE + 256;
 static_assert(SMEM <= 232448, "shared memory");
 static_assert(RAW_A % 1024 == 0 && RSTAGE % 1024 == 0, "swizzled boxes need 1 KB alignment");
-// With op(B) split ahead of the product (one B shared by many batch entries, e.g. the
-// slabs' H): a raw slot holds op(A)'s raw tile and the stage's ready B'_r, B'_i digit planes
-// (copied by one untiled bulk copy and read by the MMAs in place), a digit stage only A'.
-constexpr int BSPLIT = 2 * S * PLANE;  // B'_r and B'_i planes of one stage: 32 KB
-template <bool PB> struct Lay {
-  static constexpr int RST = PB ? 4 : RSTAGES;
-  static constexpr int RSTG = PB ? RAW_A + BSPLIT : RSTAGE;
-  static constexpr int DSTG = PB ? S * PLANE : DSTAGE;
-  static constexpr int SMEM = 1024 + RST * RSTG + DSTAGES * DSTG + 256;
-  static_assert(SMEM <= 232448, "shared memory");
-  static_assert(RSTG % 1024 == 0, "swizzled boxes need 1 KB alignment");
-};
 
 // operand tile layout in a raw slot
 enum { MN_MAJOR = 0, K_MAJOR = 1 };
@@ -898,11 +886,9 @@ __device__ __forceinline__ float2 c64_pair(uint32_t r0, uint32_t r1, uint32_t i0
   return __fadd2_rn(v, w);
 }
 
-template <bool PB>
 __global__ void __launch_bounds__(NTHREADS, 1)
     zgemm_c64_tma_kernel(const __grid_constant__ Args args, const __grid_constant__ CUtensorMap tmA,
                           const __grid_constant__ CUtensorMap tmB) {
-  constexpr int RSTAGES = Lay<PB>::RST, RSTAGE = Lay<PB>::RSTG, DSTAGE = Lay<PB>::DSTG;
   const GemmArgs& a = args.g;
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
@@ -928,12 +914,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
   if (tid == 0) {
     for (int s = 0; s < DSTAGES; ++s) { mbar_init(&dfull[s], NPROD); mbar_init(&dempty[s], 1); }
-    // a slot is free once the producers have read op(A) and, with pre-split B, the MMAs
-    // that read its B planes have completed (one commit)
-    for (int s = 0; s < RSTAGES; ++s) {
-      mbar_init(&rfull[s], 1);
-      mbar_init(&rempty[s], NPROD + (PB ? 1 : 0));
-    }
+    for (int s = 0; s < RSTAGES; ++s) { mbar_init(&rfull[s], 1); mbar_init(&rempty[s], NPROD); }
     mbar_init(tfull, 1);
     mbar_init(tempty, NEPI);
     mbar_init(drain, 1);
@@ -943,7 +924,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   if (warp == MMA_WARP) tc::tmem_alloc(tmem_slot, 512);
   if (warp == LOAD_WARP && lane == 0) {
     tc::prefetch_tmap(&tmA);
-    if (!PB) tc::prefetch_tmap(&tmB);
+    tc::prefetch_tmap(&tmB);
   }
   tc_fence_before();
   __syncthreads();
@@ -972,10 +953,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           const int k0 = c * KCC;
           if (args.layoutA == MN_MAJOR) tc::tma_load_3d(dA, &tmA, 0, k0, ea, &rfull[slot]);
           else tc::tma_load_3d(dA, &tmA, 2 * k0, 0, ea, &rfull[slot]);
-          if (PB)
-            tc::bulk_load(dB, static_cast<const unsigned char*>(a.bsplit) +
-                                  ((long long)eb * nch + c) * BSPLIT, BSPLIT, &rfull[slot]);
-          else if (args.layoutB == MN_MAJOR) tc::tma_load_3d(dB, &tmB, 0, k0, eb, &rfull[slot]);
+          if (args.layoutB == MN_MAJOR) tc::tma_load_3d(dB, &tmB, 0, k0, eb, &rfull[slot]);
           else tc::tma_load_3d(dB, &tmB, 2 * k0, 0, eb, &rfull[slot]);
           pend[slot] = true;
           pend_parity[slot] = ph;
@@ -1009,7 +987,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const unsigned char* rA = raw + (size_t)rs * RSTAGE;
         float2 xa[4], xb[4];
         raw_read4(rA, args.layoutA, r, g4, xa);
-        if (!PB) raw_read4(rA + RAW_A, args.layoutB, r, g4, xb);
+        raw_read4(rA + RAW_A, args.layoutB, r, g4, xb);
         fence_proxy_async();
         mbar_arrive(&rempty[rs]);
         if (!mbar_wait(&dempty[ds], ((g / DSTAGES) & 1) ^ 1, abort_flag, tcount)) {
@@ -1017,39 +995,30 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           break;
         }
         unsigned char* dA = dig + (size_t)ds * DSTAGE;
-        uint32_t pa[S][4];
+        unsigned char* dBr = dA + S * PLANE;
+        unsigned char* dBi = dBr + S * PLANE;
+        uint32_t pa[S][4], pr[S][4], pi[S][4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           float2 D[S];
           digits_f32x2<S>(__fmul2_rn(xa[u], mA), scA, D);
 #pragma unroll
           for (int s2 = 0; s2 < S; ++s2) pa[s2][u] = pack_pair(D[s2]);
-        }
-#pragma unroll
-        for (int s2 = 0; s2 < S; ++s2)
-          *reinterpret_cast<uint4*>(dA + (size_t)s2 * PLANE + off) =
-              make_uint4(pa[s2][0], pa[s2][1], pa[s2][2], pa[s2][3]);
-        if (!PB) {
-          uint32_t pr[S][4], pi[S][4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            float2 D[S];
-            digits_f32x2<S>(__fmul2_rn(xb[u], mB), scB, D);
-#pragma unroll
-            for (int s2 = 0; s2 < S; ++s2) {
-              pr[s2][u] = pack_pair(D[s2]) ^ 0x80000000u;
-              pi[s2][u] = __byte_perm(__float_as_uint(D[s2].x), __float_as_uint(D[s2].y), 0x3276);
-            }
-          }
-          unsigned char* dBr = dA + S * PLANE;
-          unsigned char* dBi = dBr + S * PLANE;
+          digits_f32x2<S>(__fmul2_rn(xb[u], mB), scB, D);
 #pragma unroll
           for (int s2 = 0; s2 < S; ++s2) {
-            *reinterpret_cast<uint4*>(dBr + (size_t)s2 * PLANE + off) =
-                make_uint4(pr[s2][0], pr[s2][1], pr[s2][2], pr[s2][3]);
-            *reinterpret_cast<uint4*>(dBi + (size_t)s2 * PLANE + off) =
-                make_uint4(pi[s2][0], pi[s2][1], pi[s2][2], pi[s2][3]);
+            pr[s2][u] = pack_pair(D[s2]) ^ 0x80000000u;
+            pi[s2][u] = __byte_perm(__float_as_uint(D[s2].x), __float_as_uint(D[s2].y), 0x3276);
           }
+        }
+#pragma unroll
+        for (int s2 = 0; s2 < S; ++s2) {
+          *reinterpret_cast<uint4*>(dA + (size_t)s2 * PLANE + off) =
+              make_uint4(pa[s2][0], pa[s2][1], pa[s2][2], pa[s2][3]);
+          *reinterpret_cast<uint4*>(dBr + (size_t)s2 * PLANE + off) =
+              make_uint4(pr[s2][0], pr[s2][1], pr[s2][2], pr[s2][3]);
+          *reinterpret_cast<uint4*>(dBi + (size_t)s2 * PLANE + off) =
+              make_uint4(pi[s2][0], pi[s2][1], pi[s2][2], pi[s2][3]);
         }
         fence_proxy_async();
         mbar_arrive(&dfull[ds]);
@@ -1068,18 +1037,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         uint32_t touched = 0;
         bool ok = true;
         for (int c = 0; c < nch; ++c, ++g) {
-          const int ds = (int)(g % DSTAGES), rs = (int)(g % RSTAGES);
+          const int ds = (int)(g % DSTAGES);
           if (!mbar_wait(&dfull[ds], (g / DSTAGES) & 1, abort_flag, tcount)) { ok = false; break; }
-          // pre-split B: the planes arrived by bulk copy into the raw slot; the producers'
-          // arrival on dfull already implies the slot's copies completed, and this wait makes
-          // them visible to this thread as well
-          if (PB && !mbar_wait(&rfull[rs], (g / RSTAGES) & 1, abort_flag, tcount)) {
-            ok = false;
-            break;
-          }
           tc_fence_after();
           const uint32_t sA = smem_u32(dig + (size_t)ds * DSTAGE);
-          const uint32_t sB = PB ? smem_u32(raw + (size_t)rs * RSTAGE + RAW_A) : sA + S * PLANE;
+          const uint32_t sB = sA + S * PLANE;
 #pragma unroll
           for (int part = 0; part < 2; ++part) {
 #pragma unroll
@@ -1096,7 +1058,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
           }
           umma_commit(&dempty[ds]);
-          if (PB) umma_commit(&rempty[rs]);  // the slot's B planes are read
         }
         if (!ok) break;
         umma_commit(tfull);
@@ -1206,63 +1167,8 @@ bool make_map(CUtensorMap* map, const BatchRef& R, int layout, int vecs, int K, 
             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// op(B) split ahead of the product, once per distinct B entry (a B shared by the batch,
-// e.g. the slabs' H): the B'_r, B'_i planes of chunk c of entry e go to
-// out + (e nch + c) BSPLIT in the shared-memory layout the MMAs read.  Each column's exponent
-// bound is taken here from the column itself: the scale prologue's value for every batch
-// entry that uses this B entry, so the digits are the producers' bit for bit.
-__global__ void __launch_bounds__(256) presplit_b_kernel(GemmArgs a, int nch, unsigned char* out) {
-  __shared__ unsigned long long part[256];
-  const int tid = threadIdx.x, j = tid & 127, g4 = tid >> 7;
-  const int e = blockIdx.x;
-  const int n = a.n, K = a.k, ld = a.B.ld;
-  const float2* B = reinterpret_cast<const float2*>(a.B.p) + (long long)e * a.B.stride;
-  const bool opN = a.opB == OP_N;
-  auto elem = [&](int k) {  // element (k, j) of op(B) before conjugation
-    return opN ? B[k + (long long)j * ld] : B[j + (long long)k * ld];
-  };
-  unsigned long long mx = 0;
-  if (j < n)
-    for (int k = g4; k < K; k += 2) {
-      const float2 x = elem(k);
-      mx = max(mx, max(absbits(x, 0), absbits(x, 1)));
-    }
-  part[tid] = mx;
-  __syncthreads();
-  const int f = j < n ? exp_bound_bits<float2>(max(part[j], part[j + 128])) : 0;
-  float2 mB;
-  float scB;
-  digit_scale(f, a.opB == OP_C ? -1.f : 1.f, mB, scB);
-  const uint32_t off = (uint32_t)((j >> 3) * SBO_T + g4 * 128 + (j & 7) * 16);
-  for (int c = 0; c < nch; ++c) {
-    uint32_t pr[S][4], pi[S][4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int k = c * KCC + 4 * g4 + u;
-      const float2 x = (j < n && k < K) ? elem(k) : make_float2(0.f, 0.f);
-      float2 D[S];
-      digits_f32x2<S>(__fmul2_rn(x, mB), scB, D);
-#pragma unroll
-      for (int s2 = 0; s2 < S; ++s2) {
-        pr[s2][u] = pack_pair(D[s2]) ^ 0x80000000u;
-        pi[s2][u] = __byte_perm(__float_as_uint(D[s2].x), __float_as_uint(D[s2].y), 0x3276);
-      }
-    }
-    unsigned char* o = out + ((long long)e * nch + c) * BSPLIT;
-#pragma unroll
-    for (int s2 = 0; s2 < S; ++s2) {
-      *reinterpret_cast<uint4*>(o + (size_t)s2 * PLANE + off) =
-          make_uint4(pr[s2][0], pr[s2][1], pr[s2][2], pr[s2][3]);
-      *reinterpret_cast<uint4*>(o + (size_t)(S + s2) * PLANE + off) =
-          make_uint4(pi[s2][0], pi[s2][1], pi[s2][2], pi[s2][3]);
-    }
-  }
-}
-
 // Launches the TMA-fed product when both operands qualify; *used = false otherwise (the
-// caller then runs the register-staged kernel).  op(B) is split ahead (presplit_b_kernel)
-// when at most a quarter as many distinct B entries as batch entries exist and the caller's
-// scratch holds their planes; QT_PRESPLIT=0 turns this off (for comparisons).
+// caller then runs the register-staged kernel).
 cudaError_t launch(const GemmArgs& g, cudaStream_t s, bool* used) {
   *used = false;
   Args args;
@@ -1270,36 +1176,20 @@ cudaError_t launch(const GemmArgs& g, cudaStream_t s, bool* used) {
   args.layoutA = g.opA == OP_N ? MN_MAJOR : K_MAJOR;
   args.layoutB = g.opB == OP_N ? K_MAJOR : MN_MAJOR;
   alignas(64) CUtensorMap ma, mb;
-  if (!make_map(&ma, g.A, args.layoutA, g.m, g.k, g.batch)) return cudaSuccess;
-  const long long entriesB = g.B.stride == 0 ? 1 : (g.B.mod > 0 ? g.B.mod : g.batch);
-  const int nch = (g.k + KCC - 1) / KCC;
-  const char* off_env = getenv("QT_PRESPLIT");
-  const bool pb = g.bsplit && !g.B.idx && g.B.p && entriesB * 4 <= g.batch &&
-                  entriesB * nch * (long long)BSPLIT <= g.bsplit_bytes &&
-                  (reinterpret_cast<uintptr_t>(g.bsplit) & 15) == 0 &&
-                  !(off_env && off_env[0] == '0');
-  if (!pb && !make_map(&mb, g.B, args.layoutB, g.n, g.k, g.batch)) return cudaSuccess;
+  if (!make_map(&ma, g.A, args.layoutA, g.m, g.k, g.batch) ||
+      !make_map(&mb, g.B, args.layoutB, g.n, g.k, g.batch))
+    return cudaSuccess;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int smem = pb ? Lay<true>::SMEM : Lay<false>::SMEM;
-  cudaError_t e = pb ? cudaFuncSetAttribute(zgemm_c64_tma_kernel<true>,
-                                            cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
-                     : cudaFuncSetAttribute(zgemm_c64_tma_kernel<false>,
-                                            cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaError_t e = cudaFuncSetAttribute(zgemm_c64_tma_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
   if (e != cudaSuccess) return e;
   const long long gb = g.batch < 65535 ? g.batch : 65535;
   oz_scales_kernel<float2><<<dim3((unsigned)gb, 2), 256, 0, s>>>(g);
   count_launch();
   const int grid = (int)(g.batch < sms ? g.batch : sms);
-  if (pb) {
-    presplit_b_kernel<<<(unsigned)entriesB, 256, 0, s>>>(g, nch,
-                                                       static_cast<unsigned char*>(g.bsplit));
-    count_launch();
-    zgemm_c64_tma_kernel<true><<<grid, NTHREADS, smem, s>>>(args, ma, ma);
-  } else {
-    zgemm_c64_tma_kernel<false><<<grid, NTHREADS, smem, s>>>(args, ma, mb);
-  }
+  zgemm_c64_tma_kernel<<<grid, NTHREADS, SMEM, s>>>(args, ma, mb);
   count_launch();
   *used = true;
   return cudaGetLastError();

@@ -183,42 +183,3 @@ def test_raw_slot_reuse_repeats_bitwise(ctx, kind, slices):
            + (2.0 ** -23 if kind == "c64" else 4e-16) * np.abs(exact)
            + 2 * n * 2.0 ** -53 * (np.abs(Ah) @ np.abs(Bh)))
     assert (np.abs(got - exact) <= tol).all()
-
-
-@pytest.mark.parametrize("n", [128, 120, 96, 88, 64])
-@pytest.mark.parametrize("opb", ["N", "C"])
-def test_c64_presplit_shared_operand_same_bits(ctx, n, opb, monkeypatch):
-    """A shared op(B) (stride 0, as H in the sweep) is split once, ahead of the product, into
-    the digit planes the MMAs read; the result equals the in-kernel split bit for bit
-    (QT_PRESPLIT=0 turns the pre-split off), repeats bit for bit, and meets the bound."""
-    import torch
-    from quantum_transport_gb300 import _lib
-    from quantum_transport_gb300.rgf import _ptr
-    lib = ctx._lib
-    batch = 300
-    g = torch.Generator(device="cuda").manual_seed(n + len(opb))
-    A = torch.randn(batch, n, n, dtype=torch.complex64, device="cuda", generator=g)
-    B = torch.randn(1, n, n, dtype=torch.complex64, device="cuda", generator=g)
-    B[0, :, 3] *= 1e3  # columns of different magnitude
-    D = torch.randn(batch, n, n, dtype=torch.complex64, device="cuda", generator=g)
-    al, be = np.array([-1.0, 0.0]), np.array([0.5, 0.0])
-    flags = _lib.QT_FLAG_DEVICE_POINTERS | _lib.QT_FLAG_SYNC | _lib.QT_FLAG_COMPLEX64
-
-    def run():
-        C = torch.zeros_like(A)
-        _lib.check(lib.qt_zgemm_batch(ctx.handle, n, batch, b"N", _ptr(A), n * n, opb.encode(),
-                                      _ptr(B), 0, _ptr(al), _ptr(be), _ptr(D), n * n, _ptr(C),
-                                      n * n, _lib.QT_PREC_MIXED, 4, flags))
-        return C
-
-    pre = [run() for _ in range(3)]
-    monkeypatch.setenv("QT_PRESPLIT", "0")
-    inner = run()
-    monkeypatch.delenv("QT_PRESPLIT")
-    assert all(torch.equal(pre[0], p) for p in pre[1:])
-    assert torch.equal(pre[0], inner)
-    Ah, Bh, Dh = _host(A), _host(B), _host(D)
-    exact = -(Ah @ OP[opb](Bh)) + 0.5 * Dh
-    tol = (2.0 ** -28 * _bound(Ah, np.broadcast_to(Bh, Ah.shape), "N", opb)
-           + 2.0 ** -23 * (np.abs(exact) + 0.5 * np.abs(Dh)))
-    assert (np.abs(_host(pre[0]) - exact) <= tol).all()
