@@ -45,18 +45,47 @@ __global__ void twiddle_kernel(double2* tw) {
   }
 }
 
-// in-place iterative radix-2 DIT on bit-reversed input; sign -1 forward, +1 inverse
+__device__ __forceinline__ void butterfly(double2& u, double2& v, double2 w) {
+  const double2 x = u, y = dmul(v, w);
+  u = make_double2(x.x + y.x, x.y + y.y);
+  v = make_double2(x.x - y.x, x.y - y.y);
+}
+
+// in-place iterative radix-2 DIT on bit-reversed input; sign -1 forward, +1 inverse.
+// Stages go through shared memory in pairs: a thread takes the four elements
+// base + {0, h, 2h, 3h} of a 4h-block, applies stage s to (0, h) and (2h, 3h) and stage s+1
+// to (0, 2h) and (h, 3h) in registers -- the same butterflies with the same twiddles as two
+// radix-2 passes, so the same bits, with half the shared-memory passes and barriers.  An odd
+// stage count starts with one single radix-2 pass.
 __device__ void fft_smem(double2* a, int L, int logL, const double2* tw, bool inverse) {
-  for (int s = 1; s <= logL; ++s) {
-    const int m = 1 << s, h = m >> 1, step = LMAX / m;
+  const double sg = inverse ? -1.0 : 1.0;
+  int s = 1;
+  if (logL & 1) {
     for (int t = threadIdx.x; t < L / 2; t += blockDim.x) {
+      const int i0 = 2 * t;
+      const double2 w = make_double2(tw[0].x, sg * tw[0].y);
+      butterfly(a[i0], a[i0 + 1], w);
+    }
+    __syncthreads();
+    s = 2;
+  }
+  for (; s < logL; s += 2) {
+    const int h = 1 << (s - 1);
+    const int step1 = LMAX / (2 * h), step2 = LMAX / (4 * h);
+    for (int t = threadIdx.x; t < L / 4; t += blockDim.x) {
       const int grp = t >> (s - 1), k = t & (h - 1);
-      const int i0 = grp * m + k, i1 = i0 + h;
-      double2 w = tw[k * step];
-      if (inverse) w.y = -w.y;
-      const double2 u = a[i0], v = dmul(a[i1], w);
-      a[i0] = make_double2(u.x + v.x, u.y + v.y);
-      a[i1] = make_double2(u.x - v.x, u.y - v.y);
+      const int b = grp * 4 * h + k;
+      double2 e0 = a[b], e1 = a[b + h], e2 = a[b + 2 * h], e3 = a[b + 3 * h];
+      const double2 w1 = tw[k * step1], w2a = tw[k * step2], w2b = tw[(k + h) * step2];
+      const double2 v1 = make_double2(w1.x, sg * w1.y);
+      butterfly(e0, e1, v1);  // stage s
+      butterfly(e2, e3, v1);
+      butterfly(e0, e2, make_double2(w2a.x, sg * w2a.y));  // stage s + 1
+      butterfly(e1, e3, make_double2(w2b.x, sg * w2b.y));
+      a[b] = e0;
+      a[b + h] = e1;
+      a[b + 2 * h] = e2;
+      a[b + 3 * h] = e3;
     }
     __syncthreads();
   }
