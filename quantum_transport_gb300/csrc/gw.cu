@@ -205,6 +205,218 @@ __global__ void __launch_bounds__(FFT_NT) zcorrconv_kernel(CorrConvArgs a, const
   }
 }
 
+// ---- packed transforms of purely imaginary series (one k-point)
+__device__ __forceinline__ double2 dconj(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ double2 dadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 dsub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 dscale(double2 a, double c) { return make_double2(c * a.x, c * a.y); }
+__device__ __forceinline__ double2 times_i(double2 a) { return make_double2(-a.y, a.x); }
+
+// the transforms of the real sequences a, b packed as z = a + i b: from Z(k) and Z(L - k),
+// A(k) = (Z(k) + conj Z(L-k))/2, B(k) = (Z(k) - conj Z(L-k))/(2i)
+__device__ __forceinline__ void unpack(double2 zk, double2 zkk, double2& A, double2& B) {
+  const double2 q = dconj(zkk);
+  A = dscale(dadd(zk, q), 0.5);
+  const double2 d = dscale(dsub(zk, q), 0.5);
+  B = make_double2(d.y, -d.x);  // d / i
+}
+
+// in-place bit-reversal permutation (natural order -> the FFT's bit-reversed input)
+__device__ __forceinline__ void bitrev_permute(double2* a, int L, int logL) {
+  for (int t = threadIdx.x; t < L; t += blockDim.x) {
+    const int r = (int)(__brev((unsigned)t) >> (32 - logL));
+    if (t < r) {
+      const double2 x = a[t];
+      a[t] = a[r];
+      a[r] = x;
+    }
+  }
+}
+
+// element (series r, partner rt) of one energy series; false outside the band
+__device__ __forceinline__ bool series_of(const GwFusedArgs& a, long long r, long long& rt) {
+  const long long nm2 = (long long)a.nm * a.nm, nel = a.nel ? a.nel : nm2;
+  const long long ix = r / nel, el = r - ix * nel, ij = a.ij0 + el;
+  const int i = (int)(ij % a.nm), j = (int)(ij / a.nm);
+  rt = ix * nel + i * (long long)a.nm + j;
+  return a.ndiag < 0 || abs(i - j) <= a.ndiag;
+}
+
+// P^<, P^>, P^R of one series per CTA: three packed forward transforms
+// (G^<, G^>), (rev G^>t, rev G^<t), (G^R, rev conj G^R) of the imaginary parts, the three
+// products per frequency, three inverse transforms.  Each product of two imaginary series'
+// transforms is -A B of their imaginary parts' transforms.
+__global__ void __launch_bounds__(FFT_NT) gw_pol_kernel(GwFusedArgs a, const double2* tw) {
+  extern __shared__ double2 sm[];
+  const int n = a.n, L = a.L, logL = a.logL;
+  double2 *b0 = sm, *b1 = sm + L, *b2 = sm + 2 * L;
+  const double2* GR = reinterpret_cast<const double2*>(a.GR);
+  const double2* GL = reinterpret_cast<const double2*>(a.GL);
+  const double2* GG = reinterpret_cast<const double2*>(a.GG);
+  const double2* GLt = reinterpret_cast<const double2*>(a.GLt ? a.GLt : a.GL);
+  const double2* GGt = reinterpret_cast<const double2*>(a.GGt ? a.GGt : a.GG);
+  double2* P[3] = {reinterpret_cast<double2*>(a.PL), reinterpret_cast<double2*>(a.PG),
+                   reinterpret_cast<double2*>(a.PR)};
+  const long long es = a.estride;
+  const double inv = 1.0 / L;
+  const double2 sc = make_double2(a.scale_re * inv, a.scale_im * inv);
+  for (long long r = blockIdx.x; r < a.nseries; r += gridDim.x) {
+    long long rt;
+    if (!series_of(a, r, rt)) {
+      for (int m = threadIdx.x; m < n; m += blockDim.x)
+        for (int q = 0; q < 3; ++q) P[q][(long long)m * es + r] = make_double2(0.0, 0.0);
+      continue;  // uniform over the CTA
+    }
+    const long long rp = a.GLt ? r : rt;  // where the transposed partner is stored
+    for (int t = threadIdx.x; t < L; t += blockDim.x) {
+      const int p = (int)(__brev((unsigned)t) >> (32 - logL));
+      double2 z0 = make_double2(0.0, 0.0), z1 = z0, z2 = z0;
+      if (t < n) {
+        const long long f = (long long)t * es, bk = (long long)(n - 1 - t) * es;
+        z0 = make_double2(GL[f + r].y, GG[f + r].y);
+        z1 = make_double2(GGt[bk + rp].y, GLt[bk + rp].y);
+        z2 = make_double2(GR[f + r].y, -GR[bk + r].y);  // Im conj G^R(n-1-t) = -Im G^R(n-1-t)
+      }
+      b0[p] = z0;
+      b1[p] = z1;
+      b2[p] = z2;
+    }
+    __syncthreads();
+    fft_smem(b0, L, logL, tw, false);
+    fft_smem(b1, L, logL, tw, false);
+    fft_smem(b2, L, logL, tw, false);
+    for (int k = threadIdx.x; k <= L / 2; k += blockDim.x) {
+      const int kk = (L - k) & (L - 1);
+      double2 A1, B1, A2, B2, A3, B3;
+      unpack(b0[k], b0[kk], A1, B1);
+      unpack(b1[k], b1[kk], A2, B2);
+      unpack(b2[k], b2[kk], A3, B3);
+      const double2 pl = dscale(dmul(A1, A2), -1.0);
+      const double2 pg = dscale(dmul(B1, B2), -1.0);
+      const double2 pr = dscale(dadd(dmul(A1, B3), dmul(A3, B2)), -1.0);
+      b0[k] = pl; b1[k] = pg; b2[k] = pr;
+      if (kk != k) {  // the transforms of real sequences' products: Hermitian
+        b0[kk] = dconj(pl); b1[kk] = dconj(pg); b2[kk] = dconj(pr);
+      }
+    }
+    __syncthreads();
+    bitrev_permute(b0, L, logL);
+    bitrev_permute(b1, L, logL);
+    bitrev_permute(b2, L, logL);
+    __syncthreads();
+    fft_smem(b0, L, logL, tw, true);
+    fft_smem(b1, L, logL, tw, true);
+    fft_smem(b2, L, logL, tw, true);
+    for (int m = threadIdx.x; m < n; m += blockDim.x) {
+      const int q = m - n / 2 + n - 1;
+      P[0][(long long)m * es + r] = dmul(b0[q], sc);
+      P[1][(long long)m * es + r] = dmul(b1[q], sc);
+      P[2][(long long)m * es + r] = dmul(b2[q], sc);
+    }
+    __syncthreads();
+  }
+}
+
+// Sigma^>, then Sigma^< and Sigma^R, of one series per CTA.  Phase 1: transforms of i Im G^>
+// and W^>, product, inverse.  Phase 2: the packed transform of (Im G^<, Im G^R) and the
+// transforms of W^<, W^R; per frequency S^< = i A W^<, S^R = i A W^R + i B (W^< + W^R);
+// two inverses.  The outputs may overwrite G: every read of the series precedes its writes.
+__global__ void __launch_bounds__(FFT_NT) gw_sig_kernel(GwFusedArgs a, const double2* tw) {
+  extern __shared__ double2 sm[];
+  const int n = a.n, L = a.L, logL = a.logL;
+  double2 *b0 = sm, *b1 = sm + L, *b2 = sm + 2 * L;
+  const double2* GR = reinterpret_cast<const double2*>(a.GR);
+  const double2* GL = reinterpret_cast<const double2*>(a.GL);
+  const double2* GG = reinterpret_cast<const double2*>(a.GG);
+  const double2* WR = reinterpret_cast<const double2*>(a.WR);
+  const double2* WL = reinterpret_cast<const double2*>(a.WL);
+  const double2* WG = reinterpret_cast<const double2*>(a.WG);
+  double2* SR = reinterpret_cast<double2*>(a.SR);
+  double2* SL = reinterpret_cast<double2*>(a.SL);
+  double2* SG = reinterpret_cast<double2*>(a.SG);
+  const long long es = a.estride;
+  const double inv = 1.0 / L;
+  const double2 sc = make_double2(a.scale_re * inv, a.scale_im * inv);
+  for (long long r = blockIdx.x; r < a.nseries; r += gridDim.x) {
+    long long rt;
+    if (!series_of(a, r, rt)) {
+      for (int m = threadIdx.x; m < n; m += blockDim.x) {
+        const long long o = (long long)m * es + r;
+        SR[o] = make_double2(0.0, 0.0);
+        SL[o] = make_double2(0.0, 0.0);
+        SG[o] = make_double2(0.0, 0.0);
+      }
+      continue;
+    }
+    // phase 1: Sigma^> = s conv(i Im G^>, W^>)
+    for (int t = threadIdx.x; t < L; t += blockDim.x) {
+      const int p = (int)(__brev((unsigned)t) >> (32 - logL));
+      double2 x = make_double2(0.0, 0.0), w = x;
+      if (t < n) {
+        const long long f = (long long)t * es + r;
+        x = make_double2(0.0, GG[f].y);
+        w = WG[f];
+      }
+      b0[p] = x;
+      b1[p] = w;
+    }
+    __syncthreads();
+    fft_smem(b0, L, logL, tw, false);
+    fft_smem(b1, L, logL, tw, false);
+    for (int k = threadIdx.x; k < L; k += blockDim.x) b0[k] = dmul(b0[k], b1[k]);
+    __syncthreads();
+    bitrev_permute(b0, L, logL);
+    __syncthreads();
+    fft_smem(b0, L, logL, tw, true);
+    for (int m = threadIdx.x; m < n; m += blockDim.x)
+      SG[(long long)m * es + r] = dmul(b0[m + n / 2], sc);
+    __syncthreads();
+    // phase 2: Sigma^< and Sigma^R
+    for (int t = threadIdx.x; t < L; t += blockDim.x) {
+      const int p = (int)(__brev((unsigned)t) >> (32 - logL));
+      double2 z = make_double2(0.0, 0.0), wl = z, wr = z;
+      if (t < n) {
+        const long long f = (long long)t * es + r;
+        z = make_double2(GL[f].y, GR[f].y);
+        wl = WL[f];
+        wr = WR[f];
+      }
+      b0[p] = z;
+      b1[p] = wl;
+      b2[p] = wr;
+    }
+    __syncthreads();
+    fft_smem(b0, L, logL, tw, false);
+    fft_smem(b1, L, logL, tw, false);
+    fft_smem(b2, L, logL, tw, false);
+    for (int k = threadIdx.x; k <= L / 2; k += blockDim.x) {
+      const int kk = (L - k) & (L - 1);
+      double2 A, B;
+      unpack(b0[k], b0[kk], A, B);  // transforms of Im G^< and Im G^R at k
+      const double2 wlk = b1[k], wrk = b2[k], wlkk = b1[kk], wrkk = b2[kk];
+      b1[k] = times_i(dmul(A, wlk));
+      b2[k] = times_i(dadd(dmul(A, wrk), dmul(B, dadd(wlk, wrk))));
+      if (kk != k) {
+        const double2 Ak = dconj(A), Bk = dconj(B);  // the transforms at L - k
+        b1[kk] = times_i(dmul(Ak, wlkk));
+        b2[kk] = times_i(dadd(dmul(Ak, wrkk), dmul(Bk, dadd(wlkk, wrkk))));
+      }
+    }
+    __syncthreads();
+    bitrev_permute(b1, L, logL);
+    bitrev_permute(b2, L, logL);
+    __syncthreads();
+    fft_smem(b1, L, logL, tw, true);
+    fft_smem(b2, L, logL, tw, true);
+    for (int m = threadIdx.x; m < n; m += blockDim.x) {
+      const long long o = (long long)m * es + r;
+      SL[o] = dmul(b1[m + n / 2], sc);
+      SR[o] = dmul(b2[m + n / 2], sc);
+    }
+    __syncthreads();
+  }
+}
+
 // zero |i - j| > ndiag of column-major nm x nm blocks bstride elements apart
 // (src/gw_mod.f90:527-555, 705-730)
 __global__ void band_zero_kernel(int nm, long long count, long long bstride, int ndiag,
@@ -334,6 +546,43 @@ cudaError_t zcorrconv(CorrConvArgs a, const double2* tw, cudaStream_t s) {
   const long long total = (long long)a.nk * a.nseries;
   const long long g = total < 65535LL * 16 ? total : 65535LL * 16;
   zcorrconv_kernel<<<(unsigned)g, FFT_NT, smem, s>>>(a, tw);
+  count_launch();
+  return cudaGetLastError();
+}
+
+namespace {
+cudaError_t packed_launch(GwFusedArgs& a, int* smem) {
+  if (a.nseries <= 0) return cudaSuccess;
+  int L = 1, logL = 0;
+  while (L < 2 * a.n) { L <<= 1; ++logL; }
+  if (L > LMAX) return cudaErrorInvalidValue;
+  a.L = L;
+  a.logL = logL;
+  *smem = 3 * L * (int)sizeof(double2);
+  return cudaSuccess;
+}
+}  // namespace
+
+cudaError_t gw_polarization_packed(GwFusedArgs a, const double2* tw, cudaStream_t s) {
+  int smem = 0;
+  cudaError_t e = packed_launch(a, &smem);
+  if (e != cudaSuccess || a.nseries <= 0) return e;
+  e = cudaFuncSetAttribute(gw_pol_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  const long long g = a.nseries < 65535LL * 16 ? a.nseries : 65535LL * 16;
+  gw_pol_kernel<<<(unsigned)g, FFT_NT, smem, s>>>(a, tw);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t gw_selfenergy_packed(GwFusedArgs a, const double2* tw, cudaStream_t s) {
+  int smem = 0;
+  cudaError_t e = packed_launch(a, &smem);
+  if (e != cudaSuccess || a.nseries <= 0) return e;
+  e = cudaFuncSetAttribute(gw_sig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  const long long g = a.nseries < 65535LL * 16 ? a.nseries : 65535LL * 16;
+  gw_sig_kernel<<<(unsigned)g, FFT_NT, smem, s>>>(a, tw);
   count_launch();
   return cudaGetLastError();
 }

@@ -153,6 +153,31 @@ struct CorrConvArgs {
   long long nel = 0, ij0 = 0;
   int L, logL;        // set by the launcher
 };
+// P and Sigma of one k-point with packed transforms, one energy series (matrix element) per
+// CTA: every input of P and every G of Sigma is purely imaginary once Re G is zeroed, so two
+// such series share one complex FFT (z = a + i b of the real sequences a, b; their transforms
+// follow from Z(k) and conj Z(L - k)).  P takes 6 FFTs per element for the 11 of three
+// separate correlations, Sigma 8 for 11.  Layout and band as CorrConvArgs (nk = 1).
+struct GwFusedArgs {
+  int n, nm;
+  long long nseries, estride;
+  long long nel = 0, ij0 = 0;
+  int ndiag = -1;
+  // polarisation: P^< = s corr(G^<, G^>t), P^> = s corr(G^>, G^<t),
+  // P^R = s [corr(G^<, conj G^R) + corr(G^R, G^<t)]; with GLt / GGt null the transposed
+  // partner is element (j, i) of G^< / G^> (full blocks)
+  const void *GR = nullptr, *GL = nullptr, *GG = nullptr, *GLt = nullptr, *GGt = nullptr;
+  void *PR = nullptr, *PL = nullptr, *PG = nullptr;
+  // self-energy: S^< = s conv(G^<, W^<), S^> = s conv(G^>, W^>),
+  // S^R = s [conv(G^<, W^R) + conv(G^R, W^< + W^R)]; S may overwrite G (each CTA reads its
+  // series completely before writing them)
+  const void *WR = nullptr, *WL = nullptr, *WG = nullptr;
+  void *SR = nullptr, *SL = nullptr, *SG = nullptr;
+  double scale_re = 0.0, scale_im = 0.0;
+  int L = 0, logL = 0;  // set by the launcher
+};
+cudaError_t gw_polarization_packed(GwFusedArgs a, const double2* tw, cudaStream_t s);
+cudaError_t gw_selfenergy_packed(GwFusedArgs a, const double2* tw, cudaStream_t s);
 cudaError_t gw_twiddles(double2* tw, cudaStream_t s);  // 2048 entries exp(-2 pi i k / 4096)
 cudaError_t zcorrconv(CorrConvArgs a, const double2* tw, cudaStream_t s);
 cudaError_t gw_sigma_post(int nm, long long nblocks, double2* SR, double2* SL, double2* SG,

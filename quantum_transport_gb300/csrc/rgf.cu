@@ -2131,9 +2131,20 @@ qt_status gw_map(qt_ctx* ctx, Problem pb, const GwGrid& g, const cd* V, double s
     a.imagX = imX; a.imagY = imY; a.scale_re = sr; a.scale_im = si; a.kmode = kmode;
     return run(a);
   };
-  QT_TRY(cc(w.GL, w.GG, w.PL, 1, 1, 0, 1, 1, 0.0, -pf, 1));  // P^< = corr(G^<_ij, G^>_ji)
-  QT_TRY(cc(w.GG, w.GL, w.PG, 1, 1, 0, 1, 1, 0.0, -pf, 1));  // P^> = corr(G^>_ij, G^<_ji)
-  {
+  // one k-point: all three P from packed transforms of the imaginary G in one launch
+  qt::GwFusedArgs pk{};
+  pk.n = (int)nE; pk.nm = nm; pk.nseries = nx * nm2; pk.estride = nx * nm2;
+  pk.ndiag = g.ndiag;
+  if (nk == 1) {
+    qt::GwFusedArgs a = pk;
+    a.GR = w.GR; a.GL = w.GL; a.GG = w.GG;  // transposed partners: element (j, i)
+    a.PR = w.PR; a.PL = w.PL; a.PG = w.PG;
+    a.scale_re = 0.0; a.scale_im = -pf;
+    cudaError_t e = qt::gw_polarization_packed(a, w.tw, s);
+    if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+  } else {
+    QT_TRY(cc(w.GL, w.GG, w.PL, 1, 1, 0, 1, 1, 0.0, -pf, 1));  // P^< = corr(G^<_ij, G^>_ji)
+    QT_TRY(cc(w.GG, w.GL, w.PG, 1, 1, 0, 1, 1, 0.0, -pf, 1));  // P^> = corr(G^>_ij, G^<_ji)
     // P^R = corr(G^<_ij, conj G^R_ij) + corr(G^R_ij, G^<_ji), one inverse transform
     qt::CorrConvArgs a = c;
     a.X = w.GL; a.Y = w.GR; a.conjY = 1; a.X2 = w.GR; a.Y2 = w.GL; a.transY2 = 1;
@@ -2160,16 +2171,25 @@ qt_status gw_map(qt_ctx* ctx, Problem pb, const GwGrid& g, const cd* V, double s
   // ---- self-energy: energy convolutions x i dE / (2 pi) / nk; with one k-point written
   // over G: Sigma^R first (it reads G^< and G^R), then Sigma^< over G^<, Sigma^> over G^>
   const double sf = dE / (2.0 * M_PI) / nk;
-  {
+  if (nk == 1) {
+    // Sigma^>, Sigma^<, Sigma^R of each series in one CTA, written over G
+    qt::GwFusedArgs a = pk;
+    a.GR = w.GR; a.GL = w.GL; a.GG = w.GG;
+    a.WR = w.PR; a.WL = w.PL; a.WG = w.PG;
+    a.SR = w.NR; a.SL = w.NL; a.SG = w.NG;
+    a.scale_re = 0.0; a.scale_im = sf;
+    cudaError_t e = qt::gw_selfenergy_packed(a, w.tw, s);
+    if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+  } else {
     // Sigma^R = conv(G^<, W^R) + conv(G^R, W^<) + conv(G^R, W^R)
     //         = conv(G^<, W^R) + conv(G^R, W^< + W^R)
     qt::CorrConvArgs a = c;
     a.X = w.GL; a.Y = w.PR; a.X2 = w.GR; a.Y2 = w.PL; a.Y2b = w.PR;
     a.Z = w.NR; a.corr = 0; a.imagX = 1; a.scale_re = 0.0; a.scale_im = sf; a.kmode = 2;
     QT_TRY(run(a));
+    QT_TRY(cc(w.GL, w.PL, w.NL, 0, 0, 0, 1, 0, 0.0, sf, 2));  // Sigma^< = conv(G^<, W^<)
+    QT_TRY(cc(w.GG, w.PG, w.NG, 0, 0, 0, 1, 0, 0.0, sf, 2));  // Sigma^> = conv(G^>, W^>)
   }
-  QT_TRY(cc(w.GL, w.PL, w.NL, 0, 0, 0, 1, 0, 0.0, sf, 2));  // Sigma^< = conv(G^<, W^<)
-  QT_TRY(cc(w.GG, w.PG, w.NG, 0, 0, 0, 1, 0, 0.0, sf, 2));  // Sigma^> = conv(G^>, W^>)
   // ---- band, recombination, symmetrisation, edge blocks
   QT_TRY(gw_post(ctx, nm, nx, nk * nE, w.NR, w.NL, w.NG, g.ndiag));
   return QT_OK;
@@ -2477,6 +2497,17 @@ extern "C" qt_status qt_gw_polarization(qt_ctx* ctx, int n, int64_t nseries, con
   double2* tw;
   QT_TRY(series_setup(ctx, n, nseries, flags, c, tw));
   // P = -i scale corr(...) of the Re-zeroed G (src/gw_mod.f90:444-446, 495-519)
+  if (c.nk == 1) {  // packed transforms, as qt_gw_step
+    qt::GwFusedArgs a{};
+    a.n = n; a.nm = 1; a.nseries = nseries; a.estride = nseries;
+    a.GR = GR; a.GL = GL; a.GG = GG; a.GLt = GLt; a.GGt = GGt;
+    a.PR = PR; a.PL = PL; a.PG = PG;
+    a.scale_re = 0.0; a.scale_im = -scale;
+    cudaError_t e = qt::gw_polarization_packed(a, tw, ctx->stream);
+    if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+    if (flags & QT_FLAG_SYNC) QT_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return QT_OK;
+  }
   QT_TRY(series_run(ctx, c, tw, GL, GGt, PL, 1, 0, 1, 1, 0, 0.0, -scale));
   QT_TRY(series_run(ctx, c, tw, GG, GLt, PG, 1, 0, 1, 1, 0, 0.0, -scale));
   // P^R = corr(G^<, conj G^R) + corr(G^R, G^<t), one inverse transform (as qt_gw_step)
@@ -2529,6 +2560,17 @@ extern "C" qt_status qt_gw_selfenergy(qt_ctx* ctx, int n, int64_t nseries, const
   double2* tw;
   QT_TRY(series_setup(ctx, n, nseries, flags, c, tw));
   // Sigma = i scale conv(...) with the Re-zeroed G (src/gw_mod.f90:646-698)
+  if (c.nk == 1) {  // packed transforms, as qt_gw_step
+    qt::GwFusedArgs a{};
+    a.n = n; a.nm = 1; a.nseries = nseries; a.estride = nseries;
+    a.GR = GR; a.GL = GL; a.GG = GG; a.WR = WR; a.WL = WL; a.WG = WG;
+    a.SR = SR; a.SL = SL; a.SG = SG;
+    a.scale_re = 0.0; a.scale_im = scale;
+    cudaError_t e = qt::gw_selfenergy_packed(a, tw, ctx->stream);
+    if (e != cudaSuccess) QT_FAIL(QT_ERR_CUDA, cudaGetErrorString(e));
+    if (flags & QT_FLAG_SYNC) QT_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return QT_OK;
+  }
   QT_TRY(series_run(ctx, c, tw, GL, WL, SL, 0, 0, 1, 0, 0, 0.0, scale));
   QT_TRY(series_run(ctx, c, tw, GG, WG, SG, 0, 0, 1, 0, 0, 0.0, scale));
   // Sigma^R = conv(G^<, W^R) + conv(G^R, W^< + W^R), one inverse transform (as qt_gw_step)
