@@ -51,21 +51,43 @@ __device__ __forceinline__ void butterfly(double2& u, double2& v, double2 w) {
   v = make_double2(x.x - y.x, x.y - y.y);
 }
 
-// in-place iterative radix-2 DIT on bit-reversed input; sign -1 forward, +1 inverse.
-// Stages go through shared memory in pairs: a thread takes the four elements
+// twiddle tw[j], conjugated for the inverse transform (the sign folds into the FMAs)
+template <bool INV>
+__device__ __forceinline__ double2 twiddle(const double2* tw, int j) {
+  const double2 w = tw[j];
+  return INV ? make_double2(w.x, -w.y) : w;
+}
+
+// u, v <- u + v, u - v: a butterfly whose twiddle is exactly 1
+__device__ __forceinline__ void butterfly1(double2& u, double2& v) {
+  const double2 x = u, y = v;
+  u = make_double2(x.x + y.x, x.y + y.y);
+  v = make_double2(x.x - y.x, x.y - y.y);
+}
+
+// u, v <- u + r y, u - r y with r = -i (forward) or +i (inverse) and y = v w already formed:
+// tw[j + LMAX/4] = tw[j] (-i), so the second twiddle of a radix-4 pair is a rotation of the
+// first and costs no multiply
+template <bool INV>
+__device__ __forceinline__ void butterfly_rot(double2& u, double2& v, double2 y) {
+  const double2 x = u;
+  const double2 r = INV ? make_double2(-y.y, y.x) : make_double2(y.y, -y.x);
+  u = make_double2(x.x + r.x, x.y + r.y);
+  v = make_double2(x.x - r.x, x.y - r.y);
+}
+
+// In-place iterative radix-2 DIT on bit-reversed input; exponent sign -1 forward (INV
+// false), +1 inverse.  Stages go through shared memory in pairs: a thread takes the four elements
 // base + {0, h, 2h, 3h} of a 4h-block, applies stage s to (0, h) and (2h, 3h) and stage s+1
-// to (0, 2h) and (h, 3h) in registers -- the same butterflies with the same twiddles as two
-// radix-2 passes, so the same bits, with half the shared-memory passes and barriers.  An odd
-// stage count starts with one single radix-2 pass.
-__device__ void fft_smem(double2* a, int L, int logL, const double2* tw, bool inverse) {
-  const double sg = inverse ? -1.0 : 1.0;
+// to (0, 2h) and (h, 3h) in registers -- the butterflies of two radix-2 passes with half the
+// shared-memory passes and barriers.  Stage s+1's twiddle for (h, 3h) is that of (0, 2h)
+// times -i (+i inverse), applied as a rotation; the first pair's twiddles are 1 and -i, so
+// it has no multiplies.  An odd stage count starts with one single radix-2 pass (twiddle 1).
+template <bool INV>
+__device__ __forceinline__ void fft_smem(double2* a, int L, int logL, const double2* tw) {
   int s = 1;
   if (logL & 1) {
-    for (int t = threadIdx.x; t < L / 2; t += blockDim.x) {
-      const int i0 = 2 * t;
-      const double2 w = make_double2(tw[0].x, sg * tw[0].y);
-      butterfly(a[i0], a[i0 + 1], w);
-    }
+    for (int t = threadIdx.x; t < L / 2; t += blockDim.x) butterfly1(a[2 * t], a[2 * t + 1]);
     __syncthreads();
     s = 2;
   }
@@ -76,12 +98,18 @@ __device__ void fft_smem(double2* a, int L, int logL, const double2* tw, bool in
       const int grp = t >> (s - 1), k = t & (h - 1);
       const int b = grp * 4 * h + k;
       double2 e0 = a[b], e1 = a[b + h], e2 = a[b + 2 * h], e3 = a[b + 3 * h];
-      const double2 w1 = tw[k * step1], w2a = tw[k * step2], w2b = tw[(k + h) * step2];
-      const double2 v1 = make_double2(w1.x, sg * w1.y);
-      butterfly(e0, e1, v1);  // stage s
-      butterfly(e2, e3, v1);
-      butterfly(e0, e2, make_double2(w2a.x, sg * w2a.y));  // stage s + 1
-      butterfly(e1, e3, make_double2(w2b.x, sg * w2b.y));
+      if (h == 1) {  // k = 0: twiddles 1, 1 and -i (+i); uniform over the block
+        butterfly1(e0, e1);
+        butterfly1(e2, e3);
+        butterfly1(e0, e2);
+        butterfly_rot<INV>(e1, e3, e3);
+      } else {
+        const double2 v1 = twiddle<INV>(tw, k * step1), v2 = twiddle<INV>(tw, k * step2);
+        butterfly(e0, e1, v1);  // stage s
+        butterfly(e2, e3, v1);
+        butterfly(e0, e2, v2);  // stage s + 1
+        butterfly_rot<INV>(e1, e3, dmul(e3, v2));
+      }
       a[b] = e0;
       a[b + h] = e1;
       a[b + 2 * h] = e2;
@@ -131,7 +159,7 @@ __device__ __forceinline__ int kpair(int ik, int iq, int nky, int nkz) {
 // One output series per CTA iteration: for each k-pair (one with kmode 0) and term, the
 // two series are loaded bit-reversed into b1, b2, transformed, and their product summed
 // into acc (b1 itself when there is one product only); then one inverse transform.
-__global__ void __launch_bounds__(FFT_NT) zcorrconv_kernel(CorrConvArgs a, const double2* tw) {
+__global__ void __launch_bounds__(FFT_NT, 1) zcorrconv_kernel(CorrConvArgs a, const double2* tw) {
   extern __shared__ double2 sm[];
   const int n = a.n, L = a.L, logL = a.logL, nk = a.nk;
   const bool two = a.X2 != nullptr;
@@ -173,8 +201,8 @@ __global__ void __launch_bounds__(FFT_NT) zcorrconv_kernel(CorrConvArgs a, const
           load_pair(a, X2 + xo, Y2 + yo, Y2b ? Y2b + yo : nullptr, r, a.transY2 ? rt : r,
                     a.conjY2, b1, b2);
         __syncthreads();
-        fft_smem(b1, L, logL, tw, false);
-        fft_smem(b2, L, logL, tw, false);
+        fft_smem<false>(b1, L, logL, tw);
+        fft_smem<false>(b2, L, logL, tw);
         const bool first = t == 0 && term == 0;
         for (int q = threadIdx.x; q < L; q += blockDim.x) {
           const double2 p = dmul(b1[q], b2[q]);
@@ -187,7 +215,7 @@ __global__ void __launch_bounds__(FFT_NT) zcorrconv_kernel(CorrConvArgs a, const
     for (int q = threadIdx.x; q < L; q += blockDim.x)
       inv_buf[(int)(__brev((unsigned)q) >> (32 - logL))] = acc[q];
     __syncthreads();
-    fft_smem(inv_buf, L, logL, tw, true);
+    fft_smem<true>(inv_buf, L, logL, tw);
     const double inv = 1.0 / L;
     const double2 sc = make_double2(a.scale_re * inv, a.scale_im * inv);
     for (int m = threadIdx.x; m < n; m += blockDim.x) {
@@ -246,7 +274,7 @@ __device__ __forceinline__ bool series_of(const GwFusedArgs& a, long long r, lon
 // (G^<, G^>), (rev G^>t, rev G^<t), (G^R, rev conj G^R) of the imaginary parts, the three
 // products per frequency, three inverse transforms.  Each product of two imaginary series'
 // transforms is -A B of their imaginary parts' transforms.
-__global__ void __launch_bounds__(FFT_NT) gw_pol_kernel(GwFusedArgs a, const double2* tw) {
+__global__ void __launch_bounds__(FFT_NT, 1) gw_pol_kernel(GwFusedArgs a, const double2* tw) {
   extern __shared__ double2 sm[];
   const int n = a.n, L = a.L, logL = a.logL;
   double2 *b0 = sm, *b1 = sm + L, *b2 = sm + 2 * L;
@@ -282,9 +310,9 @@ __global__ void __launch_bounds__(FFT_NT) gw_pol_kernel(GwFusedArgs a, const dou
       b2[p] = z2;
     }
     __syncthreads();
-    fft_smem(b0, L, logL, tw, false);
-    fft_smem(b1, L, logL, tw, false);
-    fft_smem(b2, L, logL, tw, false);
+    fft_smem<false>(b0, L, logL, tw);
+    fft_smem<false>(b1, L, logL, tw);
+    fft_smem<false>(b2, L, logL, tw);
     for (int k = threadIdx.x; k <= L / 2; k += blockDim.x) {
       const int kk = (L - k) & (L - 1);
       double2 A1, B1, A2, B2, A3, B3;
@@ -304,9 +332,9 @@ __global__ void __launch_bounds__(FFT_NT) gw_pol_kernel(GwFusedArgs a, const dou
     bitrev_permute(b1, L, logL);
     bitrev_permute(b2, L, logL);
     __syncthreads();
-    fft_smem(b0, L, logL, tw, true);
-    fft_smem(b1, L, logL, tw, true);
-    fft_smem(b2, L, logL, tw, true);
+    fft_smem<true>(b0, L, logL, tw);
+    fft_smem<true>(b1, L, logL, tw);
+    fft_smem<true>(b2, L, logL, tw);
     for (int m = threadIdx.x; m < n; m += blockDim.x) {
       const int q = m - n / 2 + n - 1;
       P[0][(long long)m * es + r] = dmul(b0[q], sc);
@@ -321,7 +349,7 @@ __global__ void __launch_bounds__(FFT_NT) gw_pol_kernel(GwFusedArgs a, const dou
 // and W^>, product, inverse.  Phase 2: the packed transform of (Im G^<, Im G^R) and the
 // transforms of W^<, W^R; per frequency S^< = i A W^<, S^R = i A W^R + i B (W^< + W^R);
 // two inverses.  The outputs may overwrite G: every read of the series precedes its writes.
-__global__ void __launch_bounds__(FFT_NT) gw_sig_kernel(GwFusedArgs a, const double2* tw) {
+__global__ void __launch_bounds__(FFT_NT, 1) gw_sig_kernel(GwFusedArgs a, const double2* tw) {
   extern __shared__ double2 sm[];
   const int n = a.n, L = a.L, logL = a.logL;
   double2 *b0 = sm, *b1 = sm + L, *b2 = sm + 2 * L;
@@ -361,13 +389,13 @@ __global__ void __launch_bounds__(FFT_NT) gw_sig_kernel(GwFusedArgs a, const dou
       b1[p] = w;
     }
     __syncthreads();
-    fft_smem(b0, L, logL, tw, false);
-    fft_smem(b1, L, logL, tw, false);
+    fft_smem<false>(b0, L, logL, tw);
+    fft_smem<false>(b1, L, logL, tw);
     for (int k = threadIdx.x; k < L; k += blockDim.x) b0[k] = dmul(b0[k], b1[k]);
     __syncthreads();
     bitrev_permute(b0, L, logL);
     __syncthreads();
-    fft_smem(b0, L, logL, tw, true);
+    fft_smem<true>(b0, L, logL, tw);
     for (int m = threadIdx.x; m < n; m += blockDim.x)
       SG[(long long)m * es + r] = dmul(b0[m + n / 2], sc);
     __syncthreads();
@@ -386,9 +414,9 @@ __global__ void __launch_bounds__(FFT_NT) gw_sig_kernel(GwFusedArgs a, const dou
       b2[p] = wr;
     }
     __syncthreads();
-    fft_smem(b0, L, logL, tw, false);
-    fft_smem(b1, L, logL, tw, false);
-    fft_smem(b2, L, logL, tw, false);
+    fft_smem<false>(b0, L, logL, tw);
+    fft_smem<false>(b1, L, logL, tw);
+    fft_smem<false>(b2, L, logL, tw);
     for (int k = threadIdx.x; k <= L / 2; k += blockDim.x) {
       const int kk = (L - k) & (L - 1);
       double2 A, B;
@@ -406,8 +434,8 @@ __global__ void __launch_bounds__(FFT_NT) gw_sig_kernel(GwFusedArgs a, const dou
     bitrev_permute(b1, L, logL);
     bitrev_permute(b2, L, logL);
     __syncthreads();
-    fft_smem(b1, L, logL, tw, true);
-    fft_smem(b2, L, logL, tw, true);
+    fft_smem<true>(b1, L, logL, tw);
+    fft_smem<true>(b2, L, logL, tw);
     for (int m = threadIdx.x; m < n; m += blockDim.x) {
       const long long o = (long long)m * es + r;
       SL[o] = dmul(b1[m + n / 2], sc);
