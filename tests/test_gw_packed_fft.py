@@ -55,3 +55,61 @@ def test_packed_polarisation_and_self_energy(n):
     np.testing.assert_allclose(sl, ogw.conv(gl, wl), atol=1e-12 * np.abs(sl).max())
     exp = ogw.conv(gl, wr) + ogw.conv(gr, wl) + ogw.conv(gr, wr)
     np.testing.assert_allclose(sr, exp, atol=1e-12 * np.abs(exp).max())
+
+
+LMAX = 4096
+
+
+def _stage_fft(x, inverse):
+    """The GPU kernels' in-place transform, restated stage by stage in numpy (gw.cu,
+    fft_smem): bit-reversed input, an odd stage count's first radix-2 pass (twiddle 1),
+    then stages fused in pairs over 4h-blocks.  The pair's second twiddle for (h, 3h) is
+    applied as the rotation of the (0, 2h) twiddle by -i (+i inverse), using
+    tw[j + LMAX/4] = tw[j] (-i); the first pair (h = 1) has twiddles 1, 1 and -i only."""
+    L = len(x)
+    logL = L.bit_length() - 1
+    j = np.arange(LMAX // 2)
+    tw = np.exp(-2j * np.pi * j / LMAX)
+    if inverse:
+        tw = np.conj(tw)
+    rot = 1j if inverse else -1j
+    r = np.array([int(format(t, f"0{logL}b")[::-1], 2) for t in range(L)]) if logL else [0]
+    a = np.empty(L, dtype=complex)
+    a[r] = x
+    s = 1
+    if logL & 1:
+        u, v = a[0::2].copy(), a[1::2].copy()
+        a[0::2], a[1::2] = u + v, u - v
+        s = 2
+    while s < logL:
+        h = 1 << (s - 1)
+        t = np.arange(L // 4)
+        k = t & (h - 1)
+        b = (t >> (s - 1)) * 4 * h + k
+        e0, e1, e2, e3 = a[b], a[b + h], a[b + 2 * h], a[b + 3 * h]
+        v1, v2 = tw[k * (LMAX // (2 * h))], tw[k * (LMAX // (4 * h))]
+        e0, e1 = e0 + e1 * v1, e0 - e1 * v1
+        e2, e3 = e2 + e3 * v1, e2 - e3 * v1
+        e0, e2 = e0 + e2 * v2, e0 - e2 * v2
+        y = rot * (e3 * v2)
+        e1, e3 = e1 + y, e1 - y
+        a[b], a[b + h], a[b + 2 * h], a[b + 3 * h] = e0, e1, e2, e3
+        s += 2
+    return a
+
+
+def test_rotation_identity_of_the_twiddle_table():
+    """The identity the fused stage pairs rely on: the table's entry a quarter period on is
+    the entry times -i."""
+    j = np.arange(LMAX // 4)
+    tw = np.exp(-2j * np.pi * np.arange(LMAX // 2) / LMAX)
+    assert np.abs(tw[j + LMAX // 4] - tw[j] * -1j).max() < 1e-15
+
+
+@pytest.mark.parametrize("L", [2, 4, 8, 32, 128, 2048, 4096])
+def test_stage_structure_matches_the_dft(L):
+    rng = np.random.default_rng(L)
+    x = rng.normal(size=L) + 1j * rng.normal(size=L)
+    ref_f, ref_i = np.fft.fft(x), L * np.fft.ifft(x)
+    assert np.abs(_stage_fft(x, False) - ref_f).max() <= 1e-13 * np.abs(ref_f).max()
+    assert np.abs(_stage_fft(x, True) - ref_i).max() <= 1e-13 * np.abs(ref_i).max()
