@@ -119,11 +119,14 @@ const char* qt_version(void);
  * omp_get_wtime phase times, src/cuda_rgf_mod.f90:87-412).
  * qt_kernel_launches: kernels launched by this library since load.
  * qt_ctx_profile(enable): record CUDA events around every block product and
- *   inverse on the context's stream.
+ *   inverse on the context's stream, and around the phases of each GW map.
  * qt_ctx_profile_read(kind): launches, summed device time (ms) and the
  *   algorithmic / executed-tensor flops of one kind since the last read:
  *   0 complex64 split product, 1 complex128 split product, 2 FP64 product,
- *   3 FP32 inverse, 4 FP64 inverse.
+ *   3 FP32 inverse, 4 FP64 inverse; GW map phases (qt_gw_step, qt_scba_solve;
+ *   flops 0, products and inverses inside them also counted above): 5 the RGF
+ *   of G, 6 the energy correlations / convolutions of P and Sigma, 7 the
+ *   screened interaction W, 8 Sigma's band, recombination and symmetrisation.
  * qt_ctx_stream: the context's cudaStream_t (as void*).                    */
 int64_t qt_kernel_launches(void);
 qt_status qt_ctx_profile(qt_ctx* ctx, int enable);

@@ -55,7 +55,11 @@ extern "C" const char* qt_version(void) { return "qtgpu 0.1 sm_103a"; }
 
 // Optional CUDA-event timing of the block products and inverses on the
 // context's stream (qt_ctx_profile): kinds 0 complex64 split product,
-// 1 complex128 split product, 2 FP64 product, 3 FP32 inverse, 4 FP64 inverse.
+// 1 complex128 split product, 2 FP64 product, 3 FP32 inverse, 4 FP64 inverse;
+// and of the GW map's phases: 5 the RGF of G, 6 the energy correlations and
+// convolutions of P and Sigma, 7 the screened interaction W, 8 the band,
+// recombination, symmetrisation and edge blocks of Sigma.  A phase's products and
+// inverses are also counted in kinds 0-4.
 struct Prof {
   struct Entry {
     int kind;
@@ -75,6 +79,31 @@ struct Prof {
     cudaEventCreate(&e);
     return e;
   }
+};
+
+// One timed phase on a stream while profiling is on: an event at construction, the
+// closing event at end() or destruction (an early error return still closes it).
+struct ProfPhase {
+  Prof& p;
+  cudaStream_t s;
+  int kind;
+  cudaEvent_t a = nullptr;
+  ProfPhase(Prof& prof, cudaStream_t stream, int k) : p(prof), s(stream), kind(k) {
+    if (p.on) {
+      a = p.get();
+      cudaEventRecord(a, s);
+    }
+  }
+  void end() {
+    if (!a) return;
+    cudaEvent_t b = p.get();
+    cudaEventRecord(b, s);
+    p.v.push_back({kind, a, b, 0.0, 0.0});
+    a = nullptr;
+  }
+  ~ProfPhase() { end(); }
+  ProfPhase(const ProfPhase&) = delete;
+  ProfPhase& operator=(const ProfPhase&) = delete;
 };
 
 struct qt_ctx {
@@ -2092,6 +2121,7 @@ qt_status gw_map(qt_ctx* ctx, Problem pb, const GwGrid& g, const cd* V, double s
   // ---- G with the current self-energies, one k-point at a time (its H blocks)
   const cd* Hii = pb.Hii;
   const cd* H1i = pb.H1i;
+  ProfPhase ph_rgf(ctx->prof, s, 5);
   for (int k = 0; k < nk; ++k) {
     Problem pk = pb;
     pk.Hii = Hii + k * g.hk;
@@ -2107,6 +2137,7 @@ qt_status gw_map(qt_ctx* ctx, Problem pb, const GwGrid& g, const cd* V, double s
     pk.flags &= ~QT_FLAG_CAROLI;
     QT_TRY(run_problem(ctx, pk, hii_n, h1i_n));
   }
+  ph_rgf.end();
   // ---- polarisation: energy correlations of Re-zeroed G, x -i dE/(2 pi) spindeg / nk
   double dE = 0.0;
   {
@@ -2135,6 +2166,7 @@ qt_status gw_map(qt_ctx* ctx, Problem pb, const GwGrid& g, const cd* V, double s
   qt::GwFusedArgs pk{};
   pk.n = (int)nE; pk.nm = nm; pk.nseries = nx * nm2; pk.estride = nx * nm2;
   pk.ndiag = g.ndiag;
+  ProfPhase ph_pol(ctx->prof, s, 6);
   if (nk == 1) {
     qt::GwFusedArgs a = pk;
     a.GR = w.GR; a.GL = w.GL; a.GG = w.GG;  // transposed partners: element (j, i)
@@ -2152,8 +2184,10 @@ qt_status gw_map(qt_ctx* ctx, Problem pb, const GwGrid& g, const cd* V, double s
     a.kmode = 1;
     QT_TRY(run(a));
   }
+  ph_pol.end();
   // ---- screened interaction per momentum transfer q and (w, slab) block, in place: P -> W;
   // with a Coulomb block per slab, the blocks of slab x (every energy) take V_{q,x}
+  ProfPhase ph_w(ctx->prof, s, 7);
   for (int q = 0; q < nk; ++q) {
     const long long o = q * kst;
     if (!g.v_per_slab) {
@@ -2168,9 +2202,11 @@ qt_status gw_map(qt_ctx* ctx, Problem pb, const GwGrid& g, const cd* V, double s
                                 g.ndiag, nx * nm2));
     }
   }
+  ph_w.end();
   // ---- self-energy: energy convolutions x i dE / (2 pi) / nk; with one k-point written
   // over G: Sigma^R first (it reads G^< and G^R), then Sigma^< over G^<, Sigma^> over G^>
   const double sf = dE / (2.0 * M_PI) / nk;
+  ProfPhase ph_sig(ctx->prof, s, 6);
   if (nk == 1) {
     // Sigma^>, Sigma^<, Sigma^R of each series in one CTA, written over G
     qt::GwFusedArgs a = pk;
@@ -2190,7 +2226,9 @@ qt_status gw_map(qt_ctx* ctx, Problem pb, const GwGrid& g, const cd* V, double s
     QT_TRY(cc(w.GL, w.PL, w.NL, 0, 0, 0, 1, 0, 0.0, sf, 2));  // Sigma^< = conv(G^<, W^<)
     QT_TRY(cc(w.GG, w.PG, w.NG, 0, 0, 0, 1, 0, 0.0, sf, 2));  // Sigma^> = conv(G^>, W^>)
   }
+  ph_sig.end();
   // ---- band, recombination, symmetrisation, edge blocks
+  ProfPhase ph_post(ctx->prof, s, 8);
   QT_TRY(gw_post(ctx, nm, nx, nk * nE, w.NR, w.NL, w.NG, g.ndiag));
   return QT_OK;
 }

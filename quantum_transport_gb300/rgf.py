@@ -70,11 +70,15 @@ class Context:
         check(self._lib.qt_ctx_set_wave_points(self.handle, int(points)))
 
     def profile(self, enable=True):
-        """Event-time every block product / inverse launch on this context's stream."""
+        """Event-time every block product / inverse launch on this context's stream, and the
+        phases of each GW map."""
         check(self._lib.qt_ctx_profile(self.handle, int(bool(enable))))
 
+    # kinds 5-8 are phases of the GW map; the products and inverses inside them are also
+    # counted in kinds 0-4
     PROFILE_KINDS = {0: "zgemm_oz_c64", 1: "zgemm_oz_c128", 2: "zgemm_f64", 3: "zinv_f32",
-                     4: "zinv_f64"}
+                     4: "zinv_f64", 5: "gw_rgf", 6: "gw_corrconv", 7: "gw_screened",
+                     8: "gw_post"}
 
     def profile_read(self):
         """{kind name: (launches, ms, algorithmic flops, executed tensor flops)} since last read."""
