@@ -208,3 +208,27 @@ def test_gw_green_with_sancho_reset_vs_oracle(ctx):
     assert hit.any() and not hit.all()
     assert not np.allclose(out[True]["diag_gr"].reshape(len(dev.E), -1)[hit],
                            out[False]["diag_gr"].reshape(len(dev.E), -1)[hit])
+
+
+def test_profiler_times_the_map_phases(ctx):
+    """With the context's profiler on, one SCBA iteration records each phase of the map once
+    (the correlations twice: P, then Sigma), and the phases fit inside the iteration's own
+    event time on the same stream."""
+    import torch
+    dev, V, s = _system(ctx)
+    ctx.profile_read()
+    ctx.profile(True)
+    try:
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record()
+        s.scba(alpha=0.3, tol=0.0, max_iter=1)
+        ev[1].record()
+        torch.cuda.synchronize()
+    finally:
+        ctx.profile(False)
+        prof = ctx.profile_read()
+    phases = ("gw_rgf", "gw_corrconv", "gw_screened", "gw_post")
+    assert {k: prof[k][0] for k in phases} == {"gw_rgf": 1, "gw_corrconv": 2,
+                                               "gw_screened": 1, "gw_post": 1}
+    assert all(prof[k][1] > 0 for k in phases)
+    assert sum(prof[k][1] for k in phases) <= ev[0].elapsed_time(ev[1]) + 0.05
