@@ -6,8 +6,8 @@
  *   sancho                    src/cuda_rgf_mod.f90:657-765 (src/rgf_mod.f90:482-568)
  *   cuda_rgf_constblocksize   src/cuda_rgf_mod.f90:53-413, with G^> = G^< + G - G^+
  *                             in every slab (what produced test_cnt/pdos0000.dat)
- * plus the Caroli transmission Tr[Gam_R G_N1 Gam_L G_N1^+].  Block products are
- * loops over split real / imaginary planes, four columns at a time, and inverses
+ * plus the Caroli transmission Tr[Gam_R G_N1 Gam_L G_N1^+].  Block products run on
+ * packed real / imaginary planes with register-blocked tiles of C, and inverses
  * Gauss-Jordan with partial pivoting: it
  * stands in for the reference's CPU build (no Fortran compiler exists on
  * either machine) as the timed CPU baseline and as a second checker.
@@ -24,86 +24,147 @@ typedef double complex cplx;
 
 static const double BOLTZ = 8.61734e-05;
 
-/* C = op(A) op(B)  (op: 'N' or 'C'), all n x n column-major (n <= 512).  The operands are
- * first split into real and imaginary planes (op applied), so the inner loop is plain real
- * multiply-adds that the compiler vectorises; four columns of C are formed together so
- * that each loaded entry of op(A) feeds four complex multiply-adds from L1.  Every C(i, j)
- * accumulates over k = 0 .. n-1 in order.  ta, tb hold 2 n^2 doubles each. */
+/* C = op(A) op(B)  (op: 'N' or 'C'), all n x n column-major.  The operands are first packed
+ * into real and imaginary planes with op applied: op(A) in panels of MR rows stored
+ * [panel][k][MR], op(B) in panels of NR columns stored [panel][k][NR], zero-padded past n.
+ * Each MR x NR tile of C then accumulates in registers (two-double vectors of GCC's
+ * generic vector extension, the same on every target), every loaded pair of a panel
+ * feeding NR complex multiply-adds, so the loop is bound by multiply-adds rather than by
+ * loads and stores.  Every C(i, j) accumulates over k = 0 .. n-1 in order with the same
+ * expression as an unblocked loop.  The tile is 4 x 4 where 32 vector registers hold it
+ * (aarch64) and 4 x 2 elsewhere.  ta, tb hold (n + 4) n complex each. */
+typedef double v2d __attribute__((vector_size(16)));
+#if defined(__aarch64__)
+enum { MR = 4, NR = 4 };
+#else
+enum { MR = 4, NR = 2 };
+#endif
+static inline v2d ld2(const double* p) {
+  v2d v;
+  memcpy(&v, p, sizeof v);
+  return v;
+}
 static void gemm(int n, char opa, const cplx* A, char opb, const cplx* B, cplx* C, cplx* ta,
                  cplx* tb) {
-  const size_t nn = (size_t)n * n;
+  const int pi = (n + MR - 1) / MR, pj = (n + NR - 1) / NR;
   double* restrict ar = (double*)ta;
-  double* restrict ai = ar + nn;
+  double* restrict ai = ar + (size_t)pi * n * MR;
   double* restrict br = (double*)tb;
-  double* restrict bi = br + nn;
-  for (int j = 0; j < n; ++j)
-    for (int i = 0; i < n; ++i) {
-      const cplx x = opa == 'C' ? conj(A[j + (size_t)i * n]) : A[i + (size_t)j * n];
-      const cplx y = opb == 'C' ? conj(B[j + (size_t)i * n]) : B[i + (size_t)j * n];
-      ar[i + (size_t)j * n] = creal(x);
-      ai[i + (size_t)j * n] = cimag(x);
-      br[i + (size_t)j * n] = creal(y);
-      bi[i + (size_t)j * n] = cimag(y);
+  double* restrict bi = br + (size_t)pj * n * NR;
+  for (int k = 0; k < n; ++k)
+    for (int i = 0; i < pi * MR; ++i) {
+      const cplx x = i >= n ? 0.0 : opa == 'C' ? conj(A[k + (size_t)i * n]) : A[i + (size_t)k * n];
+      const size_t o = ((size_t)(i / MR) * n + k) * MR + i % MR;
+      ar[o] = creal(x);
+      ai[o] = cimag(x);
     }
-  enum { NJ = 4 };
-  double cr[NJ][512], ci[NJ][512];
-  for (int j0 = 0; j0 < n; j0 += NJ) {
-    const int nj = n - j0 < NJ ? n - j0 : NJ;
-    for (int q = 0; q < nj; ++q)
-      for (int i = 0; i < n; ++i) cr[q][i] = ci[q][i] = 0.0;
+  for (int j = 0; j < pj * NR; ++j)
     for (int k = 0; k < n; ++k) {
-      const double* restrict xr = ar + (size_t)k * n;
-      const double* restrict xi = ai + (size_t)k * n;
-      for (int q = 0; q < nj; ++q) {
-        const double yr = br[k + (size_t)(j0 + q) * n], yi = bi[k + (size_t)(j0 + q) * n];
-        double* restrict zr = cr[q];
-        double* restrict zi = ci[q];
-        for (int i = 0; i < n; ++i) {
-          zr[i] += xr[i] * yr - xi[i] * yi;
-          zi[i] += xr[i] * yi + xi[i] * yr;
+      const cplx y = j >= n ? 0.0 : opb == 'C' ? conj(B[j + (size_t)k * n]) : B[k + (size_t)j * n];
+      const size_t o = ((size_t)(j / NR) * n + k) * NR + j % NR;
+      br[o] = creal(y);
+      bi[o] = cimag(y);
+    }
+  for (int jp = 0; jp < pj; ++jp)
+    for (int ip = 0; ip < pi; ++ip) {
+      const double* restrict xr = ar + (size_t)ip * n * MR;
+      const double* restrict xi = ai + (size_t)ip * n * MR;
+      const double* restrict yr = br + (size_t)jp * n * NR;
+      const double* restrict yi = bi + (size_t)jp * n * NR;
+      v2d cr[NR][MR / 2], ci[NR][MR / 2];
+      for (int q = 0; q < NR; ++q)
+        for (int h = 0; h < MR / 2; ++h) cr[q][h] = ci[q][h] = (v2d){0.0, 0.0};
+      for (int k = 0; k < n; ++k) {
+        v2d pr[MR / 2], pm[MR / 2];
+        for (int h = 0; h < MR / 2; ++h) {
+          pr[h] = ld2(xr + (size_t)k * MR + 2 * h);
+          pm[h] = ld2(xi + (size_t)k * MR + 2 * h);
+        }
+        for (int q = 0; q < NR; ++q) {
+          const double wr = yr[(size_t)k * NR + q], wi = yi[(size_t)k * NR + q];
+          const v2d vr = {wr, wr}, vi = {wi, wi};
+          for (int h = 0; h < MR / 2; ++h) {
+            cr[q][h] += pr[h] * vr - pm[h] * vi;
+            ci[q][h] += pr[h] * vi + pm[h] * vr;
+          }
+        }
+      }
+      for (int q = 0; q < NR; ++q) {
+        const int j = jp * NR + q;
+        if (j >= n) break;
+        for (int r = 0; r < MR; ++r) {
+          const int i = ip * MR + r;
+          if (i < n) C[i + (size_t)j * n] = cr[q][r / 2][r % 2] + I * ci[q][r / 2][r % 2];
         }
       }
     }
-    for (int q = 0; q < nj; ++q)
-      for (int i = 0; i < n; ++i) C[i + (size_t)(j0 + q) * n] = cr[q][i] + I * ci[q][i];
-  }
 }
 
-/* in-place inverse, Gauss-Jordan with row pivoting (|re|+|im| pivot measure) */
-static int invert(int n, cplx* X, int* perm) {
+/* in-place inverse, Gauss-Jordan with row pivoting (|re|+|im| pivot measure).  The
+ * elimination runs on real and imaginary planes (xr: 2 n^2 doubles of scratch), so the
+ * rank-1 update of each column is a loop of real multiply-adds that vectorises; every
+ * element sees the same complex operations as on interleaved storage. */
+static int invert(int n, cplx* X, int* perm, double* restrict xr) {
+  const size_t nn = (size_t)n * n;
+  double* restrict xi = xr + nn;
+  for (size_t e = 0; e < nn; ++e) {
+    xr[e] = creal(X[e]);
+    xi[e] = cimag(X[e]);
+  }
   int bad = 0;
   for (int k = 0; k < n; ++k) {
     int p = k;
     double best = -1.0;
     for (int i = k; i < n; ++i) {
-      const cplx v = X[i + (size_t)k * n];
-      const double m = fabs(creal(v)) + fabs(cimag(v));
+      const double m = fabs(xr[i + (size_t)k * n]) + fabs(xi[i + (size_t)k * n]);
       if (m > best) { best = m; p = i; }
     }
     if (!(best > 0.0)) bad = 1;
     perm[k] = p;
     if (p != k)
       for (int j = 0; j < n; ++j) {
-        const cplx t = X[k + (size_t)j * n];
-        X[k + (size_t)j * n] = X[p + (size_t)j * n];
-        X[p + (size_t)j * n] = t;
+        const size_t a = k + (size_t)j * n, b = p + (size_t)j * n;
+        const double tr = xr[a], ti = xi[a];
+        xr[a] = xr[b]; xi[a] = xi[b];
+        xr[b] = tr; xi[b] = ti;
       }
-    const cplx inv = best > 0.0 ? 1.0 / X[k + (size_t)k * n] : 0.0;
-    for (int j = 0; j < n; ++j) X[k + (size_t)j * n] *= inv;
-    X[k + (size_t)k * n] = inv;
+    const cplx piv = xr[k + (size_t)k * n] + I * xi[k + (size_t)k * n];
+    const cplx inv = best > 0.0 ? 1.0 / piv : 0.0;
+    const double vr = creal(inv), vi = cimag(inv);
+    for (int j = 0; j < n; ++j) {
+      const size_t a = k + (size_t)j * n;
+      const double u = xr[a], v = xi[a];
+      xr[a] = u * vr - v * vi;
+      xi[a] = u * vi + v * vr;
+    }
+    xr[k + (size_t)k * n] = vr;
+    xi[k + (size_t)k * n] = vi;
+    const double* restrict ckr = xr + (size_t)k * n;
+    const double* restrict cki = xi + (size_t)k * n;
     for (int j = 0; j < n; ++j) {
       if (j == k) continue;
-      const cplx r = X[k + (size_t)j * n];
-      cplx* restrict col = X + (size_t)j * n;
-      const cplx* restrict colk = X + (size_t)k * n;
+      const double rr = xr[k + (size_t)j * n], ri = xi[k + (size_t)j * n];
+      double* restrict cr = xr + (size_t)j * n;
+      double* restrict ci = xi + (size_t)j * n;
       /* all rows, then row k put back: the same operations on rows i != k, in a loop
          without a branch */
-      for (int i = 0; i < n; ++i) col[i] -= colk[i] * r;
-      col[k] = r;
+      for (int i = 0; i < n; ++i) {
+        cr[i] -= ckr[i] * rr - cki[i] * ri;
+        ci[i] -= ckr[i] * ri + cki[i] * rr;
+      }
+      cr[k] = rr;
+      ci[k] = ri;
     }
+    const double nr = -vr, ni = -vi;
     for (int i = 0; i < n; ++i)
-      if (i != k) X[i + (size_t)k * n] *= -inv;
+      if (i != k) {
+        const size_t a = i + (size_t)k * n;
+        const double u = xr[a], v = xi[a];
+        xr[a] = u * nr - v * ni;
+        xi[a] = u * ni + v * nr;
+      }
   }
+  for (size_t e = 0; e < nn; ++e) X[e] = xr[e] + I * xi[e];
   for (int k = n - 1; k >= 0; --k) {
     const int p = perm[k];
     if (p != k)
@@ -123,11 +184,11 @@ typedef struct {
 } Work;
 
 static void work_init(Work* w, int n) {
-  const size_t b = (size_t)n * n;
+  const size_t b = (size_t)n * n, t = b + 4 * (size_t)n;  /* packed panels, padded to 4 */
   w->n = n;
-  w->A = malloc(sizeof(cplx) * b * 10);
-  w->B = w->A + b; w->C = w->B + b; w->D = w->C + b; w->ta = w->D + b; w->tb = w->ta + b;
-  w->HBB = w->tb + b; w->HSS = w->HBB + b; w->H10 = w->HSS + b; w->H01 = w->H10 + b;
+  w->A = malloc(sizeof(cplx) * (b * 8 + 2 * t));
+  w->B = w->A + b; w->C = w->B + b; w->D = w->C + b; w->ta = w->D + b; w->tb = w->ta + t;
+  w->HBB = w->tb + t; w->HSS = w->HBB + b; w->H10 = w->HSS + b; w->H01 = w->H10 + b;
   w->perm = malloc(sizeof(int) * n);
 }
 static void work_free(Work* w) { free(w->A); free(w->perm); }
@@ -151,7 +212,7 @@ static int sancho(Work* w, double E, double eta, double tol, int nmax, const cpl
   for (it = 1; it <= nmax; ++it) {
     for (size_t e = 0; e < b; ++e) w->A[e] = -w->HBB[e];
     for (int i = 0; i < n; ++i) w->A[i + (size_t)i * n] += z;
-    *bad |= invert(n, w->A, w->perm);
+    *bad |= invert(n, w->A, w->perm, (double*)w->ta);
     gemm(n, 'N', w->A, 'N', w->H10, w->B, w->ta, w->tb);
     gemm(n, 'N', w->H01, 'N', w->B, w->C, w->ta, w->tb);
     for (size_t e = 0; e < b; ++e) { w->HSS[e] += w->C[e]; w->HBB[e] += w->C[e]; }
@@ -169,7 +230,7 @@ static int sancho(Work* w, double E, double eta, double tol, int nmax, const cpl
   if (it > nmax) it = nmax;
   for (size_t e = 0; e < b; ++e) G00[e] = -w->HSS[e];
   for (int i = 0; i < n; ++i) G00[i + (size_t)i * n] += z;
-  *bad |= invert(n, G00, w->perm);
+  *bad |= invert(n, G00, w->perm, (double*)w->ta);
   return it;
 }
 
@@ -201,7 +262,7 @@ static void point(Work* w, int nx, double E, const cplx* H0, const cplx* H10, do
   gemm(n, 'N', Y, 'C', H10, SigL, w->ta, w->tb);
   for (size_t e = 0; e < b; ++e) gl[e] = -H0[e] - SigL[e];
   for (int i = 0; i < n; ++i) gl[i + (size_t)i * n] += z;
-  bad |= invert(n, gl, w->perm);
+  bad |= invert(n, gl, w->perm, (double*)w->ta);
   for (int j = 0; j < n; ++j)
     for (int i = 0; i < n; ++i)
       GamL[i + (size_t)j * n] = -(SigL[i + (size_t)j * n] - conj(SigL[j + (size_t)i * n]));
@@ -216,7 +277,7 @@ static void point(Work* w, int nx, double E, const cplx* H0, const cplx* H10, do
     gemm(n, 'N', Y, 'C', H10, Z, w->ta, w->tb);
     for (size_t e = 0; e < b; ++e) g[e] = -H0[e] - Z[e];
     for (int i = 0; i < n; ++i) g[i + (size_t)i * n] += z;
-    bad |= invert(n, g, w->perm);
+    bad |= invert(n, g, w->perm, (double*)w->ta);
     gemm(n, 'N', H10, 'N', gln + (size_t)(l - 1) * b, Y, w->ta, w->tb);
     gemm(n, 'N', Y, 'C', H10, Z, w->ta, w->tb);
     gemm(n, 'N', g, 'N', Z, Y, w->ta, w->tb);
@@ -233,7 +294,7 @@ static void point(Work* w, int nx, double E, const cplx* H0, const cplx* H10, do
   gemm(n, 'N', Y, 'C', H10, Z, w->ta, w->tb);
   for (size_t e = 0; e < b; ++e) G[e] = -H0[e] - SigR[e] - Z[e];
   for (int i = 0; i < n; ++i) G[i + (size_t)i * n] += z;
-  bad |= invert(n, G, w->perm);
+  bad |= invert(n, G, w->perm, (double*)w->ta);
   for (int j = 0; j < n; ++j)
     for (int i = 0; i < n; ++i)
       GamR[i + (size_t)j * n] = -(SigR[i + (size_t)j * n] - conj(SigR[j + (size_t)i * n]));
@@ -294,7 +355,7 @@ int qt_ref_rgf(int nm, int nx, int nk, const double* H00, const double* H10, int
                const double* E, double eta_lead, double eta_int, double tol, int nmax, double mul,
                double mur, double templ, double tempr, int nthreads, double* T, double* tr,
                double* tre, double* dgr, double* dgl, int* status) {
-  if (nm <= 0 || nm > 512) return -1;  /* the block product's column buffers hold 512 rows */
+  if (nm <= 0) return -1;
   const long long npts = (long long)nE * nk;
   const size_t b = (size_t)nm * nm;
   int nbad = 0;

@@ -1,13 +1,16 @@
 """The C restatement (timed CPU baseline) agrees with the numpy oracle."""
 import numpy as np
+import pytest
 
 from oracle import cref
 from oracle import rgf as orc
 from quantum_transport_gb300.devices import make_chain_device
 
 
-def test_c_oracle_matches_numpy_oracle():
-    dev = make_chain_device(6, 12, 4, -2.5, 2.5, seed=5, nk=2)
+@pytest.mark.parametrize("nm", [7, 12])
+def test_c_oracle_matches_numpy_oracle(nm):
+    """nm = 7 pads the block product's 4-row panels and 2- or 4-column panels with zeros."""
+    dev = make_chain_device(6, nm, 4, -2.5, 2.5, seed=5, nk=2)
     # the C restatement takes slab-identical blocks: use the uniform device
     r = cref.rgf(dev.H00, dev.H10, dev.E, dev.nx, mul=0.1, mur=-0.1, templ=300, tempr=280)
     assert (r["status"] == 0).all()
