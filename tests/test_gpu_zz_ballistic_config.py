@@ -40,7 +40,15 @@ def test_paths_vs_c_restatement(ctx, case, precision, t_max, t_med, d_max, d_med
     eT = np.abs(r["T"] - ref["T"]) / np.abs(ref["T"])
     assert eT.max() <= t_max and np.median(eT) <= t_med
     npts = d.E.size
+    assert np.isfinite(r["diag_gr"]).all() and np.isfinite(r["diag_gl"]).all()
     for x, y in ((r["diag_gr"].imag, ref["diag_gr"].imag), (r["diag_gl"], ref["diag_gl"])):
         x, y = x.reshape(npts, -1), y.reshape(npts, -1)
-        err = np.abs(x - y).max(axis=1) / np.abs(y).max(axis=1)
+        scale = np.abs(y).max(axis=1)
+        err = np.abs(x - y).max(axis=1) / scale
+        if precision == "mixed":
+            # complex64 storage resolves G^< down to ~1e-33 (FP32's normal range); above
+            # E = mu + 76 kT (about 2 eV here) f and G^< fall below it and are flushed
+            keep = scale >= 1e-33
+            assert keep.mean() >= 0.75
+            err = err[keep]
         assert err.max() <= d_max and np.median(err) <= d_med
